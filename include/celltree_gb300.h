@@ -1,0 +1,167 @@
+/*
+ * celltree_gb300.h -- C ABI of the GB300 cell-tree library (libcelltree_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every array argument is DEVICE memory unless
+ * its comment says "host".  `stream` is a cudaStream_t passed as void*
+ * (NULL = legacy default stream).  Functions return a ct_status; on error
+ * ct_last_error_message() gives a readable reason (thread-local).  No function
+ * allocates device memory: callers pass workspaces sized by the *_workspace_size
+ * queries.
+ *
+ * Upstream interface that each entry point replaces is cited as file:line of
+ * the numba_celltree 0.4.2 sources (relative to the upstream project root).
+ * Index arrays use int64 (numpy intp, constants.py:27); coordinates float64
+ * (constants.py:28).
+ */
+#ifndef CELLTREE_GB300_H
+#define CELLTREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CT_ABI_VERSION 1
+
+typedef enum ct_status {
+    CT_OK = 0,
+    CT_ERR_CUDA = 1,      /* a CUDA call failed */
+    CT_ERR_ARG = 2,       /* invalid argument (shape, size, null pointer) */
+    CT_ERR_WORKSPACE = 3, /* workspace too small or builder capacity exceeded */
+    CT_ERR_DEVICE = 4     /* a kernel reported an error word (see ct_device_error) */
+} ct_status;
+
+/* Device-side error bits, OR-ed into the error word of a tree descriptor. */
+#define CT_DEVERR_STACK 1u    /* traversal stack overflow */
+#define CT_DEVERR_BUCKET 2u   /* a centroid fell outside every bucket (upstream raises IndexError) */
+#define CT_DEVERR_CLIP 4u     /* clip polygon scratch (64 vertices) overflow */
+#define CT_DEVERR_CAPACITY 8u /* output capacity exceeded */
+#define CT_DEVERR_LOOP 16u    /* a bounded loop gave up (Cohen-Sutherland) */
+
+int ct_abi_version(void);
+const char* ct_last_error_message(void);
+
+/* ---------------------------------------------------------------------- */
+/* Tree descriptor                                                         */
+/* ---------------------------------------------------------------------- */
+
+/* Device arrays of one built tree.  The reference-layout members mirror
+ * CellTreeData (constants.py:82-89) with the packed NodeDType record
+ * (constants.py:92-106) stored as separate arrays.  The packed members are
+ * written by ct_pack_tree and read by the query kernels. */
+typedef struct ct_tree {
+    /* reference layout */
+    const int64_t* elements;  /* faces (n_elements x n_max_vert) or edges (n_elements x 2) */
+    const double* vertices;   /* n_vertices x 2 */
+    const int64_t* bb_indices;/* n_elements */
+    const double* bb_coords;  /* n_elements x 4: xmin, xmax, ymin, ymax */
+    const int64_t* node_child;
+    const double* node_Lmax;
+    const double* node_Rmin;
+    const int64_t* node_ptr;
+    const int64_t* node_size;
+    const uint8_t* node_dim;
+    int64_t n_elements;
+    int64_t n_vertices;
+    int64_t n_nodes;
+    int32_t n_max_vert;
+    int32_t max_depth;        /* deepest node (root = 0), from ct_build_tree */
+    double bbox[4];           /* host copy: xmin, xmax, ymin, ymax (bbox_tree celltree_base.py:20-25) */
+    /* packed traversal arrays (filled by ct_pack_tree) */
+    void* nodes_f32;          /* n_nodes x 16 B: float Lmax, float Rmin, int a, int b */
+    void* nodes_f64;          /* n_nodes x 16 B: double Lmax, double Rmin */
+    void* poly_f64;           /* n_elements x n_max_vert x 16 B, leaf (bb_indices) order */
+    void* poly_f32;           /* n_elements x n_max_vert x 8 B, leaf order, relative to origin */
+    uint8_t* poly_len;        /* n_elements: polygon length (polygon_length geometry_utils.py:72-79) */
+    uint8_t* poly_len32;      /* n_elements: length after removing repeated consecutive vertices */
+    double origin[2];         /* host: origin of the float32 frame (centre of bbox) */
+    float vmax;               /* host: max |vertex - origin| (inf-norm), set by ct_pack_tree */
+    float abs_eps;            /* host: float64 rounding scale of absolute coordinates */
+    unsigned int* error_word; /* device: one uint32, OR-ed CT_DEVERR_* bits */
+} ct_tree;
+
+/* ---------------------------------------------------------------------- */
+/* Geometry preparation                                                    */
+/* ---------------------------------------------------------------------- */
+
+/* Input check for faces / edges (no upstream counterpart: upstream indexes
+ * without checks).  *bad_host = 1 when an element's first min_len entries, or
+ * any entry before its first fill value (-1), is not a vertex index in
+ * [0, n_vertices).  Synchronises the stream. */
+int ct_validate_elements(const int64_t* elements, int64_t n, int32_t n_max_vert, int32_t min_len, int64_t n_vertices,
+                         int32_t* bad_host, void* stream);
+
+/* counter_clockwise geometry_utils.py:541-561: flips clockwise faces in place. */
+int ct_counter_clockwise(const double* vertices, int64_t* faces, int64_t n_faces, int32_t n_max_vert, void* stream);
+
+/* build_face_bboxes geometry_utils.py:443-456. bb_coords: n_faces x 4. */
+int ct_face_bboxes(const double* vertices, const int64_t* faces, int64_t n_faces, int32_t n_max_vert,
+                   double* bb_coords, void* stream);
+
+/* build_edge_bboxes geometry_utils.py:473-487 (edges: n_edges x 2). */
+int ct_edge_bboxes(const double* vertices, const int64_t* edges, int64_t n_edges, double tolerance,
+                   double* bb_coords, void* stream);
+
+/* bbox_tree + bbox_distances + max diagonal (celltree_base.py:20-52).
+ * out (host, 5 doubles): xmin, xmax, ymin, ymax, max bb diagonal.
+ * distances (device, n x 3, may be NULL): dx, dy, dxy per box.
+ * Synchronises the stream. */
+int ct_bbox_summary(const double* bb_coords, int64_t n, double* distances, double* out_host5, void* stream);
+
+/* Vertex extent for EdgeCellTree2d's tolerance (edge_celltree.py:59-62).
+ * out (host, 4 doubles): xmin, xmax, ymin, ymax.  Synchronises the stream. */
+int ct_vertex_extent(const double* vertices, int64_t n, double* out_host4, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Tree construction (creation.py:27-413)                                  */
+/* ---------------------------------------------------------------------- */
+
+/* pessimistic_n_nodes creation.py:216-230 */
+int64_t ct_pessimistic_n_nodes(int64_t n_elements);
+
+/* Workspace bytes for ct_build_tree.  capacity_factor >= 1 scales the
+ * builder's node-record capacity for very unbalanced trees (retry with a larger
+ * factor when ct_build_tree returns CT_ERR_WORKSPACE). */
+size_t ct_build_workspace_size(int64_t n_elements, int32_t n_buckets, int32_t capacity_factor);
+
+/* initialize / build creation.py:233-413 on the GPU.  Builds the tree inside
+ * the workspace and returns the node count and maximum depth (host outputs).
+ * The nodes are then written by ct_build_emit, which must be called with the
+ * same workspace before it is reused. Synchronises the stream. */
+int ct_build_tree(const double* bb_coords, int64_t n_elements, int32_t n_buckets, int64_t cells_per_leaf,
+                  int32_t capacity_factor, void* workspace, size_t workspace_bytes, int64_t* n_nodes_host,
+                  int32_t* max_depth_host, void* stream);
+
+/* Writes the nodes (reference numbering, NodeDType fields as arrays of
+ * n_nodes) and bb_indices (n_elements) built by the last ct_build_tree. */
+int ct_build_emit(const void* workspace, int64_t n_elements, int32_t n_buckets, int32_t capacity_factor,
+                  int64_t* child, double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
+                  int64_t* bb_indices, void* stream);
+
+/* Fills the packed traversal arrays of `tree` (nodes_f32, nodes_f64,
+ * poly_f64, poly_f32, poly_len, poly_len32) and its origin / vmax / abs_eps.
+ * `tree` is updated in place (host struct).  Synchronises the stream. */
+int ct_pack_tree(ct_tree* tree, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Point queries                                                           */
+/* ---------------------------------------------------------------------- */
+
+#define CT_MODE_FP64 0 /* float64 traversal and leaf tests (plain form) */
+#define CT_MODE_FP32 1 /* float32 traversal + float32 leaf filter, exact float64 fallback */
+
+/* locate_points query.py:110-117 (locate_point 63-107).  out: n (int64). */
+int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t mode,
+                     int64_t* out, void* stream);
+
+/* locate_points_on_edge query.py:167-174 (locate_point_on_edge 121-164). */
+int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,
+                             int64_t* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CELLTREE_GB300_H */

@@ -1,0 +1,10 @@
+"""GB300-native cell tree: a drop-in for numba_celltree's CellTree2d and
+EdgeCellTree2d whose construction and queries run as hand-written sm_103a
+CUDA kernels (libcelltree_gb300.so)."""
+
+from .celltree import CellTree2d
+from .edge_celltree import EdgeCellTree2d
+
+__version__ = "0.1.0"
+
+__all__ = ("CellTree2d", "EdgeCellTree2d")

@@ -1,0 +1,128 @@
+"""ctypes binding of ``libcelltree_gb300.so`` (declared in include/celltree_gb300.h).
+
+The library is the product's compute path; there is no fallback.  Loading it
+fails loudly when it is missing or was built for another ABI version.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import pathlib
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_PATH
+ABI_VERSION = 1
+
+CT_OK = 0
+CT_ERR_CUDA = 1
+CT_ERR_ARG = 2
+CT_ERR_WORKSPACE = 3
+CT_ERR_DEVICE = 4
+
+CT_MODE_FP64 = 0
+CT_MODE_FP32 = 1
+
+DEVERR_STACK = 1
+DEVERR_BUCKET = 2
+DEVERR_CLIP = 4
+DEVERR_CAPACITY = 8
+DEVERR_LOOP = 16
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_D = ctypes.c_double
+_SZ = ctypes.c_size_t
+
+
+class CtTree(ctypes.Structure):
+    """Mirror of ``struct ct_tree`` in include/celltree_gb300.h."""
+
+    _fields_ = [
+        ("elements", _P),
+        ("vertices", _P),
+        ("bb_indices", _P),
+        ("bb_coords", _P),
+        ("node_child", _P),
+        ("node_Lmax", _P),
+        ("node_Rmin", _P),
+        ("node_ptr", _P),
+        ("node_size", _P),
+        ("node_dim", _P),
+        ("n_elements", _I64),
+        ("n_vertices", _I64),
+        ("n_nodes", _I64),
+        ("n_max_vert", _I32),
+        ("max_depth", _I32),
+        ("bbox", _D * 4),
+        ("nodes_f32", _P),
+        ("nodes_f64", _P),
+        ("poly_f64", _P),
+        ("poly_f32", _P),
+        ("poly_len", _P),
+        ("poly_len32", _P),
+        ("origin", _D * 2),
+        ("vmax", ctypes.c_float),
+        ("abs_eps", ctypes.c_float),
+        ("error_word", _P),
+    ]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "ct_abi_version": (ctypes.c_int, []),
+    "ct_last_error_message": (ctypes.c_char_p, []),
+    "ct_validate_elements": (ctypes.c_int, [_P, _I64, _I32, _I32, _I64, ctypes.POINTER(_I32), _P]),
+    "ct_counter_clockwise": (ctypes.c_int, [_P, _P, _I64, _I32, _P]),
+    "ct_face_bboxes": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P]),
+    "ct_edge_bboxes": (ctypes.c_int, [_P, _P, _I64, _D, _P, _P]),
+    "ct_bbox_summary": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(_D), _P]),
+    "ct_vertex_extent": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_D), _P]),
+    "ct_pessimistic_n_nodes": (_I64, [_I64]),
+    "ct_build_workspace_size": (_SZ, [_I64, _I32, _I32]),
+    "ct_build_tree": (
+        ctypes.c_int,
+        [_P, _I64, _I32, _I64, _I32, _P, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P],
+    ),
+    "ct_build_emit": (ctypes.c_int, [_P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ct_pack_tree": (ctypes.c_int, [ctypes.POINTER(CtTree), _P]),
+    "ct_locate_points": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P]),
+    "ct_locate_points_on_edge": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _P, _P]),
+}
+
+_lib = None
+
+
+class CellTreeError(RuntimeError):
+    """A call into libcelltree_gb300 failed."""
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = pathlib.Path(LIB_PATH)
+    if not path.exists() and build_if_missing:
+        _build.build()
+    if not path.exists():
+        raise ImportError(f"libcelltree_gb300.so not found at {path}; run numba_celltree_gb300.build.build()")
+    lib = ctypes.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    v = lib.ct_abi_version()
+    if v != ABI_VERSION:
+        raise ImportError(f"libcelltree_gb300 ABI {v} != expected {ABI_VERSION}")
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status == CT_OK:
+        return
+    msg = load().ct_last_error_message().decode(errors="replace")
+    if status == CT_ERR_ARG:
+        raise ValueError(f"{what}: {msg}" if what else msg)
+    raise CellTreeError(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")

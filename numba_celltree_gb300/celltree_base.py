@@ -1,0 +1,234 @@
+"""Shared machinery of the GPU cell trees (celltree_base.py:1-114 upstream).
+
+A tree lives on the GPU: the reference-layout arrays (faces/edges, vertices,
+nodes as NodeDType fields, bb_indices, bb_coords) plus the packed traversal
+arrays of ``ct_tree``.  The public numpy attributes of the upstream classes
+(``vertices``, ``faces``, ``nodes``, ``bb_indices``, ``bb_coords``,
+``bb_distances``, ``celltree_data``) are host copies made on first access.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _device
+from . import _lib
+from .constants import MAX_N_BUCKETS, MIN_TOLERANCE, TOLERANCE_FACTOR, CellTreeData, NodeDType
+
+
+def default_tolerance(max_bb_diagonal: float) -> float:
+    """default_tolerance celltree_base.py:51-52 (given the maximum diagonal)."""
+    return max(MIN_TOLERANCE, TOLERANCE_FACTOR * max_bb_diagonal)
+
+
+class _GpuTree:
+    """Device arrays of one tree and the ``ct_tree`` descriptor over them."""
+
+    def __init__(self, device, elements, vertices, bb_coords, n_buckets: int, cells_per_leaf: int):
+        torch = _device.torch()
+        lib = _lib.load()
+        st = _device.stream()
+        self.device = device
+        self.elements = elements
+        self.vertices = vertices
+        self.bb_coords = bb_coords
+        n = int(elements.shape[0])
+        K = int(elements.shape[1])
+        self.n = n
+        self.K = K
+        # bbox_tree / bbox_distances / default tolerance (celltree_base.py:20-52)
+        self.bb_distances = _device.empty((n, 3), torch.float64, device)
+        summ = (ctypes.c_double * 5)()
+        _lib.check(lib.ct_bbox_summary(_device.ptr(bb_coords), n, _device.ptr(self.bb_distances), summ, st), "bbox")
+        self.bbox = np.array(summ[:4], dtype=np.float64)
+        self.max_diagonal = float(summ[4]) if n > 0 else 0.0
+        # build (creation.py:384-413)
+        factor = 1
+        while True:
+            wsz = lib.ct_build_workspace_size(n, n_buckets, factor)
+            ws = _device.empty((max(int(wsz), 1),), torch.uint8, device)
+            n_nodes = ctypes.c_int64(0)
+            depth = ctypes.c_int32(0)
+            status = lib.ct_build_tree(
+                _device.ptr(bb_coords), n, n_buckets, cells_per_leaf, factor,
+                _device.ptr(ws), wsz, ctypes.byref(n_nodes), ctypes.byref(depth), st,
+            )
+            if status == _lib.CT_ERR_WORKSPACE and factor < 4096:
+                factor *= 8
+                del ws
+                continue
+            _lib.check(status, "build")
+            break
+        nn = int(n_nodes.value)
+        self.n_nodes = nn
+        self.max_depth = int(depth.value)
+        self.node_child = _device.empty((nn,), torch.int64, device)
+        self.node_Lmax = _device.empty((nn,), torch.float64, device)
+        self.node_Rmin = _device.empty((nn,), torch.float64, device)
+        self.node_ptr = _device.empty((nn,), torch.int64, device)
+        self.node_size = _device.empty((nn,), torch.int64, device)
+        self.node_dim = _device.empty((nn,), torch.uint8, device)
+        self.bb_indices = _device.empty((n,), torch.int64, device)
+        _lib.check(
+            lib.ct_build_emit(
+                _device.ptr(ws), n, n_buckets, factor,
+                _device.ptr(self.node_child), _device.ptr(self.node_Lmax), _device.ptr(self.node_Rmin),
+                _device.ptr(self.node_ptr), _device.ptr(self.node_size), _device.ptr(self.node_dim),
+                _device.ptr(self.bb_indices), st,
+            ),
+            "build_emit",
+        )
+        del ws
+        # packed traversal arrays
+        self.nodes_f32 = _device.empty((max(nn, 1), 4), torch.float32, device)
+        self.nodes_f64 = _device.empty((max(nn, 1), 2), torch.float64, device)
+        self.poly_f64 = _device.empty((max(n, 1), K, 2), torch.float64, device)
+        self.poly_f32 = _device.empty((max(n, 1), K, 2), torch.float32, device)
+        self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
+        self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
+        self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
+        self.desc = _lib.CtTree()
+        self._fill_desc()
+        _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
+
+    def _fill_desc(self):
+        d = self.desc
+        P = _device.ptr
+        d.elements = P(self.elements)
+        d.vertices = P(self.vertices)
+        d.bb_indices = P(self.bb_indices)
+        d.bb_coords = P(self.bb_coords)
+        d.node_child = P(self.node_child)
+        d.node_Lmax = P(self.node_Lmax)
+        d.node_Rmin = P(self.node_Rmin)
+        d.node_ptr = P(self.node_ptr)
+        d.node_size = P(self.node_size)
+        d.node_dim = P(self.node_dim)
+        d.n_elements = self.n
+        d.n_vertices = int(self.vertices.shape[0])
+        d.n_nodes = self.n_nodes
+        d.n_max_vert = self.K
+        d.max_depth = self.max_depth
+        for k in range(4):
+            d.bbox[k] = float(self.bbox[k])
+        d.nodes_f32 = P(self.nodes_f32)
+        d.nodes_f64 = P(self.nodes_f64)
+        d.poly_f64 = P(self.poly_f64)
+        d.poly_f32 = P(self.poly_f32)
+        d.poly_len = P(self.poly_len)
+        d.poly_len32 = P(self.poly_len32)
+        d.error_word = P(self.error_word)
+
+    def reset_error(self):
+        self.error_word.zero_()
+
+    def raise_on_device_error(self):
+        err = int(self.error_word.item())
+        if err:
+            bits = []
+            if err & _lib.DEVERR_STACK:
+                bits.append("traversal stack overflow")
+            if err & _lib.DEVERR_BUCKET:
+                bits.append("centroid outside every bucket")
+            if err & _lib.DEVERR_CLIP:
+                bits.append("clip polygon overflow")
+            if err & _lib.DEVERR_CAPACITY:
+                bits.append("output capacity exceeded")
+            if err & _lib.DEVERR_LOOP:
+                bits.append("bounded loop gave up")
+            raise _lib.CellTreeError("device error: " + ", ".join(bits))
+
+    def host_nodes(self) -> np.ndarray:
+        nodes = np.empty(self.n_nodes, dtype=NodeDType)
+        nodes["child"] = self.node_child.cpu().numpy()
+        nodes["Lmax"] = self.node_Lmax.cpu().numpy()
+        nodes["Rmin"] = self.node_Rmin.cpu().numpy()
+        nodes["ptr"] = self.node_ptr.cpu().numpy()
+        nodes["size"] = self.node_size.cpu().numpy()
+        nodes["dim"] = self.node_dim.cpu().numpy().astype(bool)
+        return nodes
+
+
+def validate_elements(elements, n_vertices: int, min_len: int, what: str) -> None:
+    """Reject element arrays that index outside the vertex array (a GPU kernel
+    must never read through an invalid index)."""
+    lib = _lib.load()
+    bad = ctypes.c_int32(0)
+    n, K = int(elements.shape[0]), int(elements.shape[1])
+    _lib.check(
+        lib.ct_validate_elements(_device.ptr(elements), n, K, min_len, n_vertices, ctypes.byref(bad), _device.stream()),
+        "validate",
+    )
+    if bad.value:
+        raise ValueError(f"{what} contain indices outside [0, n_vertices)")
+
+
+def _validate_params(n_buckets: int, cells_per_leaf: int) -> None:
+    if n_buckets < 2:
+        raise ValueError("n_buckets must be >= 2")
+    if cells_per_leaf < 1:
+        raise ValueError("cells_per_leaf must be >= 1")
+    if n_buckets > MAX_N_BUCKETS:
+        raise ValueError(f"n_buckets must be <= {MAX_N_BUCKETS} on the GPU builder")
+
+
+class CellTree2dBase:
+    """Common attributes and host views of CellTree2d / EdgeCellTree2d."""
+
+    _tree: _GpuTree
+    _elements_name = "faces"
+    _host: dict
+
+    # -- host views (upstream public attributes) --------------------------
+    def _cached(self, name, fn):
+        if name not in self._host:
+            self._host[name] = fn()
+        return self._host[name]
+
+    @property
+    def vertices(self) -> np.ndarray:
+        return self._cached("vertices", lambda: self._tree.vertices.cpu().numpy())
+
+    @property
+    def nodes(self) -> np.ndarray:
+        return self._cached("nodes", self._tree.host_nodes)
+
+    @property
+    def bb_indices(self) -> np.ndarray:
+        return self._cached("bb_indices", lambda: self._tree.bb_indices.cpu().numpy())
+
+    @property
+    def bb_coords(self) -> np.ndarray:
+        return self._cached("bb_coords", lambda: self._tree.bb_coords.cpu().numpy())
+
+    @property
+    def bb_distances(self) -> np.ndarray:
+        return self._cached("bb_distances", lambda: self._tree.bb_distances.cpu().numpy())
+
+    @property
+    def bbox(self) -> np.ndarray:
+        return self._tree.bbox
+
+    @property
+    def celltree_data(self) -> CellTreeData:
+        return CellTreeData(
+            getattr(self, self._elements_name), self.vertices, self.nodes, self.bb_indices, self.bb_coords,
+            self.bbox, self.cells_per_leaf,
+        )
+
+    def to_dict_of_lists(self):
+        """celltree_base.py:82-114"""
+        child = self.nodes["child"]
+        d = {}
+        for parent_index, c in enumerate(child):
+            d[parent_index] = [] if c == -1 else [int(c), int(c) + 1]
+        return d
+
+    # -- helpers -----------------------------------------------------------
+    def _tolerance(self, tolerance: Optional[float]) -> float:
+        if tolerance is None:
+            return default_tolerance(self._tree.max_diagonal)
+        return float(tolerance)

@@ -1,0 +1,1203 @@
+// ct_build.cu -- GPU construction of the cell tree (creation.py:27-413).
+//
+// The upstream builder (build creation.py:233-381) is a serial depth-first
+// loop.  Every node's work -- the bounds of its range, the n_buckets
+// equal-width centroid buckets, the stable partition of its bb_indices range
+// and the split decision -- depends only on the node's own range, never on
+// the order in which nodes are processed.  This builder therefore processes
+// nodes breadth first:
+//
+//   phase A  nodes with more than SMALL cells, one level at a time, many CTAs
+//            per node: a stats pass (per-bucket counts and first-occurrence
+//            bounds for both dimensions, warp-aggregated), a decide pass (one
+//            warp per node, upstream split logic), a stable scatter pass
+//            (match_any ranks + per-tile prefixes).  Child bounds come from the
+//            parent's per-bucket stats, so no separate bounds pass is needed.
+//   phase B  every node of <= SMALL cells roots a subtree that one warp builds
+//            depth first in shared memory, in upstream order.
+//   phase C  the node numbering.  Upstream appends the two children of every
+//            split node at the end of the node array in depth-first
+//            (pre-order, left first) processing order, so a split node v gets
+//            child = 1 + 2 * (number of split nodes before v in pre-order).
+//            Phase C computes per-subtree split counts bottom-up and pre-order
+//            ranks top-down and writes every node to its upstream position.
+//
+// Float64 comparisons use monotone 64-bit integer keys (fkey): the order is the
+// float order, and -0.0 / +0.0 share a key; where a first-occurrence minimum
+// or maximum is 0 the sign is taken from the first zero-valued element, so the
+// stored bits equal upstream's.  The float64 arithmetic of the split logic is
+// written in upstream's evaluation order (library compiled with -fmad=false).
+#include <cfloat>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ct_common.cuh"
+#include "ct_internal.h"
+
+namespace ct {
+
+constexpr int SMALL = 128;         // subtree size handled by one warp
+constexpr int NBMAX = 32;          // maximum n_buckets
+constexpr int STATS_THREADS = 256; // threads of the stats / scatter CTAs
+constexpr int TILE_MIN = 2048;     // minimum cells per tile
+constexpr int MAX_TILES = 512;     // maximum tiles per node
+constexpr int SUB_WARPS = 4;       // warps per CTA in the subtree kernel
+
+enum : int { K_PENDING = 0, K_SPLIT = 1, K_LEAF = 2, K_SUBTREE = 3 };
+
+// Phase-A node record.
+struct ARec {
+    double bnd[4];  // first-occurrence xmin, xmax, ymin, ymax of the node's boxes
+    double Lmax, Rmin;
+    long long splits;  // split nodes in the subtree rooted here
+    long long S;       // split nodes before this node in pre-order
+    long long pos;     // final node index
+    int ptr, size;
+    int dim, kind;
+    int child, parity; // child: record id of the left child (right = +1)
+    int level, tile0;
+    int tile1, split_dim;
+    int nlocal, err;
+};
+
+// Phase-B local node record (subtree numbering, local ids).
+struct LRec {
+    double Lmax, Rmin;
+    int child, ptr, size, dim;
+};
+
+struct Counters {
+    int rec_count;
+    int tile_count;
+    int small_count;
+    unsigned int err;
+    int max_depth;
+    int lb, le;  // current level record range
+    int pad;
+    unsigned long long root_key[4];
+    int root_zp[4];
+};
+
+struct WS {
+    double* f[2][6];  // lo_x, hi_x, lo_y, hi_y, c_x, c_y (two ping-pong buffers)
+    int* idx[2];
+    int* final_idx;
+    ARec* recs;
+    int rec_cap;
+    unsigned int* st_cnt;            // [rec_cap][2][NB]
+    unsigned long long* st_key;      // [rec_cap][2][NB][4]
+    int* st_zp;                      // [rec_cap][2][NB][4]
+    int* nb_base;                    // [rec_cap][NB]
+    int* tile_rec;
+    int* tile_start;
+    int* tile_end;
+    unsigned int* tile_cnt;          // [tile_cap][2][NB]
+    int* tile_pref;                  // [tile_cap][NB]
+    int tile_cap;
+    int* small_list;                 // [rec_cap]
+    LRec* lrec;                      // [2 * n]
+    Counters* cnt;
+    int* level_begin;                // [rec_cap + 1] host mirror written per level
+};
+
+static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Carves the workspace; returns total bytes.  base == nullptr -> size only.
+static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* p = base ? base + off : nullptr;
+        off += align_up(bytes);
+        return p;
+    };
+    int64_t nn = n > 0 ? n : 1;
+    int rec_cap = (int)std::min<int64_t>(INT32_MAX / 4, (int64_t)factor * (8 * (nn / SMALL) + 64));
+    int tile_cap = (int)std::min<int64_t>(INT32_MAX / 4, 2 * (nn / TILE_MIN) + 2 * (int64_t)rec_cap + 64);
+    WS w;
+    for (int b = 0; b < 2; b++) {
+        for (int k = 0; k < 6; k++) w.f[b][k] = (double*)take(sizeof(double) * nn);
+        w.idx[b] = (int*)take(sizeof(int) * nn);
+    }
+    w.final_idx = (int*)take(sizeof(int) * nn);
+    w.recs = (ARec*)take(sizeof(ARec) * rec_cap);
+    w.rec_cap = rec_cap;
+    w.st_cnt = (unsigned int*)take(sizeof(unsigned int) * (size_t)rec_cap * 2 * NB);
+    w.st_key = (unsigned long long*)take(sizeof(unsigned long long) * (size_t)rec_cap * 2 * NB * 4);
+    w.st_zp = (int*)take(sizeof(int) * (size_t)rec_cap * 2 * NB * 4);
+    w.nb_base = (int*)take(sizeof(int) * (size_t)rec_cap * NB);
+    w.tile_rec = (int*)take(sizeof(int) * tile_cap);
+    w.tile_start = (int*)take(sizeof(int) * tile_cap);
+    w.tile_end = (int*)take(sizeof(int) * tile_cap);
+    w.tile_cnt = (unsigned int*)take(sizeof(unsigned int) * (size_t)tile_cap * 2 * NB);
+    w.tile_pref = (int*)take(sizeof(int) * (size_t)tile_cap * NB);
+    w.tile_cap = tile_cap;
+    w.small_list = (int*)take(sizeof(int) * rec_cap);
+    w.lrec = (LRec*)take(sizeof(LRec) * 2 * nn);
+    w.cnt = (Counters*)take(sizeof(Counters));
+    w.level_begin = nullptr;
+    if (ws) *ws = w;
+    return off;
+}
+
+// ------------------------------------------------------------------------
+// small device helpers
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// (key, pos) lexicographic minimum over the lanes of `mask` (all call).
+__device__ __forceinline__ void group_min_kp(unsigned mask, unsigned long long k, unsigned pos,
+                                             unsigned long long* ko, unsigned* po) {
+    unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    unsigned mh = __reduce_min_sync(mask, hi);
+    unsigned ml = __reduce_min_sync(mask, hi == mh ? lo : 0xffffffffu);
+    unsigned mp = __reduce_min_sync(mask, (hi == mh && lo == ml) ? pos : 0xffffffffu);
+    *ko = ((unsigned long long)mh << 32) | ml;
+    *po = mp;
+}
+
+__device__ __forceinline__ unsigned long long group_min_k(unsigned mask, unsigned long long k) {
+    unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    unsigned mh = __reduce_min_sync(mask, hi);
+    unsigned ml = __reduce_min_sync(mask, hi == mh ? lo : 0xffffffffu);
+    return ((unsigned long long)mh << 32) | ml;
+}
+
+__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffll) == 0; }
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return (unsigned long long)(__double_as_longlong(x) & 0x7fffffffffffffffll) > 0x7ff0000000000000ull;
+}
+
+// Bucket of centroid key kc given the NB+1 boundary keys K (non-decreasing):
+// the b with K[b] <= kc < K[b+1] (centroid_test creation.py:44-51), or -1.
+__device__ __forceinline__ int find_bucket(const unsigned long long* K, int NB, unsigned long long kc) {
+    if (kc < K[0] || kc >= K[NB]) return -1;
+    int lo = 0, hi = NB;  // K[lo] <= kc < K[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (K[mid] <= kc) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Boundary j of the equal-width buckets: Min of bucket j (= Max of bucket j-1),
+// `i * bucket_length + range_Rmin` (creation.py:283-293).
+__device__ __forceinline__ double bucket_edge(int j, double bl, double R) { return exact_i2d(j) * bl + R; }
+
+// bucket_length = (range_Lmax - range_Rmin) / n_buckets (creation.py:278).
+// For a power-of-two n_buckets the quotient equals the product with the exact
+// reciprocal (same real number, same rounding), which avoids a float64 divide.
+__device__ __forceinline__ double bucket_len(double L, double R, int NB) {
+    double diff = L - R;
+    if ((NB & (NB - 1)) == 0) return diff * exact_pow2_inv(NB);
+    return diff / exact_i2d(NB);
+}
+
+struct Decision {
+    int kind;     // 0: all cells in one bucket, 1: split, -1: error
+    int nleft;    // cells in the left child
+    int rbucket;  // first bucket of the right child
+    double Lmax, Rmin;
+};
+
+// Split decision of one node for one dimension, lane-parallel (all 32 lanes
+// call, NB <= 32).  cnt / bRmin / bLmax hold the per-bucket sizes and bounds
+// (empty buckets: DBL_MAX / -DBL_MAX, get_bounds creation.py:153-171).
+// Restates the empty-bucket merge (creation.py:322-341), the all-in-one test
+// (343-358) and split_plane (174-213) on the list of non-empty buckets.
+__device__ Decision warp_decide(const int* cnt, const double* bRmin, const double* bLmax, int NB, int size,
+                                double R, double L, double bl) {
+    const unsigned FULL = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    Decision D;
+    D.kind = -1;
+    D.nleft = 0;
+    D.rbucket = -1;
+    D.Lmax = -1.0;
+    D.Rmin = -1.0;
+    bool ne = lane < NB && cnt[lane] > 0;
+    unsigned mask = __ballot_sync(FULL, ne);
+    int m = __popc(mask);
+    if (m <= 1) {
+        D.kind = (m == 1) ? 0 : -1;
+        return D;
+    }
+    int bk = (lane < m) ? (int)__fns(mask, 0, lane + 1) : 0;
+    int ck = (lane < m) ? cnt[bk] : 0;
+    int pre = ck;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(FULL, pre, o);
+        if (lane >= o) pre += t;
+    }
+    int nL = pre - ck;  // cells of the first `lane` non-empty buckets
+    int bprev = __shfl_up_sync(FULL, bk, 1);
+    int plane;
+    if (m == 2) {
+        plane = 1;
+    } else {
+        unsigned long long key = ~0ull;
+        if (lane >= 1 && lane < m) {
+            double left_volume = (bLmax[bprev] - R) / bl;
+            double right_volume = (L - bRmin[bk]) / bl;
+            double cost = left_volume * exact_i2d(nL) + right_volume * exact_i2d(size - nL);
+            // `plane_cost < plane_min_cost` with plane_min_cost = FLOAT_MAX (NaN never qualifies)
+            if (!is_nan_bits(cost) && fkey(cost) < fkey(DBL_MAX)) key = fkey(cost);
+        }
+        unsigned long long kmin;
+        unsigned pmin_;
+        group_min_kp(FULL, key, (unsigned)lane, &kmin, &pmin_);
+        if (kmin == ~0ull) return D;  // no finite cost: upstream indexes past its buckets
+        plane = (int)pmin_;
+    }
+    // Lmax = first maximum of bucket Lmax left of the plane, Rmin = first
+    // minimum of bucket Rmin right of it (split_plane creation.py:202-211).
+    unsigned long long kl = (lane < plane) ? ~fkey(bLmax[bk]) : ~0ull;
+    unsigned long long kr = (lane >= plane && lane < m) ? fkey(bRmin[bk]) : ~0ull;
+    unsigned long long ko;
+    unsigned pl, pr;
+    group_min_kp(FULL, kl, (unsigned)lane, &ko, &pl);
+    group_min_kp(FULL, kr, (unsigned)lane, &ko, &pr);
+    int bl_w = __shfl_sync(FULL, bk, (int)pl);
+    int br_w = __shfl_sync(FULL, bk, (int)pr);
+    D.Lmax = bLmax[bl_w];
+    D.Rmin = bRmin[br_w];
+    D.nleft = __shfl_sync(FULL, pre, plane - 1);
+    D.rbucket = __shfl_sync(FULL, bk, plane);
+    D.kind = 1;
+    return D;
+}
+
+// ------------------------------------------------------------------------
+// initial element buffers and root bounds
+// ------------------------------------------------------------------------
+
+__global__ void k_init_elems(const double* __restrict__ bb, int n, WS ws) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double x0 = bb[4 * (size_t)i], x1 = bb[4 * (size_t)i + 1], y0 = bb[4 * (size_t)i + 2], y1 = bb[4 * (size_t)i + 3];
+        ws.f[0][0][i] = x0;
+        ws.f[0][1][i] = x1;
+        ws.f[0][2][i] = y0;
+        ws.f[0][3][i] = y1;
+        // centroid creation.py:50: box[2d] + 0.5 * (box[2d + 1] - box[2d])
+        ws.f[0][4][i] = x0 + 0.5 * (x1 - x0);
+        ws.f[0][5][i] = y0 + 0.5 * (y1 - y0);
+        ws.idx[0][i] = i;
+    }
+}
+
+__global__ void k_reset(WS ws, int n, int cpl_small_root, int root_dim) {
+    Counters* c = ws.cnt;
+    c->rec_count = 1;
+    c->tile_count = 0;
+    c->small_count = 0;
+    c->err = 0;
+    c->max_depth = 0;
+    c->lb = 0;
+    c->le = 1;
+    for (int f = 0; f < 4; f++) {
+        c->root_key[f] = ~0ull;
+        c->root_zp[f] = INT32_MAX;
+    }
+    ARec r;
+    memset(&r, 0, sizeof(r));
+    r.ptr = 0;
+    r.size = n;
+    r.dim = root_dim;
+    r.kind = (n > SMALL) ? K_PENDING : K_SUBTREE;
+    r.child = -1;
+    r.parity = 0;
+    r.level = 0;
+    r.split_dim = -1;
+    r.Lmax = -1.0;
+    r.Rmin = -1.0;
+    ws.recs[0] = r;
+    if (n <= SMALL) {
+        ws.small_list[0] = 0;
+        c->small_count = 1;
+    }
+    (void)cpl_small_root;
+}
+
+// First-occurrence bounds of all boxes, both dimensions (root get_bounds).
+__global__ void k_root_bounds(WS ws, int n) {
+    const unsigned FULL = 0xffffffffu;
+    unsigned long long k[4] = {~0ull, ~0ull, ~0ull, ~0ull};
+    int stride = gridDim.x * blockDim.x;
+    int iters = (n + stride - 1) / stride;
+    for (int it = 0; it < iters; it++) {
+        int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < n) {
+            for (int f = 0; f < 4; f++) {
+                double v = ws.f[0][f][i];
+                unsigned long long kk = (f & 1) ? ~fkey(v) : fkey(v);
+                if (kk < k[f]) k[f] = kk;
+                if (is_zero(v)) atomicMin(&ws.cnt->root_zp[f], i);
+            }
+        }
+    }
+    for (int f = 0; f < 4; f++) {
+        unsigned long long m = group_min_k(FULL, k[f]);
+        if ((threadIdx.x & 31) == 0) atomicMin(&ws.cnt->root_key[f], m);
+    }
+}
+
+__device__ __forceinline__ double resolve_key(unsigned long long key_min_form, int f, int zp, const double* src) {
+    // key_min_form: the minimum of the min-form key (complemented for maxima)
+    unsigned long long k = (f & 1) ? ~key_min_form : key_min_form;
+    if (k == fkey(0.0)) return src[zp];
+    return fkey_inv(k);
+}
+
+__global__ void k_root_resolve(WS ws, int n) {
+    if (n <= 0) return;
+    for (int f = 0; f < 4; f++)
+        ws.recs[0].bnd[f] = resolve_key(ws.cnt->root_key[f], f, ws.cnt->root_zp[f], ws.f[0][f]);
+}
+
+// ------------------------------------------------------------------------
+// phase A
+// ------------------------------------------------------------------------
+
+__device__ __forceinline__ int tile_len_for(int size) {
+    int t = (size + MAX_TILES - 1) / MAX_TILES;
+    if (t < TILE_MIN) t = TILE_MIN;
+    t = (t + STATS_THREADS - 1) / STATS_THREADS * STATS_THREADS;
+    return t;
+}
+
+// One warp per record of the current level: make tiles for pending nodes and
+// reset their stats slots.
+__global__ void k_make_tiles(WS ws, int NB) {
+    int lb = ws.cnt->lb, le = ws.cnt->le;
+    int lane = threadIdx.x & 31;
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int r = lb + wid; r < le; r += nw) {
+        ARec* R = &ws.recs[r];
+        if (R->kind != K_PENDING) continue;
+        int size = R->size;
+        int tl = tile_len_for(size);
+        int nt = (size + tl - 1) / tl;
+        int t0 = 0;
+        if (lane == 0) t0 = atomicAdd(&ws.cnt->tile_count, nt);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 + nt > ws.tile_cap) {
+            if (lane == 0) atomicOr(&ws.cnt->err, 0x80000000u);
+            continue;
+        }
+        for (int j = lane; j < nt; j += 32) {
+            ws.tile_rec[t0 + j] = r;
+            ws.tile_start[t0 + j] = R->ptr + j * tl;
+            ws.tile_end[t0 + j] = min(R->ptr + (j + 1) * tl, R->ptr + size);
+        }
+        if (lane == 0) {
+            R->tile0 = t0;
+            R->tile1 = t0 + nt;
+        }
+        size_t s = (size_t)(r - lb);
+        for (int j = lane; j < 2 * NB; j += 32) ws.st_cnt[s * 2 * NB + j] = 0u;
+        for (int j = lane; j < 2 * NB * 4; j += 32) {
+            ws.st_key[s * 2 * NB * 4 + j] = ~0ull;
+            ws.st_zp[s * 2 * NB * 4 + j] = INT32_MAX;
+        }
+    }
+}
+
+// Per tile: bucket membership in both dimensions; per (dim, bucket): count,
+// first-occurrence min of lo_x / lo_y and max of hi_x / hi_y (as min-form
+// keys) and the first position of a zero value.
+__global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int NB) {
+    __shared__ unsigned long long K[2][NBMAX + 1];
+    __shared__ unsigned int cnt[2][NBMAX];
+    __shared__ unsigned long long key[2][NBMAX][4];
+    __shared__ int zp[2][NBMAX][4];
+    const unsigned FULL = 0xffffffffu;
+    int t = blockIdx.x;
+    int r = ws.tile_rec[t];
+    int s = ws.tile_start[t], e = ws.tile_end[t];
+    int lb = ws.cnt->lb;
+    const ARec* R = &ws.recs[r];
+    int tid = threadIdx.x;
+    for (int j = tid; j < 2 * NBMAX; j += blockDim.x) (&cnt[0][0])[j] = 0u;
+    for (int j = tid; j < 2 * NBMAX * 4; j += blockDim.x) {
+        (&key[0][0][0])[j] = ~0ull;
+        (&zp[0][0][0])[j] = INT32_MAX;
+    }
+    if (tid < 2 * (NB + 1)) {
+        int d = tid / (NB + 1), j = tid % (NB + 1);
+        double Rd = R->bnd[2 * d], Ld = R->bnd[2 * d + 1];
+        K[d][j] = fkey(bucket_edge(j, bucket_len(Ld, Rd, NB), Rd));
+    }
+    __syncthreads();
+    const double* F0 = ws.f[parity][0];
+    const double* F1 = ws.f[parity][1];
+    const double* F2 = ws.f[parity][2];
+    const double* F3 = ws.f[parity][3];
+    const double* C0 = ws.f[parity][4];
+    const double* C1 = ws.f[parity][5];
+    for (int base = s; base < e; base += blockDim.x) {
+        int i = base + tid;
+        bool valid = i < e;
+        double v0 = 0, v1 = 0, v2 = 0, v3 = 0, c0 = 0, c1 = 0;
+        if (valid) {
+            v0 = F0[i];
+            v1 = F1[i];
+            v2 = F2[i];
+            v3 = F3[i];
+            c0 = C0[i];
+            c1 = C1[i];
+        }
+        unsigned long long k0 = fkey(v0), k1 = ~fkey(v1), k2 = fkey(v2), k3 = ~fkey(v3);
+#pragma unroll
+        for (int d = 0; d < 2; d++) {
+            int b = -2;
+            if (valid) {
+                b = find_bucket(K[d], NB, fkey(d ? c1 : c0));
+                if (b < 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
+            }
+            unsigned grp = __match_any_sync(FULL, b);
+            if (b >= 0) {
+                unsigned long long m0 = group_min_k(grp, k0);
+                unsigned long long m1 = group_min_k(grp, k1);
+                unsigned long long m2 = group_min_k(grp, k2);
+                unsigned long long m3 = group_min_k(grp, k3);
+                if ((int)(__ffs(grp) - 1) == (tid & 31)) {
+                    atomicAdd(&cnt[d][b], (unsigned)__popc(grp));
+                    atomicMin(&key[d][b][0], m0);
+                    atomicMin(&key[d][b][1], m1);
+                    atomicMin(&key[d][b][2], m2);
+                    atomicMin(&key[d][b][3], m3);
+                }
+                if (is_zero(v0)) atomicMin(&zp[d][b][0], i);
+                if (is_zero(v1)) atomicMin(&zp[d][b][1], i);
+                if (is_zero(v2)) atomicMin(&zp[d][b][2], i);
+                if (is_zero(v3)) atomicMin(&zp[d][b][3], i);
+            }
+        }
+    }
+    __syncthreads();
+    size_t sidx = (size_t)(r - lb);
+    for (int j = tid; j < 2 * NB; j += blockDim.x) {
+        int d = j / NB, b = j % NB;
+        unsigned c = cnt[d][b];
+        ws.tile_cnt[(size_t)t * 2 * NB + j] = c;
+        if (c) atomicAdd(&ws.st_cnt[sidx * 2 * NB + j], c);
+    }
+    for (int j = tid; j < 2 * NB * 4; j += blockDim.x) {
+        int d = j / (NB * 4), b = (j / 4) % NB, f = j % 4;
+        if (cnt[d][b]) {
+            atomicMin(&ws.st_key[sidx * 2 * NB * 4 + j], key[d][b][f]);
+            if (zp[d][b][f] != INT32_MAX) atomicMin(&ws.st_zp[sidx * 2 * NB * 4 + j], zp[d][b][f]);
+        }
+    }
+}
+
+// One warp per record of the current level: the upstream split decision for
+// pending nodes, children records, bucket bases and tile prefixes.
+__global__ void k_decide(WS ws, int NB, long long cpl) {
+    __shared__ int s_cnt[4][2][NBMAX];
+    __shared__ double s_Rmin[4][2][NBMAX];
+    __shared__ double s_Lmax[4][2][NBMAX];
+    const unsigned FULL = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    int w = threadIdx.x >> 5;  // blockDim = 128
+    int lb = ws.cnt->lb, le = ws.cnt->le;
+    int r = lb + blockIdx.x * 4 + w;
+    if (r >= le) return;
+    ARec* R = &ws.recs[r];
+    if (R->kind != K_PENDING) return;
+    int parity = R->parity;
+    size_t sidx = (size_t)(r - lb);
+    int size = R->size, ptr = R->ptr;
+    // resolve per-bucket bounds of both dimensions
+    for (int j = lane; j < 2 * NB; j += 32) {
+        int d = j / NB, b = j % NB;
+        int c = (int)ws.st_cnt[sidx * 2 * NB + j];
+        s_cnt[w][d][b] = c;
+        double rmin = DBL_MAX, lmax = -DBL_MAX;
+        if (c > 0) {
+            size_t kb = (sidx * 2 * NB + j) * 4;
+            int flo = 2 * d, fhi = 2 * d + 1;
+            rmin = resolve_key(ws.st_key[kb + flo], flo, ws.st_zp[kb + flo], ws.f[parity][flo]);
+            lmax = resolve_key(ws.st_key[kb + fhi], fhi, ws.st_zp[kb + fhi], ws.f[parity][fhi]);
+        }
+        s_Rmin[w][d][b] = rmin;
+        s_Lmax[w][d][b] = lmax;
+    }
+    __syncwarp();
+    int d0 = R->dim;
+    int stored_dim = d0;
+    int ds = -1;
+    Decision D;
+    D.kind = -1;
+    bool bad = false;
+    if ((long long)size <= cpl) {
+        D.kind = 2;  // leaf (creation.py:267)
+    } else {
+        for (int attempt = 0; attempt < 2; attempt++) {
+            int d = attempt == 0 ? d0 : 1 - d0;
+            int tot = 0;
+            for (int b = 0; b < NB; b++) tot += s_cnt[w][d][b];
+            if (tot != size) {
+                bad = true;
+                break;
+            }
+            double Rd = R->bnd[2 * d], Ld = R->bnd[2 * d + 1];
+            double bl = bucket_len(Ld, Rd, NB);
+            D = warp_decide(s_cnt[w][d], s_Rmin[w][d], s_Lmax[w][d], NB, size, Rd, Ld, bl);
+            if (D.kind == 1) {
+                ds = d;
+                break;
+            }
+            if (D.kind < 0) {
+                bad = true;
+                break;
+            }
+            // all cells in one bucket: flip the stored dim once, then give up
+            if (attempt == 0) stored_dim = 1 - d0;
+            else D.kind = 2;
+        }
+    }
+    if (bad) {
+        if (lane == 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
+        D.kind = 2;
+    }
+    if (D.kind == 2) {
+        if (lane == 0) {
+            R->kind = K_LEAF;
+            R->dim = stored_dim;
+            R->split_dim = -1;
+            R->Lmax = -1.0;
+            R->Rmin = -1.0;
+        }
+        return;
+    }
+    // split in ds
+    int c = 0;
+    if (lane == 0) c = atomicAdd(&ws.cnt->rec_count, 2);
+    c = __shfl_sync(FULL, c, 0);
+    if (c + 2 > ws.rec_cap) {
+        if (lane == 0) {
+            atomicOr(&ws.cnt->err, 0x80000000u);
+            R->kind = K_LEAF;
+            R->split_dim = -1;
+        }
+        return;
+    }
+    int rb = D.rbucket;
+    // child bounds: first occurrence over the child's buckets in order
+    size_t kb0 = sidx * 2 * NB * 4 + (size_t)ds * NB * 4;
+    double cb[2][4];
+    for (int f = 0; f < 4; f++) {
+        for (int side = 0; side < 2; side++) {
+            int b0 = side ? rb : 0, b1 = side ? NB : rb;
+            unsigned long long best = ~0ull;
+            int bb = -1;
+            for (int b = b0; b < b1; b++) {
+                if (s_cnt[w][ds][b] == 0) continue;
+                unsigned long long k = ws.st_key[kb0 + (size_t)b * 4 + f];
+                if (k < best) {
+                    best = k;
+                    bb = b;
+                }
+            }
+            cb[side][f] = (bb < 0) ? ((f & 1) ? -DBL_MAX : DBL_MAX)
+                                   : resolve_key(best, f, ws.st_zp[kb0 + (size_t)bb * 4 + f], ws.f[parity][f]);
+        }
+    }
+    int child_dim = 1 - ds;
+    if (lane < 2) {
+        ARec ch;
+        memset(&ch, 0, sizeof(ch));
+        ch.ptr = lane ? ptr + D.nleft : ptr;
+        ch.size = lane ? size - D.nleft : D.nleft;
+        ch.dim = child_dim;
+        ch.child = -1;
+        ch.parity = 1 - parity;
+        ch.level = R->level + 1;
+        ch.split_dim = -1;
+        ch.Lmax = -1.0;
+        ch.Rmin = -1.0;
+        for (int f = 0; f < 4; f++) ch.bnd[f] = cb[lane][f];
+        ch.kind = (ch.size > SMALL) ? K_PENDING : K_SUBTREE;
+        ws.recs[c + lane] = ch;
+        if (ch.kind == K_SUBTREE) {
+            int sl = atomicAdd(&ws.cnt->small_count, 1);
+            ws.small_list[sl] = c + lane;
+        }
+        atomicMax(&ws.cnt->max_depth, ch.level);
+    }
+    if (lane == 0) {
+        R->kind = K_SPLIT;
+        R->dim = stored_dim;
+        R->split_dim = ds;
+        R->Lmax = D.Lmax;
+        R->Rmin = D.Rmin;
+        R->child = c;
+    }
+    // bucket bases in the node and per-tile prefixes
+    if (lane == 0) {
+        int acc = ptr;
+        for (int b = 0; b < NB; b++) {
+            ws.nb_base[sidx * NB + b] = acc;
+            acc += s_cnt[w][ds][b];
+        }
+    }
+    int t0 = R->tile0, t1 = R->tile1;
+    int nt = t1 - t0;
+    int per = (nt + 31) / 32;
+    int my0 = t0 + lane * per, my1 = min(t0 + (lane + 1) * per, t1);
+    for (int b = 0; b < NB; b++) {
+        int sum = 0;
+        for (int t = my0; t < my1; t++) sum += (int)ws.tile_cnt[(size_t)t * 2 * NB + ds * NB + b];
+        int incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int run = incl - sum;
+        for (int t = my0; t < my1; t++) {
+            ws.tile_pref[(size_t)t * NB + b] = run;
+            run += (int)ws.tile_cnt[(size_t)t * 2 * NB + ds * NB + b];
+        }
+    }
+}
+
+// Per tile: stable partition of split nodes into the other buffer; leaf cells
+// go straight to their final position.
+__global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, int NB) {
+    __shared__ unsigned long long K[NBMAX + 1];
+    __shared__ int base[NBMAX];
+    __shared__ int run[NBMAX];
+    __shared__ int wcnt[STATS_THREADS / 32][NBMAX];
+    const unsigned FULL = 0xffffffffu;
+    int t = blockIdx.x;
+    int r = ws.tile_rec[t];
+    int s = ws.tile_start[t], e = ws.tile_end[t];
+    int lb = ws.cnt->lb;
+    const ARec* R = &ws.recs[r];
+    int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int* idx_in = ws.idx[parity];
+    if (R->kind != K_SPLIT) {
+        for (int i = s + tid; i < e; i += blockDim.x) ws.final_idx[i] = idx_in[i];
+        return;
+    }
+    int ds = R->split_dim;
+    size_t sidx = (size_t)(r - lb);
+    if (tid <= NB) {
+        double Rd = R->bnd[2 * ds], Ld = R->bnd[2 * ds + 1];
+        K[tid] = fkey(bucket_edge(tid, bucket_len(Ld, Rd, NB), Rd));
+    }
+    if (tid < NB) {
+        base[tid] = ws.nb_base[sidx * NB + tid] + ws.tile_pref[(size_t)t * NB + tid];
+        run[tid] = 0;
+    }
+    __syncthreads();
+    const double* Cd = ws.f[parity][4 + ds];
+    for (int b0 = s; b0 < e; b0 += blockDim.x) {
+        int i = b0 + tid;
+        bool valid = i < e;
+        int b = valid ? find_bucket(K, NB, fkey(Cd[i])) : -2;
+        if (valid && b < 0) b = -1;  // counted nowhere: flagged by k_stats
+        unsigned grp = __match_any_sync(FULL, b);
+        int rank = __popc(grp & lanemask_lt());
+        for (int j = tid; j < (STATS_THREADS / 32) * NBMAX; j += blockDim.x) (&wcnt[0][0])[j] = 0;
+        __syncthreads();
+        if (b >= 0 && (int)(__ffs(grp) - 1) == lane) wcnt[w][b] = __popc(grp);
+        __syncthreads();
+        int off = 0;
+        if (b >= 0) {
+            for (int ww = 0; ww < w; ww++) off += wcnt[ww][b];
+            int dst = base[b] + run[b] + off + rank;
+            int op = 1 - parity;
+#pragma unroll
+            for (int k = 0; k < 6; k++) ws.f[op][k][dst] = ws.f[parity][k][i];
+            ws.idx[op][dst] = idx_in[i];
+        }
+        __syncthreads();
+        if (tid < NB) {
+            int tot = 0;
+            for (int ww = 0; ww < STATS_THREADS / 32; ww++) tot += wcnt[ww][tid];
+            run[tid] += tot;
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------
+// phase B: one warp builds a subtree of <= SMALL cells in shared memory
+// ------------------------------------------------------------------------
+
+struct SubSmem {
+    double F[6][SMALL];
+    int gid[SMALL];
+    unsigned short perm[SMALL];
+    unsigned short tmp[SMALL];
+    unsigned char bkt[SMALL];
+    int stk[SMALL + 2][5];  // node, local ptr, size, dim flag, depth
+    unsigned long long K[NBMAX + 1];
+    int cnt[NBMAX];
+    int bstart[NBMAX];
+    int brun[NBMAX];
+    double bRmin[NBMAX];
+    double bLmax[NBMAX];
+};
+
+// First-occurrence min over perm[p .. p+n) of field f (min-form key: maxima
+// complemented when `is_max`); returns the exact value.  All lanes call.
+__device__ __forceinline__ double warp_range_extreme(const SubSmem& S, int f, bool is_max, int p, int n) {
+    const unsigned FULL = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    unsigned long long best = ~0ull;
+    unsigned bpos = 0;  // always a valid position, even for NaN-only ranges
+    for (int i = lane; i < n; i += 32) {
+        unsigned long long k = fkey(S.F[f][S.perm[p + i]]);
+        if (is_max) k = ~k;
+        if (k < best) {
+            best = k;
+            bpos = (unsigned)i;
+        }
+    }
+    unsigned long long ko;
+    unsigned po;
+    group_min_kp(FULL, best, bpos, &ko, &po);
+    return S.F[f][S.perm[p + (int)po]];
+}
+
+__global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long long cpl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const unsigned FULL = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    int w = threadIdx.x >> 5;
+    SubSmem& S = reinterpret_cast<SubSmem*>(smem_raw)[w];
+    int sidx = blockIdx.x * SUB_WARPS + w;
+    if (sidx >= ws.cnt->small_count) return;
+    int r = ws.small_list[sidx];
+    ARec* RR = &ws.recs[r];
+    int p0 = RR->ptr, s = RR->size, par = RR->parity, d0 = RR->dim, lvl = RR->level;
+    for (int i = lane; i < s; i += 32) {
+        for (int k = 0; k < 6; k++) S.F[k][i] = ws.f[par][k][p0 + i];
+        S.gid[i] = ws.idx[par][p0 + i];
+        S.perm[i] = (unsigned short)i;
+    }
+    LRec* L = ws.lrec + 2 * (size_t)p0;
+    if (lane == 0) {
+        LRec z;
+        z.Lmax = -1.0;
+        z.Rmin = -1.0;
+        z.child = -1;
+        z.ptr = p0;
+        z.size = s;
+        z.dim = d0;
+        L[0] = z;
+        S.stk[0][0] = 0;
+        S.stk[0][1] = 0;
+        S.stk[0][2] = s;
+        S.stk[0][3] = d0;
+        S.stk[0][4] = lvl;
+    }
+    __syncwarp();
+    int sp = 1, nloc = 1, maxd = lvl;
+    bool err = false;
+    while (sp > 0) {
+        sp--;
+        int v = S.stk[sp][0], p = S.stk[sp][1], n = S.stk[sp][2], flag = S.stk[sp][3], depth = S.stk[sp][4];
+        __syncwarp();
+        int d = flag < 0 ? flag + 2 : flag;
+        if ((long long)n <= cpl) continue;
+        // get_bounds of the node (creation.py:271-277)
+        double R = warp_range_extreme(S, 2 * d, false, p, n);
+        double Lr = warp_range_extreme(S, 2 * d + 1, true, p, n);
+        double bl = bucket_len(Lr, R, NB);
+        for (int j = lane; j <= NB; j += 32) S.K[j] = fkey(bucket_edge(j, bl, R));  // NB + 1 edges
+        if (lane < NB) {
+            S.cnt[lane] = 0;
+            S.brun[lane] = 0;
+        }
+        __syncwarp();
+        bool lbad = false;
+        for (int i = lane; i < n; i += 32) {
+            int b = find_bucket(S.K, NB, fkey(S.F[4 + d][S.perm[p + i]]));
+            if (b < 0) {
+                lbad = true;
+                b = 0;
+            }
+            S.bkt[i] = (unsigned char)b;
+            atomicAdd(&S.cnt[b], 1);
+        }
+        if (__any_sync(FULL, lbad)) {
+            err = true;
+            continue;  // upstream indexes past its buckets; keep a leaf
+        }
+        __syncwarp();
+        if (lane < 32) {
+            int c = lane < NB ? S.cnt[lane] : 0;
+            int incl = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                int t = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (lane < NB) S.bstart[lane] = incl - c;
+        }
+        __syncwarp();
+        // stable partition (stable_partition / sort_bbox_indices creation.py:54-150)
+        for (int c0 = 0; c0 < n; c0 += 32) {
+            int i = c0 + lane;
+            int b = i < n ? (int)S.bkt[i] : 255;
+            unsigned grp = __match_any_sync(FULL, b);
+            int rank = __popc(grp & lanemask_lt());
+            if (i < n) S.tmp[S.bstart[b] + S.brun[b] + rank] = S.perm[p + i];
+            __syncwarp();
+            if (i < n && (int)(__ffs(grp) - 1) == lane) S.brun[b] += __popc(grp);
+            __syncwarp();
+        }
+        for (int i = lane; i < n; i += 32) S.perm[p + i] = S.tmp[i];
+        __syncwarp();
+        // special case creation.py:311-320
+        if (cpl == 1 && n == 2) {
+            if (lane == 0) {
+                L[v].Lmax = Lr;
+                L[v].Rmin = R;
+                L[v].child = nloc;
+                LRec a;
+                a.Lmax = -1.0;
+                a.Rmin = -1.0;
+                a.child = -1;
+                a.size = 1;
+                a.dim = 1 - d;
+                a.ptr = p0 + p;
+                L[nloc] = a;
+                a.ptr = p0 + p + 1;
+                L[nloc + 1] = a;
+            }
+            nloc += 2;
+            maxd = max(maxd, depth + 1);
+            __syncwarp();
+            continue;
+        }
+        // per-bucket bounds (creation.py:300-306)
+        for (int b = 0; b < NB; b++) {
+            int c = S.cnt[b];
+            double rmin = DBL_MAX, lmax = -DBL_MAX;
+            if (c > 0) {
+                rmin = warp_range_extreme(S, 2 * d, false, p + S.bstart[b], c);
+                lmax = warp_range_extreme(S, 2 * d + 1, true, p + S.bstart[b], c);
+            }
+            if (lane == 0) {
+                S.bRmin[b] = rmin;
+                S.bLmax[b] = lmax;
+            }
+        }
+        __syncwarp();
+        Decision D = warp_decide(S.cnt, S.bRmin, S.bLmax, NB, n, R, Lr, bl);
+        if (D.kind == 0) {
+            // all cells in one bucket (creation.py:345-358)
+            if (flag >= 0) {
+                if (lane == 0) {
+                    L[v].dim = 1 - L[v].dim;
+                    S.stk[sp][0] = v;
+                    S.stk[sp][1] = p;
+                    S.stk[sp][2] = n;
+                    S.stk[sp][3] = (1 - d) - 2;
+                    S.stk[sp][4] = depth;
+                }
+                sp++;
+            } else if (lane == 0) {
+                L[v].Lmax = -1.0;
+                L[v].Rmin = -1.0;
+            }
+            __syncwarp();
+            continue;
+        }
+        if (D.kind < 0) {
+            err = true;
+            continue;
+        }
+        int nl = D.nleft;
+        if (lane == 0) {
+            L[v].Lmax = D.Lmax;
+            L[v].Rmin = D.Rmin;
+            L[v].child = nloc;
+            LRec a;
+            a.Lmax = -1.0;
+            a.Rmin = -1.0;
+            a.child = -1;
+            a.dim = 1 - d;
+            a.ptr = p0 + p;
+            a.size = nl;
+            L[nloc] = a;
+            a.ptr = p0 + p + nl;
+            a.size = n - nl;
+            L[nloc + 1] = a;
+            // push right, then left (creation.py:378-379)
+            S.stk[sp][0] = nloc + 1;
+            S.stk[sp][1] = p + nl;
+            S.stk[sp][2] = n - nl;
+            S.stk[sp][3] = 1 - d;
+            S.stk[sp][4] = depth + 1;
+            S.stk[sp + 1][0] = nloc;
+            S.stk[sp + 1][1] = p;
+            S.stk[sp + 1][2] = nl;
+            S.stk[sp + 1][3] = 1 - d;
+            S.stk[sp + 1][4] = depth + 1;
+        }
+        sp += 2;
+        nloc += 2;
+        maxd = max(maxd, depth + 1);
+        __syncwarp();
+    }
+    __syncwarp();
+    for (int i = lane; i < s; i += 32) ws.final_idx[p0 + i] = S.gid[S.perm[i]];
+    if (lane == 0) {
+        RR->splits = (nloc - 1) / 2;
+        RR->nlocal = nloc;
+        RR->err = err ? 1 : 0;
+        atomicMax(&ws.cnt->max_depth, maxd);
+        if (err) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
+    }
+}
+
+// ------------------------------------------------------------------------
+// phase C: numbering and emission
+// ------------------------------------------------------------------------
+
+__global__ void k_count_up(WS ws, int b, int e) {
+    int r = b + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= e) return;
+    ARec* R = &ws.recs[r];
+    if (R->kind == K_SPLIT) R->splits = 1 + ws.recs[R->child].splits + ws.recs[R->child + 1].splits;
+    else if (R->kind == K_LEAF) R->splits = 0;
+    // K_SUBTREE: set by k_subtree
+}
+
+__global__ void k_number_down(WS ws, int b, int e) {
+    int r = b + blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= e) return;
+    ARec* R = &ws.recs[r];
+    if (r == 0) {
+        R->S = 0;
+        R->pos = 0;
+    }
+    if (R->kind == K_SPLIT) {
+        ARec* A = &ws.recs[R->child];
+        ARec* B = &ws.recs[R->child + 1];
+        A->S = R->S + 1;
+        B->S = R->S + 1 + A->splits;
+        A->pos = 1 + 2 * R->S;
+        B->pos = 2 + 2 * R->S;
+    }
+}
+
+struct NodesOut {
+    int64_t* child;
+    double* Lmax;
+    double* Rmin;
+    int64_t* ptr;
+    int64_t* size;
+    uint8_t* dim;
+};
+
+__device__ __forceinline__ void put_node(const NodesOut& o, long long pos, long long child, double Lmax, double Rmin,
+                                         long long ptr, long long size, int dim) {
+    o.child[pos] = child;
+    o.Lmax[pos] = Lmax;
+    o.Rmin[pos] = Rmin;
+    o.ptr[pos] = ptr;
+    o.size[pos] = size;
+    o.dim[pos] = (uint8_t)(dim != 0);
+}
+
+__global__ void k_emit_phaseA(WS ws, int nrec, long long n_nodes, NodesOut o) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const ARec* R = &ws.recs[r];
+    if (R->kind != K_SPLIT && R->kind != K_LEAF) return;
+    if (R->pos < 0 || R->pos >= n_nodes) {
+        atomicOr(&ws.cnt->err, 0x40000000u);
+        return;
+    }
+    if (R->kind == K_SPLIT) put_node(o, R->pos, 1 + 2 * R->S, R->Lmax, R->Rmin, R->ptr, R->size, R->dim);
+    else put_node(o, R->pos, -1, R->Lmax, R->Rmin, R->ptr, R->size, R->dim);
+}
+
+// One warp per subtree root: local records to their final positions.
+__global__ void k_emit_subtrees(WS ws, long long n_nodes, NodesOut o) {
+    int lane = threadIdx.x & 31;
+    int sidx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (sidx >= ws.cnt->small_count) return;
+    const ARec* R = &ws.recs[ws.small_list[sidx]];
+    const LRec* L = ws.lrec + 2 * (size_t)R->ptr;
+    long long off = 2 * R->S;
+    for (int j = lane; j < R->nlocal; j += 32) {
+        LRec a = L[j];
+        long long pos = (j == 0) ? R->pos : (long long)j + off;
+        long long child = (a.child < 0) ? -1 : (long long)a.child + off;
+        if (pos < 0 || pos >= n_nodes || child >= n_nodes) {
+            atomicOr(&ws.cnt->err, 0x40000000u);
+            continue;
+        }
+        put_node(o, pos, child, a.Lmax, a.Rmin, a.ptr, a.size, a.dim);
+    }
+}
+
+__global__ void k_emit_indices(WS ws, int n, int64_t* bb_indices) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        bb_indices[i] = ws.final_idx[i];
+}
+
+}  // namespace ct
+
+using namespace ct;
+
+extern "C" {
+
+int64_t ct_pessimistic_n_nodes(int64_t n) {
+    // creation.py:216-230
+    int64_t n_nodes = n;
+    int64_t nodes = (n + 1) / 2;
+    while (nodes > 1) {
+        n_nodes += nodes;
+        nodes = (nodes + 1) / 2;
+    }
+    return n_nodes + 1;
+}
+
+size_t ct_build_workspace_size(int64_t n, int32_t NB, int32_t factor) {
+    if (NB < 2 || NB > NBMAX || n < 0 || factor < 1) return 0;
+    return carve(nullptr, n, NB, factor, nullptr);
+}
+
+int ct_build_tree(const double* bb, int64_t n, int32_t NB, int64_t cpl, int32_t factor, void* workspace,
+                  size_t ws_bytes, int64_t* n_nodes_host, int32_t* max_depth_host, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
+    if (cpl < 1) return ct_fail(CT_ERR_ARG, "cells_per_leaf must be >= 1");
+    if (n < 0 || n >= (int64_t)INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "n_elements out of range");
+    if (factor < 1) return ct_fail(CT_ERR_ARG, "capacity_factor must be >= 1");
+    size_t need = carve(nullptr, n, NB, factor, nullptr);
+    if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
+    if (n > 0 && !bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
+    WS ws;
+    carve((char*)workspace, n, NB, factor, &ws);
+    int ni = (int)n;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(SUB_WARPS * sizeof(SubSmem)));
+        attr_set = true;
+    }
+    int root_dim = 0;
+    k_reset<<<1, 1, 0, st>>>(ws, ni, 0, root_dim);
+    if (ni > 0) {
+        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        k_init_elems<<<g, 256, 0, st>>>(bb, ni, ws);
+        k_root_bounds<<<g, 256, 0, st>>>(ws, ni);
+        k_root_resolve<<<1, 1, 0, st>>>(ws, ni);
+    }
+    CT_CHECK_LAUNCH("build init");
+    std::vector<int> level_b, level_e;
+    level_b.push_back(0);
+    level_e.push_back(1);
+    int parity = 0;
+    Counters hc;
+    if (ni > SMALL) {
+        while (true) {
+            int lb = level_b.back(), le = level_e.back();
+            int width = le - lb;
+            // tiles for pending nodes of this level
+            cudaMemsetAsync(&ws.cnt->tile_count, 0, sizeof(int), st);
+            int g = std::max(1, std::min((width + 3) / 4, 4096));
+            k_make_tiles<<<g, 128, 0, st>>>(ws, NB);
+            CT_CHECK_LAUNCH("make_tiles");
+            CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+            CT_CUDA(cudaStreamSynchronize(st));
+            if (hc.err & 0x80000000u) return ct_fail(CT_ERR_WORKSPACE, "builder tile capacity exceeded");
+            int ntiles = hc.tile_count;
+            if (ntiles == 0) break;
+            k_stats<<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_decide<<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
+            k_scatter<<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            CT_CHECK_LAUNCH("phase A level");
+            CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+            CT_CUDA(cudaStreamSynchronize(st));
+            if (hc.err & 0x80000000u)
+                return ct_fail(CT_ERR_WORKSPACE, "builder node-record capacity exceeded (unbalanced tree)");
+            int nb_ = le, ne_ = hc.rec_count;
+            if (ne_ == nb_) break;
+            level_b.push_back(nb_);
+            level_e.push_back(ne_);
+            parity = 1 - parity;
+            // publish the next level range to the device
+            int range[2] = {nb_, ne_};
+            CT_CUDA(cudaMemcpyAsync(&ws.cnt->lb, range, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+            CT_CUDA(cudaStreamSynchronize(st));
+        }
+    }
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    int nsmall = hc.small_count;
+    if (nsmall > 0) {
+        int blocks = (nsmall + SUB_WARPS - 1) / SUB_WARPS;
+        k_subtree<<<blocks, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
+        CT_CHECK_LAUNCH("subtree");
+    }
+    // phase C: split counts bottom-up, pre-order ranks top-down
+    for (int L = (int)level_b.size() - 1; L >= 0; L--) {
+        int b = level_b[L], e = level_e[L];
+        k_count_up<<<(e - b + 255) / 256, 256, 0, st>>>(ws, b, e);
+    }
+    for (size_t L = 0; L < level_b.size(); L++) {
+        int b = level_b[L], e = level_e[L];
+        k_number_down<<<(e - b + 255) / 256, 256, 0, st>>>(ws, b, e);
+    }
+    CT_CHECK_LAUNCH("numbering");
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    long long root_splits = 0;
+    CT_CUDA(cudaMemcpyAsync(&root_splits, &ws.recs[0].splits, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    if (hc.err & CT_DEVERR_BUCKET)
+        return ct_fail(CT_ERR_DEVICE, "tree construction failed: a cell centroid fell outside every bucket");
+    if (n_nodes_host) *n_nodes_host = 1 + 2 * root_splits;
+    if (max_depth_host) *max_depth_host = hc.max_depth;
+    // remember the record count for ct_build_emit
+    CT_CUDA(cudaMemcpyAsync(&ws.cnt->pad, &hc.rec_count, sizeof(int), cudaMemcpyHostToDevice, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    return CT_OK;
+}
+
+int ct_build_emit(const void* workspace, int64_t n, int32_t NB, int32_t factor, int64_t* child, double* Lmax,
+                  double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim, int64_t* bb_indices, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX || factor < 1) return ct_fail(CT_ERR_ARG, "bad n_buckets / capacity_factor");
+    WS ws;
+    carve((char*)workspace, n, NB, factor, &ws);
+    Counters hc;
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    int nrec = hc.pad;
+    long long root_splits = 0;
+    CT_CUDA(cudaMemcpyAsync(&root_splits, &ws.recs[0].splits, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    long long n_nodes = 1 + 2 * root_splits;
+    NodesOut o{child, Lmax, Rmin, ptr, size, dim};
+    k_emit_phaseA<<<(nrec + 255) / 256, 256, 0, st>>>(ws, nrec, n_nodes, o);
+    if (hc.small_count > 0) k_emit_subtrees<<<(hc.small_count * 32 + 127) / 128, 128, 0, st>>>(ws, n_nodes, o);
+    if (n > 0) {
+        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        k_emit_indices<<<g, 256, 0, st>>>(ws, (int)n, bb_indices);
+    }
+    CT_CHECK_LAUNCH("emit");
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    if (hc.err & 0x40000000u) return ct_fail(CT_ERR_DEVICE, "tree emission: node position out of range");
+    return CT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+"""EdgeCellTree2d on the GPU -- drop-in for numba_celltree.EdgeCellTree2d
+(edge_celltree.py:25-146 upstream)."""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _device, _lib
+from .cast import cast_vertices, is_cuda_tensor
+from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, validate_elements
+from .constants import MIN_TOLERANCE, TOLERANCE_FACTOR
+
+
+class EdgeCellTree2d(CellTree2dBase):
+    """
+    Construct a cell tree from 2D vertices and an edges indexing array.
+
+    Parameters
+    ----------
+    vertices: ndarray of floats with shape ``(n_point, 2)``
+    edges: ndarray of integers with shape ``(n_edge, 2)``
+    n_buckets: int, optional, default: 4
+    cells_per_leaf: int, optional, default: 2
+    """
+
+    _elements_name = "edges"
+
+    def __init__(self, vertices, edges, n_buckets: int = 4, cells_per_leaf: int = 2):
+        _validate_params(n_buckets, cells_per_leaf)
+        device = _device.require_cuda()
+        torch = _device.torch()
+        vertices = cast_vertices(vertices, copy=True)
+        v_d = _device.to_device(vertices, torch.float64, device)
+        e_d = _device.to_device(edges, torch.int64, device)
+        if e_d.ndim != 2 or e_d.shape[1] != 2:
+            raise ValueError("edges must have shape (n_edge, 2)")
+        if e_d.shape[0] == 0:
+            raise ValueError("zero-size array to reduction operation minimum which has no identity")
+        validate_elements(e_d, int(v_d.shape[0]), 2, "edges")
+        lib = _lib.load()
+        st = _device.stream()
+        # global tolerance from the vertex extent (edge_celltree.py:59-62)
+        ext = (ctypes.c_double * 4)()
+        _lib.check(lib.ct_vertex_extent(_device.ptr(v_d), int(v_d.shape[0]), ext, st), "vertex_extent")
+        dx = ext[1] - ext[0]
+        dy = ext[3] - ext[2]
+        global_tolerance = max(MIN_TOLERANCE, TOLERANCE_FACTOR * max(dx, dy))
+        n = int(e_d.shape[0])
+        bb = _device.empty((n, 4), torch.float64, device)
+        _lib.check(
+            lib.ct_edge_bboxes(_device.ptr(v_d), _device.ptr(e_d), n, global_tolerance, _device.ptr(bb), st),
+            "edge_bboxes",
+        )
+        self._tree = _GpuTree(device, e_d, v_d, bb, n_buckets, cells_per_leaf)
+        self._host = {}
+        self._edges_in = edges
+        self.n_buckets = n_buckets
+        self.cells_per_leaf = cells_per_leaf
+
+    @property
+    def edges(self):
+        return self._edges_in
+
+    def locate_points(self, points, tolerance: Optional[float] = None):
+        """Index of an edge each point lies on, -1 if none (query.py:167-174)."""
+        tol = self._tolerance(tolerance)
+        cuda_in = is_cuda_tensor(points)
+        points = cast_vertices(points)
+        t = self._tree
+        torch = _device.torch()
+        p_d = _device.to_device(points, torch.float64, t.device)
+        n = int(p_d.shape[0])
+        out = _device.empty((n,), torch.int64, t.device)
+        t.reset_error()
+        _lib.check(
+            _lib.load().ct_locate_points_on_edge(
+                ctypes.byref(t.desc), _device.ptr(p_d), n, tol, _device.ptr(out), _device.stream()
+            ),
+            "locate_points",
+        )
+        t.raise_on_device_error()
+        return out if cuda_in else out.cpu().numpy()

@@ -1,0 +1,114 @@
+"""locate_points on the GPU (float32 and float64 forms) against the oracle
+and the upstream fixtures: identical cell indices."""
+
+import numpy as np
+import pytest
+
+from meshes import GOLDEN, meshes
+from numba_celltree_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+
+def _points(xy, f, n, seed):
+    lo, hi = xy.min(0), xy.max(0)
+    span = float((hi - lo).max())
+    pts = [
+        syn.uniform_points(n, lo, hi, seed=seed, margin=0.05),
+        xy[np.random.default_rng(seed).integers(0, len(xy), n // 10)],
+        syn.near_edge_points(xy, f[:, :3], n // 4, dist=1e-9 * span, seed=seed + 1),
+        syn.near_edge_points(xy, f[:, :3], n // 4, dist=1e-6 * span, seed=seed + 2),
+        syn.near_edge_points(xy, f[:, :3], n // 8, dist=0.0, seed=seed + 3),
+    ]
+    return np.concatenate(pts)
+
+
+@pytest.mark.parametrize("name", list(meshes().keys()))
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_locate_matches_oracle(oracle, name, precision):
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = meshes()[name]
+    g = CellTree2d(xy, f, -1)
+    g.precision = precision
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = _points(xy, f, 20000, seed=hash(name) % 1000)
+    assert np.array_equal(g.locate_points(pts), o.locate_points(pts))
+    span = float((xy.max(0) - xy.min(0)).max())
+    for tol in (1e-9 * span, 1e-4 * span, 0.0):
+        assert np.array_equal(g.locate_points(pts, tol), o.locate_points(pts, tol))
+
+
+def test_locate_matches_upstream_fixtures():
+    from numba_celltree_gb300 import CellTree2d
+
+    G = np.load(GOLDEN / "golden_trees.npz")
+    for i in range(int(G["n_cases"])):
+        p = f"c{i}_"
+        nb, cpl = (int(x) for x in G[p + "params"])
+        g = CellTree2d(G[p + "vertices"], G[p + "faces_in"], -1, nb, cpl)
+        span = float((G[p + "vertices"].max(0) - G[p + "vertices"].min(0)).max())
+        for prec in ("fp32", "fp64"):
+            g.precision = prec
+            assert np.array_equal(g.locate_points(G[p + "points"]), G[p + "locate"]), (i, prec)
+            assert np.array_equal(g.locate_points(G[p + "points"], 1e-3 * span), G[p + "locate_tol"]), (i, prec)
+
+
+def test_locate_utm_precision_stress(oracle):
+    """UTM-like offsets (5e5, 4.2e6), 1 m cells, points within 1e-9 m of edges."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(300, seed=21, extent=(300.0, 300.0), offset=(5.0e5, 4.2e6))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    rng = np.random.default_rng(5)
+    pts = np.concatenate([
+        syn.uniform_points(200000, xy.min(0), xy.max(0), seed=3),
+        syn.near_edge_points(xy, f, 50000, dist=1e-9, seed=4),
+        syn.near_edge_points(xy, f, 20000, dist=0.0, seed=6),
+        xy[rng.integers(0, len(xy), 5000)],
+    ])
+    ref = o.locate_points(pts)
+    for prec in ("fp32", "fp64"):
+        g.precision = prec
+        assert np.array_equal(g.locate_points(pts), ref)
+
+
+def test_locate_device_tensors(oracle):
+    import torch
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(50, seed=2)
+    g = CellTree2d(torch.as_tensor(xy, device="cuda"), torch.as_tensor(f, device="cuda"), -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = syn.uniform_points(5000, (0, 0), (1, 1), seed=1, margin=0.1)
+    out = g.locate_points(torch.as_tensor(pts, device="cuda"))
+    assert out.is_cuda and out.dtype == torch.int64
+    assert np.array_equal(out.cpu().numpy(), o.locate_points(pts))
+
+
+def test_locate_known_answers():
+    """test_celltree.py:167-330 through the GPU classes."""
+    from numba_celltree_gb300 import CellTree2d
+
+    nodes2 = np.array([[0.0, 0.0], [2.0, 0.0], [1.0, 2.0], [3.0, 2.0]])
+    faces2 = np.array([[0, 1, 2], [1, 3, 2]], dtype=np.intc)
+    t = CellTree2d(nodes2, faces2, -1)
+    for prec in ("fp32", "fp64"):
+        t.precision = prec
+        assert np.array_equal(t.locate_points(np.array([[1.0, 1.0], [2.0, 1.0], [-1.0, 1.0]])), [0, 1, -1])
+        pts = np.array([[-0.09, 0.0], [2.0, 1.0], [-1.0, 1.0]])
+        assert np.array_equal(t.locate_points(pts, tolerance=1e-9), [-1, 1, -1])
+        assert np.array_equal(t.locate_points(pts, tolerance=1e-1), [0, 1, -1])
+    nodes = np.array([[0.0, 0.0], [0.0, 2.0], [2.0, 0.0], [2.0, 2.0], [4.0, 0.0], [4.0, 2.0], [6.0, 0.0],
+                      [6.0, 2.0], [0.0, 4.0], [2.0, 4.0], [4.0, 4.0], [6.0, 4.0]])
+    faces = np.array([[0, 8, 9, 5, 2], [9, 11, 7, 5, -1], [4, 7, 6, -1, -1]], dtype=np.intc)
+    t = CellTree2d(nodes, faces, -1, n_buckets=2, cells_per_leaf=1)
+    pts = np.array([[-9e-9, 0.0], [2.0, -9e-9], [-9e-9, 1.0], [1.0, -9e-9], [-1.1e-8, 1.0], [1.0, -1.1e-8],
+                    [-1.1e-8, 0.0], [2.0, -1.5e-8]])
+    for prec in ("fp32", "fp64"):
+        t.precision = prec
+        assert np.array_equal(t.locate_points(np.array([[1.0, 1.0], [5.0, 0.5], [5.0, 3.0], [-1.0, 1.0]])),
+                              [0, 2, 1, -1])
+        assert np.array_equal(t.locate_points(pts), [-1] * 8)
+        assert np.array_equal(t.locate_points(pts, tolerance=1e-8), [0, 0, 0, 0, -1, -1, -1, -1])
