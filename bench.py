@@ -1,0 +1,410 @@
+"""Benchmark: locate_points Mpoints/s and tree build ms on a 16M-cell mesh.
+
+Workload (defaults): a 4000 x 2000 jittered quad grid with 1 m cells offset
+by (5.0e5, 4.2e6) m, every quad split into two triangles (16,000,000 cells,
+float64); 256M query points, 99% uniform in the mesh bounding box and 1%
+within 1e-9 m of shared edges and vertices.  A step is one locate_points pass
+over all points with points and tree resident in HBM (4 GB of points, larger
+than L2, so no flush is needed).
+
+`value` is the float32-traversal form (exact float64 fallback; identical
+indices to the float64 form, checked every run); the plain float64 form, the
+build time and the end-to-end call through the public API with host numpy
+arrays are reported beside it.  `--impl reference` times the CPU restatement
+of the upstream algorithm (oracle/) on all host cores instead.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpoints/s locate_points + build ms, 16M cells, 1 GB300: FP32/batched vs plain FP64"
+UNIT = "Mpoints/s"
+BYTES_PER_POINT = 24  # 16 B xy in + 8 B index out
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=4000)
+    ap.add_argument("--ny", type=int, default=2000)
+    ap.add_argument("--points", type=int, default=256 * 1024 * 1024)
+    ap.add_argument("--cpu-sample", type=int, default=4 * 1024 * 1024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="small fixed run for ncu captures")
+    return ap.parse_args()
+
+
+def workload(args, seed=0):
+    from numba_celltree_gb300 import synthetic as syn
+
+    xy, faces = syn.triangle_mesh(args.nx, args.ny, seed=seed, extent=(float(args.nx), float(args.ny)),
+                                  offset=(5.0e5, 4.2e6))
+    return xy, faces
+
+
+def make_points(xy, faces, n, seed=1):
+    from numba_celltree_gb300 import synthetic as syn
+
+    lo, hi = xy.min(0), xy.max(0)
+    pts = np.empty((n, 2), dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    chunk = 1 << 24
+    for s in range(0, n, chunk):
+        e = min(s + chunk, n)
+        pts[s:e] = rng.uniform(lo, hi, size=(e - s, 2))
+    # every 100th point lies within 1e-9 m of an edge or vertex
+    near = pts[::100]
+    near[:] = syn.near_edge_points(xy, faces, len(near), dist=1e-9, seed=seed + 1)
+    return pts
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_point():
+    """DRAM bytes per point of the float32 locate kernel from the committed ncu
+    summary (a smaller capture, scaled per point), or None."""
+    f = ROOT / "profiles" / "locate_points_fp32.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_point:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """CPU restatement (oracle/) of the upstream algorithm on all host cores."""
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    os.environ.setdefault("OMP_NUM_THREADS", str(cpu_threads()))
+    from oracle import oracle as O
+
+    O.build()
+    xy, faces = workload(args)
+    t0 = time.perf_counter()
+    tree = O.OracleCellTree2d(xy, faces, -1)
+    build_s = time.perf_counter() - t0
+    n = min(args.cpu_sample, args.points)
+    pts = make_points(xy, faces, n, seed=1)
+    tol = O.default_tolerance(tree.bb_distances[:, 2])
+    for _ in range(args.warmup):
+        tree.locate_points(pts[: max(1, n // 8)], tol)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tree.locate_points(pts, tol)
+        times.append(time.perf_counter() - t0)
+    step = max(times)
+    value = n / step / 1e6
+    out = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(1e3 * step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{2 * args.nx * args.ny} jittered triangles, 1 m cells at (5.0e5, 4.2e6); "
+                               f"locate_points sample of {n} points per step", "cells": 2 * args.nx * args.ny,
+                   "points_per_step": n},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                         "sample": f"{n} of the {args.points} points per step, full tree; build {build_s:.2f} s"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cpu_build_s": round(build_s, 3),
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.profile:
+        args.nx, args.ny, args.points, args.steps, args.warmup = 1000, 500, 16 * 1024 * 1024, 2, 1
+        args.no_e2e = True
+        args.no_cpu = True
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_setup()
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    xy, faces = workload(args)
+    n_cells = faces.shape[0]
+    xy_d = torch.as_tensor(xy, device=dev)
+    f_d = torch.as_tensor(faces, device=dev)
+    torch.cuda.synchronize()
+
+    # ---- build (ccw, bboxes, build, emit, pack) from device arrays
+    build_ms = []
+    tree = None
+    for i in range(3 if not args.profile else 1):
+        del tree
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tree = CellTree2d(xy_d, f_d, -1)
+        e1.record()
+        torch.cuda.synchronize()
+        build_ms.append(e0.elapsed_time(e1))
+    build_ms_val = min(build_ms[1:]) if len(build_ms) > 1 else build_ms[0]
+    tol = tree.default_tolerance()
+
+    # ---- points resident in HBM
+    n = args.points
+    pts_h = make_points(xy, faces, n, seed=1 + rank)
+    pts_d = torch.as_tensor(pts_h, device=dev)
+    out32 = torch.empty(n, dtype=torch.int64, device=dev)
+    out64 = torch.empty(n, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
+
+    def timed(precision, steps, warmup, out):
+        for _ in range(warmup):
+            tree.launch_locate(pts_d, out, tol, precision)
+        torch.cuda.synchronize()
+        barrier(ws)
+        torch.cuda.synchronize()
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            tree.launch_locate(pts_d, out, tol, precision)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier(ws)
+        return e0.elapsed_time(e1) / steps
+
+    with ClockSampler(local) as clk:
+        ms32 = timed("fp32", args.steps, args.warmup, out32)
+    clocks = clk.summary()
+    ms64 = timed("fp64", max(1, min(args.steps, 3)), 1, out64)
+    ms32 = max_over_ranks(ws, ms32)
+    ms64 = max_over_ranks(ws, ms64)
+    tree._tree.reset_error()
+    tree.launch_locate(pts_d, out32, tol, "fp32")
+    tree.launch_locate(pts_d, out64, tol, "fp64")
+    torch.cuda.synchronize()
+    tree._tree.raise_on_device_error()
+    identical = bool(torch.equal(out32, out64))
+    found = int((out32 >= 0).sum().item())
+
+    value = ws * n / (ms32 * 1e-3) / 1e6
+    value64 = ws * n / (ms64 * 1e-3) / 1e6
+
+    # ---- end to end through the public API with host numpy arrays
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = max(1, min(args.steps, 3))
+        tree.locate_points(pts_h[: 1 << 20], tol)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            res = tree.locate_points(pts_h, tol)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / e2e_steps)
+        assert np.array_equal(res[:1000], out32[:1000].cpu().numpy())
+        e2e = {"value": round(ws * n / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(pts_h.nbytes),
+               "d2h_bytes_per_step": int(n * 8)}
+
+    # ---- CPU baseline: the oracle on a bounded sample of the same workload
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        from oracle import oracle as O
+
+        O.build()
+        h = tree
+        arrs = O._TreeArrays(h.faces, h.vertices, h.nodes, h.bb_indices, h.bb_coords, h.bbox)
+        m = min(args.cpu_sample, n)
+        sample = np.ascontiguousarray(pts_h[:m])
+        outc = np.empty(m, dtype=np.int64)
+        import ctypes
+
+        lib = O.lib()
+        lib.cto_locate_points(ctypes.byref(arrs.desc), sample.ctypes.data, m, float(tol), outc.ctypes.data)
+        t0 = time.perf_counter()
+        lib.cto_locate_points(ctypes.byref(arrs.desc), sample.ctypes.data, m, float(tol), outc.ctypes.data)
+        cpu_s = time.perf_counter() - t0
+        assert np.array_equal(outc, out32[:m].cpu().numpy()), "GPU result differs from the oracle"
+        cpu = {"value": round(m / cpu_s / 1e6, 3), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+               "sample": f"first {m} of the {n} points on the same tree (oracle = C restatement, OpenMP)"}
+
+    peak, peak_kind = peaks()
+    achieved = BYTES_PER_POINT * n / (ms32 * 1e-3) / 1e9
+    tpp = traffic_per_point()
+    roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+            "traffic": (round(tpp * n) if tpp is not None else None),
+            "kernel": "k_locate_points<FP32> (one launch per step)"}
+    result = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": UNIT,
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms32, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": f"{n_cells} jittered triangles (1 m cells, offset 5.0e5/4.2e6 m), {n} points "
+                        f"(1% within 1e-9 m of edges/vertices)",
+            "cells": n_cells, "points_per_step": n, "n_buckets": 4, "cells_per_leaf": 2,
+            "l2": "inputs (4 GB) larger than L2, no flush",
+            "precision": "fp32 traversal + fp32 leaf filter, exact fp64 fallback",
+        },
+        "build_ms": round(build_ms_val, 3),
+        "fp64_plain": {"value": round(value64, 3), "unit": UNIT, "ms_per_step": round(ms64, 3)},
+        "fp32_vs_fp64": round(value / value64, 3),
+        "indices_identical_fp32_fp64": identical,
+        "points_found": found,
+        "gpu_launches": args.steps,
+        "clocks": clocks,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+    }
+    if rank == 0:
+        print(json.dumps(result))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -75,6 +75,22 @@ class CellTree2d(CellTree2dBase):
     def faces(self) -> np.ndarray:
         return self._cached("faces", lambda: self._tree.elements.cpu().numpy())
 
+    def default_tolerance(self) -> float:
+        return self._tolerance(None)
+
+    def launch_locate(self, points_dev, out_dev, tolerance: float, precision: str = "fp32") -> None:
+        """Enqueue locate_points on the current stream for device-resident
+        float64 points (n, 2) and an int64 output (n,); no synchronisation and
+        no error-word check (for pipelines and timing loops)."""
+        mode = _lib.CT_MODE_FP64 if precision == "fp64" else _lib.CT_MODE_FP32
+        _lib.check(
+            _lib.load().ct_locate_points(
+                ctypes.byref(self._tree.desc), _device.ptr(points_dev), int(points_dev.shape[0]), float(tolerance),
+                mode, _device.ptr(out_dev), _device.stream(),
+            ),
+            "locate_points",
+        )
+
     def locate_points(self, points, tolerance: Optional[float] = None):
         """
         Find the index of a face that contains a point (query.py:110-117).
