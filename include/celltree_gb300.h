@@ -140,6 +140,25 @@ int ct_build_emit(const void* workspace, int64_t n_elements, int32_t n_buckets, 
                   int64_t* child, double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
                   int64_t* bb_indices, void* stream);
 
+/* Allocation-free variant of ct_build_tree + ct_build_emit, for callers that
+ * cannot allocate device memory (code inside a runtime that owns the device
+ * memory, plugins that may not call cudaMalloc).  No counterpart in the
+ * upstream package.  Its scratch is a fixed 8 MiB device array inside the
+ * library, so n_elements must be <= 16384 (larger inputs return CT_ERR_ARG);
+ * every GPU that loads the library holds the array until the process exits.
+ * The outputs are the caller's: node arrays of node_capacity >=
+ * ct_pessimistic_n_nodes(n_elements) entries and bb_indices of n_elements.
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU (other streams, other host threads) race.
+ * Extremely unbalanced trees that exceed the builder's record capacity return
+ * CT_ERR_WORKSPACE; use ct_build_tree with a larger capacity_factor.
+ * Synchronises the stream. */
+int ct_build_tree_noalloc(const double* bb_coords, int64_t n_elements, int32_t n_buckets, int64_t cells_per_leaf,
+                          int64_t* child, double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
+                          int64_t node_capacity, int64_t* bb_indices, int64_t* n_nodes_host, int32_t* max_depth_host,
+                          void* stream);
+
 /* Fills the packed traversal arrays of `tree` (nodes_f32, nodes_f64,
  * poly_f64, poly_f32, poly_len, poly_len32) and its origin / vmax / abs_eps.
  * `tree` is updated in place (host struct).  Synchronises the stream. */

@@ -86,6 +86,10 @@ SIGNATURES = {
         [_P, _I64, _I32, _I64, _I32, _P, _SZ, ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P],
     ),
     "ct_build_emit": (ctypes.c_int, [_P, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ct_build_tree_noalloc": (
+        ctypes.c_int,
+        [_P, _I64, _I32, _I64, _P, _P, _P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P],
+    ),
     "ct_pack_tree": (ctypes.c_int, [ctypes.POINTER(CtTree), _P]),
     "ct_locate_points": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P]),
     "ct_locate_points_on_edge": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _P, _P]),

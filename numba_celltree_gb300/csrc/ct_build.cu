@@ -30,6 +30,7 @@
 #include <cfloat>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "ct_common.cuh"
@@ -1201,3 +1202,74 @@ int ct_build_emit(const void* workspace, int64_t n, int32_t NB, int32_t factor, 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Allocation-free build
+//
+// Some callers cannot call cudaMalloc: code running inside another runtime
+// that owns all device memory (a host application with its own pool, a
+// plugin that may not touch the allocator), or code on a path where an
+// allocation could block or fail.  ct_build_tree_noalloc builds a tree for
+// them with its scratch in the fixed device array below instead of a caller
+// workspace.  The array is 8 MiB, enough for 16384 cells with any n_buckets
+// <= 32; every GPU that loads the library holds it until the process exits.
+// Host code only sees a stand-in for the array's name, so the device address
+// is looked up once per device (with that device current) and cached.
+// ------------------------------------------------------------------------
+
+namespace ct {
+
+constexpr int64_t NOALLOC_MAX_CELLS = 16384;
+constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(8) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[256] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device.
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    CT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return ct_fail(CT_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return ct_fail(CT_ERR_CUDA, cudaGetErrorString(e));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return CT_OK;
+}
+
+}  // namespace ct
+
+extern "C" int ct_build_tree_noalloc(const double* bb, int64_t n, int32_t NB, int64_t cpl, int64_t* child,
+                                     double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
+                                     int64_t node_capacity, int64_t* bb_indices, int64_t* n_nodes_host,
+                                     int32_t* max_depth_host, void* stream) {
+    if (n < 0 || n > NOALLOC_MAX_CELLS)
+        return ct_fail(CT_ERR_ARG, "ct_build_tree_noalloc: n_elements must be in [0, 16384] (8 MiB static scratch)");
+    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
+    size_t need = carve(nullptr, n, NB, 1, nullptr);
+    if (need > NOALLOC_SCRATCH_BYTES) return ct_fail(CT_ERR_ARG, "ct_build_tree_noalloc: static scratch too small");
+    void* scratch = nullptr;
+    int s = noalloc_scratch(&scratch);
+    if (s != CT_OK) return s;
+    // The array keeps the previous call's contents: start from zeroed counters.
+    WS ws;
+    carve((char*)scratch, n, NB, 1, &ws);
+    CT_CUDA(cudaMemsetAsync(ws.cnt, 0, sizeof(Counters), (cudaStream_t)stream));
+    int64_t nn = 0;
+    int32_t md = 0;
+    s = ct_build_tree(bb, n, NB, cpl, 1, scratch, NOALLOC_SCRATCH_BYTES, &nn, &md, stream);
+    if (s != CT_OK) return s;
+    if (nn > node_capacity)
+        return ct_fail(CT_ERR_ARG, "node_capacity too small: pass ct_pessimistic_n_nodes(n_elements)");
+    s = ct_build_emit(scratch, n, NB, 1, child, Lmax, Rmin, ptr, size, dim, bb_indices, stream);
+    if (s != CT_OK) return s;
+    if (n_nodes_host) *n_nodes_host = nn;
+    if (max_depth_host) *max_depth_host = md;
+    return CT_OK;
+}
