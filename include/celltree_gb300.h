@@ -179,6 +179,88 @@ int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, doubl
 int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,
                              int64_t* out, void* stream);
 
+/* ---------------------------------------------------------------------- */
+/* Multi-result queries: count -> exclusive scan -> write                  */
+/* (the upstream chunked grow-and-retry, query.py:46-59, 247-289, 458-533) */
+/* ---------------------------------------------------------------------- */
+
+/* Workspace bytes / exclusive scan of n int64 values; *total_host receives
+ * the sum (synchronises the stream when total_host is not NULL). */
+size_t ct_scan_workspace_size(int64_t n);
+int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* workspace, size_t workspace_bytes,
+                      int64_t* total_host, void* stream);
+
+/* locate_box query.py:177-244: per box (xmin, xmax, ymin, ymax) the number of
+ * cells whose bbox overlaps it (strict, boxes_intersect geometry_utils.py:292-300). */
+int ct_count_boxes(const ct_tree* tree, const double* boxes, int64_t n, int64_t* counts, void* stream);
+/* Writes (box index, cell index) pairs at the scanned offsets, box-major and
+ * in traversal order -- upstream's locate_boxes output order. */
+int ct_write_boxes(const ct_tree* tree, const double* boxes, int64_t n, const int64_t* offsets, int64_t* ii,
+                   int64_t* jj, void* stream);
+
+/* locate_edge query.py:357-455 over segments (n x 2 x 2).  mode 1: edge vs
+ * face (Cohen-Sutherland + Cyrus-Beck, compute_edge_face_intersect
+ * query.py:309-328); mode 0: edge vs edge (lines_intersect,
+ * compute_edge_edge_intersect query.py:292-306, edge trees only). */
+int ct_count_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, int64_t* counts, void* stream);
+/* Writes (segment, cell) pairs and the clipped segment / point (xy: R x 2 x 2). */
+int ct_write_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int64_t* offsets,
+                   int64_t* ii, int64_t* jj, double* xy, void* stream);
+
+/* sort_intersections_by_edge geometry_utils.py:564-574: stable sort of each
+ * segment's results by t = (c - a) . (b - a), NaN last; writes the permuted
+ * jj / xy (ii is unchanged: results are already grouped by segment). */
+size_t ct_sort_workspace_size(int64_t total);
+int ct_sort_intersections(const double* segs, int64_t n_segs, const int64_t* offsets, const int64_t* counts,
+                          const int64_t* ii, const int64_t* jj_in, const double* xy_in, int64_t total,
+                          int64_t* jj_out, double* xy_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Per-pair kernels                                                        */
+/* ---------------------------------------------------------------------- */
+
+/* polygons_intersect algorithms/separating_axis.py:58-75 (out: 1 = overlap or touch). */
+int ct_polygons_intersect(const double* vertices_a, const int64_t* faces_a, int32_t n_max_vert_a,
+                          const double* vertices_b, const int64_t* faces_b, int32_t n_max_vert_b,
+                          const int64_t* indices_a, const int64_t* indices_b, int64_t n, uint8_t* out, void* stream);
+
+/* area_of_intersection algorithms/sutherland_hodgman.py:151-168 (subject: face a, clipper: face b). */
+int ct_area_of_intersection(const double* vertices_a, const int64_t* faces_a, int32_t n_max_vert_a,
+                            const double* vertices_b, const int64_t* faces_b, int32_t n_max_vert_b,
+                            const int64_t* indices_a, const int64_t* indices_b, int64_t n, double* out,
+                            unsigned int* error_word, void* stream);
+
+/* box_area_of_intersection algorithms/sutherland_hodgman.py:171-187 (subject: the box). */
+int ct_box_area_of_intersection(const double* boxes, const double* vertices, const int64_t* faces,
+                                int32_t n_max_vert, const int64_t* indices_box, const int64_t* indices_face,
+                                int64_t n, double* out, unsigned int* error_word, void* stream);
+
+/* Keeps the pairs with area > 0 (area != NULL) or flag != 0 (celltree.py:183,
+ * 226, 268); outputs have capacity n; *total_host = kept count (synchronises). */
+size_t ct_compact_workspace_size(int64_t n);
+int ct_compact_pairs(const double* area, const uint8_t* flag, int64_t n, const int64_t* ii, const int64_t* jj,
+                     int64_t* ii_out, int64_t* jj_out, double* area_out, void* workspace, size_t workspace_bytes,
+                     int64_t* total_host, void* stream);
+
+/* compute_barycentric_weights celltree.py:306-351: triangle weights
+ * (barycentric_triangle.py:46-64) when n_max_vert <= 3, else Wachspress
+ * (barycentric_wachspress.py:88-107); rows of points not found are zero.
+ * weights: n x max(3, n_max_vert). */
+int ct_barycentric_weights(const ct_tree* tree, const double* points, const int64_t* face_indices, int64_t n,
+                           double tolerance, double* weights, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Node-bound diagnostics                                                  */
+/* ---------------------------------------------------------------------- */
+
+/* collect_node_bounds query.py:568-622 (out: n_nodes x 4; parent_ws: n_nodes int64). */
+int ct_node_bounds(const int64_t* child, const double* Lmax, const double* Rmin, const uint8_t* dim, int64_t n_nodes,
+                   const double* bbox_host4, int64_t* parent_ws, double* out, void* stream);
+/* validate_node_bounds query.py:625-663 (valid: n_nodes). */
+int ct_validate_node_bounds(const int64_t* child, const int64_t* ptr, const int64_t* size, int64_t n_nodes,
+                            const int64_t* bb_indices, const double* bb_coords, const double* node_bounds,
+                            uint8_t* valid, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -93,6 +93,22 @@ SIGNATURES = {
     "ct_pack_tree": (ctypes.c_int, [ctypes.POINTER(CtTree), _P]),
     "ct_locate_points": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P]),
     "ct_locate_points_on_edge": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _P, _P]),
+    "ct_scan_workspace_size": (_SZ, [_I64]),
+    "ct_exclusive_scan": (ctypes.c_int, [_P, _I64, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
+    "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P]),
+    "ct_write_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P]),
+    "ct_count_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P]),
+    "ct_write_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_sort_workspace_size": (_SZ, [_I64]),
+    "ct_sort_intersections": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
+    "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),
+    "ct_area_of_intersection": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "ct_box_area_of_intersection": (ctypes.c_int, [_P, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "ct_compact_workspace_size": (_SZ, [_I64]),
+    "ct_compact_pairs": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
+    "ct_barycentric_weights": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _P, _I64, _D, _P, _P]),
+    "ct_node_bounds": (ctypes.c_int, [_P, _P, _P, _P, _I64, ctypes.POINTER(_D), _P, _P, _P]),
+    "ct_validate_node_bounds": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

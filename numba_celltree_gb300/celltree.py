@@ -9,7 +9,7 @@ from typing import Optional, Tuple
 import numpy as np
 
 from . import _device, _lib
-from .cast import cast_faces, cast_vertices, is_cuda_tensor
+from .cast import cast_bboxes, cast_edges, cast_faces, cast_vertices, is_cuda_tensor
 from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, validate_elements
 
 
@@ -117,3 +117,175 @@ class CellTree2d(CellTree2dBase):
         )
         t.raise_on_device_error()
         return _as_output(out, cuda_in)
+
+    # -- box queries -----------------------------------------------------------
+    def locate_boxes(self, bbox_coords):
+        """
+        Find the index of a face intersecting with a bounding box
+        (celltree.py:130-148, query.py:177-289).
+
+        Returns ``(bbox_indices, tree_face_indices)``, box-major, in the
+        upstream order.
+        """
+        cuda_in = is_cuda_tensor(bbox_coords)
+        b = cast_bboxes(bbox_coords)
+        t = self._tree
+        b_d = _device.to_device(b, _device.torch().float64, t.device)
+        ii, jj = t.locate_boxes(b_d)
+        return _as_output(ii, cuda_in), _as_output(jj, cuda_in)
+
+    def intersect_boxes(self, bbox_coords):
+        """
+        Boxes, intersecting faces and the area of intersection
+        (celltree.py:150-184); only pairs with area > 0 are kept.
+        """
+        cuda_in = is_cuda_tensor(bbox_coords)
+        b = cast_bboxes(bbox_coords)
+        t = self._tree
+        torch = _device.torch()
+        b_d = _device.to_device(b, torch.float64, t.device)
+        ii, jj = t.locate_boxes(b_d)
+        n = int(ii.shape[0])
+        area = _device.empty((n,), torch.float64, t.device)
+        t.reset_error()
+        _lib.check(
+            _lib.load().ct_box_area_of_intersection(
+                _device.ptr(b_d), _device.ptr(t.vertices), _device.ptr(t.elements), t.K, _device.ptr(ii),
+                _device.ptr(jj), n, _device.ptr(area), _device.ptr(t.error_word), _device.stream(),
+            ),
+            "intersect_boxes",
+        )
+        t.raise_on_device_error()
+        i, j, a = t.compact(ii, jj, area=area)
+        return _as_output(i, cuda_in), _as_output(j, cuda_in), _as_output(a, cuda_in)
+
+    # -- face queries ----------------------------------------------------------
+    def _faces_on_device(self, vertices, faces):
+        torch = _device.torch()
+        t = self._tree
+        v_d = _device.to_device(vertices, torch.float64, t.device)
+        f_d = _device.to_device(faces, torch.int64, t.device)
+        if v_d.ndim != 2 or v_d.shape[1] != 2:
+            raise ValueError("vertices must have shape (n_points, 2)")
+        if f_d.ndim != 2:
+            raise ValueError("faces must have shape (n_face, n_max_vert)")
+        if f_d is faces:
+            f_d = f_d.clone()
+        if f_d.shape[0] > 0:
+            if f_d.shape[1] < 3:
+                raise ValueError("faces must have at least 3 columns")
+            validate_elements(f_d, int(v_d.shape[0]), 3, "faces")
+        return v_d, f_d
+
+    def _locate_faces_dev(self, v_d, f_d):
+        torch = _device.torch()
+        t = self._tree
+        lib = _lib.load()
+        st = _device.stream()
+        n, K = int(f_d.shape[0]), int(f_d.shape[1])
+        # counter_clockwise + build_face_bboxes of the query faces (celltree.py:212-213)
+        _lib.check(lib.ct_counter_clockwise(_device.ptr(v_d), _device.ptr(f_d), n, K, st), "counter_clockwise")
+        bb = _device.empty((n, 4), torch.float64, t.device)
+        _lib.check(lib.ct_face_bboxes(_device.ptr(v_d), _device.ptr(f_d), n, K, _device.ptr(bb), st), "face_bboxes")
+        si, sj = t.locate_boxes(bb)
+        m = int(si.shape[0])
+        flag = _device.empty((m,), torch.uint8, t.device)
+        _lib.check(
+            lib.ct_polygons_intersect(
+                _device.ptr(v_d), _device.ptr(f_d), K, _device.ptr(t.vertices), _device.ptr(t.elements), t.K,
+                _device.ptr(si), _device.ptr(sj), m, _device.ptr(flag), st,
+            ),
+            "polygons_intersect",
+        )
+        return t.compact(si, sj, flag=flag)
+
+    def locate_faces(self, vertices, faces):
+        """
+        Find the index of a face intersecting with another face
+        (celltree.py:186-226).  Like upstream, a numpy ``faces`` argument is
+        reoriented counter-clockwise in place.
+        """
+        cuda_in = is_cuda_tensor(faces)
+        v_d, f_d = self._faces_on_device(vertices, faces)
+        if f_d.shape[0] == 0:
+            e = _device.empty((0,), _device.torch().int64, self._tree.device)
+            return _as_output(e, cuda_in), _as_output(e, cuda_in)
+        i, j = self._locate_faces_dev(v_d, f_d)
+        if isinstance(faces, np.ndarray):
+            faces[...] = f_d.cpu().numpy().astype(faces.dtype, copy=False)
+        elif cuda_in:
+            faces.copy_(f_d.to(faces.dtype))
+        return _as_output(i, cuda_in), _as_output(j, cuda_in)
+
+    def intersect_faces(self, vertices, faces, fill_value: int):
+        """
+        Faces of another mesh, intersecting tree faces and the area of
+        intersection (celltree.py:228-269); only pairs with area > 0 are kept.
+        """
+        cuda_in = is_cuda_tensor(faces)
+        vertices = cast_vertices(vertices)
+        faces = cast_faces(faces, fill_value)
+        v_d, f_d = self._faces_on_device(vertices, faces)
+        t = self._tree
+        torch = _device.torch()
+        if f_d.shape[0] == 0:
+            e = _device.empty((0,), torch.int64, t.device)
+            return _as_output(e, cuda_in), _as_output(e, cuda_in), _as_output(e.double(), cuda_in)
+        i, j = self._locate_faces_dev(v_d, f_d)
+        n = int(i.shape[0])
+        area = _device.empty((n,), torch.float64, t.device)
+        t.reset_error()
+        _lib.check(
+            _lib.load().ct_area_of_intersection(
+                _device.ptr(v_d), _device.ptr(f_d), int(f_d.shape[1]), _device.ptr(t.vertices),
+                _device.ptr(t.elements), t.K, _device.ptr(i), _device.ptr(j), n, _device.ptr(area),
+                _device.ptr(t.error_word), _device.stream(),
+            ),
+            "area_of_intersection",
+        )
+        t.raise_on_device_error()
+        i2, j2, a2 = t.compact(i, j, area=area)
+        return _as_output(i2, cuda_in), _as_output(j2, cuda_in), _as_output(a2, cuda_in)
+
+    # -- segments --------------------------------------------------------------
+    def intersect_edges(self, edge_coords):
+        """
+        Find the faces intersected by each edge and the clipped edge
+        (celltree.py:271-304); results of each edge are ordered by distance
+        along it.  Returns ``(edge_indices, tree_face_indices, xy)`` with xy of
+        shape ``(n_found, 2, 2)``.
+        """
+        cuda_in = is_cuda_tensor(edge_coords)
+        e = cast_edges(edge_coords)
+        t = self._tree
+        e_d = _device.to_device(e, _device.torch().float64, t.device)
+        ii, jj, xy = t.locate_edges(e_d, 1)
+        return _as_output(ii, cuda_in), _as_output(jj, cuda_in), _as_output(xy, cuda_in)
+
+    # -- barycentric -----------------------------------------------------------
+    def compute_barycentric_weights(self, points, tolerance: Optional[float] = None):
+        """
+        Locate points and compute barycentric weights of their face's vertices
+        (celltree.py:306-351): triangle weights when faces have at most 3
+        vertices, else Wachspress weights.  Rows of points not found are zero.
+        """
+        tol = self._tolerance(tolerance)
+        cuda_in = is_cuda_tensor(points)
+        points = cast_vertices(points)
+        t = self._tree
+        torch = _device.torch()
+        p_d = _device.to_device(points, torch.float64, t.device)
+        n = int(p_d.shape[0])
+        idx = _device.empty((n,), torch.int64, t.device)
+        t.reset_error()
+        self.launch_locate(p_d, idx, tol, self.precision)
+        K = t.K
+        w = _device.empty((n, K if K > 3 else 3), torch.float64, t.device)
+        _lib.check(
+            _lib.load().ct_barycentric_weights(
+                ctypes.byref(t.desc), _device.ptr(p_d), _device.ptr(idx), n, tol, _device.ptr(w), _device.stream()
+            ),
+            "barycentric",
+        )
+        t.raise_on_device_error()
+        return _as_output(idx, cuda_in), _as_output(w, cuda_in)

@@ -141,6 +141,144 @@ class _GpuTree:
                 bits.append("bounded loop gave up")
             raise _lib.CellTreeError("device error: " + ", ".join(bits))
 
+    # -- multi-result helpers ------------------------------------------------
+    def scan(self, counts):
+        """Exclusive scan of int64 counts on the device -> (offsets, total)."""
+        torch = _device.torch()
+        lib = _lib.load()
+        n = int(counts.shape[0])
+        wsz = lib.ct_scan_workspace_size(n)
+        ws = _device.empty((max(int(wsz), 8),), torch.uint8, self.device)
+        offsets = _device.empty((n,), torch.int64, self.device)
+        total = ctypes.c_int64(0)
+        _lib.check(
+            lib.ct_exclusive_scan(_device.ptr(counts), n, _device.ptr(offsets), _device.ptr(ws), wsz,
+                                  ctypes.byref(total), _device.stream()),
+            "scan",
+        )
+        return offsets, int(total.value)
+
+    def locate_boxes(self, boxes_d):
+        torch = _device.torch()
+        lib = _lib.load()
+        st = _device.stream()
+        n = int(boxes_d.shape[0])
+        counts = _device.empty((n,), torch.int64, self.device)
+        self.reset_error()
+        _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(counts), st),
+                   "locate_boxes")
+        offsets, total = self.scan(counts)
+        ii = _device.empty((total,), torch.int64, self.device)
+        jj = _device.empty((total,), torch.int64, self.device)
+        _lib.check(
+            lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(offsets),
+                               _device.ptr(ii), _device.ptr(jj), st),
+            "locate_boxes",
+        )
+        self.raise_on_device_error()
+        return ii, jj
+
+    def locate_edges(self, segs_d, mode: int):
+        """count -> scan -> write -> per-segment sort by t; returns ii, jj, xy (R, 2, 2)."""
+        torch = _device.torch()
+        lib = _lib.load()
+        st = _device.stream()
+        n = int(segs_d.shape[0])
+        counts = _device.empty((n,), torch.int64, self.device)
+        self.reset_error()
+        _lib.check(
+            lib.ct_count_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(counts), st),
+            "intersect_edges",
+        )
+        offsets, total = self.scan(counts)
+        ii = _device.empty((total,), torch.int64, self.device)
+        jj = _device.empty((total,), torch.int64, self.device)
+        xy = _device.empty((total, 2, 2), torch.float64, self.device)
+        _lib.check(
+            lib.ct_write_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(offsets),
+                               _device.ptr(ii), _device.ptr(jj), _device.ptr(xy), st),
+            "intersect_edges",
+        )
+        if total > 0:
+            jj2 = _device.empty((total,), torch.int64, self.device)
+            xy2 = _device.empty((total, 2, 2), torch.float64, self.device)
+            wsz = lib.ct_sort_workspace_size(total)
+            ws = _device.empty((int(wsz),), torch.uint8, self.device)
+            _lib.check(
+                lib.ct_sort_intersections(
+                    _device.ptr(segs_d), n, _device.ptr(offsets), _device.ptr(counts), _device.ptr(ii),
+                    _device.ptr(jj), _device.ptr(xy), total, _device.ptr(jj2), _device.ptr(xy2),
+                    _device.ptr(ws), wsz, st,
+                ),
+                "sort_intersections",
+            )
+            jj, xy = jj2, xy2
+        self.raise_on_device_error()
+        return ii, jj, xy
+
+    def compact(self, ii, jj, area=None, flag=None):
+        """Keep pairs with area > 0 (or flag != 0)."""
+        torch = _device.torch()
+        lib = _lib.load()
+        n = int(ii.shape[0])
+        ii_o = _device.empty((n,), torch.int64, self.device)
+        jj_o = _device.empty((n,), torch.int64, self.device)
+        a_o = _device.empty((n,), torch.float64, self.device) if area is not None else None
+        wsz = lib.ct_compact_workspace_size(n)
+        ws = _device.empty((int(wsz),), torch.uint8, self.device)
+        total = ctypes.c_int64(0)
+        _lib.check(
+            lib.ct_compact_pairs(
+                _device.ptr(area), _device.ptr(flag), n, _device.ptr(ii), _device.ptr(jj), _device.ptr(ii_o),
+                _device.ptr(jj_o), _device.ptr(a_o), _device.ptr(ws), wsz, ctypes.byref(total), _device.stream(),
+            ),
+            "compact",
+        )
+        m = int(total.value)
+        out = (ii_o[:m], jj_o[:m])
+        if a_o is not None:
+            out = out + (a_o[:m],)
+        return out
+
+    def node_bounds(self, nodes_host=None):
+        """collect_node_bounds query.py:568-622 on the device."""
+        torch = _device.torch()
+        lib = _lib.load()
+        child, Lmax, Rmin, dim = self.node_child, self.node_Lmax, self.node_Rmin, self.node_dim
+        if nodes_host is not None:
+            child = torch.as_tensor(np.ascontiguousarray(nodes_host["child"], dtype=np.int64), device=self.device)
+            Lmax = torch.as_tensor(np.ascontiguousarray(nodes_host["Lmax"]), device=self.device)
+            Rmin = torch.as_tensor(np.ascontiguousarray(nodes_host["Rmin"]), device=self.device)
+            dim = torch.as_tensor(np.ascontiguousarray(nodes_host["dim"], dtype=np.uint8), device=self.device)
+        n = int(child.shape[0])
+        parent = _device.empty((max(n, 1),), torch.int64, self.device)
+        out = _device.empty((n, 4), torch.float64, self.device)
+        bbox = (ctypes.c_double * 4)(*[float(x) for x in self.bbox])
+        _lib.check(
+            lib.ct_node_bounds(_device.ptr(child), _device.ptr(Lmax), _device.ptr(Rmin), _device.ptr(dim), n, bbox,
+                               _device.ptr(parent), _device.ptr(out), _device.stream()),
+            "node_bounds",
+        )
+        return out, (child, Lmax, Rmin, dim)
+
+    def validate_node_bounds(self, nodes_host=None):
+        torch = _device.torch()
+        lib = _lib.load()
+        nbnd, (child, _, _, _) = self.node_bounds(nodes_host)
+        ptr, size = self.node_ptr, self.node_size
+        if nodes_host is not None:
+            ptr = torch.as_tensor(np.ascontiguousarray(nodes_host["ptr"], dtype=np.int64), device=self.device)
+            size = torch.as_tensor(np.ascontiguousarray(nodes_host["size"], dtype=np.int64), device=self.device)
+        n = int(child.shape[0])
+        valid = _device.empty((n,), torch.uint8, self.device)
+        _lib.check(
+            lib.ct_validate_node_bounds(_device.ptr(child), _device.ptr(ptr), _device.ptr(size), n,
+                                        _device.ptr(self.bb_indices), _device.ptr(self.bb_coords),
+                                        _device.ptr(nbnd), _device.ptr(valid), _device.stream()),
+            "validate_node_bounds",
+        )
+        return valid
+
     def host_nodes(self) -> np.ndarray:
         nodes = np.empty(self.n_nodes, dtype=NodeDType)
         nodes["child"] = self.node_child.cpu().numpy()
@@ -218,6 +356,18 @@ class CellTree2dBase:
             getattr(self, self._elements_name), self.vertices, self.nodes, self.bb_indices, self.bb_coords,
             self.bbox, self.cells_per_leaf,
         )
+
+    @property
+    def node_bounds(self) -> np.ndarray:
+        """Bounds (xmin, xmax, ymin, ymax) of every node (celltree_base.py:62-64)."""
+        out, _ = self._tree.node_bounds(self._host.get("nodes"))
+        return out.cpu().numpy()
+
+    def validate_node_bounds(self) -> np.ndarray:
+        """For every node whether its children (or leaf boxes) lie inside its
+        bounds (celltree_base.py:66-80).  Uses the host ``nodes`` array when it
+        has been accessed (and possibly edited), like upstream."""
+        return self._tree.validate_node_bounds(self._host.get("nodes")).cpu().numpy().astype(bool)
 
     def to_dict_of_lists(self):
         """celltree_base.py:82-114"""

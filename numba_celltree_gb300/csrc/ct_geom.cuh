@@ -1,0 +1,426 @@
+// ct_geom.cuh -- exact float64 restatements of the upstream clipping, overlap,
+// area and barycentric algorithms (numba_celltree 0.4.2 algorithms/*.py and
+// geometry_utils.py), in upstream evaluation order.  Compiled with
+// -fmad=false, so results are bit-identical to the upstream CPU code.
+#pragma once
+
+#include <cfloat>
+
+#include "ct_common.cuh"
+
+__device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// ---------------------------------------------------------------------------
+// Cohen-Sutherland (algorithms/cohen_sutherland.py:18-101)
+// ---------------------------------------------------------------------------
+enum { CS_INSIDE = 0, CS_LEFT = 1, CS_RIGHT = 2, CS_LOWER = 4, CS_UPPER = 8 };
+
+__device__ __forceinline__ int cs_code(dpt a, const dbox& b) {
+    int p = CS_INSIDE;
+    if (a.x < b.xmin) p |= CS_LEFT;
+    else if (a.x > b.xmax) p |= CS_RIGHT;
+    if (a.y < b.ymin) p |= CS_LOWER;
+    else if (a.y > b.ymax) p |= CS_UPPER;
+    return p;
+}
+
+// Returns 1 (clipped segment c-d), 0 (no intersection, c = d = NaN) or -1
+// when the loop did not settle within 64 rounds (upstream loops until done;
+// each round fixes one outcode bit, so it settles in at most four).
+__device__ __forceinline__ int cohen_sutherland(dpt a, dpt b, const dbox& box, dpt* c, dpt* d) {
+    *c = mkp(dnan(), dnan());
+    *d = *c;
+    double dx = b.x - a.x, dy = b.y - a.y;
+    if (dx == 0.0 && dy == 0.0) return 0;
+    int k1 = cs_code(a, box), k2 = cs_code(b, box);
+    int iter = 0;
+    while ((k1 | k2) != CS_INSIDE) {
+        if ((k1 & k2) != 0) return 0;
+        if (++iter > 64) return -1;
+        int opt = k1 ? k1 : k2;
+        double x, y;
+        if (opt & CS_UPPER) {
+            x = a.x + dx * (box.ymax - a.y) / dy;
+            y = box.ymax;
+        } else if (opt & CS_LOWER) {
+            x = a.x + dx * (box.ymin - a.y) / dy;
+            y = box.ymin;
+        } else if (opt & CS_RIGHT) {
+            y = a.y + dy * (box.xmax - a.x) / dx;
+            x = box.xmax;
+        } else {
+            y = a.y + dy * (box.xmin - a.x) / dx;
+            x = box.xmin;
+        }
+        if (opt == k1) {
+            a = mkp(x, y);
+            k1 = cs_code(a, box);
+        } else if (opt == k2) {
+            b = mkp(x, y);
+            k2 = cs_code(b, box);
+        }
+        dx = b.x - a.x;
+        dy = b.y - a.y;
+        if (dx == 0.0 && dy == 0.0) return 0;
+    }
+    *c = a;
+    *d = b;
+    return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Cyrus-Beck / Skala (algorithms/cyrus_beck.py:26-241)
+// ---------------------------------------------------------------------------
+
+// compute_intersection cyrus_beck.py:26-43
+__device__ __forceinline__ double cb_param(dpt a, dpt s, dpt v0, dpt v1, bool* entering) {
+    dpt si = vsub(v0, a);
+    dpt n = mkp(-(v1.y - v0.y), (v1.x - v0.x));
+    double n_si = dotp(n, si);
+    double k = dotp(n, s);
+    double t = n_si / k;
+    *entering = n_si > 0;
+    return t;
+}
+
+// aligned cyrus_beck.py:76-91
+__device__ __forceinline__ bool cb_aligned(dpt U, dpt V) {
+    if ((U.x == 0 && U.y == 0) || (V.x == 0 && V.y == 0)) return true;
+    if (U.x != 0 && V.x != 0) return (U.x > 0) == (V.x > 0);
+    if (U.y != 0 && V.y != 0) return (U.y > 0) == (V.y > 0);
+    return false;
+}
+
+// collinear_case cyrus_beck.py:94-130 (overlap 66-73)
+__device__ __forceinline__ bool cb_collinear(dpt a, dpt b, dpt v0, dpt v1, dpt* c, dpt* d) {
+    dpt _b = mkp(b.x - a.x, b.y - a.y);
+    dpt _v0 = mkp(v0.x - a.x, v0.y - a.y);
+    dpt _v1 = mkp(v1.x - a.x, v1.y - a.y);
+    if (!cb_aligned(_b, vsub(_v1, _v0))) {
+        dpt t = v0;
+        v0 = v1;
+        v1 = t;
+        t = _v0;
+        _v0 = _v1;
+        _v1 = t;
+    }
+    dpt n = mkp(-_b.y, _b.x);
+    double ta = 0.0, tb = crossp(n, _b), t0 = crossp(n, _v0), t1 = crossp(n, _v1);
+    double xa = ta, xb = tb, x0 = t0, x1 = t1;
+    if (xa > xb) {
+        double t = xa;
+        xa = xb;
+        xb = t;
+    }
+    if (x0 > x1) {
+        double t = x0;
+        x0 = x1;
+        x1 = t;
+    }
+    double ov = pmin(xb, x1) - pmax(xa, x0);
+    if (!(ov > 0.0)) return false;  // max(0, ov) > 0
+    *c = (t0 < ta) ? v0 : a;
+    *d = (t1 > tb) ? v1 : b;
+    return true;
+}
+
+// cyrus_beck_line_polygon_clip cyrus_beck.py:133-241
+__device__ __forceinline__ bool cyrus_beck(dpt a, dpt b, const dpt* poly, int length, double tol, dpt* c, dpt* d) {
+    *c = mkp(dnan(), dnan());
+    *d = *c;
+    dpt s = vsub(b, a);
+    if (s.x == 0 && s.y == 0) return false;
+    bool a_inside = pip_or_edge(a, poly, length, tol);
+    bool b_inside = pip_or_edge(b, poly, length, tol);
+    if (a_inside && b_inside) {
+        *c = a;
+        *d = b;
+        return true;
+    }
+    int i0 = -1, i1 = -1, i = 0, k = 0;
+    double ksi = crossp(vsub(poly[0], a), s);
+    while (i < length && k < 2) {
+        dpt v0 = poly[i], v1 = poly[(i + 1) % length];
+        double eta = crossp(vsub(v1, a), s);
+        if ((ksi < 0.0) != (eta < 0.0)) {
+            if (k == 0) i0 = i;
+            else i1 = i;
+            k++;
+        } else if (ksi == 0.0 && eta == 0.0) {
+            bool r = cb_collinear(a, b, v0, v1, c, d);
+            if (!r) {
+                *c = mkp(dnan(), dnan());
+                *d = *c;
+            }
+            return r;
+        }
+        ksi = eta;
+        i++;
+    }
+    if (k == 0) return false;
+    // intersections cyrus_beck.py:46-63 (Python index -1 wraps)
+    int j0 = i0 < 0 ? i0 + length : i0, j1 = i1 < 0 ? i1 + length : i1;
+    dpt v0 = poly[j0], v01 = poly[(i0 + 1) % length];
+    dpt v1 = poly[j1], v11 = poly[((i1 + 1) % length + length) % length];
+    bool e0, e1;
+    double t0 = cb_param(a, s, v0, v01, &e0);
+    double t1 = cb_param(a, s, v1, v11, &e1);
+    if (e1) {
+        double t = t0;
+        t0 = t1;
+        t1 = t;
+    }
+    if (t0 == t1) {
+        if (a_inside && t1 != 0.0) t0 = 0.0;
+        else if (b_inside && t0 != 1.0) t1 = 1.0;
+        else return false;
+    }
+    if (t1 < t0) {
+        double t = t0;
+        t0 = t1;
+        t1 = t;
+    }
+    bool valid0 = t0 >= 0 && t0 < 1;
+    bool valid1 = t1 > 0 && t1 <= 1;
+    if (valid0 && valid1) {
+        *c = mkp(a.x + t0 * s.x, a.y + t0 * s.y);
+        *d = mkp(a.x + t1 * s.x, a.y + t1 * s.y);
+        return true;
+    } else if (valid0) {
+        *c = mkp(a.x + t0 * s.x, a.y + t0 * s.y);
+        *d = b;
+        return true;
+    } else if (valid1) {
+        *c = a;
+        *d = mkp(a.x + t1 * s.x, a.y + t1 * s.y);
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// lines_intersect geometry_utils.py:318-418
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool left_of(dpt a, dpt p, dpt U) { return U.x * (a.y - p.y) > U.y * (a.x - p.x); }
+__device__ __forceinline__ bool has_overlap(double a, double b, double p, double q, double tol) {
+    return ((pmin(a, b) - pmax(p, q)) < tol) && ((pmin(p, q) - pmax(a, b)) < tol);
+}
+
+__device__ __forceinline__ bool lines_intersect(dpt a, dpt b, dpt p, dpt q, double* x, double* y) {
+    dpt V = vsub(b, a), U = vsub(q, p);
+    *x = dnan();
+    *y = dnan();
+    if ((U.x == 0 && U.y == 0) || (V.x == 0 && V.y == 0)) return false;
+    if ((U.x == 0) && (V.x == 0) && a.x != p.x) return false;
+    if ((U.y == 0) && (V.y == 0) && a.y != p.y) return false;
+    double tol = pmax(CT_MIN_TOLERANCE, CT_TOLERANCE_FACTOR * pmax(fabs(U.x), fabs(U.y)));
+    if (!has_overlap(a.x, b.x, p.x, q.x, tol) || !has_overlap(a.y, b.y, p.y, q.y, tol)) return false;
+    if ((left_of(a, p, U) != left_of(b, p, U)) && (left_of(p, a, V) != left_of(q, a, V))) {
+        double denom = crossp(V, U);
+        if (within_perp(denom, V, tol)) return true;  // parallel: NaN point
+        dpt R = vsub(p, a);
+        double t = crossp(R, U) / denom;
+        *x = a.x + t * V.x;
+        *y = a.y + t * V.y;
+        return true;
+    }
+    dpt R = vsub(p, a), S = vsub(q, a);
+    if (within_perp(crossp(V, R), V, tol) && within_perp(crossp(V, S), V, tol)) {
+        dpt aa = a, bb = b, pp = p, qq = q, t;
+        if (aa.x > bb.x || (aa.x == bb.x && aa.y > bb.y)) {
+            t = aa;
+            aa = bb;
+            bb = t;
+        }
+        if (pp.x > qq.x || (pp.x == qq.x && pp.y > qq.y)) {
+            t = pp;
+            pp = qq;
+            qq = t;
+        }
+        double sx = pmax(aa.x, pp.x), sy = pmax(aa.y, pp.y);
+        double ex = pmin(bb.x, qq.x), ey = pmin(bb.y, qq.y);
+        if (sx > ex || sy > ey) return true;  // no overlap: NaN point
+        *x = 0.5 * (sx + ex);
+        *y = 0.5 * (sy + ey);
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// separating axes (algorithms/separating_axis.py:17-55)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool separating_axes(const dpt* a, int la, const dpt* b, int lb) {
+    dpt p = a[la - 1];
+    for (int i = 0; i < la; i++) {
+        dpt q = a[i];
+        dpt norm = mkp(p.y - q.y, q.x - p.x);
+        p = q;
+        if (norm.x == 0.0 && norm.y == 0.0) continue;
+        double mina = DBL_MAX, maxa = -DBL_MAX, minb = DBL_MAX, maxb = -DBL_MAX;
+        for (int j = 0; j < la; j++) {
+            double proj = dotp(a[j], norm);
+            mina = pmin(mina, proj);
+            maxa = pmax(maxa, proj);
+        }
+        for (int j = 0; j < lb; j++) {
+            double proj = dotp(b[j], norm);
+            minb = pmin(minb, proj);
+            maxb = pmax(maxb, proj);
+        }
+        if (!(maxa > minb && maxb > mina)) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Sutherland-Hodgman (algorithms/sutherland_hodgman.py:56-148) and
+// polygon_area (geometry_utils.py:82-95)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double polygon_area(const dpt* poly, int len) {
+    double area = 0.0;
+    dpt a = poly[0], b = poly[1];
+    dpt U = vsub(b, a);
+    for (int i = 2; i < len; i++) {
+        dpt c = poly[i];
+        dpt V = vsub(a, c);
+        area += fabs(crossp(U, V));
+        U = V;
+    }
+    return 0.5 * area;
+}
+
+__device__ __forceinline__ bool sh_inside(dpt p, dpt r, dpt U) { return U.x * (p.y - r.y) > U.y * (p.x - r.x); }
+
+__device__ __forceinline__ bool sh_intersection(dpt a, dpt V, dpt r, dpt N, dpt* out) {
+    dpt W = mkp(r.x - a.x, r.y - a.y);
+    double nw = dotp(N, W), nv = dotp(N, V);
+    if (nv != 0) {
+        double t = nw / nv;
+        *out = mkp(a.x + t * V.x, a.y + t * V.y);
+        return true;
+    }
+    return false;
+}
+
+// polygon_polygon_clip_area: `subject` is clipped by `clipper`.  Uses two
+// CT_CLIP_MAX-vertex scratch polygons; returns NaN and sets *overflow if the
+// clipped polygon would exceed them (upstream writes past its stack arrays).
+__device__ __forceinline__ double clip_area(const dpt* polygon, int n_poly, const dpt* clipper, int n_clip, dpt* bufA,
+                                            dpt* bufB, bool* overflow) {
+    dpt* output = bufA;
+    dpt* subject = bufB;
+    int n_output = n_poly;
+    for (int i = 0; i < n_poly; i++) output[i] = polygon[i];
+    dpt r = clipper[n_clip - 1];
+    for (int i = 0; i < n_clip; i++) {
+        dpt s = clipper[i];
+        dpt U = mkp(s.x - r.x, s.y - r.y);
+        if (U.x == 0 && U.y == 0) continue;
+        dpt N = mkp(-U.y, U.x);
+        int length = n_output;
+        dpt* t = subject;  // swap roles instead of copying output into subject
+        subject = output;
+        output = t;
+        n_output = 0;
+        dpt a = subject[length - 1];
+        bool a_inside = sh_inside(a, r, U);
+        for (int j = 0; j < length; j++) {
+            dpt b = subject[j];
+            dpt V = mkp(b.x - a.x, b.y - a.y);
+            if (V.x == 0 && V.y == 0) continue;
+            bool b_inside = sh_inside(b, r, U);
+            dpt pnt;
+            if (b_inside) {
+                if (!a_inside) {
+                    if (sh_intersection(a, V, r, N, &pnt)) {
+                        if (n_output >= CT_CLIP_MAX) {
+                            *overflow = true;
+                            return dnan();
+                        }
+                        output[n_output++] = pnt;
+                    }
+                }
+                if (n_output >= CT_CLIP_MAX) {
+                    *overflow = true;
+                    return dnan();
+                }
+                output[n_output++] = b;
+            } else if (a_inside) {
+                if (sh_intersection(a, V, r, N, &pnt)) {
+                    if (n_output >= CT_CLIP_MAX) {
+                        *overflow = true;
+                        return dnan();
+                    }
+                    output[n_output++] = pnt;
+                } else {
+                    b_inside = true;
+                    if (n_output >= CT_CLIP_MAX) {
+                        *overflow = true;
+                        return dnan();
+                    }
+                    output[n_output++] = b;
+                }
+            }
+            a = b;
+            a_inside = b_inside;
+        }
+        if (n_output < 3) return 0.0;
+        r = s;
+    }
+    return polygon_area(output, n_output);
+}
+
+// ---------------------------------------------------------------------------
+// barycentric weights (algorithms/barycentric_triangle.py:28-43,
+// barycentric_wachspress.py:26-85)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tri_weights(dpt a, dpt b, dpt c, dpt p, double* w) {
+    dpt ab = vsub(b, a), ac = vsub(c, a), ap = vsub(p, a);
+    double Aa = fabs(crossp(ab, ap)), Ac = fabs(crossp(ac, ap)), A = fabs(crossp(ab, ac));
+    double inv_denom = 1.0 / A;
+    double ww = inv_denom * Aa, v = inv_denom * Ac;
+    double u = 1.0 - v - ww;
+    w[0] = u;
+    w[1] = v;
+    w[2] = ww;
+}
+
+__device__ __forceinline__ void interp_edge(dpt a, dpt U, dpt p, double* w, int K, int i, int j) {
+    for (int k = 0; k < K; k++) w[k] = 0.0;
+    dpt V = vsub(p, a);
+    double ww = sqrt(dotp(V, V)) / sqrt(dotp(U, U));
+    w[i] = 1.0 - ww;
+    w[j] = ww;
+}
+
+__device__ __forceinline__ void wachspress(const dpt* poly, int n, dpt p, double* w, int K, double tol) {
+    double w_sum = 0.0;
+    dpt a = poly[n - 1], b = poly[0];
+    dpt U = vsub(b, a), V = vsub(p, a);
+    double Ai = fabs(crossp(U, V));
+    if (within_perp(Ai, U, tol)) {
+        interp_edge(a, U, p, w, K, n - 1, 0);
+        return;
+    }
+    for (int i = 0; i < n; i++) {
+        int i_next = (i + 1) % n;
+        dpt c = poly[i_next];
+        dpt W = vsub(c, a);
+        double Ci = fabs(crossp(U, W));
+        U = vsub(c, b);
+        V = vsub(p, b);
+        double Aj = fabs(crossp(U, V));
+        if (within_perp(Aj, U, tol)) {
+            interp_edge(b, U, p, w, K, i, i_next);
+            return;
+        }
+        double ww = 2.0 * Ci / (Ai * Aj);
+        w[i] = ww;
+        w_sum += ww;
+        a = b;
+        b = c;
+        Ai = Aj;
+    }
+    for (int i = 0; i < n; i++) w[i] /= w_sum;
+}

@@ -1,0 +1,811 @@
+// ct_multi.cu -- multi-result queries, per-pair kernels, barycentric weights
+// and node-bound diagnostics.
+//
+// Multi-result queries (locate_boxes query.py:177-289, _locate_edges
+// query.py:357-533) are rebuilt as count -> exclusive scan -> write: the
+// count and write kernels run the same traversal, so the write pass knows
+// each query's output offset.  Results come out query-major and, within a
+// query, in traversal order -- exactly upstream's concatenated order.
+#include <cfloat>
+#include <cmath>
+
+#include "ct_common.cuh"
+#include "ct_geom.cuh"
+#include "ct_internal.h"
+
+namespace ctm {
+
+struct TreeQ {
+    const float4* nf;    // packed node meta: z = child / ptr, w = -1 - dim / size
+    const double2* nd;   // Lmax, Rmin
+    const double2* poly; // leaf-ordered polygons (K per cell)
+    const uint8_t* plen;
+    const int64_t* bbi;
+    const double* bb;    // bb_coords (cell order)
+    unsigned int* err;
+    int64_t n_nodes;
+    dbox bbox;
+    int K;
+};
+
+__device__ __forceinline__ int na(const float4& q) { return __float_as_int(q.z); }
+__device__ __forceinline__ int nb(const float4& q) { return __float_as_int(q.w); }
+
+constexpr int STK = 128;  // traversal stack (tree depth + 2 must fit; checked on the host)
+
+// ---------------------------------------------------------------------------
+// locate_box query.py:177-244
+// ---------------------------------------------------------------------------
+template <bool WRITE>
+__global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restrict__ boxes, int64_t n,
+                                               int64_t* __restrict__ cnt_or_off, int64_t* __restrict__ ii,
+                                               int64_t* __restrict__ jj) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 q4 = boxes[i];
+    dbox box;
+    box.xmin = q4.x;
+    box.xmax = q4.y;
+    box.ymin = q4.z;
+    box.ymax = q4.w;
+    int64_t count = 0;
+    int64_t base = WRITE ? cnt_or_off[i] : 0;
+    if (boxes_intersect(box, T.bbox)) {
+        int st[STK];
+        int sp = 1;
+        st[0] = 0;
+        int64_t budget = T.n_nodes;
+        while (sp > 0) {
+            if (--budget < 0) {
+                set_error(T.err, CT_DEVERR_LOOP);
+                break;
+            }
+            int v = st[--sp];
+            float4 q = T.nf[v];
+            int b = nb(q);
+            if (b >= 0) {
+                int ptr = na(q);
+                for (int j = ptr; j < ptr + b; j++) {
+                    int64_t cell = T.bbi[j];
+                    dbox lb = load_box(T.bb + 4 * cell);
+                    if (boxes_intersect(box, lb)) {
+                        if (WRITE) {
+                            ii[base + count] = i;
+                            jj[base + count] = cell;
+                        }
+                        count++;
+                    }
+                }
+                continue;
+            }
+            int dim = -1 - b;
+            double2 d = T.nd[v];
+            double bmin = dim ? box.ymin : box.xmin, bmax = dim ? box.ymax : box.xmax;
+            bool left = bmin <= d.x, right = bmax >= d.y;
+            int child = na(q);
+            if (sp + 2 > STK) {
+                set_error(T.err, CT_DEVERR_STACK);
+                break;
+            }
+            if (left && right) {
+                st[sp++] = child;
+                st[sp++] = child + 1;
+            } else if (left) {
+                st[sp++] = child;
+            } else if (right) {
+                st[sp++] = child + 1;
+            }
+        }
+    }
+    if (!WRITE) cnt_or_off[i] = count;
+}
+
+// ---------------------------------------------------------------------------
+// locate_edge query.py:357-455 with compute_edge_edge_intersect (292-306,
+// mode 0) or compute_edge_face_intersect (309-328, mode 1)
+// ---------------------------------------------------------------------------
+template <bool WRITE, int MODE>
+__global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restrict__ segs, int64_t n,
+                                               int64_t* __restrict__ cnt_or_off, int64_t* __restrict__ ii,
+                                               int64_t* __restrict__ jj, double4* __restrict__ xy) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 s4 = segs[i];
+    dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+    int64_t count = 0;
+    int64_t base = WRITE ? cnt_or_off[i] : 0;
+    dpt c, d;
+    int r = cohen_sutherland(a, b, T.bbox, &c, &d);
+    if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
+    if (r == 1) {
+        dpt V = vsub(b, a);
+        int st[STK];
+        int sp = 1;
+        st[0] = 0;
+        int64_t budget = T.n_nodes;
+        while (sp > 0) {
+            if (--budget < 0) {
+                set_error(T.err, CT_DEVERR_LOOP);
+                break;
+            }
+            int v = st[--sp];
+            float4 q = T.nf[v];
+            int bq = nb(q);
+            if (bq >= 0) {
+                int ptr = na(q);
+                for (int j = ptr; j < ptr + bq; j++) {
+                    int64_t cell = T.bbi[j];
+                    bool hit;
+                    if (MODE == 0) {
+                        double2 p0 = T.poly[(size_t)j * 2], p1 = T.poly[(size_t)j * 2 + 1];
+                        double x, y;
+                        hit = lines_intersect(a, b, mkp(p0.x, p0.y), mkp(p1.x, p1.y), &x, &y);
+                        c = mkp(x, y);
+                        d = c;
+                    } else {
+                        dbox bx = load_box(T.bb + 4 * cell);
+                        int rr = cohen_sutherland(a, b, bx, &c, &d);
+                        if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
+                        hit = rr == 1;
+                        if (hit) {
+                            const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
+                            int len = T.plen ? (int)T.plen[j] : T.K;
+                            double tol = pmax(CT_MIN_TOLERANCE,
+                                              CT_TOLERANCE_FACTOR * pmax(bx.xmax - bx.xmin, bx.ymax - bx.ymin));
+                            hit = cyrus_beck(a, b, poly, len, tol, &c, &d);
+                        }
+                    }
+                    if (hit) {
+                        if (WRITE) {
+                            ii[base + count] = i;
+                            jj[base + count] = cell;
+                            xy[base + count] = make_double4(c.x, c.y, d.x, d.y);
+                        }
+                        count++;
+                    }
+                }
+                continue;
+            }
+            int dim = -1 - bq;
+            double2 nd = T.nd[v];
+            double dx = dim ? V.y : V.x;
+            double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
+            double dx_left, dx_right;
+            if (dx > 0.0) {
+                dx_left = nd.x - an;
+                dx_right = nd.y - bn;
+            } else {
+                dx_left = nd.x - bn;
+                dx_right = nd.y - an;
+            }
+            bool left = dx_left >= 0.0, right = dx_right <= 0.0;
+            if (dx > 0.0) {
+                if (left) left = (dx_left / dx) >= 0.0;
+                if (right) right = (dx_right / dx) <= 1.0;
+            } else if (dx < 0.0) {
+                if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
+                if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+            }
+            int child = na(q);
+            if (sp + 2 > STK) {
+                set_error(T.err, CT_DEVERR_STACK);
+                break;
+            }
+            if (left && right) {
+                st[sp++] = child;
+                st[sp++] = child + 1;
+            } else if (left) {
+                st[sp++] = child;
+            } else if (right) {
+                st[sp++] = child + 1;
+            }
+        }
+    }
+    if (!WRITE) cnt_or_off[i] = count;
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of int64 counts
+// ---------------------------------------------------------------------------
+constexpr int SCAN_T = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_T * SCAN_ITEMS;
+
+// Block-wide exclusive scan; every thread receives the block total in *total.
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t* total) {
+    __shared__ int64_t warp_sums[SCAN_T / 32];
+    __shared__ int64_t block_total;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t t = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) warp_sums[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int64_t s = lane < SCAN_T / 32 ? warp_sums[lane] : 0;
+        int64_t y = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t t = __shfl_up_sync(0xffffffffu, y, o);
+            if (lane >= o) y += t;
+        }
+        if (lane < SCAN_T / 32) warp_sums[lane] = y - s;
+        if (lane == SCAN_T / 32 - 1) block_total = y;
+    }
+    __syncthreads();
+    int64_t r = x - v + warp_sums[w];
+    *total = block_total;
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_scan_reduce(const int64_t* __restrict__ in, int64_t n, int64_t* __restrict__ sums) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int64_t s = 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        int64_t i = base + (int64_t)k * SCAN_T + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ int64_t ws[SCAN_T / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 0;
+        for (int k = 0; k < SCAN_T / 32; k++) t += ws[k];
+        sums[blockIdx.x] = t;
+    }
+}
+
+// single block: exclusive scan of the block sums in place, total at sums[nb]
+__global__ void k_scan_sums(int64_t* sums, int64_t nblocks) {
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < nblocks; base += SCAN_T) {
+        int64_t i = base + threadIdx.x;
+        int64_t v = i < nblocks ? sums[i] : 0;
+        int64_t tot;
+        int64_t ex = block_exclusive_scan(v, &tot);
+        if (i < nblocks) sums[i] = ex + carry;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[nblocks] = carry;
+}
+
+__global__ void k_scan_down(const int64_t* __restrict__ in, int64_t n, const int64_t* __restrict__ sums,
+                            int64_t* __restrict__ out) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    int64_t v[SCAN_ITEMS];
+    int64_t s = 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int64_t tot;
+    int64_t ex = block_exclusive_scan(s, &tot) + sums[blockIdx.x];
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        int64_t i = base + k;
+        if (i < n) out[i] = ex;
+        ex += v[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-segment stable sort by t (sort_intersections_by_edge
+// geometry_utils.py:564-574: np.lexsort((t, ii)), NaN last)
+// ---------------------------------------------------------------------------
+
+// sortable key of t: NaN greatest, otherwise the float order
+__device__ __forceinline__ unsigned long long tkey(double t) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return ~0ull;
+    return fkey(t);
+}
+
+__global__ void k_tkeys(const double4* __restrict__ segs, const int64_t* __restrict__ ii,
+                        const double4* __restrict__ xy, int64_t total, unsigned long long* __restrict__ key,
+                        int64_t* __restrict__ idx) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= total) return;
+    double4 s = segs[ii[r]];
+    double4 c = xy[r];
+    double abx = s.z - s.x, aby = s.w - s.y;
+    double acx = c.x - s.x, acy = c.y - s.y;
+    double t = acx * abx + acy * aby;
+    key[r] = tkey(t);
+    idx[r] = r;
+}
+
+__device__ __forceinline__ bool kless(unsigned long long ka, int64_t ia, unsigned long long kb, int64_t ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+constexpr int SORT_T = 128;
+constexpr int SORT_SMEM = 1024;  // 2 x 1024 x (8 + 8) B = 32 KB static shared memory
+
+// One block per segment: stable sort of (key, idx) pairs of the segment by
+// bottom-up merging; (key, idx) pairs are unique, so each element's output
+// rank is its rank in its own run plus the number of smaller elements in the
+// partner run (binary search).  Small segments are sorted in shared memory,
+// large ones in global memory (A/B ping-pong); the result lands in `idx_out`.
+__global__ void __launch_bounds__(SORT_T) k_segsort(const int64_t* __restrict__ off, const int64_t* __restrict__ cnt,
+                                                    int64_t nseg, unsigned long long* __restrict__ kA,
+                                                    int64_t* __restrict__ iA, unsigned long long* __restrict__ kB,
+                                                    int64_t* __restrict__ iB, int64_t* __restrict__ idx_out) {
+    __shared__ unsigned long long sk[2][SORT_SMEM];
+    __shared__ int64_t si[2][SORT_SMEM];
+    int64_t sgi = blockIdx.x;
+    if (sgi >= nseg) return;
+    int64_t c = cnt[sgi], o = off[sgi];
+    if (c <= 0) return;
+    if (c == 1) {
+        if (threadIdx.x == 0) idx_out[o] = iA[o];
+        return;
+    }
+    bool smem = c <= SORT_SMEM;
+    unsigned long long* k0 = smem ? sk[0] : kA + o;
+    int64_t* i0 = smem ? si[0] : iA + o;
+    unsigned long long* k1 = smem ? sk[1] : kB + o;
+    int64_t* i1 = smem ? si[1] : iB + o;
+    if (smem) {
+        for (int64_t t = threadIdx.x; t < c; t += blockDim.x) {
+            sk[0][t] = kA[o + t];
+            si[0][t] = iA[o + t];
+        }
+    }
+    __syncthreads();
+    for (int64_t w = 1; w < c; w <<= 1) {
+        for (int64_t t = threadIdx.x; t < c; t += blockDim.x) {
+            int64_t run = t / w;
+            int64_t r0 = (run ^ 1) * w;  // partner run start
+            bool left = (run & 1) == 0;
+            int64_t own0 = run * w;
+            int64_t pair0 = left ? own0 : r0;
+            unsigned long long mk = k0[t];
+            int64_t mi = i0[t];
+            int64_t plo = r0, phi = min(r0 + w, c);
+            if (plo > c) plo = c;
+            int64_t lo = plo, hi = phi;  // count partner elements smaller than (mk, mi)
+            while (lo < hi) {
+                int64_t mid = (lo + hi) >> 1;
+                if (kless(k0[mid], i0[mid], mk, mi)) lo = mid + 1;
+                else hi = mid;
+            }
+            int64_t dst = pair0 + (t - own0) + (lo - plo);
+            k1[dst] = mk;
+            i1[dst] = mi;
+        }
+        __syncthreads();
+        unsigned long long* tk = k0;
+        k0 = k1;
+        k1 = tk;
+        int64_t* ti = i0;
+        i0 = i1;
+        i1 = ti;
+    }
+    for (int64_t t = threadIdx.x; t < c; t += blockDim.x) idx_out[o + t] = i0[t];
+}
+
+__global__ void k_gather_results(const int64_t* __restrict__ perm, int64_t total, const int64_t* __restrict__ jj_in,
+                                 const double4* __restrict__ xy_in, int64_t* __restrict__ jj_out,
+                                 double4* __restrict__ xy_out) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= total) return;
+    int64_t s = perm[r];
+    jj_out[r] = jj_in[s];
+    xy_out[r] = xy_in[s];
+}
+
+// ---------------------------------------------------------------------------
+// per-pair kernels
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int load_poly(const double* __restrict__ v, const int64_t* __restrict__ faces, int K,
+                                         int64_t f, dpt* out) {
+    return gather_polygon(v, faces + f * K, K, out);
+}
+
+// polygons_intersect separating_axis.py:58-75
+__global__ void k_sat(const double* __restrict__ va, const int64_t* __restrict__ fa, int Ka,
+                      const double* __restrict__ vb, const int64_t* __restrict__ fb, int Kb,
+                      const int64_t* __restrict__ ia, const int64_t* __restrict__ ib, int64_t n,
+                      uint8_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dpt a[CT_MAX_N_VERTEX], b[CT_MAX_N_VERTEX];
+    int la = load_poly(va, fa, Ka, ia[i], a);
+    int lb = load_poly(vb, fb, Kb, ib[i], b);
+    out[i] = (uint8_t)(separating_axes(a, la, b, lb) && separating_axes(b, lb, a, la));
+}
+
+// area_of_intersection sutherland_hodgman.py:151-168 (subject: face of a,
+// clipper: face of b)
+__global__ void k_clip_area(const double* __restrict__ va, const int64_t* __restrict__ fa, int Ka,
+                            const double* __restrict__ vb, const int64_t* __restrict__ fb, int Kb,
+                            const int64_t* __restrict__ ia, const int64_t* __restrict__ ib, int64_t n,
+                            double* __restrict__ out, unsigned int* __restrict__ err) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dpt a[CT_MAX_N_VERTEX], b[CT_MAX_N_VERTEX];
+    dpt A[CT_CLIP_MAX], B[CT_CLIP_MAX];
+    int la = load_poly(va, fa, Ka, ia[i], a);
+    int lb = load_poly(vb, fb, Kb, ib[i], b);
+    bool of = false;
+    out[i] = clip_area(a, la, b, lb, A, B, &of);
+    if (of) set_error(err, CT_DEVERR_CLIP);
+}
+
+// box_area_of_intersection sutherland_hodgman.py:171-187 (subject: the box)
+__global__ void k_box_area(const double4* __restrict__ boxes, const double* __restrict__ vb,
+                           const int64_t* __restrict__ fb, int Kb, const int64_t* __restrict__ ibox,
+                           const int64_t* __restrict__ iface, int64_t n, double* __restrict__ out,
+                           unsigned int* __restrict__ err) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4 q = boxes[ibox[i]];
+    dpt a[4] = {mkp(q.x, q.z), mkp(q.y, q.z), mkp(q.y, q.w), mkp(q.x, q.w)};
+    dpt b[CT_MAX_N_VERTEX];
+    dpt A[CT_CLIP_MAX], B[CT_CLIP_MAX];
+    int lb = load_poly(vb, fb, Kb, iface[i], b);
+    bool of = false;
+    out[i] = clip_area(a, 4, b, lb, A, B, &of);
+    if (of) set_error(err, CT_DEVERR_CLIP);
+}
+
+// keep = area > 0 (celltree.py:183, 268) or keep = flag
+__global__ void k_keep(const double* __restrict__ area, const uint8_t* __restrict__ flag, int64_t n,
+                       int64_t* __restrict__ keep) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keep[i] = area ? (int64_t)(area[i] > 0) : (int64_t)(flag[i] != 0);
+}
+
+__global__ void k_compact(const int64_t* __restrict__ keep, const int64_t* __restrict__ pos, int64_t n,
+                          const int64_t* __restrict__ ii, const int64_t* __restrict__ jj,
+                          const double* __restrict__ vals, int64_t* __restrict__ ii_out, int64_t* __restrict__ jj_out,
+                          double* __restrict__ vals_out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !keep[i]) return;
+    int64_t p = pos[i];
+    ii_out[p] = ii[i];
+    jj_out[p] = jj[i];
+    if (vals) vals_out[p] = vals[i];
+}
+
+// ---------------------------------------------------------------------------
+// barycentric weights (barycentric_triangle.py:46-64,
+// barycentric_wachspress.py:88-107)
+// ---------------------------------------------------------------------------
+__global__ void k_barycentric(const double2* __restrict__ pts, const int64_t* __restrict__ fidx, int64_t n,
+                              const double* __restrict__ v, const int64_t* __restrict__ faces, int K, int KW,
+                              double tol, double* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double* w = out + i * KW;
+    for (int k = 0; k < KW; k++) w[k] = 0.0;
+    int64_t f = fidx[i];
+    if (f == -1) return;
+    double2 pp = pts[i];
+    dpt p = mkp(pp.x, pp.y);
+    const int64_t* face = faces + f * K;
+    if (K > 3) {
+        dpt poly[CT_MAX_N_VERTEX];
+        double ww[CT_MAX_N_VERTEX];
+        int len = gather_polygon(v, face, K, poly);
+        for (int k = 0; k < K; k++) ww[k] = 0.0;
+        wachspress(poly, len, p, ww, K, tol);
+        for (int k = 0; k < K; k++) w[k] = ww[k];
+    } else {
+        double ww[3];
+        tri_weights(mkp(v[2 * face[0]], v[2 * face[0] + 1]), mkp(v[2 * face[1]], v[2 * face[1] + 1]),
+                    mkp(v[2 * face[2]], v[2 * face[2] + 1]), p, ww);
+        w[0] = ww[0];
+        w[1] = ww[1];
+        w[2] = ww[2];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// node-bound diagnostics (collect_node_bounds query.py:568-622,
+// validate_node_bounds 625-663)
+// ---------------------------------------------------------------------------
+__global__ void k_parents(const int64_t* __restrict__ child, int64_t n_nodes, int64_t* __restrict__ parent) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_nodes) return;
+    if (v == 0) parent[0] = -1;
+    int64_t c = child[v];
+    if (c > v && c + 1 < n_nodes) {
+        parent[c] = v;
+        parent[c + 1] = v;
+    }
+}
+
+// A node's bounds are its parent's with one coordinate overwritten (left
+// child: max of the parent's dim = Lmax; right child: min = Rmin).  Walking up
+// from the node, the first ancestor edge that sets a coordinate wins.
+__global__ void k_node_bounds(const int64_t* __restrict__ child, const double* __restrict__ Lmax,
+                              const double* __restrict__ Rmin, const uint8_t* __restrict__ dim,
+                              const int64_t* __restrict__ parent, int64_t n_nodes, double4 bbox,
+                              double4* __restrict__ out) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_nodes) return;
+    double b[4] = {bbox.x, bbox.y, bbox.z, bbox.w};
+    bool set[4] = {false, false, false, false};
+    int64_t u = v;
+    int64_t guard = n_nodes;
+    while (u > 0 && guard-- > 0) {
+        int64_t p = parent[u];
+        if (p < 0) break;
+        int d = dim[p] ? 1 : 0;
+        int side = (u == child[p]) ? 1 : 0;  // left child: side 1 (max), right: side 0 (min)
+        int k = d * 2 + side;
+        if (!set[k]) {
+            b[k] = side ? Lmax[p] : Rmin[p];
+            set[k] = true;
+        }
+        u = p;
+    }
+    out[v] = make_double4(b[0], b[1], b[2], b[3]);
+}
+
+__global__ void k_validate_bounds(const int64_t* __restrict__ child, const int64_t* __restrict__ ptr,
+                                  const int64_t* __restrict__ size, const int64_t* __restrict__ bbi,
+                                  const double* __restrict__ bb, const double4* __restrict__ nbnd, int64_t n_nodes,
+                                  uint8_t* __restrict__ valid) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_nodes) return;
+    double4 q = nbnd[v];
+    dbox bx;
+    bx.xmin = q.x;
+    bx.xmax = q.y;
+    bx.ymin = q.z;
+    bx.ymax = q.w;
+    int64_t c = child[v];
+    bool ok = true;
+    if (c == -1) {
+        for (int64_t i = ptr[v]; i < ptr[v] + size[v]; i++) ok = ok && box_contained(load_box(bb + 4 * bbi[i]), bx);
+    } else {
+        double4 l = nbnd[c], r = nbnd[c + 1];
+        dbox lb, rb;
+        lb.xmin = l.x;
+        lb.xmax = l.y;
+        lb.ymin = l.z;
+        lb.ymax = l.w;
+        rb.xmin = r.x;
+        rb.xmax = r.y;
+        rb.ymin = r.z;
+        rb.ymax = r.w;
+        ok = box_contained(lb, bx) && box_contained(rb, bx);
+    }
+    valid[v] = (uint8_t)ok;
+}
+
+TreeQ make_q(const ct_tree* t) {
+    TreeQ T;
+    T.nf = (const float4*)t->nodes_f32;
+    T.nd = (const double2*)t->nodes_f64;
+    T.poly = (const double2*)t->poly_f64;
+    T.plen = t->n_max_vert == 3 || t->n_max_vert == 2 ? nullptr : t->poly_len;
+    T.bbi = t->bb_indices;
+    T.bb = t->bb_coords;
+    T.err = t->error_word;
+    T.n_nodes = t->n_nodes;
+    T.bbox.xmin = t->bbox[0];
+    T.bbox.xmax = t->bbox[1];
+    T.bbox.ymin = t->bbox[2];
+    T.bbox.ymax = t->bbox[3];
+    T.K = t->n_max_vert;
+    return T;
+}
+
+static inline unsigned grid_of(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace ctm
+
+using namespace ctm;
+
+extern "C" {
+
+size_t ct_scan_workspace_size(int64_t n) {
+    int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    return (size_t)(nb + 1) * sizeof(int64_t);
+}
+
+int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* ws, size_t ws_bytes, int64_t* total_host,
+                      void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 0) return ct_fail(CT_ERR_ARG, "negative length");
+    if (ws_bytes < ct_scan_workspace_size(n) || !ws) return ct_fail(CT_ERR_WORKSPACE, "scan workspace too small");
+    int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    int64_t* sums = (int64_t*)ws;
+    if (nb > 0) {
+        k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums);
+        k_scan_sums<<<1, SCAN_T, 0, st>>>(sums, nb);
+        k_scan_down<<<(unsigned)nb, SCAN_T, 0, st>>>(in, n, sums, out);
+    } else {
+        CT_CUDA(cudaMemsetAsync(sums, 0, sizeof(int64_t), st));
+    }
+    CT_CHECK_LAUNCH("scan");
+    if (total_host) {
+        CT_CUDA(cudaMemcpyAsync(total_host, sums + nb, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CT_CUDA(cudaStreamSynchronize(st));
+    }
+    return CT_OK;
+}
+
+static int check_tree(const ct_tree* t) {
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
+    if (t->max_depth + 2 > STK) return ct_fail(CT_ERR_ARG, "tree deeper than 126 levels for multi-result queries");
+    return CT_OK;
+}
+
+int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, int64_t* counts, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    k_boxes<false><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, counts,
+                                                                       nullptr, nullptr);
+    CT_CHECK_LAUNCH("count_boxes");
+    return CT_OK;
+}
+
+int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int64_t* offsets, int64_t* ii,
+                   int64_t* jj, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    k_boxes<true><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+                                                                      (int64_t*)offsets, ii, jj);
+    CT_CHECK_LAUNCH("write_boxes");
+    return CT_OK;
+}
+
+int ct_count_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, int64_t* counts, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    if (mode == 0) k_edges<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, counts, 0, 0, 0);
+    else k_edges<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, counts, 0, 0, 0);
+    CT_CHECK_LAUNCH("count_edges");
+    return CT_OK;
+}
+
+int ct_write_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int64_t* offsets, int64_t* ii,
+                   int64_t* jj, double* xy, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    if (mode == 0)
+        k_edges<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, (int64_t*)offsets, ii, jj,
+                                                          (double4*)xy);
+    else
+        k_edges<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, (int64_t*)offsets, ii, jj,
+                                                          (double4*)xy);
+    CT_CHECK_LAUNCH("write_edges");
+    return CT_OK;
+}
+
+size_t ct_sort_workspace_size(int64_t total) { return (size_t)(total > 0 ? total : 1) * 4 * 8 + 1024; }
+
+int ct_sort_intersections(const double* segs, int64_t n_segs, const int64_t* offsets, const int64_t* counts,
+                          const int64_t* ii, const int64_t* jj_in, const double* xy_in, int64_t total,
+                          int64_t* jj_out, double* xy_out, void* ws, size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (total == 0) return CT_OK;
+    if (!ws || ws_bytes < ct_sort_workspace_size(total)) return ct_fail(CT_ERR_WORKSPACE, "sort workspace too small");
+    unsigned long long* kA = (unsigned long long*)ws;
+    int64_t* iA = (int64_t*)(kA + total);
+    unsigned long long* kB = (unsigned long long*)(iA + total);
+    int64_t* iB = (int64_t*)(kB + total);
+    k_tkeys<<<grid_of(total, 256), 256, 0, st>>>((const double4*)segs, ii, (const double4*)xy_in, total, kA, iA);
+    k_segsort<<<(unsigned)n_segs, SORT_T, 0, st>>>(offsets, counts, n_segs, kA, iA, kB, iB, iB);
+    // iB now holds, per segment, the sorted source positions (segments of one
+    // result write them directly)
+    k_gather_results<<<grid_of(total, 256), 256, 0, st>>>(iB, total, jj_in, (const double4*)xy_in, jj_out,
+                                                          (double4*)xy_out);
+    CT_CHECK_LAUNCH("sort_intersections");
+    return CT_OK;
+}
+
+int ct_polygons_intersect(const double* va, const int64_t* fa, int32_t Ka, const double* vb, const int64_t* fb,
+                          int32_t Kb, const int64_t* ia, const int64_t* ib, int64_t n, uint8_t* out, void* stream) {
+    if (n == 0) return CT_OK;
+    k_sat<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>(va, fa, Ka, vb, fb, Kb, ia, ib, n, out);
+    CT_CHECK_LAUNCH("polygons_intersect");
+    return CT_OK;
+}
+
+int ct_area_of_intersection(const double* va, const int64_t* fa, int32_t Ka, const double* vb, const int64_t* fb,
+                            int32_t Kb, const int64_t* ia, const int64_t* ib, int64_t n, double* out,
+                            unsigned int* error_word, void* stream) {
+    if (n == 0) return CT_OK;
+    k_clip_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>(va, fa, Ka, vb, fb, Kb, ia, ib, n, out,
+                                                                    error_word);
+    CT_CHECK_LAUNCH("area_of_intersection");
+    return CT_OK;
+}
+
+int ct_box_area_of_intersection(const double* boxes, const double* vb, const int64_t* fb, int32_t Kb,
+                                const int64_t* ibox, const int64_t* iface, int64_t n, double* out,
+                                unsigned int* error_word, void* stream) {
+    if (n == 0) return CT_OK;
+    k_box_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>((const double4*)boxes, vb, fb, Kb, ibox, iface, n,
+                                                                   out, error_word);
+    CT_CHECK_LAUNCH("box_area_of_intersection");
+    return CT_OK;
+}
+
+int ct_compact_pairs(const double* area, const uint8_t* flag, int64_t n, const int64_t* ii, const int64_t* jj,
+                     int64_t* ii_out, int64_t* jj_out, double* area_out, void* ws, size_t ws_bytes,
+                     int64_t* total_host, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n == 0) {
+        if (total_host) *total_host = 0;
+        return CT_OK;
+    }
+    size_t scan_ws = ct_scan_workspace_size(n);
+    if (!ws || ws_bytes < scan_ws + 2 * (size_t)n * sizeof(int64_t))
+        return ct_fail(CT_ERR_WORKSPACE, "compaction workspace too small");
+    int64_t* keep = (int64_t*)ws;
+    int64_t* pos = keep + n;
+    void* sws = pos + n;
+    k_keep<<<grid_of(n, 256), 256, 0, st>>>(area, flag, n, keep);
+    int s = ct_exclusive_scan(keep, n, pos, sws, scan_ws, total_host, stream);
+    if (s) return s;
+    k_compact<<<grid_of(n, 256), 256, 0, st>>>(keep, pos, n, ii, jj, area, ii_out, jj_out, area_out);
+    CT_CHECK_LAUNCH("compact");
+    return CT_OK;
+}
+
+size_t ct_compact_workspace_size(int64_t n) {
+    return ct_scan_workspace_size(n) + 2 * (size_t)(n > 0 ? n : 1) * sizeof(int64_t);
+}
+
+int ct_barycentric_weights(const ct_tree* t, const double* points, const int64_t* face_indices, int64_t n,
+                           double tolerance, double* weights, void* stream) {
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (n == 0) return CT_OK;
+    int K = t->n_max_vert;
+    int KW = K > 3 ? K : 3;
+    k_barycentric<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>((const double2*)points, face_indices, n,
+                                                                      t->vertices, t->elements, K, KW, tolerance,
+                                                                      weights);
+    CT_CHECK_LAUNCH("barycentric");
+    return CT_OK;
+}
+
+int ct_node_bounds(const int64_t* child, const double* Lmax, const double* Rmin, const uint8_t* dim, int64_t n_nodes,
+                   const double* bbox_host4, int64_t* parent_ws, double* out, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_nodes <= 0) return CT_OK;
+    CT_CUDA(cudaMemsetAsync(parent_ws, 0xff, sizeof(int64_t) * n_nodes, st));
+    k_parents<<<grid_of(n_nodes, 256), 256, 0, st>>>(child, n_nodes, parent_ws);
+    double4 b = make_double4(bbox_host4[0], bbox_host4[1], bbox_host4[2], bbox_host4[3]);
+    k_node_bounds<<<grid_of(n_nodes, 256), 256, 0, st>>>(child, Lmax, Rmin, dim, parent_ws, n_nodes, b,
+                                                          (double4*)out);
+    CT_CHECK_LAUNCH("node_bounds");
+    return CT_OK;
+}
+
+int ct_validate_node_bounds(const int64_t* child, const int64_t* ptr, const int64_t* size, int64_t n_nodes,
+                            const int64_t* bb_indices, const double* bb_coords, const double* node_bounds,
+                            uint8_t* valid, void* stream) {
+    if (n_nodes <= 0) return CT_OK;
+    k_validate_bounds<<<grid_of(n_nodes, 256), 256, 0, (cudaStream_t)stream>>>(
+        child, ptr, size, bb_indices, bb_coords, (const double4*)node_bounds, n_nodes, valid);
+    CT_CHECK_LAUNCH("validate_node_bounds");
+    return CT_OK;
+}
+
+}  // extern "C"

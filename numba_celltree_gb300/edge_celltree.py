@@ -9,7 +9,7 @@ from typing import Optional
 import numpy as np
 
 from . import _device, _lib
-from .cast import cast_vertices, is_cuda_tensor
+from .cast import cast_edges, cast_vertices, is_cuda_tensor
 from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, validate_elements
 from .constants import MIN_TOLERANCE, TOLERANCE_FACTOR
 
@@ -83,3 +83,19 @@ class EdgeCellTree2d(CellTree2dBase):
         )
         t.raise_on_device_error()
         return out if cuda_in else out.cpu().numpy()
+
+    def intersect_edges(self, edge_coords):
+        """
+        Find the tree edges intersected by each edge (edge_celltree.py:114-146):
+        ``(edge_indices, tree_edge_indices, intersection_xy)``, each edge's
+        results ordered by distance along it.
+        """
+        cuda_in = is_cuda_tensor(edge_coords)
+        e = cast_edges(edge_coords)
+        t = self._tree
+        e_d = _device.to_device(e, _device.torch().float64, t.device)
+        ii, jj, xy = t.locate_edges(e_d, 0)
+        xy0 = xy[:, 0].contiguous()
+        if cuda_in:
+            return ii, jj, xy0
+        return ii.cpu().numpy(), jj.cpu().numpy(), xy0.cpu().numpy()

@@ -1,0 +1,251 @@
+"""Multi-result queries, pair kernels, barycentric weights and node-bound
+diagnostics on the GPU against the upstream fixtures and the oracle.
+Indices must be identical (and in the same order); float outputs are computed
+in the upstream evaluation order and must be identical too."""
+
+import numpy as np
+import pytest
+
+from meshes import GOLDEN, meshes
+from numba_celltree_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+G = np.load(GOLDEN / "golden_trees.npz")
+
+
+def same(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    if a.dtype.kind == "f":
+        assert np.array_equal(a, b, equal_nan=True)
+    else:
+        assert np.array_equal(a, b)
+
+
+def case(i):
+    p = f"c{i}_"
+    return {k[len(p):]: G[k] for k in G.files if k.startswith(p)}
+
+
+@pytest.mark.parametrize("i", range(int(G["n_cases"])))
+def test_queries_match_upstream_fixtures(i):
+    from numba_celltree_gb300 import CellTree2d
+
+    c = case(i)
+    nb, cpl = (int(x) for x in c["params"])
+    t = CellTree2d(c["vertices"], c["faces_in"], -1, nb, cpl)
+    bi, bj = t.locate_boxes(c["boxes"])
+    same(bi, c["box_i"])
+    same(bj, c["box_j"])
+    for got, key in zip(t.intersect_boxes(c["boxes"]), ("ibox_i", "ibox_j", "ibox_a")):
+        same(got, c[key])
+    for got, key in zip(t.intersect_edges(c["edges"]), ("edge_i", "edge_j", "edge_xy")):
+        same(got, c[key])
+    for got, key in zip(t.intersect_faces(c["qv"], c["qf"], -1), ("face_i", "face_j", "face_a")):
+        same(got, c[key])
+    qf = c["qf"].astype(np.int64).copy()
+    for got, key in zip(t.locate_faces(c["qv"].copy(), qf), ("lface_i", "lface_j")):
+        same(got, c[key])
+    for prec in ("fp32", "fp64"):
+        t.precision = prec
+        for got, key in zip(t.compute_barycentric_weights(c["points"]), ("bary_i", "bary_w")):
+            same(got, c[key])
+    same(t.node_bounds, c["node_bounds"])
+    same(t.validate_node_bounds(), c["node_valid"])
+
+
+@pytest.mark.parametrize("i", range(int(G["n_edge_cases"])))
+def test_edge_tree_matches_upstream_fixtures(i):
+    from numba_celltree_gb300 import EdgeCellTree2d
+
+    p = f"e{i}_"
+    c = {k[len(p):]: G[k] for k in G.files if k.startswith(p)}
+    nb, cpl = (int(x) for x in c["params"])
+    t = EdgeCellTree2d(c["vertices"], c["edges"], nb, cpl)
+    for f in ("child", "Lmax", "Rmin", "ptr", "size", "dim"):
+        same(t.nodes[f], c["node_" + f])
+    same(t.bb_indices, c["bb_indices"])
+    same(t.bb_coords, c["bb_coords"])
+    same(t.locate_points(c["points"]), c["locate"])
+    for got, key in zip(t.intersect_edges(c["segs"]), ("edge_i", "edge_j", "edge_xy")):
+        same(got, c[key])
+
+
+@pytest.mark.parametrize("name", ["tri150", "mixed60", "utm80", "rot_quads"])
+def test_queries_match_oracle(oracle, name):
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = meshes()[name]
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    lo, hi = xy.min(0), xy.max(0)
+    span = float((hi - lo).max())
+    boxes = syn.random_boxes(3000, lo, hi, 0.001 * span, 0.05 * span, seed=1)
+    for a, b in zip(g.locate_boxes(boxes), o.locate_boxes(boxes)):
+        same(a, b)
+    for a, b in zip(g.intersect_boxes(boxes), o.intersect_boxes(boxes)):
+        same(a, b)
+    segs = np.concatenate([syn.random_segments(400, lo, hi, seed=2), xy[f[:200, :2]], xy[f[:50, [1, 2]]]])
+    for a, b in zip(g.intersect_edges(segs), o.intersect_edges(segs)):
+        same(a, b)
+    # a second mesh for face queries (shifted, so faces straddle tree faces)
+    qxy, qf = syn.triangle_mesh(25, seed=9, extent=tuple(hi - lo), offset=tuple(lo + 0.013 * span))
+    for a, b in zip(g.intersect_faces(qxy, qf, -1), o.intersect_faces(qxy, qf, -1)):
+        same(a, b)
+    qf1 = qf.copy()
+    qf2 = qf.copy()
+    for a, b in zip(g.locate_faces(qxy, qf1), o.locate_faces(qxy, qf2)):
+        same(a, b)
+    same(qf1, qf2)
+    pts = np.concatenate([syn.uniform_points(5000, lo, hi, seed=3, margin=0.02), xy[:300],
+                          syn.near_edge_points(xy, f[:, :3], 500, dist=1e-9 * span, seed=4)])
+    for a, b in zip(g.compute_barycentric_weights(pts), o.compute_barycentric_weights(pts)):
+        same(a, b)
+    same(g.node_bounds, o.node_bounds)
+    same(g.validate_node_bounds(), o.validate_node_bounds())
+
+
+def test_edge_tree_matches_oracle(oracle):
+    from numba_celltree_gb300 import EdgeCellTree2d
+
+    xy, f = syn.triangle_mesh(60, seed=12)
+    e = np.unique(np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1), axis=0)
+    for nb, cpl in [(4, 2), (2, 1), (7, 3)]:
+        g = EdgeCellTree2d(xy, e, nb, cpl)
+        o = oracle.OracleEdgeCellTree2d(xy, e, nb, cpl)
+        for fld in ("child", "Lmax", "Rmin", "ptr", "size", "dim"):
+            same(g.nodes[fld], o.nodes[fld])
+        same(g.bb_indices, o.bb_indices)
+        pts = np.concatenate([syn.uniform_points(4000, (0, 0), (1, 1), seed=5), xy,
+                              0.5 * (xy[e[:, 0]] + xy[e[:, 1]]), 0.3 * xy[e[:, 0]] + 0.7 * xy[e[:, 1]]])
+        same(g.locate_points(pts), o.locate_points(pts))
+        same(g.locate_points(pts, 1e-3), o.locate_points(pts, 1e-3))
+        segs = np.concatenate([syn.random_segments(300, (0, 0), (1, 1), seed=6), xy[e[:100]]])
+        for a, b in zip(g.intersect_edges(segs), o.intersect_edges(segs)):
+            same(a, b)
+
+
+def test_long_segments_sorted(oracle):
+    """Segments crossing thousands of cells: the per-segment sort runs in
+    global memory (more than 1024 results per segment)."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(300, seed=13)
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    segs = np.array([[[0.0, 0.0], [1.0, 1.0]], [[0.0, 1.0], [1.0, 0.0]], [[0.0, 0.5], [1.0, 0.5]],
+                     [[0.5, 0.0], [0.5, 1.0]], [[0.7, 0.7], [0.7, 0.7]]])
+    got = g.intersect_edges(segs)
+    exp = o.intersect_edges(segs)
+    assert np.bincount(got[0]).max() > 1024
+    for a, b in zip(got, exp):
+        same(a, b)
+
+
+def test_known_answers():
+    """test_celltree.py:333-420, 528-618, 631-639 through the GPU classes."""
+    from numba_celltree_gb300 import CellTree2d
+
+    nodes = np.array([[0.0, 0.0], [0.0, 2.0], [2.0, 0.0], [2.0, 2.0], [4.0, 0.0], [4.0, 2.0], [6.0, 0.0],
+                      [6.0, 2.0], [0.0, 4.0], [2.0, 4.0], [4.0, 4.0], [6.0, 4.0]])
+    faces = np.array([[0, 8, 9, 5, 2], [9, 11, 7, 5, -1], [4, 7, 6, -1, -1]], dtype=np.intc)
+    t = CellTree2d(nodes, faces, -1, n_buckets=2, cells_per_leaf=1)
+    boxes = np.array([[1.0, 2.0, 1.0, 2.0], [4.0, 5.0, 0.0, 1.0], [4.0, 5.0, 2.0, 3.0], [-1.0, 0.0, 0.0, 4.0],
+                      [6.0, 8.0, 0.0, 4.0], [0.0, 6.0, -1.0, 0.0], [0.0, 6.0, 4.0, 5.0]])
+    i, j = t.locate_boxes(boxes)
+    assert np.array_equal(i, [0, 1, 2]) and np.array_equal(j, [0, 2, 1])
+    i, j, _ = t.intersect_boxes(boxes)
+    assert np.array_equal(i, [0, 1, 2]) and np.array_equal(j, [0, 2, 1])
+    edges = np.array([[[1.0, 1.0], [2.0, 2.0]], [[4.0, 3.0], [5.0, 4.0]], [[5.0, 0.0], [6.0, 1.0]],
+                      [[-2.0, -1.0], [0.0, 1.0]], [[-2.0, -1.0], [-2.0, -1.0]]])
+    i, j, xy = t.intersect_edges(edges)
+    assert np.array_equal(i, [0, 1, 2]) and np.array_equal(j, [0, 1, 2]) and np.allclose(xy, edges[:3])
+    i, j, xy = t.intersect_edges(edges[:, ::-1])
+    assert np.array_equal(i, [0, 1, 2]) and np.allclose(xy, edges[:3, ::-1])
+    nodes2 = np.array([[0.0, 0.0], [2.0, 0.0], [1.0, 2.0], [3.0, 2.0]])
+    t = CellTree2d(nodes2, np.array([[0, 1, 2], [1, 3, 2]]), -1)
+    idx, w = t.compute_barycentric_weights(np.array([[0.0, 0.0], [1.0, 1.0], [2.0, 1.0]]))
+    assert np.array_equal(idx, [0, 0, 1])
+    assert np.allclose(w, [[1.0, 0.0, 0.0], [0.25, 0.25, 0.5], [0.5, 0.25, 0.25]])
+    q = np.array([[0.0, 0.0], [2.0, 0.0], [2.0, 2.0], [0.0, 2.0], [4.0, 0.0], [4.0, 4.0]])
+    t = CellTree2d(q, np.array([[0, 1, 2, 3], [1, 4, 5, 2]]), -1)
+    idx, w = t.compute_barycentric_weights(np.array([[0.0, 0.0], [1.0, 1.0], [2.0, 1.0]]))
+    assert np.array_equal(idx, [0, 0, 0])
+    assert np.allclose(w, [[1, 0, 0, 0], [0.25, 0.25, 0.25, 0.25], [0, 0.5, 0.5, 0]])
+    d = np.load(GOLDEN / "reference_data.npz")
+    t = CellTree2d(d["voronoi_xy"], d["voronoi"], -1)
+    nbnd = t.node_bounds
+    xmin, xmax, ymin, ymax = t.bbox
+    assert nbnd.shape == (len(t.nodes), 4)
+    assert (nbnd[:, 0] >= xmin).all() and (nbnd[:, 1] <= xmax).all()
+    assert (nbnd[:, 2] >= ymin).all() and (nbnd[:, 3] <= ymax).all()
+    assert t.validate_node_bounds().all()
+    t.nodes[71]["Lmax"] = -0.02319655  # upstream issue #2 (test_celltree.py:613-618)
+    assert not t.validate_node_bounds()[73]
+    t = CellTree2d(d["xy"], d["triangles"], -1, n_buckets=4)
+    dl = t.to_dict_of_lists()
+    assert list(dl.keys()) == list(range(len(t.nodes)))
+    assert max(len(v) for v in dl.values()) == 2
+    centroids = d["xy"][d["triangles"]].mean(axis=1)
+    assert np.array_equal(t.locate_points(centroids), np.arange(len(centroids)))
+
+
+def test_edge_tree_known_answers():
+    """test_edgecelltree.py:12-92 through the GPU class."""
+    from numba_celltree_gb300 import EdgeCellTree2d
+
+    v = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0], [2.0, 1.0]])
+    e = np.array([[0, 1], [1, 2], [2, 3]], dtype=np.int32)
+    t = EdgeCellTree2d(v, e)
+    assert t.vertices.shape == (4, 2) and t.edges.shape == (3, 2) and t.nodes.shape == (3,)
+    assert t.n_buckets == 4 and t.cells_per_leaf == 2
+    assert np.array_equal(t.bb_indices, [0, 1, 2])
+    assert np.allclose(t.bb_coords, [[0, 1, 0, 0], [1, 2, 0, 0], [2, 2, 0, 1]], atol=1e-9)
+    assert np.allclose(t.bbox, [0.0, 2.0, 0.0, 1.0], atol=1e-9)
+    assert np.array_equal(t.locate_points(np.array([[0.5, 0.0], [1.5, 0.0], [2.0, 0.5]])), [0, 1, 2])
+    assert np.array_equal(t.locate_points(np.array([[0.5, 0.5], [1.5, 0.5], [2.0, 0.5]])), [-1, -1, 2])
+    vv = np.array([[171805.657000002, 563516.366], [171889.594000001, 563437.333000001]])
+    t2 = EdgeCellTree2d(vv, np.array([[0, 1]]))
+    p = np.array([[171882.49385095935, 563444.0183244612]])
+    assert np.array_equal(t2.locate_points(p, tolerance=1e-8), [0])
+    assert np.array_equal(t2.locate_points(p, tolerance=1e-9), [0])
+    segs = np.array([[[1.0, -1.0], [1.0, 1.0]], [[3.0, 1.0], [-1.0, -1.0]], [[0.0, -1.0], [0.0, 1.0]],
+                     [[-2.0, -1.0], [-3.0, -1.0]]])
+    i, j, xy = t.intersect_edges(segs)
+    assert np.array_equal(i, [0, 1, 1]) and np.array_equal(j, [0, 2, 1])
+    assert np.allclose(xy, [[1.0, 0.0], [2.0, 0.5], [1.0, 0.0]], atol=1e-9)
+
+
+def test_errors_and_casting():
+    """test_celltree.py:95-164: casting, shape and bound errors."""
+    from numba_celltree_gb300 import CellTree2d
+
+    nodes2 = [[0.0, 0.0], [2.0, 0.0], [1.0, 2.0], [3.0, 2.0]]
+    faces2 = [[0, 1, 2], [1, 3, 2]]
+    CellTree2d(nodes2, faces2, -1)
+    CellTree2d(np.array(nodes2, dtype=np.float32), np.array(faces2, dtype=np.int32), -1)
+    t = CellTree2d(np.array(nodes2), np.array([[0, 1, 2, -999], [1, 3, 2, -999]]), -999)
+    assert t.faces[0, -1] == -1 and t.faces[1, -1] == -1
+    with pytest.raises(ValueError):
+        CellTree2d([(1, 2, 3), (3, 4, 5), (4, 5, 6)], faces2, -1)
+    with pytest.raises(ValueError):
+        CellTree2d(nodes2, [0, 1, 2, 1, 3, 2], -1)
+    with pytest.raises(ValueError):
+        CellTree2d(np.array(nodes2), np.array(faces2), -1, cells_per_leaf=-1)
+    with pytest.raises(ValueError):
+        CellTree2d(np.array(nodes2), np.array(faces2), -1, n_buckets=0)
+    with pytest.raises(ValueError):
+        CellTree2d(np.array(nodes2), np.array([[0, 1, 7], [1, 3, 2]]), -1)  # index out of range
+    t = CellTree2d(nodes2, faces2, -1)
+    with pytest.raises(ValueError):
+        t.locate_points([(1, 2, 3), (3, 4, 5), (4, 5, 6)])
+    with pytest.raises(ValueError):
+        t.intersect_faces([(1, 2, 3), (3, 4, 5), (4, 5, 6)], faces2, -1)
+    with pytest.raises(ValueError):
+        t.locate_boxes(np.array([0.0, 1.0, 2.0, 3.0]))
+    with pytest.raises(ValueError):
+        t.intersect_boxes(np.array([0.0, 1.0, 2.0, 3.0]))
+    with pytest.raises(ValueError):
+        t.intersect_edges(np.array([[0.0, 1.0], [2.0, 3.0]]))
