@@ -73,11 +73,11 @@ typedef struct ct_tree {
     void* nodes_f32;          /* n_nodes x 16 B: float Lmax, float Rmin, int a, int b */
     void* nodes_f64;          /* n_nodes x 16 B: double Lmax, double Rmin */
     void* poly_f64;           /* n_elements x n_max_vert x 16 B, leaf (bb_indices) order */
-    void* poly_f32;           /* n_elements x n_max_vert x 8 B, leaf order, relative to origin */
+    void* poly_f32;           /* n_elements x ct_poly32_stride(n_max_vert) x 16 B, leaf order, local frame */
     uint8_t* poly_len;        /* n_elements: polygon length (polygon_length geometry_utils.py:72-79) */
     uint8_t* poly_len32;      /* n_elements: length after removing repeated consecutive vertices */
     double origin[2];         /* host: origin of the float32 frame (centre of bbox) */
-    float vmax;               /* host: max |vertex - origin| (inf-norm), set by ct_pack_tree */
+    float vmax;               /* host: unused (kept for layout stability) */
     float abs_eps;            /* host: float64 rounding scale of absolute coordinates */
     unsigned int* error_word; /* device: one uint32, OR-ed CT_DEVERR_* bits */
 } ct_tree;
@@ -159,6 +159,10 @@ int ct_build_tree_noalloc(const double* bb_coords, int64_t n_elements, int32_t n
                           int64_t node_capacity, int64_t* bb_indices, int64_t* n_nodes_host, int32_t* max_depth_host,
                           void* stream);
 
+/* float4 units of one cell in ct_tree.poly_f32: the cell's first vertex as
+ * float hi/lo pairs, then the other vertices relative to it (float2). */
+int ct_poly32_stride(int32_t n_max_vert);
+
 /* Fills the packed traversal arrays of `tree` (nodes_f32, nodes_f64,
  * poly_f64, poly_f32, poly_len, poly_len32) and its origin / vmax / abs_eps.
  * `tree` is updated in place (host struct).  Synchronises the stream. */
@@ -174,6 +178,31 @@ int ct_pack_tree(ct_tree* tree, void* stream);
 /* locate_points query.py:110-117 (locate_point 63-107).  out: n (int64). */
 int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t mode,
                      int64_t* out, void* stream);
+
+/* Batched float32 form of locate_points (query.py:110-117): queries are
+ * ordered along a Morton curve over the tree bbox (radix sort by the top
+ * sort_bits of a 24-bit key, 4096 x 4096 grid; sort_bits 0 = input order,
+ * else 8, 16 or 24), located by a float32 pass that collects candidate cells
+ * for queries whose float32 leaf test is ambiguous, then finished by float64
+ * tests of those candidates (and a float64 traversal for the rare query with
+ * too many candidates).  Output identical to ct_locate_points.
+ * Workspace: ct_locate_workspace_size(n, sort_bits) bytes. */
+size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits);
+int ct_locate_points_batched(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t sort_bits,
+                             int64_t* out, void* workspace, size_t workspace_bytes, void* stream);
+/* The three stages of ct_locate_points_batched, callable separately (same
+ * arguments and workspace): order, float32 pass, float64 pass over the
+ * deferred queries.  ct_locate_deferred_count reports what the last float32
+ * pass deferred (synchronises). */
+int ct_locate_bin(const ct_tree* tree, const double* points, int64_t n, int32_t sort_bits, void* workspace,
+                  size_t workspace_bytes, void* stream);
+int ct_locate_fast(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t sort_bits,
+                   int64_t* out, void* workspace, size_t workspace_bytes, void* stream);
+int ct_locate_exact(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t sort_bits,
+                    int64_t* out, void* workspace, size_t workspace_bytes, void* stream);
+/* counts_host3: queries sent to the overflow pass, queries with candidate
+ * records, candidate pairs of the last float32 pass (synchronises). */
+int ct_locate_deferred_count(const void* workspace, int64_t n, int32_t sort_bits, int64_t* counts_host3, void* stream);
 
 /* locate_points_on_edge query.py:167-174 (locate_point_on_edge 121-164). */
 int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,

@@ -91,8 +91,15 @@ SIGNATURES = {
         [_P, _I64, _I32, _I64, _P, _P, _P, _P, _P, _P, _I64, _P, ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P],
     ),
     "ct_pack_tree": (ctypes.c_int, [ctypes.POINTER(CtTree), _P]),
+    "ct_poly32_stride": (ctypes.c_int, [_I32]),
     "ct_locate_points": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P]),
     "ct_locate_points_on_edge": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _P, _P]),
+    "ct_locate_workspace_size": (_SZ, [_I64, _I32]),
+    "ct_locate_points_batched": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P, _SZ, _P]),
+    "ct_locate_bin": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _I32, _P, _SZ, _P]),
+    "ct_locate_fast": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P, _SZ, _P]),
+    "ct_locate_exact": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P, _SZ, _P]),
+    "ct_locate_deferred_count": (ctypes.c_int, [_P, _I64, _I32, ctypes.POINTER(_I64), _P]),
     "ct_scan_workspace_size": (_SZ, [_I64]),
     "ct_exclusive_scan": (ctypes.c_int, [_P, _I64, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
     "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P]),

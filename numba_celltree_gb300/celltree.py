@@ -38,9 +38,11 @@ class CellTree2d(CellTree2dBase):
     Results are identical to the upstream package: the same ``nodes`` and
     ``bb_indices`` arrays, the same cells for every query.  Queries given numpy
     arrays return numpy arrays; queries given CUDA tensors return CUDA tensors.
-    ``precision`` selects the point-location form: ``"fp32"`` (float32
-    traversal and leaf filter with exact float64 fallback, the default) or
-    ``"fp64"`` (plain float64); both return identical indices.
+    ``precision`` selects the point-location form, all returning identical
+    indices: ``"fp32"`` (default: queries binned for coherent traversal, a
+    float32 pass that defers ambiguous leaf tests, a float64-exact pass over
+    the deferred ones), ``"fp32-inline"`` (one float32 kernel with in-line
+    float64 fallbacks) or ``"fp64"`` (plain float64).
     """
 
     _elements_name = "faces"
@@ -82,14 +84,7 @@ class CellTree2d(CellTree2dBase):
         """Enqueue locate_points on the current stream for device-resident
         float64 points (n, 2) and an int64 output (n,); no synchronisation and
         no error-word check (for pipelines and timing loops)."""
-        mode = _lib.CT_MODE_FP64 if precision == "fp64" else _lib.CT_MODE_FP32
-        _lib.check(
-            _lib.load().ct_locate_points(
-                ctypes.byref(self._tree.desc), _device.ptr(points_dev), int(points_dev.shape[0]), float(tolerance),
-                mode, _device.ptr(out_dev), _device.stream(),
-            ),
-            "locate_points",
-        )
+        self._tree.locate(points_dev, out_dev, tolerance, precision)
 
     def locate_points(self, points, tolerance: Optional[float] = None):
         """
@@ -107,14 +102,8 @@ class CellTree2d(CellTree2dBase):
         p_d = _device.to_device(points, torch.float64, t.device)
         n = int(p_d.shape[0])
         out = _device.empty((n,), torch.int64, t.device)
-        mode = _lib.CT_MODE_FP64 if self.precision == "fp64" else _lib.CT_MODE_FP32
         t.reset_error()
-        _lib.check(
-            _lib.load().ct_locate_points(
-                ctypes.byref(t.desc), _device.ptr(p_d), n, tol, mode, _device.ptr(out), _device.stream()
-            ),
-            "locate_points",
-        )
+        t.locate(p_d, out, tol, self.precision)
         t.raise_on_device_error()
         return _as_output(out, cuda_in)
 

@@ -86,7 +86,7 @@ class _GpuTree:
         self.nodes_f32 = _device.empty((max(nn, 1), 4), torch.float32, device)
         self.nodes_f64 = _device.empty((max(nn, 1), 2), torch.float64, device)
         self.poly_f64 = _device.empty((max(n, 1), K, 2), torch.float64, device)
-        self.poly_f32 = _device.empty((max(n, 1), K, 2), torch.float32, device)
+        self.poly_f32 = _device.empty((max(n, 1), lib.ct_poly32_stride(K), 4), torch.float32, device)
         self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
         self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
         self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
@@ -140,6 +140,40 @@ class _GpuTree:
             if err & _lib.DEVERR_LOOP:
                 bits.append("bounded loop gave up")
             raise _lib.CellTreeError("device error: " + ", ".join(bits))
+
+    # -- point location ---------------------------------------------------------
+    @staticmethod
+    def auto_sort_bits(n_points: int) -> int:
+        """Bits of the 24-bit Morton key the batched float32 form sorts the
+        queries by: none for small batches (the sort costs more than the
+        divergence it removes), else all 24 (a 4096 x 4096 grid)."""
+        return 0 if n_points < (1 << 16) else 24
+
+    def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None) -> None:
+        """Enqueue point location on the current stream (no synchronisation)."""
+        lib = _lib.load()
+        n = int(points_d.shape[0])
+        if precision == "fp32":
+            g = self.auto_sort_bits(n) if sort_bits is None else int(sort_bits)
+            need = int(lib.ct_locate_workspace_size(n, g))
+            ws = getattr(self, "_locate_ws", None)
+            if ws is None or ws.numel() < need:
+                torch = _device.torch()
+                self._locate_ws = ws = _device.empty((need,), torch.uint8, self.device)
+            _lib.check(
+                lib.ct_locate_points_batched(
+                    ctypes.byref(self.desc), _device.ptr(points_d), n, float(tolerance), g, _device.ptr(out_d),
+                    _device.ptr(ws), int(ws.numel()), _device.stream(),
+                ),
+                "locate_points",
+            )
+            return
+        mode = _lib.CT_MODE_FP64 if precision == "fp64" else _lib.CT_MODE_FP32
+        _lib.check(
+            lib.ct_locate_points(ctypes.byref(self.desc), _device.ptr(points_d), n, float(tolerance), mode,
+                                 _device.ptr(out_d), _device.stream()),
+            "locate_points",
+        )
 
     # -- multi-result helpers ------------------------------------------------
     def scan(self, counts):

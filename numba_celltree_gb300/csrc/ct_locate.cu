@@ -1,0 +1,732 @@
+// ct_locate.cu -- the batched point-location pipeline (locate_points
+// query.py:63-117), float32 form.
+//
+//   1. order    queries are sorted along a Morton curve over the tree bbox
+//               (LSD radix sort of 24-bit keys with 8-bit digits: per-block
+//               shared-memory histograms, one scan, stable block-local
+//               scatter), so consecutive threads traverse nearly the same path;
+//   2. fast     float32 traversal (node bounds inside their error band are
+//               re-decided in-line with one float64 compare) and the float32
+//               leaf filter in each cell's local frame.  A polygon the filter
+//               cannot decide (UNSURE) becomes a candidate and the traversal
+//               continues, in upstream order, until a polygon is surely hit or
+//               the traversal ends.  Queries without candidates are final;
+//               the others get a record and their candidates are appended to
+//               a dense (record, ordinal, polygon) list;
+//   3. pip      the exact float64 point_in_polygon_or_on_edge of every
+//               candidate pair, one pair per thread (full warps);
+//               a true result lowers the record's first-true ordinal;
+//   4. resolve  per record: the first candidate whose exact test is true,
+//               else the surely-hit cell of the fast pass, else -1 -- which is
+//               exactly upstream's first hit, since node decisions do not
+//               depend on polygon results;
+//   5. exact    queries with more than CMAX candidates (or beyond the record
+//               capacity) run the float32-with-float64-fallback traversal.
+//
+// Query order does not affect any result (queries are independent), so the
+// binning is safe.  The traversal stack lives in shared memory.
+#include <cfloat>
+#include <cmath>
+
+#include "ct_common.cuh"
+#include "ct_internal.h"
+#include "ct_locf.cuh"
+
+extern "C" int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* ws, size_t ws_bytes,
+                                 int64_t* total_host, void* stream);
+extern "C" size_t ct_scan_workspace_size(int64_t n);
+
+namespace ctl {
+
+constexpr int CMAX = 6;             // candidates kept per query
+constexpr int LOC_THREADS = 256;
+constexpr int GRID_STRIDE = 152 * 8;
+
+struct TreeL {
+    const float4* nf;
+    const double2* nd;
+    const double2* poly;
+    const float4* polyf;
+    const uint8_t* plen;
+    const uint8_t* plen32;
+    const int64_t* bbi;
+    unsigned int* err;
+    int64_t n_nodes;
+    double ox, oy;
+    float dabs;
+    float bandG;  // error band of every float32 node bound: 2^-22 * max |bound - origin|
+    int K;
+    int S4;     // float4 units per cell in polyf
+    int stack;  // stack entries per thread (>= max_depth + 2)
+};
+
+struct Recs {
+    int* orig;                 // query index in the caller's order
+    int64_t* res;              // surely-hit cell of the fast pass or -1
+    unsigned long long* first; // (ordinal << 32 | polygon) of the first true candidate
+    int4* pairs;               // (record, ordinal, polygon, -)
+    int cap;
+};
+
+__device__ __forceinline__ int na(const float4& q) { return __float_as_int(q.z); }
+__device__ __forceinline__ int nbq(const float4& q) { return __float_as_int(q.w); }
+__device__ __forceinline__ float bandf(float x) { return fabsf(x) * 2.384185791015625e-07f + 1e-30f; }
+
+__device__ __forceinline__ unsigned lane_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// float32 value of (x - o) in the global frame and its error bound (no
+// float64 instruction): x split exactly into hi + lo, o = ohi + olo.
+__device__ __forceinline__ void to_frame(double x, float ohi, float olo, float* v, float* err, float* xh_out,
+                                         float* xl_out) {
+    float lo;
+    float hi = split_hi(x, &lo);
+    float t1 = hi - ohi, t2 = lo - olo, r = t1 + t2;
+    *v = r;
+    *err = 5.9604644775390625e-08f * (fabsf(t1) + fabsf(t2) + fabsf(r) + fabsf(lo) + fabsf(olo)) + 1e-30f;
+    *xh_out = hi;
+    *xl_out = lo;
+}
+
+// Warp-aggregated append of `idx` to a list.
+__device__ __forceinline__ void append(bool d, int idx, int* list, int* count) {
+    unsigned m = __ballot_sync(__activemask(), d);
+    if (!d) return;
+    int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    list[base + __popc(m & lane_lt())] = idx;
+}
+
+// Node step of the float32 traversal with in-line float64 re-decisions for
+// bounds inside their band (locate_point query.py:87-105).  Returns false on
+// stack overflow.
+__device__ __forceinline__ bool node_step(const TreeL& T, int* s, int B, int& sp, int v, const float4& q, float x,
+                                          float dx, const double2* __restrict__ pts, int i, int dim) {
+    float Lf = q.x, Rf = q.y;
+    float bL = dx, bR = dx;  // dx already holds the point's error plus the tree-wide bound band
+    float dl = x - Lf, dr = x - Rf;
+    bool left, right, have = false;
+    double2 nd;
+    double pd = 0.0;
+    if (dl > bL) left = false;
+    else if (-dl > bL) left = true;
+    else {
+        nd = T.nd[v];
+        double2 p2 = pts[i];
+        pd = dim ? p2.y : p2.x;
+        have = true;
+        left = pd <= nd.x;
+    }
+    if (dr > bR) right = true;
+    else if (-dr > bR) right = false;
+    else {
+        if (!have) {
+            nd = T.nd[v];
+            double2 p2 = pts[i];
+            pd = dim ? p2.y : p2.x;
+            have = true;
+        }
+        right = pd >= nd.y;
+    }
+    int child = na(q);
+    if (sp + 2 > T.stack) return false;
+    if (left && right) {
+        float aF = Lf - x, bF = x - Rf;
+        float bo = 2.0f * dx + 2.384185791015625e-07f * (fabsf(aF) + fabsf(bF)) + 1e-30f;
+        bool near_first;
+        if (fabsf(aF - bF) > bo) near_first = aF < bF;
+        else {
+            if (!have) {
+                nd = T.nd[v];
+                double2 p2 = pts[i];
+                pd = dim ? p2.y : p2.x;
+            }
+            near_first = (nd.x - pd) < (pd - nd.y);
+        }
+        if (near_first) {
+            s[(sp++) * B] = child;
+            s[(sp++) * B] = child + 1;
+        } else {
+            s[(sp++) * B] = child + 1;
+            s[(sp++) * B] = child;
+        }
+    } else if (left) {
+        s[(sp++) * B] = child;
+    } else if (right) {
+        s[(sp++) * B] = child + 1;
+    }
+    return true;
+}
+
+// Stage 2: float32 traversal with candidate collection.
+template <int KT>
+__global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __restrict__ pts,
+                                                      const int* __restrict__ order, int64_t n, float tolf, float ohx,
+                                                      float olx, float ohy, float oly, int64_t* __restrict__ out,
+                                                      Recs R, int* __restrict__ counters, int* __restrict__ ovf) {
+    extern __shared__ int stk[];
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = i < n;
+    int nc = 0;
+    int cand[CMAX];
+    bool overflow = false;
+    int64_t res = -1;
+    // queries are taken in the sorted order; oi is the query's own index
+    const int oi = active ? (order ? order[i] : (int)i) : 0;
+    if (active) {
+        double2 pp = pts[oi];
+        float px, py, dpx, dpy;
+        PtSplit P;
+        to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
+        to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+        dpx += T.bandG;
+        dpy += T.bandG;
+        const int B = blockDim.x;
+        int* s = stk + threadIdx.x;
+        int sp = 1;
+        s[0] = 0;
+        int budget = (int)min(T.n_nodes, (int64_t)INT32_MAX);
+        bool done = false;
+        while (sp > 0 && !done) {
+            if (--budget < 0) {
+                set_error(T.err, CT_DEVERR_LOOP);
+                break;
+            }
+            int v = s[(--sp) * B];
+            float4 q = T.nf[v];
+            int b = nbq(q);
+            if (b >= 0) {
+                int ptr = na(q);
+                for (int j = ptr; j < ptr + b; j++) {
+                    int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                                           (int)T.plen32[j])
+                                      : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                              (int)T.plen32[j]);
+                    if (r == LF_INSIDE) {
+                        res = T.bbi[j];
+                        done = true;
+                        break;
+                    }
+                    if (r == LF_UNSURE) {
+                        if (nc < CMAX) {
+                            cand[nc++] = j;
+                        } else {
+                            overflow = true;
+                            done = true;
+                            break;
+                        }
+                    }
+                }
+                continue;
+            }
+            int dim = -1 - b;
+            if (!node_step(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, oi, dim)) {
+                set_error(T.err, CT_DEVERR_STACK);
+                break;
+            }
+        }
+    }
+    if (active && !overflow && nc == 0) out[oi] = res;
+    // records for queries with candidates
+    bool want = active && !overflow && nc > 0;
+    unsigned m = __ballot_sync(0xffffffffu, want);
+    if (want) {
+        int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&counters[1], __popc(m));
+        base = __shfl_sync(m, base, leader);
+        int rec = base + __popc(m & lane_lt());
+        if (rec >= R.cap) {
+            overflow = true;  // no record left: the exact pass takes it
+        } else {
+            R.orig[rec] = oi;
+            R.res[rec] = res;
+            R.first[rec] = ~0ull;
+            int pb = atomicAdd(&counters[2], nc);
+            for (int c = 0; c < CMAX; c++)
+                if (c < nc) R.pairs[pb + c] = make_int4(rec, c, cand[c], 0);
+        }
+    }
+    append(active && overflow, oi, ovf, &counters[0]);
+}
+
+// Stage 3: exact float64 test of every candidate pair.
+__global__ void __launch_bounds__(LOC_THREADS) k_pip(TreeL T, const double2* __restrict__ pts, Recs R,
+                                                     const int* __restrict__ counters, double tol) {
+    int npairs = counters[2];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += gridDim.x * blockDim.x) {
+        int4 pr = R.pairs[t];
+        double2 pp = pts[R.orig[pr.x]];
+        int j = pr.z;
+        const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
+        int len = T.plen ? (int)T.plen[j] : T.K;
+        if (pip_or_edge(mkp(pp.x, pp.y), poly, len, tol))
+            atomicMin(&R.first[pr.x], ((unsigned long long)(unsigned)pr.y << 32) | (unsigned)j);
+    }
+}
+
+// Stage 4: first true candidate, else the fast pass's hit.
+__global__ void k_resolve(TreeL T, Recs R, const int* __restrict__ counters, int64_t* __restrict__ out) {
+    int nrec = min(counters[1], R.cap);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
+        unsigned long long f = R.first[r];
+        out[R.orig[r]] = (f != ~0ull) ? T.bbi[(int)(f & 0xffffffffull)] : R.res[r];
+    }
+}
+
+// Stage 5: overflow queries, float32 bands with float64 re-decisions.
+template <int KT>
+__global__ void __launch_bounds__(LOC_THREADS) k_exact(TreeL T, const double2* __restrict__ pts,
+                                                       const int* __restrict__ list,
+                                                       const int* __restrict__ counters, double tol, float tolf,
+                                                       float ohx, float olx, float ohy, float oly,
+                                                       int64_t* __restrict__ out) {
+    extern __shared__ int stk[];
+    const int B = blockDim.x;
+    int* s = stk + threadIdx.x;
+    int cnt = counters[0];
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
+        int i = list[t];
+        double2 pp = pts[i];
+        dpt p = mkp(pp.x, pp.y);
+        float px, py, dpx, dpy;
+        PtSplit P;
+        to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
+        to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+        dpx += T.bandG;
+        dpy += T.bandG;
+        int sp = 1;
+        s[0] = 0;
+        int64_t res = -1;
+        int64_t budget = T.n_nodes;
+        while (sp > 0) {
+            if (--budget < 0) {
+                set_error(T.err, CT_DEVERR_LOOP);
+                break;
+            }
+            int v = s[(--sp) * B];
+            float4 q = T.nf[v];
+            int b = nbq(q);
+            if (b >= 0) {
+                int ptr = na(q);
+                bool hit = false;
+                for (int j = ptr; j < ptr + b; j++) {
+                    int r = leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j]);
+                    if (r == LF_UNSURE) {
+                        const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
+                        int len = T.plen ? (int)T.plen[j] : T.K;
+                        r = pip_or_edge(p, poly, len, tol) ? LF_INSIDE : LF_OUTSIDE;
+                    }
+                    if (r == LF_INSIDE) {
+                        hit = true;
+                        res = T.bbi[j];
+                        break;
+                    }
+                }
+                if (hit) break;
+                continue;
+            }
+            int dim = -1 - b;
+            if (!node_step(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, i, dim)) {
+                set_error(T.err, CT_DEVERR_STACK);
+                break;
+            }
+        }
+        out[i] = res;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// query ordering: LSD radix sort of (Morton key, index) pairs
+// ---------------------------------------------------------------------------
+constexpr int RS_BLOCKS = 152 * 4;  // fixed grid (4 resident blocks per SM); each block owns a contiguous chunk
+constexpr int RS_T = 256;
+constexpr int RS_IPT = 16;  // keys per thread per tile of the scatter
+constexpr int RS_TILE = RS_T * RS_IPT;
+
+struct Grid {
+    float x0, y0, sx, sy;  // cell = floor((x - x0) * sx), 2^12 cells per axis
+};
+
+__device__ __forceinline__ unsigned spread12(unsigned v) {  // 12 bits -> even bit positions
+    v &= 0xfff;
+    v = (v | (v << 8)) & 0x00ff00ff;
+    v = (v | (v << 4)) & 0x0f0f0f0f;
+    v = (v | (v << 2)) & 0x33333333;
+    v = (v | (v << 1)) & 0x55555555;
+    return v;
+}
+
+__device__ __forceinline__ unsigned morton24(const Grid& g, double2 p) {
+    float lo;
+    float fx = (split_hi(p.x, &lo) - g.x0) * g.sx;
+    float fy = (split_hi(p.y, &lo) - g.y0) * g.sy;
+    unsigned bx = (fx > 0.0f) ? (unsigned)fminf(fx, 4095.0f) : 0u;  // NaN -> 0
+    unsigned by = (fy > 0.0f) ? (unsigned)fminf(fy, 4095.0f) : 0u;
+    return spread12(bx) | (spread12(by) << 1);
+}
+
+// Every sort kernel runs on RS_BLOCKS blocks; block b owns the chunk
+// [b * chunk, min((b + 1) * chunk, n)) of its input (chunk a multiple of
+// RS_TILE, so each chunk starts 16-byte aligned).  hist[d * RS_BLOCKS + b]
+// counts digit d in block b's chunk; its exclusive scan is where block b
+// writes its keys of digit d.
+
+// Keys of the queries and the histogram of the first digit.
+__global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, int64_t n, int64_t chunk, Grid g,
+                                                int shift, unsigned* __restrict__ key, int* __restrict__ idx,
+                                                int64_t* __restrict__ hist) {
+    __shared__ int h[RS_T / 32][256];
+    const int t = threadIdx.x, w = t >> 5;
+    for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
+    __syncthreads();
+    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    for (int64_t i = s + t; i < e; i += RS_T) {
+        unsigned k = morton24(g, pts[i]);
+        key[i] = k;
+        idx[i] = (int)i;
+        atomicAdd(&h[w][(k >> shift) & 255u], 1);
+    }
+    __syncthreads();
+    int c = 0;
+    for (int k = 0; k < RS_T / 32; k++) c += h[k][t];
+    hist[(int64_t)t * gridDim.x + blockIdx.x] = c;
+}
+
+// Histogram of one 8-bit digit per block chunk (warp-private counters).
+__global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* __restrict__ key, int64_t n, int64_t chunk,
+                                                   int shift, int64_t* __restrict__ hist) {
+    __shared__ int h[RS_T / 32][256];
+    const int t = threadIdx.x, w = t >> 5;
+    for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
+    __syncthreads();
+    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    int64_t ev = s + ((e - s) & ~(int64_t)3);  // end of the whole uint4 groups
+    for (int64_t i = s + 4 * t; i < ev; i += 4 * RS_T) {
+        uint4 k4 = *reinterpret_cast<const uint4*>(key + i);
+        atomicAdd(&h[w][(k4.x >> shift) & 255u], 1);
+        atomicAdd(&h[w][(k4.y >> shift) & 255u], 1);
+        atomicAdd(&h[w][(k4.z >> shift) & 255u], 1);
+        atomicAdd(&h[w][(k4.w >> shift) & 255u], 1);
+    }
+    for (int64_t i = ev + t; i < e; i += RS_T) atomicAdd(&h[w][(key[i] >> shift) & 255u], 1);
+    __syncthreads();
+    int c = 0;
+    for (int k = 0; k < RS_T / 32; k++) c += h[k][t];
+    hist[(int64_t)t * gridDim.x + blockIdx.x] = c;
+}
+
+// Scatter of one digit.  The block walks its chunk in tiles of RS_TILE
+// keys; a key's rank within its digit in the tile comes from a shared-memory
+// atomic (so equal digits of one tile may be permuted -- the order of the
+// queries only has to be coherent, every result is written by the query's
+// own index), the tile is regrouped by digit in shared memory and written
+// out in runs.
+__global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ iin,
+                                                      int64_t n, int64_t chunk, int shift,
+                                                      const int64_t* __restrict__ offs, unsigned* __restrict__ kout,
+                                                      int* __restrict__ iout) {
+    __shared__ int cur[256];    // output position of the digit's next key
+    __shared__ int cnt[256];    // digit counts of the tile
+    __shared__ int tbase[256];  // exclusive scan of cnt
+    __shared__ int wsum[RS_T / 32];
+    __shared__ unsigned sk[RS_TILE];
+    __shared__ int si[RS_TILE];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    cur[t] = (int)offs[(int64_t)t * gridDim.x + blockIdx.x];
+    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    for (int64_t base = s; base < e; base += RS_TILE) {
+        cnt[t] = 0;
+        __syncthreads();
+        unsigned key[RS_IPT];
+        int id[RS_IPT], rk[RS_IPT];
+#pragma unroll
+        for (int k = 0; k < RS_IPT; k++) {
+            int64_t i = base + k * RS_T + t;
+            bool v = i < e;
+            key[k] = v ? kin[i] : 0u;
+            id[k] = v ? iin[i] : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < RS_IPT; k++) rk[k] = (id[k] >= 0) ? atomicAdd(&cnt[(key[k] >> shift) & 255u], 1) : 0;
+        __syncthreads();
+        int c = cnt[t];
+        int x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[w] = x;
+        __syncthreads();
+        int pre = 0;
+        for (int ww = 0; ww < w; ww++) pre += wsum[ww];
+        tbase[t] = pre + x - c;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < RS_IPT; k++)
+            if (id[k] >= 0) {
+                int pos = tbase[(key[k] >> shift) & 255u] + rk[k];
+                sk[pos] = key[k];
+                si[pos] = id[k];
+            }
+        __syncthreads();
+        int m = (int)min((int64_t)RS_TILE, e - base);
+        for (int j = t; j < m; j += RS_T) {
+            unsigned kk = sk[j];
+            int dd = (int)((kk >> shift) & 255u);
+            int dst = cur[dd] + (j - tbase[dd]);
+            kout[dst] = kk;
+            iout[dst] = si[j];
+        }
+        __syncthreads();
+        cur[t] += c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct LocWS {
+    unsigned* keyA;
+    int* order;       // sorted position -> input index (idxA after the last pass)
+    unsigned* keyB;
+    int* idxB;
+    int* ovf;
+    Recs R;
+    int64_t* hist;
+    void* scan_ws;
+    size_t scan_bytes;
+    int* counters;  // [0] overflow, [1] records, [2] pairs
+};
+
+static int rec_cap_for(int64_t n) { return (int)std::min<int64_t>(n / 8 + 4096, (int64_t)INT32_MAX / 8); }
+
+static size_t carve_loc(void* ws, int64_t n, int32_t sort_bits, LocWS* L) {
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    size_t rc = (size_t)rec_cap_for(n);
+    size_t nh = (size_t)256 * RS_BLOCKS;
+    size_t off = 0;
+    char* base = (char*)ws;
+    auto take = [&](size_t b) {
+        char* p = base ? base + off : nullptr;
+        off += a256(b);
+        return p;
+    };
+    LocWS l;
+    bool sorted = sort_bits > 0;
+    l.keyA = (unsigned*)take(sorted ? 4 * nn : 16);
+    l.order = (int*)take(sorted ? 4 * nn : 16);
+    l.keyB = (unsigned*)take(sorted ? 4 * nn : 16);
+    l.idxB = (int*)take(sorted ? 4 * nn : 16);
+    l.ovf = (int*)take(4 * nn);
+    l.R.orig = (int*)take(4 * rc);
+    l.R.res = (int64_t*)take(8 * rc);
+    l.R.first = (unsigned long long*)take(8 * rc);
+    l.R.pairs = (int4*)take(16 * rc * CMAX);
+    l.R.cap = (int)rc;
+    l.hist = (int64_t*)take(8 * nh);
+    l.scan_bytes = ct_scan_workspace_size((int64_t)nh);
+    l.scan_ws = take(l.scan_bytes);
+    l.counters = (int*)take(64);
+    if (L) *L = l;
+    return off;
+}
+
+static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws_bytes, TreeL* T) {
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (n >= INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "at most 2^30 points per call");
+    if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
+    if (G != 0 && G != 8 && G != 16 && G != 24) return ct_fail(CT_ERR_ARG, "sort_bits must be 0, 8, 16 or 24");
+    if (!ws || ws_bytes < carve_loc(nullptr, n, G, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "locate workspace too small");
+    T->nf = (const float4*)t->nodes_f32;
+    T->nd = (const double2*)t->nodes_f64;
+    T->poly = (const double2*)t->poly_f64;
+    T->polyf = (const float4*)t->poly_f32;
+    T->plen = (t->n_max_vert == 3) ? nullptr : t->poly_len;
+    T->plen32 = t->poly_len32;
+    T->bbi = t->bb_indices;
+    T->err = t->error_word;
+    T->n_nodes = t->n_nodes;
+    T->ox = t->origin[0];
+    T->oy = t->origin[1];
+    T->dabs = t->abs_eps;
+    {
+        double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
+                            std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
+        if (!(F >= 0.0) || !std::isfinite(F)) F = 0.0;
+        T->bandG = (float)(F * 2.384185791015625e-07 * 1.0001) + 1e-30f;  // bounds are inside the bbox
+    }
+    T->K = t->n_max_vert;
+    T->S4 = poly32_stride(t->n_max_vert);
+    T->stack = t->max_depth + 2;
+    if (T->stack > 128) return ct_fail(CT_ERR_ARG, "tree deeper than 126 levels for the batched form");
+    return CT_OK;
+}
+
+template <int KT>
+static void smem_attr(size_t smem) {
+    if (smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_fast<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_exact<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+}
+
+static void origin_split(double o, float* hi, float* lo) {
+    *hi = (float)o;
+    *lo = (float)(o - (double)*hi);
+}
+
+}  // namespace ctl
+
+using namespace ctl;
+
+extern "C" {
+
+int ct_poly32_stride(int32_t K) { return poly32_stride(K); }
+
+size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits) {
+    if (sort_bits != 0 && sort_bits != 8 && sort_bits != 16 && sort_bits != 24) return 0;
+    return carve_loc(nullptr, n, sort_bits, nullptr);
+}
+
+// Stage 1: order the queries along a Morton curve over the tree bbox (4096 x
+// 4096 grid): the top `sort_bits` bits of the 24-bit key, LSD radix sort with
+// 8-bit digits, then one gather of the points.  No-op when sort_bits == 0.
+int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sort_bits, void* ws, size_t ws_bytes,
+                  void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeL T;
+    int s = make_tree(t, n, sort_bits, ws, ws_bytes, &T);
+    if (s) return s;
+    if (n == 0 || sort_bits == 0) return CT_OK;
+    LocWS L;
+    carve_loc(ws, n, sort_bits, &L);
+    Grid g;
+    double xmin = t->bbox[0], xmax = t->bbox[1], ymin = t->bbox[2], ymax = t->bbox[3];
+    double wx = xmax - xmin, wy = ymax - ymin;
+    g.x0 = (float)xmin;
+    g.y0 = (float)ymin;
+    g.sx = (wx > 0) ? (float)(4096.0 / wx) : 0.0f;
+    g.sy = (wy > 0) ? (float)(4096.0 / wy) : 0.0f;
+    int passes = sort_bits / 8;
+    // ping-pong so that the last pass writes the permutation into L.order
+    unsigned* kin = (passes & 1) ? L.keyB : L.keyA;
+    int* iin = (passes & 1) ? L.idxB : L.order;
+    unsigned* kout = (passes & 1) ? L.keyA : L.keyB;
+    int* iout = (passes & 1) ? L.order : L.idxB;
+    int64_t chunk = (n + RS_BLOCKS - 1) / RS_BLOCKS;
+    chunk = (chunk + RS_TILE - 1) / RS_TILE * RS_TILE;
+    const int64_t nh = (int64_t)256 * RS_BLOCKS;
+    for (int pss = 0; pss < passes; pss++) {
+        int shift = 24 - sort_bits + 8 * pss;
+        if (pss == 0)
+            k_keys<<<RS_BLOCKS, RS_T, 0, st>>>((const double2*)points, n, chunk, g, shift, kin, iin, L.hist);
+        else
+            k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
+        s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
+        if (s) return s;
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, L.hist, kout, iout);
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    CT_CHECK_LAUNCH("locate order");
+    return CT_OK;
+}
+
+int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol, int32_t G, int64_t* out, void* ws,
+                   size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeL T;
+    int s = make_tree(t, n, G, ws, ws_bytes, &T);
+    if (s) return s;
+    LocWS L;
+    carve_loc(ws, n, G, &L);
+    CT_CUDA(cudaMemsetAsync(L.counters, 0, 64, st));
+    if (n == 0) return CT_OK;
+    const double2* P = (const double2*)points;
+    const int* ord = G > 0 ? L.order : nullptr;
+    float ohx, olx, ohy, oly;
+    origin_split(T.ox, &ohx, &olx);
+    origin_split(T.oy, &ohy, &oly);
+    float tolf = (float)tol;
+    if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
+    size_t smem = (size_t)T.stack * LOC_THREADS * sizeof(int);
+    unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
+    if (T.K == 3) {
+        smem_attr<3>(smem);
+        k_fast<3><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters, L.ovf);
+    } else if (T.K == 4) {
+        smem_attr<4>(smem);
+        k_fast<4><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters, L.ovf);
+    } else {
+        smem_attr<32>(smem);
+        k_fast<32><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters,
+                                                    L.ovf);
+    }
+    CT_CHECK_LAUNCH("locate fast");
+    return CT_OK;
+}
+
+int ct_locate_exact(const ct_tree* t, const double* points, int64_t n, double tol, int32_t G, int64_t* out, void* ws,
+                    size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeL T;
+    int s = make_tree(t, n, G, ws, ws_bytes, &T);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    LocWS L;
+    carve_loc(ws, n, G, &L);
+    const double2* P = (const double2*)points;
+    float ohx, olx, ohy, oly;
+    origin_split(T.ox, &ohx, &olx);
+    origin_split(T.oy, &ohy, &oly);
+    float tolf = (float)tol;
+    if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
+    k_pip<<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, P, L.R, L.counters, tol);
+    k_resolve<<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, L.R, L.counters, out);
+    size_t smem = (size_t)T.stack * LOC_THREADS * sizeof(int);
+    if (T.K == 3)
+        k_exact<3><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy, oly,
+                                                          out);
+    else if (T.K == 4)
+        k_exact<4><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy, oly,
+                                                          out);
+    else
+        k_exact<32><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy,
+                                                           oly, out);
+    CT_CHECK_LAUNCH("locate exact");
+    return CT_OK;
+}
+
+int ct_locate_deferred_count(const void* ws, int64_t n, int32_t G, int64_t* counts_host3, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    LocWS L;
+    carve_loc((void*)ws, n, G, &L);
+    int c[3] = {0, 0, 0};
+    CT_CUDA(cudaMemcpyAsync(c, L.counters, sizeof(c), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    counts_host3[0] = c[0];
+    counts_host3[1] = c[1];
+    counts_host3[2] = c[2];
+    return CT_OK;
+}
+
+int ct_locate_points_batched(const ct_tree* t, const double* points, int64_t n, double tol, int32_t G, int64_t* out,
+                             void* ws, size_t ws_bytes, void* stream) {
+    int s = ct_locate_bin(t, points, n, G, ws, ws_bytes, stream);
+    if (s) return s;
+    s = ct_locate_fast(t, points, n, tol, G, out, ws, ws_bytes, stream);
+    if (s) return s;
+    return ct_locate_exact(t, points, n, tol, G, out, ws, ws_bytes, stream);
+}
+
+}  // extern "C"

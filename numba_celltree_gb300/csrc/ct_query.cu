@@ -18,6 +18,7 @@
 
 #include "ct_common.cuh"
 #include "ct_internal.h"
+#include "ct_locf.cuh"
 
 namespace ctq {
 
@@ -26,16 +27,16 @@ struct TreeDev {
     const float4* nf;       // Lmax_f, Rmin_f, a, b (a/b as int bits)
     const double2* nd;      // Lmax, Rmin
     const double2* poly;    // leaf-ordered float64 polygons, K per cell
-    const float2* polyf;    // leaf-ordered float32 polygons (relative to origin, deduplicated)
+    const float4* polyf;    // leaf-ordered float32 cells in their local frame (ct_locf.cuh)
     const uint8_t* plen;    // polygon length (nullptr: all K)
     const uint8_t* plen32;  // deduplicated length
     const int64_t* bbi;     // bb_indices
     unsigned int* err;
     int64_t n_nodes;
     double ox, oy;
-    float dv;               // error bound of a float32 vertex coordinate
     float dabs;             // float64 rounding scale of absolute coordinates
     int K;
+    int S4;                 // float4 units per cell in polyf
 };
 
 __device__ __forceinline__ int node_a(const float4& q) { return __float_as_int(q.z); }
@@ -44,65 +45,6 @@ __device__ __forceinline__ int node_b(const float4& q) { return __float_as_int(q
 // Error band of a float32 value obtained by (directed or nearest) rounding of
 // a float64 difference: 2^-22 relative covers both roundings with margin.
 __device__ __forceinline__ float band(float x) { return fabsf(x) * 2.384185791015625e-07f + 1e-30f; }
-
-enum { OUTSIDE = 0, INSIDE = 1, UNSURE = 2 };
-
-// Float32 filter for point_in_polygon_or_on_edge (geometry_utils.py:195-223).
-// U_k = v_k - p in the float32 frame.  For an edge (U0, U1) the float32 cross
-// product A differs from the exact one of the original float64 geometry by at
-// most errA = 8u m^2 + 4 m e + 2 e^2 (m: largest |component| of U0, U1; e:
-// per-component error of U); moving the vertices along the segment from their
-// float64 to their float32 positions changes A by at most 4 m e + 6 e^2.
-// When |A| exceeds 2 (8u m^2 + 4 m e + 6 e^2) plus the on-edge
-// tolerance term, (1) the float64 on-edge test of the edge is false, (2) the
-// point stays off the edge line while the vertices move from their float64 to
-// their float32 positions, so the crossing parity of the float32
-// configuration -- evaluated exactly from the signs of A and of the y
-// components -- equals the float64 parity.  Otherwise the polygon is UNSURE.
-template <int KT>
-__device__ __forceinline__ int leaf_filter(float px, float py, float ep, float tolf, const float2* __restrict__ poly,
-                                           int len) {
-    const float u = 5.9604644775390625e-08f;  // 2^-24
-    if (len < 3) return UNSURE;
-    float2 q = poly[len - 1];
-    float ux = q.x - px, uy = q.y - py;
-    int parity = 0;
-#pragma unroll
-    for (int k = 0; k < KT; k++) {
-        if (k >= len) break;
-        float2 r = poly[k];
-        float vx = r.x - px, vy = r.y - py;
-        float A = ux * vy - uy * vx;
-        float m = fmaxf(fmaxf(fabsf(ux), fabsf(uy)), fmaxf(fabsf(vx), fabsf(vy)));
-        float e = ep + 1.1920928955078125e-07f * m;
-        float wx = vx - ux, wy = vy - uy;
-        float thr = 2.0f * (8.0f * u * m * m + 4.0f * m * e + 6.0f * e * e) +
-                    tolf * (fabsf(wx) + fabsf(wy) + 2.0f * e) * 1.000001f + 1e-30f;
-        if (!(fabsf(A) > thr)) return UNSURE;
-        if ((uy > 0.0f) != (vy > 0.0f)) {
-            bool cross = (vy > uy) ? (A > 0.0f) : (A < 0.0f);
-            parity ^= (int)cross;
-        }
-        ux = vx;
-        uy = vy;
-    }
-    return parity ? INSIDE : OUTSIDE;
-}
-
-// Float32 filter for point_on_edge (geometry_utils.py:226-238): the point is
-// certainly not on the edge when its distance to the edge line clearly exceeds
-// the tolerance.
-__device__ __forceinline__ bool edge_surely_off(float px, float py, float ep, float tolf, float2 a, float2 b) {
-    const float u = 5.9604644775390625e-08f;
-    float ux = a.x - px, uy = a.y - py, vx = b.x - px, vy = b.y - py;
-    float A = ux * vy - uy * vx;
-    float m = fmaxf(fmaxf(fabsf(ux), fabsf(uy)), fmaxf(fabsf(vx), fabsf(vy)));
-    float e = ep + 1.1920928955078125e-07f * m;
-    float wx = vx - ux, wy = vy - uy;
-    float thr = 2.0f * (8.0f * u * m * m + 4.0f * m * e + 6.0f * e * e) +
-                tolf * (fabsf(wx) + fabsf(wy) + 2.0f * e) * 1.000001f + 1e-30f;
-    return fabsf(A) > thr;
-}
 
 template <int STACK>
 struct Stack {
@@ -199,13 +141,14 @@ __global__ void __launch_bounds__(256) k_locate_points(TreeDev T, const double2*
     if (i >= n) return;
     double2 pp = pts[i];
     dpt p = mkp(pp.x, pp.y);
-    float px = 0.f, py = 0.f, dpx = 0.f, dpy = 0.f, ep = 0.f;
+    float px = 0.f, py = 0.f, dpx = 0.f, dpy = 0.f;
+    PtSplit P;
     if (MODE == CT_MODE_FP32) {
         px = __double2float_rn(p.x - T.ox);
         py = __double2float_rn(p.y - T.oy);
         dpx = band(px);
         dpy = band(py);
-        ep = fmaxf(dpx, dpy) + T.dv + T.dabs;
+        P = split_point(p.x, p.y);
     }
     const int K = KT == 32 ? T.K : KT;
     Stack<STACK> st;
@@ -228,10 +171,9 @@ __global__ void __launch_bounds__(256) k_locate_points(TreeDev T, const double2*
                 const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * K);
                 int len = (KT == 3) ? 3 : (T.plen ? (int)T.plen[j] : K);
                 if (MODE == CT_MODE_FP32) {
-                    int len32 = (KT == 3) ? (int)T.plen32[j] : (int)T.plen32[j];
-                    int r = leaf_filter<KT>(px, py, ep, tolf, T.polyf + (size_t)j * K, len32);
-                    if (r == INSIDE) hit = true;
-                    else if (r == UNSURE) hit = pip_or_edge(p, poly, len, tol);
+                    int r = leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j]);
+                    if (r == LF_INSIDE) hit = true;
+                    else if (r == LF_UNSURE) hit = pip_or_edge(p, poly, len, tol);
                 } else {
                     hit = pip_or_edge(p, poly, len, tol);
                 }
@@ -267,7 +209,7 @@ __global__ void __launch_bounds__(256) k_locate_on_edge(TreeDev T, const double2
     dpt p = mkp(pp.x, pp.y);
     float px = __double2float_rn(p.x - T.ox), py = __double2float_rn(p.y - T.oy);
     float dpx = band(px), dpy = band(py);
-    float ep = fmaxf(dpx, dpy) + T.dv + T.dabs;
+    PtSplit P = split_point(p.x, p.y);
     Stack<STACK> st;
     st.n = 1;
     st.s[0] = 0;
@@ -285,8 +227,7 @@ __global__ void __launch_bounds__(256) k_locate_on_edge(TreeDev T, const double2
             int ptr = node_a(q);
             bool hit = false;
             for (int j = ptr; j < ptr + b; j++) {
-                const float2* ef = T.polyf + (size_t)j * 2;
-                if (T.plen32[j] == 2 && edge_surely_off(px, py, ep, tolf, ef[0], ef[1])) continue;
+                if (T.plen32[j] == 2 && edge_surely_off_local(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4)) continue;
                 const double2* e = T.poly + (size_t)j * 2;
                 if (point_on_edge(p, mkp(e[0].x, e[0].y), mkp(e[1].x, e[1].y), tol)) {
                     hit = true;
@@ -472,49 +413,47 @@ __global__ void k_pack_nodes(int64_t n_nodes, const int64_t* __restrict__ child,
     nf[v] = q;
 }
 
-// Leaf-ordered polygons: float64 copy as given, float32 copy relative to the
-// origin with repeated consecutive vertices removed (the float64 predicate
-// skips them: `if v1 == v0: continue`, geometry_utils.py:203-204).
+// Leaf-ordered polygons: the float64 copy as given, and the float32 cell in
+// its local frame (ct_locf.cuh) with repeated consecutive vertices removed
+// (the float64 predicate skips them: `if v1 == v0: continue`,
+// geometry_utils.py:203-204).
 __global__ void k_pack_polys(int64_t n, int K, bool is_edge, const int64_t* __restrict__ elems,
-                             const int64_t* __restrict__ bbi, const double* __restrict__ v, double ox, double oy,
-                             double2* __restrict__ poly, float2* __restrict__ polyf, uint8_t* __restrict__ plen,
+                             const int64_t* __restrict__ bbi, const double* __restrict__ v,
+                             double2* __restrict__ poly, float4* __restrict__ polyf, uint8_t* __restrict__ plen,
                              uint8_t* __restrict__ plen32) {
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int64_t* e = elems + bbi[j] * K;
     int len = is_edge ? 2 : polygon_length(e, K);
     double2* P = poly + j * K;
-    float2* Pf = polyf + j * K;
+    int S4 = poly32_stride(K);
+    float4* C = polyf + j * S4;
+    float2* rel = reinterpret_cast<float2*>(C + 1);
     for (int k = 0; k < len; k++) P[k] = make_double2(v[2 * e[k]], v[2 * e[k] + 1]);
     for (int k = len; k < K; k++) P[k] = make_double2(__longlong_as_double(0x7ff8000000000000ll), 0.0);
-    // cyclic removal of consecutive duplicates
     int m = 0;
+    double2 v0 = make_double2(0.0, 0.0);
     if (len > 0) {
         double2 prev = P[len - 1];
         for (int k = 0; k < len; k++) {
             double2 c = P[k];
             if (c.x == prev.x && c.y == prev.y) continue;
-            Pf[m++] = make_float2(__double2float_rn(c.x - ox), __double2float_rn(c.y - oy));
+            if (m == 0) {
+                v0 = c;
+                float xl, yl;
+                float xh = split_hi(c.x, &xl), yh = split_hi(c.y, &yl);
+                C[0] = make_float4(xh, xl, yh, yl);
+            } else {
+                rel[m - 1] = make_float2(__double2float_rn(c.x - v0.x), __double2float_rn(c.y - v0.y));
+            }
+            m++;
             prev = c;
         }
     }
-    for (int k = m; k < K; k++) Pf[k] = make_float2(0.f, 0.f);
+    if (m == 0) C[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = (m > 0 ? m - 1 : 0); k < 2 * (S4 - 1); k++) rel[k] = make_float2(0.f, 0.f);
     if (plen) plen[j] = (uint8_t)len;
     plen32[j] = (uint8_t)m;
-}
-
-__global__ void k_vmax(int64_t n, int K, const float2* __restrict__ polyf, const uint8_t* __restrict__ plen32,
-                       unsigned int* __restrict__ red) {
-    float m = 0.f;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        int l = plen32[j];
-        for (int k = 0; k < l; k++) {
-            float2 q = polyf[j * K + k];
-            m = fmaxf(m, fmaxf(fabsf(q.x), fabsf(q.y)));
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(red, __float_as_uint(m));
 }
 
 TreeDev make_dev(const ct_tree* t) {
@@ -522,7 +461,7 @@ TreeDev make_dev(const ct_tree* t) {
     T.nf = (const float4*)t->nodes_f32;
     T.nd = (const double2*)t->nodes_f64;
     T.poly = (const double2*)t->poly_f64;
-    T.polyf = (const float2*)t->poly_f32;
+    T.polyf = (const float4*)t->poly_f32;
     T.plen = t->n_max_vert == 3 ? nullptr : t->poly_len;
     T.plen32 = t->poly_len32;
     T.bbi = t->bb_indices;
@@ -530,10 +469,9 @@ TreeDev make_dev(const ct_tree* t) {
     T.n_nodes = t->n_nodes;
     T.ox = t->origin[0];
     T.oy = t->origin[1];
-    // float32 vertex error: rounding of (v - o) to float, bounded relative to vmax
-    T.dv = t->vmax * 2.384185791015625e-07f + 1e-30f;
     T.dabs = t->abs_eps;
     T.K = t->n_max_vert;
+    T.S4 = poly32_stride(t->n_max_vert);
     return T;
 }
 
@@ -669,19 +607,15 @@ int ct_pack_tree(ct_tree* t, void* stream) {
     }
     if (t->n_elements > 0) {
         k_pack_polys<<<grid_for(t->n_elements, 256), 256, 0, st>>>(
-            t->n_elements, t->n_max_vert, is_edge, t->elements, t->bb_indices, t->vertices, ox, oy,
-            (double2*)t->poly_f64, (float2*)t->poly_f32, t->poly_len, t->poly_len32);
-        int g = (int)std::min<int64_t>(grid_for(t->n_elements, 256), 152 * 8);
-        k_vmax<<<g, 256, 0, st>>>(t->n_elements, t->n_max_vert, (const float2*)t->poly_f32, t->poly_len32, red);
+            t->n_elements, t->n_max_vert, is_edge, t->elements, t->bb_indices, t->vertices, (double2*)t->poly_f64,
+            (float4*)t->poly_f32, t->poly_len, t->poly_len32);
         CT_CHECK_LAUNCH("pack_polys");
     }
     unsigned int hv[2] = {0, 0};
     CT_CUDA(cudaMemcpyAsync(hv, red, sizeof(hv), cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
     if (hv[1]) return ct_fail(CT_ERR_DEVICE, "tree structure check failed (child or leaf range out of order)");
-    float vm;
-    memcpy(&vm, &hv[0], 4);
-    t->vmax = vm;
+    t->vmax = 0.0f;  // unused by the local-frame float32 cells
     // float64 rounding of absolute vertex coordinates (the float64 predicate
     // rounds relative to them): 2^-50 * max |coordinate|
     double amax = std::max(std::max(std::fabs(t->bbox[0]), std::fabs(t->bbox[1])),

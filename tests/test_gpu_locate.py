@@ -24,7 +24,7 @@ def _points(xy, f, n, seed):
 
 
 @pytest.mark.parametrize("name", list(meshes().keys()))
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision", ["fp32", "fp32-inline", "fp64"])
 def test_locate_matches_oracle(oracle, name, precision):
     from numba_celltree_gb300 import CellTree2d
 
@@ -48,7 +48,7 @@ def test_locate_matches_upstream_fixtures():
         nb, cpl = (int(x) for x in G[p + "params"])
         g = CellTree2d(G[p + "vertices"], G[p + "faces_in"], -1, nb, cpl)
         span = float((G[p + "vertices"].max(0) - G[p + "vertices"].min(0)).max())
-        for prec in ("fp32", "fp64"):
+        for prec in ("fp32", "fp32-inline", "fp64"):
             g.precision = prec
             assert np.array_equal(g.locate_points(G[p + "points"]), G[p + "locate"]), (i, prec)
             assert np.array_equal(g.locate_points(G[p + "points"], 1e-3 * span), G[p + "locate_tol"]), (i, prec)
@@ -69,9 +69,15 @@ def test_locate_utm_precision_stress(oracle):
         xy[rng.integers(0, len(xy), 5000)],
     ])
     ref = o.locate_points(pts)
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "fp32-inline", "fp64"):
         g.precision = prec
         assert np.array_equal(g.locate_points(pts), ref)
+    for bits in (0, 8, 16, 24):
+        import torch
+        p_d = torch.as_tensor(pts, device="cuda")
+        o_d = torch.empty(len(pts), dtype=torch.int64, device="cuda")
+        g._tree.locate(p_d, o_d, g.default_tolerance(), "fp32", sort_bits=bits)
+        assert np.array_equal(o_d.cpu().numpy(), ref), bits
 
 
 def test_locate_device_tensors(oracle):
@@ -94,7 +100,7 @@ def test_locate_known_answers():
     nodes2 = np.array([[0.0, 0.0], [2.0, 0.0], [1.0, 2.0], [3.0, 2.0]])
     faces2 = np.array([[0, 1, 2], [1, 3, 2]], dtype=np.intc)
     t = CellTree2d(nodes2, faces2, -1)
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "fp32-inline", "fp64"):
         t.precision = prec
         assert np.array_equal(t.locate_points(np.array([[1.0, 1.0], [2.0, 1.0], [-1.0, 1.0]])), [0, 1, -1])
         pts = np.array([[-0.09, 0.0], [2.0, 1.0], [-1.0, 1.0]])
@@ -106,7 +112,7 @@ def test_locate_known_answers():
     t = CellTree2d(nodes, faces, -1, n_buckets=2, cells_per_leaf=1)
     pts = np.array([[-9e-9, 0.0], [2.0, -9e-9], [-9e-9, 1.0], [1.0, -9e-9], [-1.1e-8, 1.0], [1.0, -1.1e-8],
                     [-1.1e-8, 0.0], [2.0, -1.5e-8]])
-    for prec in ("fp32", "fp64"):
+    for prec in ("fp32", "fp32-inline", "fp64"):
         t.precision = prec
         assert np.array_equal(t.locate_points(np.array([[1.0, 1.0], [5.0, 0.5], [5.0, 3.0], [-1.0, 1.0]])),
                               [0, 2, 1, -1])
