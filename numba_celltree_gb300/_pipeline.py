@@ -1,0 +1,76 @@
+"""Host-resident query batches: chunked, double-buffered host <-> device
+streaming around a device query.
+
+A batch of host points is cut into chunks.  Chunk c is copied to the device
+on an upload stream, queried on the caller's current stream and its result
+copied back on a download stream, so the upload of chunk c+1 and the
+download of chunk c-1 overlap the query of chunk c.  Results land in pinned
+host memory (the CUDA runtime copies into pageable memory through a single
+staging thread, an order of magnitude slower than a DMA into pinned memory);
+the returned numpy array is a view of that pinned block, which goes back to
+PyTorch's pinned-block cache when the array is dropped.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import _device
+
+CHUNK_POINTS = 1 << 25  # points per chunk (512 MiB of float64 pairs)
+
+
+def pinned_empty(shape, dtype):
+    """Pinned host tensor (PyTorch's cached pinned allocator)."""
+    torch = _device.torch()
+    return torch.empty(shape, dtype=dtype, pin_memory=True)
+
+
+def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> np.ndarray:
+    """Run ``query(points_d, out_d)`` over `points` (n, 2) float64 host array
+    in chunks; returns the concatenated results as a numpy array over pinned
+    memory.  ``query`` enqueues work on the current stream and must not
+    synchronise."""
+    torch = _device.torch()
+    chunk = CHUNK_POINTS if chunk is None else int(chunk)
+    n = int(points.shape[0])
+    out_h = pinned_empty((n,), out_dtype)
+    if n == 0:
+        return out_h.numpy()
+    src = torch.from_numpy(points)
+    compute = torch.cuda.current_stream(device)
+    up = torch.cuda.Stream(device)
+    down = torch.cuda.Stream(device)
+    m = min(chunk, n)
+    nbuf = 2 if n > m else 1
+    pin_in = src.is_pinned()
+    p_d = [torch.empty((m, 2), dtype=torch.float64, device=device) for _ in range(nbuf)]
+    o_d = [torch.empty((m,), dtype=out_dtype, device=device) for _ in range(nbuf)]
+    done = [None] * nbuf  # query of the chunk that last used buffer b
+    fetched = [None] * nbuf  # download of the chunk that last used buffer b
+    for c, s in enumerate(range(0, n, m)):
+        e = min(s + m, n)
+        b = c % nbuf
+        k = e - s
+        with torch.cuda.stream(up):
+            if done[b] is not None:
+                up.wait_event(done[b])
+            p_d[b][:k].copy_(src[s:e], non_blocking=pin_in)
+            uploaded = torch.cuda.Event()
+            uploaded.record(up)
+        compute.wait_event(uploaded)
+        if fetched[b] is not None:
+            compute.wait_event(fetched[b])
+        query(p_d[b][:k], o_d[b][:k])
+        ev = torch.cuda.Event()
+        ev.record(compute)
+        done[b] = ev
+        with torch.cuda.stream(down):
+            down.wait_event(ev)
+            out_h[s:e].copy_(o_d[b][:k], non_blocking=True)
+            ev2 = torch.cuda.Event()
+            ev2.record(down)
+            fetched[b] = ev2
+    down.synchronize()
+    compute.synchronize()
+    return out_h.numpy()

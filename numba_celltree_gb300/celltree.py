@@ -8,7 +8,7 @@ from typing import Optional, Tuple
 
 import numpy as np
 
-from . import _device, _lib
+from . import _device, _pipeline, _lib
 from .cast import cast_bboxes, cast_edges, cast_faces, cast_vertices, is_cuda_tensor
 from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, validate_elements
 
@@ -99,13 +99,19 @@ class CellTree2d(CellTree2dBase):
         points = cast_vertices(points)
         t = self._tree
         torch = _device.torch()
-        p_d = _device.to_device(points, torch.float64, t.device)
-        n = int(p_d.shape[0])
-        out = _device.empty((n,), torch.int64, t.device)
         t.reset_error()
+        if not cuda_in:
+            # host batch: chunked upload / query / download, result in pinned memory
+            res = _pipeline.stream_points(
+                points, t.device, lambda p_d, o_d: t.locate(p_d, o_d, tol, self.precision), torch.int64
+            )
+            t.raise_on_device_error()
+            return res
+        p_d = _device.to_device(points, torch.float64, t.device)
+        out = _device.empty((int(p_d.shape[0]),), torch.int64, t.device)
         t.locate(p_d, out, tol, self.precision)
         t.raise_on_device_error()
-        return _as_output(out, cuda_in)
+        return out
 
     # -- box queries -----------------------------------------------------------
     def locate_boxes(self, bbox_coords):

@@ -163,6 +163,57 @@ __device__ __forceinline__ bool node_step(const TreeL& T, int* s, int B, int& sp
     return true;
 }
 
+// float64 re-decision of node v (locate_point query.py:87-105) for a query
+// whose float32 margins were inside the band: bit 0 left child, bit 1 right
+// child, bit 2 right child first.  Kept out of line so that no float64
+// instruction is scheduled on the float32 path (GB300 runs float64 at 1/64
+// of the float32 rate).
+__device__ __noinline__ int node_exact_code(const double2* __restrict__ nd_all, int v, const double2* __restrict__ pts,
+                                            int oi, int dim) {
+    double2 nd = nd_all[v];
+    double2 p2 = pts[oi];
+    double pd = dim ? p2.y : p2.x;
+    int left = pd <= nd.x, right = pd >= nd.y;
+    int rf = (nd.x - pd) < (pd - nd.y);
+    return left | (right << 1) | (rf << 2);
+}
+
+// Children of internal node v for the float32 traversal: returns the child to
+// visit next, or -1 when neither child contains the point, and pushes the
+// second child of a two-child visit (the reference pushes both and pops the
+// nearer bound's child first).  Decisions whose float32 margin is within the
+// band `dx` are taken from node_exact_code.  `ok` is cleared on stack
+// overflow.
+__device__ __forceinline__ int node_next(const TreeL& T, int* s, int B, int& sp, int v, const float4& q, float x,
+                                         float dx, const double2* __restrict__ pts, int oi, int dim, bool& ok) {
+    const float Lf = q.x, Rf = q.y;
+    const float dl = x - Lf, dr = x - Rf;
+    const int child = na(q);
+    bool left = dl < 0.0f, right = dr > 0.0f;
+    bool sure = fabsf(dl) > dx && fabsf(dr) > dx;
+    bool right_first = false;
+    if (sure && left && right) {
+        float aF = Lf - x, bF = x - Rf;
+        float bo = 2.0f * dx + 2.384185791015625e-07f * (fabsf(aF) + fabsf(bF)) + 1e-30f;
+        sure = fabsf(aF - bF) > bo;
+        right_first = aF < bF;
+    }
+    if (!sure) {
+        int c = node_exact_code(T.nd, v, pts, oi, dim);
+        // float32-sure decisions stand; only the uncertain ones are replaced
+        if (!(fabsf(dl) > dx)) left = c & 1;
+        if (!(fabsf(dr) > dx)) right = (c >> 1) & 1;
+        right_first = (c >> 2) & 1;
+    }
+    if (!(left && right)) return left ? child : (right ? child + 1 : -1);
+    if (sp + 1 > T.stack) {
+        ok = false;
+        return -1;
+    }
+    s[(sp++) * B] = right_first ? child : child + 1;
+    return right_first ? child + 1 : child;
+}
+
 // Stage 2: float32 traversal with candidate collection.
 template <int KT>
 __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __restrict__ pts,
@@ -188,20 +239,31 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
         dpy += T.bandG;
         const int B = blockDim.x;
         int* s = stk + threadIdx.x;
-        int sp = 1;
-        s[0] = 0;
+        int sp = 0;
+        int v = 0;
         int budget = (int)min(T.n_nodes, (int64_t)INT32_MAX);
-        bool done = false;
-        while (sp > 0 && !done) {
+        while (true) {
             if (--budget < 0) {
                 set_error(T.err, CT_DEVERR_LOOP);
                 break;
             }
-            int v = s[(--sp) * B];
             float4 q = T.nf[v];
             int b = nbq(q);
-            if (b >= 0) {
+            if (b < 0) {
+                int dim = -1 - b;
+                bool ok = true;
+                int nx = node_next(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, oi, dim, ok);
+                if (nx >= 0) {
+                    v = nx;
+                    continue;
+                }
+                if (!ok) {
+                    set_error(T.err, CT_DEVERR_STACK);
+                    break;
+                }
+            } else {
                 int ptr = na(q);
+                bool done = false;
                 for (int j = ptr; j < ptr + b; j++) {
                     int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
                                                                            (int)T.plen32[j])
@@ -222,13 +284,10 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
                         }
                     }
                 }
-                continue;
+                if (done) break;
             }
-            int dim = -1 - b;
-            if (!node_step(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, oi, dim)) {
-                set_error(T.err, CT_DEVERR_STACK);
-                break;
-            }
+            if (sp == 0) break;
+            v = s[(--sp) * B];
         }
     }
     if (active && !overflow && nc == 0) out[oi] = res;

@@ -118,3 +118,32 @@ def test_locate_known_answers():
                               [0, 2, 1, -1])
         assert np.array_equal(t.locate_points(pts), [-1] * 8)
         assert np.array_equal(t.locate_points(pts, tolerance=1e-8), [0, 0, 0, 0, -1, -1, -1, -1])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("chunk", [1000, 4096, 1 << 25])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_locate_host_pipeline(oracle, monkeypatch, chunk, pinned):
+    """Host batches stream through the chunked upload / query / download
+    pipeline: ragged last chunk, pageable and pinned inputs, empty input."""
+    import torch
+    from numba_celltree_gb300 import CellTree2d, _pipeline
+    from numba_celltree_gb300 import synthetic as syn
+
+    monkeypatch.setattr(_pipeline, "CHUNK_POINTS", chunk)
+    xy, f = syn.triangle_mesh(40, seed=8, extent=(40.0, 40.0), offset=(1.0e3, -2.0e3))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = np.concatenate([
+        syn.uniform_points(9000, xy.min(0) - 1.0, xy.max(0) + 1.0, seed=2),
+        syn.near_edge_points(xy, f, 1500, dist=0.0, seed=3),
+    ])
+    if pinned:
+        buf = torch.empty(pts.shape, dtype=torch.float64, pin_memory=True)
+        buf.numpy()[:] = pts
+        pts = buf.numpy()
+    ref = o.locate_points(pts)
+    got = g.locate_points(pts)
+    assert isinstance(got, np.ndarray) and got.dtype == np.int64
+    assert np.array_equal(got, ref)
+    assert g.locate_points(pts[:0]).shape == (0,)
