@@ -80,6 +80,12 @@ typedef struct ct_tree {
     float vmax;               /* host: unused (kept for layout stability) */
     float abs_eps;            /* host: float64 rounding scale of absolute coordinates */
     unsigned int* error_word; /* device: one uint32, OR-ed CT_DEVERR_* bits */
+    /* start-node grid of the batched float32 locate (filled by ct_pack_grid;
+     * grid_n = 0 disables it) */
+    int32_t* grid_start;      /* device: grid_n x grid_n node ids (-1: no cell), row = y */
+    int32_t grid_n;           /* cells per axis */
+    float grid_x0, grid_y0;   /* host: grid origin in the float32 frame */
+    float grid_sx, grid_sy;   /* host: cells per unit length */
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */
@@ -174,6 +180,21 @@ int ct_pack_tree(ct_tree* tree, void* stream);
 
 #define CT_MODE_FP64 0 /* float64 traversal and leaf tests (plain form) */
 #define CT_MODE_FP32 1 /* float32 traversal + float32 leaf filter, exact float64 fallback */
+
+/* Start-node grid (no upstream counterpart; an index over the tree that
+ * shortens the batched float32 locate).  For each cell of a grid_n x grid_n
+ * grid over the tree bbox it stores the first node of the root path of
+ * locate_point (query.py:63-107) at which the points of that cell (plus a
+ * rounding margin) stop taking one and the same single child -- a leaf, a
+ * node with a bound inside the cell, or a node whose two children are both
+ * taken -- or -1 when the path ends without a child.  Every traversal of the
+ * reference from the root reaches that node with an empty stack, so starting
+ * there gives the same result.  ct_grid_resolution: grid_n for n_elements
+ * (smallest power of two >= sqrt(n_elements), in [16, 4096]).
+ * ct_pack_grid needs the packed tree (ct_pack_tree) and tree->grid_start /
+ * grid_n set by the caller; it sets grid_n = 0 for a degenerate bbox. */
+int32_t ct_grid_resolution(int64_t n_elements);
+int ct_pack_grid(ct_tree* tree, void* stream);
 
 /* locate_points query.py:110-117 (locate_point 63-107).  out: n (int64). */
 int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t mode,

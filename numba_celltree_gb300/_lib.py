@@ -66,6 +66,12 @@ class CtTree(ctypes.Structure):
         ("vmax", ctypes.c_float),
         ("abs_eps", ctypes.c_float),
         ("error_word", _P),
+        ("grid_start", _P),
+        ("grid_n", _I32),
+        ("grid_x0", ctypes.c_float),
+        ("grid_y0", ctypes.c_float),
+        ("grid_sx", ctypes.c_float),
+        ("grid_sy", ctypes.c_float),
     ]
 
 
@@ -80,6 +86,8 @@ SIGNATURES = {
     "ct_bbox_summary": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(_D), _P]),
     "ct_vertex_extent": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_D), _P]),
     "ct_pessimistic_n_nodes": (_I64, [_I64]),
+    "ct_grid_resolution": (_I32, [_I64]),
+    "ct_pack_grid": (ctypes.c_int, [_P, _P]),
     "ct_build_workspace_size": (_SZ, [_I64, _I32, _I32]),
     "ct_build_tree": (
         ctypes.c_int,

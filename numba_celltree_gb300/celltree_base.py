@@ -90,9 +90,13 @@ class _GpuTree:
         self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
         self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
         self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
+        gn = int(lib.ct_grid_resolution(n))
+        self.grid_start = _device.empty((gn * gn,), torch.int32, device)
         self.desc = _lib.CtTree()
         self._fill_desc()
+        self.desc.grid_n = gn
         _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
+        _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
 
     def _fill_desc(self):
         d = self.desc
@@ -121,6 +125,7 @@ class _GpuTree:
         d.poly_len = P(self.poly_len)
         d.poly_len32 = P(self.poly_len32)
         d.error_word = P(self.error_word)
+        d.grid_start = P(self.grid_start)
 
     def reset_error(self):
         self.error_word.zero_()

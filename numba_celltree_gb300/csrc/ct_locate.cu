@@ -58,6 +58,9 @@ struct TreeL {
     int K;
     int S4;     // float4 units per cell in polyf
     int stack;  // stack entries per thread (>= max_depth + 2)
+    const int* gstart;  // start-node grid (null: start at the root)
+    int gn;
+    float gx0, gy0, gsx, gsy;
 };
 
 struct Recs {
@@ -241,9 +244,16 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
         int* s = stk + threadIdx.x;
         int sp = 0;
         int v = 0;
-        int budget = (int)min(T.n_nodes, (int64_t)INT32_MAX);
-        while (true) {
-            if (--budget < 0) {
+        if (T.gstart) {
+            // grid cell of the point; outside the grid (or NaN): the root
+            float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
+            float gn = (float)T.gn;
+            if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) v = T.gstart[(int)fy * T.gn + (int)fx];
+        }
+        // at most n_nodes visits; v = -1: the root path ends without a child
+        int budget = (v < 0) ? 0 : (int)min(T.n_nodes, (int64_t)INT32_MAX - 1) + 1;
+        while (budget > 0) {
+            if (--budget == 0) {
                 set_error(T.err, CT_DEVERR_LOOP);
                 break;
             }
@@ -549,6 +559,44 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// start-node grid
+// ---------------------------------------------------------------------------
+// One thread per grid cell: follow the root path while every point of the
+// cell (its range widened by `m`) takes one and the same single child.  The
+// float32 node bounds are within `band` of the float64 bounds, so a decision
+// is certain when the cell range clears bound -/+ band (directed rounding).
+__global__ void k_grid_start(const float4* __restrict__ nf, int gn, float x0, float y0, float sx, float sy, double m,
+                             float band, int max_steps, int* __restrict__ start) {
+    int64_t total = (int64_t)gn * gn;
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+        int gx = (int)(c % gn), gy = (int)(c / gn);
+        float xlo = __double2float_rd((double)x0 + (double)gx / (double)sx - m);
+        float xhi = __double2float_ru((double)x0 + (double)(gx + 1) / (double)sx + m);
+        float ylo = __double2float_rd((double)y0 + (double)gy / (double)sy - m);
+        float yhi = __double2float_ru((double)y0 + (double)(gy + 1) / (double)sy + m);
+        int v = 0;
+        for (int k = 0; k < max_steps; k++) {
+            float4 q = nf[v];
+            int b = nbq(q);
+            if (b >= 0) break;  // leaf
+            int dim = -1 - b;
+            float lo = dim ? ylo : xlo, hi = dim ? yhi : xhi;
+            bool all_left = hi < __fsub_rd(q.x, band), no_left = lo > __fadd_ru(q.x, band);
+            bool all_right = lo > __fadd_ru(q.y, band), no_right = hi < __fsub_rd(q.y, band);
+            if (!((all_left || no_left) && (all_right || no_right))) break;  // a bound inside the cell
+            if (all_left && all_right) break;                                // both children taken
+            if (all_left) v = na(q);
+            else if (all_right) v = na(q) + 1;
+            else {
+                v = -1;  // no child: locate_point returns -1
+                break;
+            }
+        }
+        start[c] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -624,6 +672,12 @@ static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws
         if (!(F >= 0.0) || !std::isfinite(F)) F = 0.0;
         T->bandG = (float)(F * 2.384185791015625e-07 * 1.0001) + 1e-30f;  // bounds are inside the bbox
     }
+    T->gstart = (t->grid_start && t->grid_n > 0) ? t->grid_start : nullptr;
+    T->gn = T->gstart ? t->grid_n : 0;
+    T->gx0 = t->grid_x0;
+    T->gy0 = t->grid_y0;
+    T->gsx = t->grid_sx;
+    T->gsy = t->grid_sy;
     T->K = t->n_max_vert;
     T->S4 = poly32_stride(t->n_max_vert);
     T->stack = t->max_depth + 2;
@@ -651,6 +705,49 @@ using namespace ctl;
 extern "C" {
 
 int ct_poly32_stride(int32_t K) { return poly32_stride(K); }
+
+int32_t ct_grid_resolution(int64_t n_elements) {
+    int32_t g = 16;
+    while (g < 4096 && (int64_t)g * g < n_elements) g *= 2;
+    return g;
+}
+
+int ct_pack_grid(ct_tree* t, void* stream) {
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (!t->grid_start || t->grid_n <= 0) {
+        t->grid_n = 0;
+        return CT_OK;
+    }
+    if (t->grid_n > 8192) return ct_fail(CT_ERR_ARG, "grid_n above 8192");
+    if (t->n_nodes <= 0 || !t->nodes_f32) return ct_fail(CT_ERR_ARG, "tree is not packed");
+    double ex = t->bbox[1] - t->bbox[0], ey = t->bbox[3] - t->bbox[2];
+    double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
+                        std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
+    if (!(ex > 0.0 && ey > 0.0) || !std::isfinite(ex) || !std::isfinite(ey) || !std::isfinite(F)) {
+        t->grid_n = 0;  // degenerate bbox: every query starts at the root
+        return CT_OK;
+    }
+    const int gn = t->grid_n;
+    t->grid_x0 = (float)(t->bbox[0] - t->origin[0]);
+    t->grid_y0 = (float)(t->bbox[2] - t->origin[1]);
+    t->grid_sx = (float)(gn / ex);
+    t->grid_sy = (float)(gn / ey);
+    if (!(t->grid_sx > 0.0f && t->grid_sy > 0.0f && std::isfinite(t->grid_sx) && std::isfinite(t->grid_sy))) {
+        t->grid_n = 0;
+        return CT_OK;
+    }
+    // margin over the cell of a point: float32 rounding of the point in the
+    // frame and of (p - x0) * s is below 2^-21 (extent + F); 4x that
+    double m = std::ldexp(std::max(ex, ey) + F, -19);
+    float band = (float)(F * 2.384185791015625e-07 * 1.0001) + 1e-30f;
+    int64_t total = (int64_t)gn * gn;
+    unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
+    k_grid_start<<<blocks, 256, 0, (cudaStream_t)stream>>>((const float4*)t->nodes_f32, gn, t->grid_x0, t->grid_y0,
+                                                          t->grid_sx, t->grid_sy, m, band, t->max_depth + 2,
+                                                          t->grid_start);
+    CT_CHECK_LAUNCH("pack grid");
+    return CT_OK;
+}
 
 size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits) {
     if (sort_bits != 0 && sort_bits != 8 && sort_bits != 16 && sort_bits != 24) return 0;

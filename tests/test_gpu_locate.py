@@ -147,3 +147,82 @@ def test_locate_host_pipeline(oracle, monkeypatch, chunk, pinned):
     assert isinstance(got, np.ndarray) and got.dtype == np.int64
     assert np.array_equal(got, ref)
     assert g.locate_points(pts[:0]).shape == (0,)
+
+
+@pytest.mark.gpu
+def test_locate_start_grid_edges(oracle):
+    """Queries on the lines of the start-node grid, on the bbox boundary and
+    just outside it, and on vertices: same result as the oracle in every
+    form; the grid is populated (most cells skip at least the root)."""
+    import torch
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(120, 60, seed=17, extent=(120.0, 60.0), offset=(7.5e5, 5.1e6))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    t = g._tree
+    gn = int(t.desc.grid_n)
+    assert gn == 128
+    starts = t.grid_start.cpu().numpy()
+    assert (starts > 0).mean() > 0.5
+    xmin, xmax, ymin, ymax = [float(v) for v in g.bbox]
+    gx = np.linspace(xmin, xmax, gn + 1)
+    gy = np.linspace(ymin, ymax, gn + 1)
+    rng = np.random.default_rng(9)
+    line_pts = np.concatenate([
+        np.stack([rng.choice(gx, 4000), rng.uniform(ymin, ymax, 4000)], 1),
+        np.stack([rng.uniform(xmin, xmax, 4000), rng.choice(gy, 4000)], 1),
+    ])
+    eps = np.array([0.0, 1e-12, -1e-12, 1e-7, -1e-7])
+    border = np.concatenate([
+        np.stack([xmin + rng.choice(eps, 2000), rng.uniform(ymin, ymax, 2000)], 1),
+        np.stack([xmax + rng.choice(eps, 2000), rng.uniform(ymin, ymax, 2000)], 1),
+        np.stack([rng.uniform(xmin, xmax, 2000), ymin + rng.choice(eps, 2000)], 1),
+        np.stack([rng.uniform(xmin, xmax, 2000), ymax + rng.choice(eps, 2000)], 1),
+        np.array([[xmin, ymin], [xmax, ymax], [xmin, ymax], [xmax, ymin]]),
+    ])
+    pts = np.concatenate([line_pts, border, xy[rng.integers(0, len(xy), 3000)],
+                          syn.near_edge_points(xy, f, 4000, dist=0.0, seed=12)])
+    ref = o.locate_points(pts)
+    for prec in ("fp32", "fp32-inline", "fp64"):
+        g.precision = prec
+        assert np.array_equal(g.locate_points(pts), ref), prec
+    p_d = torch.as_tensor(pts, device="cuda")
+    o_d = torch.empty(len(pts), dtype=torch.int64, device="cuda")
+    for bits in (0, 24):
+        t.locate(p_d, o_d, g.default_tolerance(), "fp32", sort_bits=bits)
+        assert np.array_equal(o_d.cpu().numpy(), ref), bits
+
+
+@pytest.mark.gpu
+def test_locate_without_start_grid(oracle):
+    """grid_n = 0 (the state for a degenerate bbox): every query starts at the
+    root, same results."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.quad_mesh(50, 30, seed=4)
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = np.concatenate([syn.uniform_points(20000, xy.min(0) - 0.5, xy.max(0) + 0.5, seed=1),
+                          syn.near_edge_points(xy, f, 3000, dist=0.0, seed=2)])
+    ref = o.locate_points(pts)
+    g._tree.desc.grid_n = 0
+    for prec in ("fp32", "fp64"):
+        g.precision = prec
+        assert np.array_equal(g.locate_points(pts), ref), prec
+
+
+@pytest.mark.gpu
+def test_build_rejects_zero_height_mesh(oracle):
+    """Cells on one line: the reference's bucket test cannot place the
+    centroids, the oracle raises, and so does the GPU build."""
+    from numba_celltree_gb300 import CellTree2d
+    from numba_celltree_gb300._lib import CellTreeError
+
+    x = np.arange(20, dtype=np.float64)
+    xy = np.stack([x, np.zeros_like(x)], 1)
+    f = np.stack([np.arange(18), np.arange(1, 19), np.arange(2, 20)], 1).astype(np.int64)
+    with pytest.raises(Exception):
+        oracle.OracleCellTree2d(xy, f, -1)
+    with pytest.raises(CellTreeError):
+        CellTree2d(xy, f, -1)
