@@ -326,7 +326,7 @@ def main():
     ms_fast = timed(lambda: lib.ct_locate_fast(ctypes.byref(t.desc), _device.ptr(pts_d), n, float(tol), bins,
                                                _device.ptr(out64), _device.ptr(wsb), int(wsb.numel()),
                                                _device.stream()), max(1, min(args.steps, 3)), 1)
-    dcount = (ctypes.c_int64 * 3)()
+    dcount = (ctypes.c_int64 * 4)()
     lib.ct_locate_deferred_count(_device.ptr(wsb), n, bins, dcount, _device.stream())
     ms_inline = timed(lambda: run("fp32-inline", out64), max(1, min(args.steps, 3)), 1)
     ms64 = timed(lambda: run("fp64", out64), max(1, min(args.steps, 3)), 1)
@@ -423,8 +423,8 @@ def main():
         "fp32_vs_fp64": round(value / value64, 3),
         "fp32_inline": {"value": round(ws * n / (ms_inline * 1e-3) / 1e6, 3), "unit": UNIT,
                         "ms_per_step": round(ms_inline, 3)},
-        "deferred": {"overflow": int(dcount[0]), "records": int(dcount[1]), "pairs": int(dcount[2]),
-                     "fraction": round((dcount[0] + dcount[1]) / n, 5)},
+        "deferred": {"open_after_lists": int(dcount[3]), "overflow": int(dcount[0]), "records": int(dcount[1]),
+                     "pairs": int(dcount[2]), "fraction": round((dcount[0] + dcount[1]) / n, 5)},
         "indices_identical_fp32_fp64": identical,
         "points_found": found,
         "gpu_launches": args.steps * (7 if bins else 4),

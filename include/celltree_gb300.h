@@ -86,6 +86,15 @@ typedef struct ct_tree {
     int32_t grid_n;           /* cells per axis */
     float grid_x0, grid_y0;   /* host: grid origin in the float32 frame */
     float grid_sx, grid_sy;   /* host: cells per unit length */
+    /* per-grid-cell candidate lists of the batched float32 locate (filled by
+     * ct_cand_count + ct_cand_fill; cand_tol = 0 disables them) */
+    int64_t* cand_off;        /* device: grid_n * grid_n + 1 offsets into cand_idx */
+    int32_t* cand_idx;        /* device: leaf-order cell ids of each grid cell */
+    void* cand_lbox;          /* device: cand_n x float4, the widened box of each cand_idx entry */
+    void* cand_box;           /* device: n_elements x float4 widened bbox (xmin, xmax, ymin, ymax),
+                                 float32 frame, leaf order */
+    int64_t cand_n;           /* host: entries of cand_idx */
+    double cand_tol;          /* host: largest query tolerance the lists cover */
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */
@@ -196,6 +205,25 @@ int ct_pack_tree(ct_tree* tree, void* stream);
 int32_t ct_grid_resolution(int64_t n_elements);
 int ct_pack_grid(ct_tree* tree, void* stream);
 
+/* Candidate lists (no upstream counterpart; an index that lets most batched
+ * float32 queries skip the traversal).  For grid cell g the list holds every
+ * cell whose bbox, widened by 2 * cover_tol plus the float64 rounding of the
+ * coordinates, meets g widened by the cell-assignment margin: every cell for
+ * which point_in_polygon_or_on_edge (geometry_utils.py:195-223) can be true
+ * for a point of g.  A query tests its list with the float32 leaf filter; one
+ * sure hit and sure misses elsewhere is locate_point's answer (a sure hit is
+ * an interior point, inside the cell's bbox, so the reference reaches that
+ * leaf), all sure misses is -1, anything else goes through the traversal.
+ * Needs ct_pack_grid first and the caller's arrays cand_off
+ * (grid_n^2 + 1 int64) and cand_box (n_elements float4).  ct_cand_count
+ * fills the boxes and offsets and returns the number of entries (sets
+ * cand_n, cand_tol; synchronises); the caller then allocates cand_idx and
+ * cand_lbox (cand_n entries each) and calls ct_cand_fill.  scratch: ct_cand_scratch_size bytes. */
+size_t ct_cand_scratch_size(const ct_tree* tree);
+int ct_cand_count(ct_tree* tree, double cover_tol, void* scratch, size_t scratch_bytes, int64_t* total_host,
+                  void* stream);
+int ct_cand_fill(ct_tree* tree, void* scratch, size_t scratch_bytes, void* stream);
+
 /* locate_points query.py:110-117 (locate_point 63-107).  out: n (int64). */
 int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t mode,
                      int64_t* out, void* stream);
@@ -221,9 +249,10 @@ int ct_locate_fast(const ct_tree* tree, const double* points, int64_t n, double 
                    int64_t* out, void* workspace, size_t workspace_bytes, void* stream);
 int ct_locate_exact(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t sort_bits,
                     int64_t* out, void* workspace, size_t workspace_bytes, void* stream);
-/* counts_host3: queries sent to the overflow pass, queries with candidate
- * records, candidate pairs of the last float32 pass (synchronises). */
-int ct_locate_deferred_count(const void* workspace, int64_t n, int32_t sort_bits, int64_t* counts_host3, void* stream);
+/* counts_host4: queries sent to the overflow pass, queries with candidate
+ * records, candidate pairs, queries the candidate lists left to the
+ * traversal -- of the last float32 pass (synchronises). */
+int ct_locate_deferred_count(const void* workspace, int64_t n, int32_t sort_bits, int64_t* counts_host4, void* stream);
 
 /* locate_points_on_edge query.py:167-174 (locate_point_on_edge 121-164). */
 int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,
@@ -298,6 +327,32 @@ int ct_compact_pairs(const double* area, const uint8_t* flag, int64_t n, const i
  * weights: n x max(3, n_max_vert). */
 int ct_barycentric_weights(const ct_tree* tree, const double* points, const int64_t* face_indices, int64_t n,
                            double tolerance, double* weights, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Adjoints (no upstream counterpart)                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Reverse-mode derivative of ct_area_of_intersection (polygon_polygon_clip_area
+ * sutherland_hodgman.py:83-148 + polygon_area geometry_utils.py:82-95) with
+ * the pairs held fixed: grad_va (n_vertices_a x 2) and grad_vb
+ * (n_vertices_b x 2) are ACCUMULATED (+=) with sum_t grad_area[t] *
+ * d area[t] / d vertex.  The clip is replayed with a tape of at most 160
+ * vertices per pair; CT_DEVERR_CLIP in *error_word if it overflows. */
+int ct_area_of_intersection_grad(const double* vertices_a, const int64_t* faces_a, int32_t n_max_vert_a,
+                                 const double* vertices_b, const int64_t* faces_b, int32_t n_max_vert_b,
+                                 const int64_t* indices_a, const int64_t* indices_b, int64_t n,
+                                 const double* grad_area, double* grad_va, double* grad_vb,
+                                 unsigned int* error_word, void* stream);
+
+/* Reverse-mode derivative of ct_barycentric_weights (barycentric_triangle.py:28-43,
+ * barycentric_wachspress.py:26-85, on-edge branch included) with the face
+ * indices held fixed.  grad_weights: n x n_weights (n_weights = max(3, n_max_vert));
+ * grad_vertices (n_vertices x 2) is ACCUMULATED; grad_points (n x 2, may be
+ * NULL) is written. */
+int ct_barycentric_weights_grad(const double* points, const int64_t* face_indices, int64_t n, const double* vertices,
+                                const int64_t* faces, int32_t n_max_vert, int32_t n_weights, double tolerance,
+                                const double* grad_weights, double* grad_vertices, double* grad_points,
+                                void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Node-bound diagnostics                                                  */

@@ -72,6 +72,12 @@ class CtTree(ctypes.Structure):
         ("grid_y0", ctypes.c_float),
         ("grid_sx", ctypes.c_float),
         ("grid_sy", ctypes.c_float),
+        ("cand_off", _P),
+        ("cand_idx", _P),
+        ("cand_lbox", _P),
+        ("cand_box", _P),
+        ("cand_n", _I64),
+        ("cand_tol", _D),
     ]
 
 
@@ -88,6 +94,9 @@ SIGNATURES = {
     "ct_pessimistic_n_nodes": (_I64, [_I64]),
     "ct_grid_resolution": (_I32, [_I64]),
     "ct_pack_grid": (ctypes.c_int, [_P, _P]),
+    "ct_cand_scratch_size": (_SZ, [_P]),
+    "ct_cand_count": (ctypes.c_int, [_P, _D, _P, _SZ, ctypes.POINTER(_I64), _P]),
+    "ct_cand_fill": (ctypes.c_int, [_P, _P, _SZ, _P]),
     "ct_build_workspace_size": (_SZ, [_I64, _I32, _I32]),
     "ct_build_tree": (
         ctypes.c_int,
@@ -119,6 +128,8 @@ SIGNATURES = {
     "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),
     "ct_area_of_intersection": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
     "ct_box_area_of_intersection": (ctypes.c_int, [_P, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "ct_area_of_intersection_grad": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_barycentric_weights_grad": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I32, _I32, _D, _P, _P, _P, _P]),
     "ct_compact_workspace_size": (_SZ, [_I64]),
     "ct_compact_pairs": (ctypes.c_int, [_P, _P, _I64, _P, _P, _P, _P, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
     "ct_barycentric_weights": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _P, _I64, _D, _P, _P]),

@@ -27,7 +27,12 @@ def default_tolerance(max_bb_diagonal: float) -> float:
 class _GpuTree:
     """Device arrays of one tree and the ``ct_tree`` descriptor over them."""
 
-    def __init__(self, device, elements, vertices, bb_coords, n_buckets: int, cells_per_leaf: int):
+    # query tolerances up to this multiple of the default one use the
+    # candidate lists (widening 2 * 1e-6 of the largest cell diagonal)
+    CAND_TOL_FACTOR = 1.0e6
+
+    def __init__(self, device, elements, vertices, bb_coords, n_buckets: int, cells_per_leaf: int,
+                 candidate_lists: bool = True):
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
@@ -97,6 +102,35 @@ class _GpuTree:
         self.desc.grid_n = gn
         _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
         _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
+        self.cand_off = self.cand_box = self.cand_idx = self.cand_lbox = None
+        if candidate_lists and int(self.desc.grid_n) > 0 and n > 0:
+            self._build_candidate_lists(lib, st)
+
+    def _build_candidate_lists(self, lib, st):
+        """Per-grid-cell candidate lists of the batched float32 locate."""
+        torch = _device.torch()
+        d = self.desc
+        gn = int(d.grid_n)
+        self.cand_off = _device.empty((gn * gn + 1,), torch.int64, self.device)
+        self.cand_box = _device.empty((self.n, 4), torch.float32, self.device)
+        d.cand_off = _device.ptr(self.cand_off)
+        d.cand_box = _device.ptr(self.cand_box)
+        nbytes = int(lib.ct_cand_scratch_size(ctypes.byref(d)))
+        scratch = _device.empty((nbytes,), torch.uint8, self.device)
+        total = ctypes.c_int64(0)
+        cover = default_tolerance(self.max_diagonal) * self.CAND_TOL_FACTOR
+        _lib.check(lib.ct_cand_count(ctypes.byref(d), cover, _device.ptr(scratch), nbytes, ctypes.byref(total), st),
+                   "candidate lists")
+        if d.cand_tol <= 0.0:
+            self.cand_off = self.cand_box = None
+            d.cand_off = d.cand_box = None
+            return
+        m = max(int(total.value), 1)
+        self.cand_idx = _device.empty((m,), torch.int32, self.device)
+        self.cand_lbox = _device.empty((m, 4), torch.float32, self.device)
+        d.cand_idx = _device.ptr(self.cand_idx)
+        d.cand_lbox = _device.ptr(self.cand_lbox)
+        _lib.check(lib.ct_cand_fill(ctypes.byref(d), _device.ptr(scratch), nbytes, st), "candidate lists")
 
     def _fill_desc(self):
         d = self.desc

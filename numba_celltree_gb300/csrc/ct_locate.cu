@@ -61,6 +61,9 @@ struct TreeL {
     const int* gstart;  // start-node grid (null: start at the root)
     int gn;
     float gx0, gy0, gsx, gsy;
+    const int64_t* coff;  // candidate lists (null: off)
+    const int* cidx;
+    const float4* cbox;   // widened box of each list entry
 };
 
 struct Recs {
@@ -217,111 +220,192 @@ __device__ __forceinline__ int node_next(const TreeL& T, int* s, int B, int& sp,
     return right_first ? child + 1 : child;
 }
 
-// Stage 2: float32 traversal with candidate collection.
+// Stage 2b: float32 traversal with candidate collection, over every query
+// (qlist null) or over the queries stage 2a left open (qlist, *qcount).
 template <int KT>
 __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __restrict__ pts,
                                                       const int* __restrict__ order, int64_t n, float tolf, float ohx,
                                                       float olx, float ohy, float oly, int64_t* __restrict__ out,
-                                                      Recs R, int* __restrict__ counters, int* __restrict__ ovf) {
+                                                      Recs R, int* __restrict__ counters, int* __restrict__ ovf,
+                                                      const int* __restrict__ qlist, const int* __restrict__ qcount) {
     extern __shared__ int stk[];
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = i < n;
-    int nc = 0;
-    int cand[CMAX];
-    bool overflow = false;
-    int64_t res = -1;
-    // queries are taken in the sorted order; oi is the query's own index
-    const int oi = active ? (order ? order[i] : (int)i) : 0;
+    const int64_t nq = qlist ? (int64_t)min(*qcount, (int)min(n, (int64_t)INT32_MAX)) : n;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nq; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tq = base + threadIdx.x;
+        bool active = tq < nq;
+        const int64_t i = active ? (qlist ? (int64_t)qlist[tq] : tq) : 0;
+        int nc = 0;
+        int cand[CMAX];
+        bool overflow = false;
+        int64_t res = -1;
+        // queries are taken in the sorted order; oi is the query's own index
+        const int oi = active ? (order ? order[i] : (int)i) : 0;
+        if (active) {
+            double2 pp = pts[oi];
+            float px, py, dpx, dpy;
+            PtSplit P;
+            to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
+            to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+            dpx += T.bandG;
+            dpy += T.bandG;
+            const int B = blockDim.x;
+            int* s = stk + threadIdx.x;
+            int sp = 0;
+            int v = 0;
+            if (T.gstart) {
+                // grid cell of the point; outside the grid (or NaN): the root
+                float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
+                float gn = (float)T.gn;
+                if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) v = T.gstart[(int)fy * T.gn + (int)fx];
+            }
+            // at most n_nodes visits; v = -1: the root path ends without a child
+            int budget = (v < 0) ? 0 : (int)min(T.n_nodes, (int64_t)INT32_MAX - 1) + 1;
+            while (budget > 0) {
+                if (--budget == 0) {
+                    set_error(T.err, CT_DEVERR_LOOP);
+                    break;
+                }
+                float4 q = T.nf[v];
+                int b = nbq(q);
+                if (b < 0) {
+                    int dim = -1 - b;
+                    bool ok = true;
+                    int nx = node_next(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, oi, dim, ok);
+                    if (nx >= 0) {
+                        v = nx;
+                        continue;
+                    }
+                    if (!ok) {
+                        set_error(T.err, CT_DEVERR_STACK);
+                        break;
+                    }
+                } else {
+                    int ptr = na(q);
+                    bool done = false;
+                    for (int j = ptr; j < ptr + b; j++) {
+                        int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                                               (int)T.plen32[j])
+                                          : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                                  (int)T.plen32[j]);
+                        if (r == LF_INSIDE) {
+                            res = T.bbi[j];
+                            done = true;
+                            break;
+                        }
+                        if (r == LF_UNSURE) {
+                            if (nc < CMAX) {
+                                cand[nc++] = j;
+                            } else {
+                                overflow = true;
+                                done = true;
+                                break;
+                            }
+                        }
+                    }
+                    if (done) break;
+                }
+                if (sp == 0) break;
+                v = s[(--sp) * B];
+            }
+        }
+        if (active && !overflow && nc == 0) out[oi] = res;
+        // records for queries with candidates
+        bool want = active && !overflow && nc > 0;
+        unsigned m = __ballot_sync(0xffffffffu, want);
+        if (want) {
+            int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&counters[1], __popc(m));
+            base = __shfl_sync(m, base, leader);
+            int rec = base + __popc(m & lane_lt());
+            if (rec >= R.cap) {
+                overflow = true;  // no record left: the exact pass takes it
+            } else {
+                R.orig[rec] = oi;
+                R.res[rec] = res;
+                R.first[rec] = ~0ull;
+                int pb = atomicAdd(&counters[2], nc);
+                for (int c = 0; c < CMAX; c++)
+                    if (c < nc) R.pairs[pb + c] = make_int4(rec, c, cand[c], 0);
+            }
+        }
+        append(active && overflow, oi, ovf, &counters[0]);
+    }
+}
+
+// Stage 2a: candidate lists.  Per query the cells listed for its grid cell:
+// a float32 bbox reject, then the float32 leaf filter.  Exactly one sure hit
+// with sure misses elsewhere, or sure misses only, is final; otherwise the
+// query's sorted position goes to the list of stage 2b.
+template <int KT>
+__global__ void __launch_bounds__(LOC_THREADS) k_cells(TreeL T, const double2* __restrict__ pts,
+                                                       const int* __restrict__ order, int64_t n, float tolf, float ohx,
+                                                       float olx, float ohy, float oly, int64_t* __restrict__ out,
+                                                       int* __restrict__ qlist, int* __restrict__ qcount) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool active = i < n;
+    bool open = false;
     if (active) {
+        const int oi = order ? order[i] : (int)i;
         double2 pp = pts[oi];
         float px, py, dpx, dpy;
         PtSplit P;
         to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
         to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
-        dpx += T.bandG;
-        dpy += T.bandG;
-        const int B = blockDim.x;
-        int* s = stk + threadIdx.x;
-        int sp = 0;
-        int v = 0;
-        if (T.gstart) {
-            // grid cell of the point; outside the grid (or NaN): the root
-            float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
-            float gn = (float)T.gn;
-            if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) v = T.gstart[(int)fy * T.gn + (int)fx];
-        }
-        // at most n_nodes visits; v = -1: the root path ends without a child
-        int budget = (v < 0) ? 0 : (int)min(T.n_nodes, (int64_t)INT32_MAX - 1) + 1;
-        while (budget > 0) {
-            if (--budget == 0) {
-                set_error(T.err, CT_DEVERR_LOOP);
-                break;
+        float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
+        float gn = (float)T.gn;
+        if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) {
+            const int64_t g = (int64_t)(int)fy * T.gn + (int)fx;
+            const int64_t s0 = T.coff[g], s1 = T.coff[g + 1];
+            // the point's float32 interval
+            const float xl = __fsub_rd(px, dpx), xh = __fadd_ru(px, dpx);
+            const float yl = __fsub_rd(py, dpy), yh = __fadd_ru(py, dpy);
+            int hits = 0, hit = -1;
+            // entry k+1 is loaded while entry k is tested
+            int jn = 0;
+            float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (s0 < s1) {
+                jn = T.cidx[s0];
+                bn = T.cbox[s0];
             }
-            float4 q = T.nf[v];
-            int b = nbq(q);
-            if (b < 0) {
-                int dim = -1 - b;
-                bool ok = true;
-                int nx = node_next(T, s, B, sp, v, q, dim ? py : px, dim ? dpy : dpx, pts, oi, dim, ok);
-                if (nx >= 0) {
-                    v = nx;
-                    continue;
+            for (int64_t k = s0; k < s1; k++) {
+                const int j = jn;
+                const float4 b = bn;
+                if (k + 1 < s1) {
+                    jn = T.cidx[k + 1];
+                    bn = T.cbox[k + 1];
                 }
-                if (!ok) {
-                    set_error(T.err, CT_DEVERR_STACK);
+                if (xh < b.x || xl > b.y || yh < b.z || yl > b.w) continue;  // outside: predicate false
+                int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                                       (int)T.plen32[j])
+                                  : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                                                          (int)T.plen32[j]);
+                if (r == LF_UNSURE) {
+                    open = true;
                     break;
                 }
-            } else {
-                int ptr = na(q);
-                bool done = false;
-                for (int j = ptr; j < ptr + b; j++) {
-                    int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
-                                                                           (int)T.plen32[j])
-                                      : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
-                                                              (int)T.plen32[j]);
-                    if (r == LF_INSIDE) {
-                        res = T.bbi[j];
-                        done = true;
+                if (r == LF_INSIDE) {
+                    hit = j;
+                    if (++hits > 1) {
+                        open = true;
                         break;
                     }
-                    if (r == LF_UNSURE) {
-                        if (nc < CMAX) {
-                            cand[nc++] = j;
-                        } else {
-                            overflow = true;
-                            done = true;
-                            break;
-                        }
-                    }
                 }
-                if (done) break;
             }
-            if (sp == 0) break;
-            v = s[(--sp) * B];
-        }
-    }
-    if (active && !overflow && nc == 0) out[oi] = res;
-    // records for queries with candidates
-    bool want = active && !overflow && nc > 0;
-    unsigned m = __ballot_sync(0xffffffffu, want);
-    if (want) {
-        int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(&counters[1], __popc(m));
-        base = __shfl_sync(m, base, leader);
-        int rec = base + __popc(m & lane_lt());
-        if (rec >= R.cap) {
-            overflow = true;  // no record left: the exact pass takes it
+            if (!open) out[oi] = hits ? T.bbi[hit] : -1;
         } else {
-            R.orig[rec] = oi;
-            R.res[rec] = res;
-            R.first[rec] = ~0ull;
-            int pb = atomicAdd(&counters[2], nc);
-            for (int c = 0; c < CMAX; c++)
-                if (c < nc) R.pairs[pb + c] = make_int4(rec, c, cand[c], 0);
+            open = true;
         }
     }
-    append(active && overflow, oi, ovf, &counters[0]);
+    // warp-aggregated append of the open queries
+    unsigned m = __ballot_sync(0xffffffffu, open);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int b0 = 0;
+        if (lane == leader) b0 = atomicAdd(qcount, __popc(m));
+        b0 = __shfl_sync(0xffffffffu, b0, leader);
+        if (open) qlist[b0 + __popc(m & lane_lt())] = (int)i;
+    }
 }
 
 // Stage 3: exact float64 test of every candidate pair.
@@ -597,6 +681,54 @@ __global__ void k_grid_start(const float4* __restrict__ nf, int gn, float x0, fl
 }
 
 // ---------------------------------------------------------------------------
+// candidate lists
+// ---------------------------------------------------------------------------
+// Widened bbox of every cell (leaf order) in the float32 frame, rounded
+// outward: the region where the cell's predicate can be true.
+__global__ void k_cand_box(const double* __restrict__ bb, const int64_t* __restrict__ bbi, int64_t n, double ox,
+                           double oy, double M, float4* __restrict__ box) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double* b = bb + 4 * bbi[j];
+        box[j] = make_float4(__double2float_rd((b[0] - ox) - M), __double2float_ru((b[1] - ox) + M),
+                             __double2float_rd((b[2] - oy) - M), __double2float_ru((b[3] - oy) + M));
+    }
+}
+
+// Grid cells met by a widened box: cell gx spans [x0 + gx / sx, x0 + (gx + 1) / sx]
+// widened by m.
+__device__ __forceinline__ bool cand_range(float4 b, int gn, double x0, double y0, double sx, double sy, double m,
+                                           int* gx0, int* gx1, int* gy0, int* gy1) {
+    double ax = ((double)b.x - m - x0) * sx, bx = ((double)b.y + m - x0) * sx;
+    double ay = ((double)b.z - m - y0) * sy, by = ((double)b.w + m - y0) * sy;
+    if (!(bx >= 0.0 && ax < (double)gn && by >= 0.0 && ay < (double)gn)) return false;  // also NaN
+    *gx0 = (int)fmax(floor(ax - 1e-9), 0.0);
+    *gx1 = (int)fmin(floor(bx + 1e-9), (double)(gn - 1));
+    *gy0 = (int)fmax(floor(ay - 1e-9), 0.0);
+    *gy1 = (int)fmin(floor(by + 1e-9), (double)(gn - 1));
+    return true;
+}
+
+template <bool FILL>
+__global__ void k_cand_lists(const float4* __restrict__ box, int64_t n, int gn, double x0, double y0, double sx,
+                             double sy, double m, unsigned long long* __restrict__ count,
+                             const int64_t* __restrict__ off, int* __restrict__ idx, float4* __restrict__ lbox) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        int a0, a1, b0, b1;
+        const float4 b = box[j];
+        if (!cand_range(b, gn, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) continue;
+        for (int gy = b0; gy <= b1; gy++)
+            for (int gx = a0; gx <= a1; gx++) {
+                int64_t g = (int64_t)gy * gn + gx;
+                unsigned long long k = atomicAdd(&count[g], 1ull);
+                if (FILL) {
+                    idx[off[g] + (int64_t)k] = (int)j;
+                    lbox[off[g] + (int64_t)k] = b;
+                }
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 static inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -607,11 +739,12 @@ struct LocWS {
     unsigned* keyB;
     int* idxB;
     int* ovf;
+    int* open;  // sorted positions left open by the candidate-list stage
     Recs R;
     int64_t* hist;
     void* scan_ws;
     size_t scan_bytes;
-    int* counters;  // [0] overflow, [1] records, [2] pairs
+    int* counters;  // [0] overflow, [1] records, [2] pairs, [3] open after the candidate lists
 };
 
 static int rec_cap_for(int64_t n) { return (int)std::min<int64_t>(n / 8 + 4096, (int64_t)INT32_MAX / 8); }
@@ -634,6 +767,7 @@ static size_t carve_loc(void* ws, int64_t n, int32_t sort_bits, LocWS* L) {
     l.keyB = (unsigned*)take(sorted ? 4 * nn : 16);
     l.idxB = (int*)take(sorted ? 4 * nn : 16);
     l.ovf = (int*)take(4 * nn);
+    l.open = (int*)take(4 * nn);
     l.R.orig = (int*)take(4 * rc);
     l.R.res = (int64_t*)take(8 * rc);
     l.R.first = (unsigned long long*)take(8 * rc);
@@ -674,6 +808,9 @@ static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws
     }
     T->gstart = (t->grid_start && t->grid_n > 0) ? t->grid_start : nullptr;
     T->gn = T->gstart ? t->grid_n : 0;
+    T->coff = (T->gstart && t->cand_off && t->cand_idx && t->cand_lbox && t->cand_tol > 0.0) ? t->cand_off : nullptr;
+    T->cidx = t->cand_idx;
+    T->cbox = (const float4*)t->cand_lbox;
     T->gx0 = t->grid_x0;
     T->gy0 = t->grid_y0;
     T->gsx = t->grid_sx;
@@ -749,6 +886,79 @@ int ct_pack_grid(ct_tree* t, void* stream) {
     return CT_OK;
 }
 
+// cell-assignment margin of the grid (same bound as the start-node grid)
+static double grid_margin(const ct_tree* t) {
+    double ex = t->bbox[1] - t->bbox[0], ey = t->bbox[3] - t->bbox[2];
+    double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
+                        std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
+    return std::ldexp(std::max(ex, ey) + F, -19);
+}
+
+size_t ct_cand_scratch_size(const ct_tree* t) {
+    if (!t || t->grid_n <= 0) return 256;
+    int64_t cells = (int64_t)t->grid_n * t->grid_n;
+    return a256(8 * (size_t)(cells + 1)) + a256(ct_scan_workspace_size(cells + 1)) + 256;
+}
+
+int ct_cand_count(ct_tree* t, double cover_tol, void* scratch, size_t scratch_bytes, int64_t* total_host,
+                  void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!t || !total_host) return ct_fail(CT_ERR_ARG, "null argument");
+    *total_host = 0;
+    t->cand_n = 0;
+    t->cand_tol = 0.0;
+    if (t->grid_n <= 0 || !t->grid_start) return CT_OK;  // no grid: lists off
+    if (!t->cand_off || !t->cand_box) return ct_fail(CT_ERR_ARG, "cand_off / cand_box not set");
+    if (!(cover_tol >= 0.0) || !std::isfinite(cover_tol)) return ct_fail(CT_ERR_ARG, "cover_tol must be finite and >= 0");
+    if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
+    const int gn = t->grid_n;
+    const int64_t cells = (int64_t)gn * gn;
+    unsigned long long* count = (unsigned long long*)scratch;  // cells + 1 entries, the last stays 0
+    void* scan_ws = (char*)scratch + a256(8 * (size_t)(cells + 1));
+    size_t scan_bytes = scratch_bytes - a256(8 * (size_t)(cells + 1));
+    // widening: the on-edge test reaches 2 tol beyond an edge's bbox; float64
+    // rounding of the coordinates (abs_eps each) moves the tests by a few ulp
+    double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
+                        std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
+    double M = 2.0 * cover_tol * (1.0 + 1e-6) + 16.0 * (double)t->abs_eps + std::ldexp(F, -48);
+    int64_t n = t->n_elements;
+    unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    k_cand_box<<<blocks, 256, 0, st>>>(t->bb_coords, t->bb_indices, n, t->origin[0], t->origin[1], M,
+                                       (float4*)t->cand_box);
+    CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)(cells + 1), st));
+    double m = grid_margin(t);
+    k_cand_lists<false><<<blocks, 256, 0, st>>>((const float4*)t->cand_box, n, gn, t->grid_x0, t->grid_y0,
+                                                t->grid_sx, t->grid_sy, m, count, nullptr, nullptr, nullptr);
+    CT_CHECK_LAUNCH("candidate counts");
+    int64_t total = 0;
+    int s = ct_exclusive_scan((const int64_t*)count, cells + 1, t->cand_off, scan_ws, scan_bytes, &total, stream);
+    if (s) return s;
+    if (total > INT32_MAX) return CT_OK;  // too many entries for int offsets of the pairs: lists off
+    t->cand_n = total;
+    t->cand_tol = cover_tol > 0.0 ? cover_tol : 1e-300;
+    *total_host = total;
+    return CT_OK;
+}
+
+int ct_cand_fill(ct_tree* t, void* scratch, size_t scratch_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (t->cand_tol <= 0.0 || t->grid_n <= 0) return CT_OK;
+    if ((!t->cand_idx || !t->cand_lbox) && t->cand_n > 0) return ct_fail(CT_ERR_ARG, "cand_idx / cand_lbox not set");
+    if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
+    const int gn = t->grid_n;
+    const int64_t cells = (int64_t)gn * gn;
+    unsigned long long* count = (unsigned long long*)scratch;
+    CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)cells, st));
+    int64_t n = t->n_elements;
+    unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    k_cand_lists<true><<<blocks, 256, 0, st>>>((const float4*)t->cand_box, n, gn, t->grid_x0, t->grid_y0,
+                                               t->grid_sx, t->grid_sy, grid_margin(t), count, t->cand_off,
+                                               t->cand_idx, (float4*)t->cand_lbox);
+    CT_CHECK_LAUNCH("candidate lists");
+    return CT_OK;
+}
+
 size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits) {
     if (sort_bits != 0 && sort_bits != 8 && sort_bits != 16 && sort_bits != 24) return 0;
     return carve_loc(nullptr, n, sort_bits, nullptr);
@@ -817,17 +1027,27 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
     size_t smem = (size_t)T.stack * LOC_THREADS * sizeof(int);
     unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
+    // stage 2a (candidate lists) when they cover this tolerance; stage 2b
+    // then traverses only the queries left open
+    const bool lists = T.coff && tol <= t->cand_tol;
+    const int* qlist = lists ? L.open : nullptr;
+    const int* qcount = lists ? &L.counters[3] : nullptr;
+    unsigned grid_b = lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16) : grid;
+#define CT_FAST_STAGES(KT)                                                                                       \
+    if (lists)                                                                                                    \
+        k_cells<KT><<<grid, LOC_THREADS, 0, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.open,            \
+                                                  &L.counters[3]);                                                \
+    smem_attr<KT>(smem);                                                                                          \
+    k_fast<KT><<<grid_b, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters,  \
+                                                  L.ovf, qlist, qcount);
     if (T.K == 3) {
-        smem_attr<3>(smem);
-        k_fast<3><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters, L.ovf);
+        CT_FAST_STAGES(3)
     } else if (T.K == 4) {
-        smem_attr<4>(smem);
-        k_fast<4><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters, L.ovf);
+        CT_FAST_STAGES(4)
     } else {
-        smem_attr<32>(smem);
-        k_fast<32><<<grid, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters,
-                                                    L.ovf);
+        CT_FAST_STAGES(32)
     }
+#undef CT_FAST_STAGES
     CT_CHECK_LAUNCH("locate fast");
     return CT_OK;
 }
@@ -863,16 +1083,14 @@ int ct_locate_exact(const ct_tree* t, const double* points, int64_t n, double to
     return CT_OK;
 }
 
-int ct_locate_deferred_count(const void* ws, int64_t n, int32_t G, int64_t* counts_host3, void* stream) {
+int ct_locate_deferred_count(const void* ws, int64_t n, int32_t G, int64_t* counts_host4, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     LocWS L;
     carve_loc((void*)ws, n, G, &L);
-    int c[3] = {0, 0, 0};
+    int c[4] = {0, 0, 0, 0};
     CT_CUDA(cudaMemcpyAsync(c, L.counters, sizeof(c), cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
-    counts_host3[0] = c[0];
-    counts_host3[1] = c[1];
-    counts_host3[2] = c[2];
+    for (int k = 0; k < 4; k++) counts_host4[k] = c[k];
     return CT_OK;
 }
 

@@ -54,7 +54,7 @@ class EdgeCellTree2d(CellTree2dBase):
             lib.ct_edge_bboxes(_device.ptr(v_d), _device.ptr(e_d), n, global_tolerance, _device.ptr(bb), st),
             "edge_bboxes",
         )
-        self._tree = _GpuTree(device, e_d, v_d, bb, n_buckets, cells_per_leaf)
+        self._tree = _GpuTree(device, e_d, v_d, bb, n_buckets, cells_per_leaf, candidate_lists=False)
         self._host = {}
         self._edges_in = edges
         self.n_buckets = n_buckets

@@ -226,3 +226,47 @@ def test_build_rejects_zero_height_mesh(oracle):
         oracle.OracleCellTree2d(xy, f, -1)
     with pytest.raises(CellTreeError):
         CellTree2d(xy, f, -1)
+
+
+@pytest.mark.gpu
+def test_locate_record_capacity_overflow(oracle):
+    """Every query on an edge or vertex: far more uncertain queries than
+    candidate records (n/8 + 4096), so most take the float64 overflow pass."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(80, seed=31, extent=(80.0, 80.0), offset=(3.0e5, 6.0e6))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    rng = np.random.default_rng(3)
+    pts = np.concatenate([syn.near_edge_points(xy, f, 60000, dist=0.0, seed=5),
+                          xy[rng.integers(0, len(xy), 20000)]])
+    ref = o.locate_points(pts)
+    g.precision = "fp32"
+    assert np.array_equal(g.locate_points(pts), ref)
+
+
+@pytest.mark.gpu
+def test_locate_candidate_lists_and_overlaps(oracle):
+    """Candidate lists: populated for face trees; overlapping cells (every
+    point inside two cells) go through the traversal and keep the
+    reference's first hit; a tolerance above the lists' cover uses the
+    traversal for every query."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.quad_mesh(40, 30, seed=6, extent=(40.0, 30.0), offset=(2.0e5, 3.0e6))
+    g = CellTree2d(xy, f, -1)
+    d = g._tree.desc
+    assert d.cand_tol > 0 and d.cand_n >= len(f)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = np.concatenate([syn.uniform_points(30000, xy.min(0) - 0.3, xy.max(0) + 0.3, seed=8),
+                          syn.near_edge_points(xy, f, 5000, dist=1e-9, seed=9)])
+    ref = o.locate_points(pts)
+    assert np.array_equal(g.locate_points(pts), ref)
+    for tol in (d.cand_tol * 0.5, d.cand_tol * 4.0, 1e-3):
+        assert np.array_equal(g.locate_points(pts, tol), o.locate_points(pts, tol)), tol
+    # two copies of the mesh, the second shifted by half a cell
+    xy2 = np.concatenate([xy, xy + [0.5, 0.5]])
+    f2 = np.concatenate([f, f + len(xy)])
+    g2 = CellTree2d(xy2, f2, -1)
+    o2 = oracle.OracleCellTree2d(xy2, f2, -1)
+    assert np.array_equal(g2.locate_points(pts), o2.locate_points(pts))
