@@ -41,7 +41,7 @@ BYTES_PER_POINT = 24  # 16 B xy in + 8 B index out
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nx", type=int, default=4000)
@@ -93,7 +93,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
                  "-i", str(self.index)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
             )
@@ -217,7 +217,7 @@ def run_reference(args):
         t0 = time.perf_counter()
         tree.locate_points(pts, tol)
         times.append(time.perf_counter() - t0)
-    step = max(times)
+    step = sum(times) / len(times)
     value = n / step / 1e6
     out = {
         "impl": "reference",
@@ -340,6 +340,12 @@ def main():
     identical = bool(torch.equal(out32, out64))
     found = int((out32 >= 0).sum().item())
 
+    # kernels per batched step: radix sort (key+hist, scan x3, scatter for the
+    # first 8-bit digit; hist, scan x3, scatter for each further digit),
+    # candidate lists + open-query traversal, pair tests, resolve, overflow
+    passes = bins // 8
+    lists = t.cand_idx is not None and tol <= float(t.desc.cand_tol)
+    launches_per_step = (5 * passes if bins else 0) + (2 if lists else 1) + 3
     value = ws * n / (ms32 * 1e-3) / 1e6
     value64 = ws * n / (ms64 * 1e-3) / 1e6
 
@@ -395,7 +401,7 @@ def main():
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "traffic": (round(tpp * n) if tpp is not None else None),
-            "kernel": "ctl::k_fast<3> (float32 pass, one launch per step)",
+            "kernel": "float32 pass: ctl::k_cells<3> (candidate lists) + ctl::k_fast<3> over the open queries",
             "kernel_ms": round(ms_fast, 3)}
     result = {
         "metric": METRIC,
@@ -427,7 +433,7 @@ def main():
                      "pairs": int(dcount[2]), "fraction": round((dcount[0] + dcount[1]) / n, 5)},
         "indices_identical_fp32_fp64": identical,
         "points_found": found,
-        "gpu_launches": args.steps * (7 if bins else 4),
+        "gpu_launches": args.steps * launches_per_step,
         "clocks": clocks,
         "roofline": roof,
         "cpu_baseline": cpu,
