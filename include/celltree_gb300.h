@@ -254,6 +254,29 @@ int ct_locate_exact(const ct_tree* tree, const double* points, int64_t n, double
  * traversal -- of the last float32 pass (synchronises). */
 int ct_locate_deferred_count(const void* workspace, int64_t n, int32_t sort_bits, int64_t* counts_host4, void* stream);
 
+/* A batch of face trees (no upstream counterpart): the points of every tree
+ * located by one pipeline -- queries sorted by (tree, Morton key over that
+ * tree's bbox), then the candidate-list, traversal, float64-pair, resolve and
+ * overflow stages with the tree looked up per query.  Results equal
+ * ct_locate_points on each tree.  points: n_points x 2, the points of tree i
+ * at rows point_off[i] .. point_off[i + 1] - 1; tolerances: one per tree.
+ * ct_forest_locate_prepare uploads the tree records (synchronises; call it
+ * again when a tree or a tolerance changes); ct_forest_locate only enqueues
+ * kernels and memsets, so it can be captured in a CUDA graph and replayed. */
+typedef struct ct_forest_plan {
+    int64_t n_points;
+    int32_t n_trees;
+    int32_t kt;           /* leaf-filter width: 3, 4 or 32 (largest n_max_vert) */
+    int32_t stack;        /* traversal stack entries per query (deepest tree + 2) */
+    int32_t morton_bits;  /* Morton bits of the sort key below the tree bits */
+} ct_forest_plan;
+size_t ct_forest_locate_workspace_size(int64_t n_points, int32_t n_trees);
+int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double* tolerances,
+                             const int64_t* point_off, int64_t n_points, ct_forest_plan* plan, void* workspace,
+                             size_t workspace_bytes, void* stream);
+int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* out, void* workspace,
+                     size_t workspace_bytes, void* stream);
+
 /* locate_points_on_edge query.py:167-174 (locate_point_on_edge 121-164). */
 int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,
                              int64_t* out, void* stream);
@@ -327,6 +350,27 @@ int ct_compact_pairs(const double* area, const uint8_t* flag, int64_t n, const i
  * weights: n x max(3, n_max_vert). */
 int ct_barycentric_weights(const ct_tree* tree, const double* points, const int64_t* face_indices, int64_t n,
                            double tolerance, double* weights, void* stream);
+
+/* ---------------------------------------------------------------------- */
+/* Batched build (no upstream counterpart)                                 */
+/* ---------------------------------------------------------------------- */
+
+/* build (creation.py:233-381) of n_trees trees at once: the bounding boxes of
+ * all trees concatenated (tree i at rows tree_off[i] .. tree_off[i + 1] - 1,
+ * tree_off host memory, every tree non-empty), built level by level together
+ * (one host synchronisation per level for the whole batch).  n_nodes_host /
+ * max_depth_host: one entry per tree.  Each tree's nodes and bb_indices are
+ * identical to ct_build_tree on its own boxes. */
+size_t ct_build_forest_workspace_size(int64_t n_total, int32_t n_trees, int32_t n_buckets, int32_t capacity_factor);
+int ct_build_forest(const double* bb_coords, int64_t n_total, const int64_t* tree_off, int32_t n_trees,
+                    int32_t n_buckets, int64_t cells_per_leaf, int32_t capacity_factor, void* workspace,
+                    size_t workspace_bytes, int64_t* n_nodes_host, int32_t* max_depth_host, void* stream);
+/* node_off: device, n_trees + 1 node offsets (prefix sums of n_nodes); the
+ * node arrays hold every tree's nodes at its offset (child, ptr relative to
+ * the tree); bb_indices (n_total) hold each tree's indices at its rows. */
+int ct_build_forest_emit(const void* workspace, int64_t n_total, int32_t n_trees, int32_t n_buckets,
+                         int32_t capacity_factor, const int64_t* node_off, int64_t* child, double* Lmax, double* Rmin,
+                         int64_t* ptr, int64_t* size, uint8_t* dim, int64_t* bb_indices, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Adjoints (no upstream counterpart)                                      */

@@ -2,9 +2,10 @@
 EdgeCellTree2d whose construction and queries run as hand-written sm_103a
 CUDA kernels (libcelltree_gb300.so)."""
 
+from .batch import CellTreeBatch
 from .celltree import CellTree2d
 from .edge_celltree import EdgeCellTree2d
 
 __version__ = "0.1.0"
 
-__all__ = ("CellTree2d", "EdgeCellTree2d")
+__all__ = ("CellTree2d", "CellTreeBatch", "EdgeCellTree2d")

@@ -81,6 +81,18 @@ class CtTree(ctypes.Structure):
     ]
 
 
+class CtForestPlan(ctypes.Structure):
+    """Mirror of ``struct ct_forest_plan``."""
+
+    _fields_ = [
+        ("n_points", _I64),
+        ("n_trees", _I32),
+        ("kt", _I32),
+        ("stack", _I32),
+        ("morton_bits", _I32),
+    ]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "ct_abi_version": (ctypes.c_int, []),
@@ -93,6 +105,14 @@ SIGNATURES = {
     "ct_vertex_extent": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_D), _P]),
     "ct_pessimistic_n_nodes": (_I64, [_I64]),
     "ct_grid_resolution": (_I32, [_I64]),
+    "ct_build_forest_workspace_size": (_SZ, [_I64, _I32, _I32, _I32]),
+    "ct_build_forest": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), _I32, _I32, _I64, _I32, _P, _SZ,
+                                       ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P]),
+    "ct_build_forest_emit": (ctypes.c_int, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ct_forest_locate_workspace_size": (_SZ, [_I64, _I32]),
+    "ct_forest_locate_prepare": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_D), ctypes.POINTER(_I64), _I64,
+                                                _P, _P, _SZ, _P]),
+    "ct_forest_locate": (ctypes.c_int, [_P, _P, _P, _P, _SZ, _P]),
     "ct_pack_grid": (ctypes.c_int, [_P, _P]),
     "ct_cand_scratch_size": (_SZ, [_P]),
     "ct_cand_count": (ctypes.c_int, [_P, _D, _P, _SZ, ctypes.POINTER(_I64), _P]),

@@ -32,7 +32,7 @@ class _GpuTree:
     CAND_TOL_FACTOR = 1.0e6
 
     def __init__(self, device, elements, vertices, bb_coords, n_buckets: int, cells_per_leaf: int,
-                 candidate_lists: bool = True):
+                 candidate_lists: bool = True, prebuilt=None):
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
@@ -50,7 +50,36 @@ class _GpuTree:
         _lib.check(lib.ct_bbox_summary(_device.ptr(bb_coords), n, _device.ptr(self.bb_distances), summ, st), "bbox")
         self.bbox = np.array(summ[:4], dtype=np.float64)
         self.max_diagonal = float(summ[4]) if n > 0 else 0.0
-        # build (creation.py:384-413)
+        if prebuilt is not None:
+            # nodes and bb_indices built elsewhere (a batched forest build)
+            (self.node_child, self.node_Lmax, self.node_Rmin, self.node_ptr, self.node_size, self.node_dim,
+             self.bb_indices, self.max_depth) = prebuilt
+            nn = int(self.node_child.shape[0])
+            self.n_nodes = nn
+        else:
+            nn = self._build(lib, st, device, bb_coords, n, n_buckets, cells_per_leaf)
+        # packed traversal arrays
+        self.nodes_f32 = _device.empty((max(nn, 1), 4), torch.float32, device)
+        self.nodes_f64 = _device.empty((max(nn, 1), 2), torch.float64, device)
+        self.poly_f64 = _device.empty((max(n, 1), K, 2), torch.float64, device)
+        self.poly_f32 = _device.empty((max(n, 1), lib.ct_poly32_stride(K), 4), torch.float32, device)
+        self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
+        self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
+        self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
+        gn = int(lib.ct_grid_resolution(n))
+        self.grid_start = _device.empty((gn * gn,), torch.int32, device)
+        self.desc = _lib.CtTree()
+        self._fill_desc()
+        self.desc.grid_n = gn
+        _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
+        _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
+        self.cand_off = self.cand_box = self.cand_idx = self.cand_lbox = None
+        if candidate_lists and int(self.desc.grid_n) > 0 and n > 0:
+            self._build_candidate_lists(lib, st)
+
+    def _build(self, lib, st, device, bb_coords, n, n_buckets, cells_per_leaf) -> int:
+        """build (creation.py:384-413) into node_* and bb_indices; returns n_nodes."""
+        torch = _device.torch()
         factor = 1
         while True:
             wsz = lib.ct_build_workspace_size(n, n_buckets, factor)
@@ -87,24 +116,7 @@ class _GpuTree:
             "build_emit",
         )
         del ws
-        # packed traversal arrays
-        self.nodes_f32 = _device.empty((max(nn, 1), 4), torch.float32, device)
-        self.nodes_f64 = _device.empty((max(nn, 1), 2), torch.float64, device)
-        self.poly_f64 = _device.empty((max(n, 1), K, 2), torch.float64, device)
-        self.poly_f32 = _device.empty((max(n, 1), lib.ct_poly32_stride(K), 4), torch.float32, device)
-        self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
-        self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
-        self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
-        gn = int(lib.ct_grid_resolution(n))
-        self.grid_start = _device.empty((gn * gn,), torch.int32, device)
-        self.desc = _lib.CtTree()
-        self._fill_desc()
-        self.desc.grid_n = gn
-        _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
-        _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
-        self.cand_off = self.cand_box = self.cand_idx = self.cand_lbox = None
-        if candidate_lists and int(self.desc.grid_n) > 0 and n > 0:
-            self._build_candidate_lists(lib, st)
+        return nn
 
     def _build_candidate_lists(self, lib, st):
         """Per-grid-cell candidate lists of the batched float32 locate."""

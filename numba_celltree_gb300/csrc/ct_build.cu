@@ -60,6 +60,7 @@ struct ARec {
     int level, tile0;
     int tile1, split_dim;
     int nlocal, err;
+    int tree, pad_;    // tree of the node (forest builds; 0 otherwise)
 };
 
 // Phase-B local node record (subtree numbering, local ids).
@@ -100,12 +101,19 @@ struct WS {
     LRec* lrec;                      // [2 * n]
     Counters* cnt;
     int* level_begin;                // [rec_cap + 1] host mirror written per level
+    // per tree (a forest build has n_roots trees, root records 0 .. n_roots-1)
+    int n_roots;
+    int64_t* tree_off;               // [n_roots + 1] element offsets
+    int* elem_tree;                  // [n] tree of each element position
+    unsigned long long* root_key;    // [n_roots][4]
+    int* root_zp;                    // [n_roots][4]
+    int* tree_depth;                 // [n_roots]
 };
 
 static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Carves the workspace; returns total bytes.  base == nullptr -> size only.
-static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws) {
+static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_trees = 1) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> char* {
         char* p = base ? base + off : nullptr;
@@ -113,7 +121,8 @@ static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws) {
         return p;
     };
     int64_t nn = n > 0 ? n : 1;
-    int rec_cap = (int)std::min<int64_t>(INT32_MAX / 4, (int64_t)factor * (8 * (nn / SMALL) + 64));
+    int rec_cap = (int)std::min<int64_t>(INT32_MAX / 4,
+                                         (int64_t)factor * (8 * (nn / SMALL) + 64) + 3 * (int64_t)n_trees);
     int tile_cap = (int)std::min<int64_t>(INT32_MAX / 4, 2 * (nn / TILE_MIN) + 2 * (int64_t)rec_cap + 64);
     WS w;
     for (int b = 0; b < 2; b++) {
@@ -137,6 +146,12 @@ static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws) {
     w.lrec = (LRec*)take(sizeof(LRec) * 2 * nn);
     w.cnt = (Counters*)take(sizeof(Counters));
     w.level_begin = nullptr;
+    w.n_roots = n_trees;
+    w.tree_off = (int64_t*)take(sizeof(int64_t) * ((size_t)n_trees + 1));
+    w.elem_tree = (int*)take(n_trees > 1 ? sizeof(int) * nn : 16);
+    w.root_key = (unsigned long long*)take(sizeof(unsigned long long) * 4 * (size_t)n_trees);
+    w.root_zp = (int*)take(sizeof(int) * 4 * (size_t)n_trees);
+    w.tree_depth = (int*)take(sizeof(int) * (size_t)n_trees);
     if (ws) *ws = w;
     return off;
 }
@@ -319,6 +334,7 @@ __global__ void k_reset(WS ws, int n, int cpl_small_root, int root_dim) {
     r.Lmax = -1.0;
     r.Rmin = -1.0;
     ws.recs[0] = r;
+    ws.tree_depth[0] = 0;
     if (n <= SMALL) {
         ws.small_list[0] = 0;
         c->small_count = 1;
@@ -623,6 +639,7 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
         ch.child = -1;
         ch.parity = 1 - parity;
         ch.level = R->level + 1;
+        ch.tree = R->tree;
         ch.split_dim = -1;
         ch.Lmax = -1.0;
         ch.Rmin = -1.0;
@@ -634,6 +651,7 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
             ws.small_list[sl] = c + lane;
         }
         atomicMax(&ws.cnt->max_depth, ch.level);
+        atomicMax(&ws.tree_depth[R->tree], ch.level);
     }
     if (lane == 0) {
         R->kind = K_SPLIT;
@@ -961,6 +979,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         RR->nlocal = nloc;
         RR->err = err ? 1 : 0;
         atomicMax(&ws.cnt->max_depth, maxd);
+        atomicMax(&ws.tree_depth[RR->tree], maxd);
         if (err) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
     }
 }
@@ -982,7 +1001,7 @@ __global__ void k_number_down(WS ws, int b, int e) {
     int r = b + blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= e) return;
     ARec* R = &ws.recs[r];
-    if (r == 0) {
+    if (r < ws.n_roots) {  // every tree is numbered from its own root
         R->S = 0;
         R->pos = 0;
     }
@@ -1015,42 +1034,148 @@ __device__ __forceinline__ void put_node(const NodesOut& o, long long pos, long 
     o.dim[pos] = (uint8_t)(dim != 0);
 }
 
-__global__ void k_emit_phaseA(WS ws, int nrec, long long n_nodes, NodesOut o) {
+// node_off (forest builds): first output node of every tree; node counts
+// n_nodes of one tree are node_off[t + 1] - node_off[t].  Positions, children
+// and ptr are written relative to the node's own tree.
+__device__ __forceinline__ void tree_frame(const WS& ws, const int64_t* node_off, long long n_nodes, int t,
+                                           long long* noff, long long* nn, long long* eoff) {
+    if (node_off) {
+        *noff = node_off[t];
+        *nn = node_off[t + 1] - node_off[t];
+        *eoff = ws.tree_off[t];
+    } else {
+        *noff = 0;
+        *nn = n_nodes;
+        *eoff = 0;
+    }
+}
+
+__global__ void k_emit_phaseA(WS ws, int nrec, long long n_nodes, NodesOut o, const int64_t* node_off) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrec) return;
     const ARec* R = &ws.recs[r];
     if (R->kind != K_SPLIT && R->kind != K_LEAF) return;
-    if (R->pos < 0 || R->pos >= n_nodes) {
+    long long noff, nn, eoff;
+    tree_frame(ws, node_off, n_nodes, R->tree, &noff, &nn, &eoff);
+    if (R->pos < 0 || R->pos >= nn) {
         atomicOr(&ws.cnt->err, 0x40000000u);
         return;
     }
-    if (R->kind == K_SPLIT) put_node(o, R->pos, 1 + 2 * R->S, R->Lmax, R->Rmin, R->ptr, R->size, R->dim);
-    else put_node(o, R->pos, -1, R->Lmax, R->Rmin, R->ptr, R->size, R->dim);
+    if (R->kind == K_SPLIT) put_node(o, noff + R->pos, 1 + 2 * R->S, R->Lmax, R->Rmin, R->ptr - eoff, R->size, R->dim);
+    else put_node(o, noff + R->pos, -1, R->Lmax, R->Rmin, R->ptr - eoff, R->size, R->dim);
 }
 
 // One warp per subtree root: local records to their final positions.
-__global__ void k_emit_subtrees(WS ws, long long n_nodes, NodesOut o) {
+__global__ void k_emit_subtrees(WS ws, long long n_nodes, NodesOut o, const int64_t* node_off) {
     int lane = threadIdx.x & 31;
     int sidx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (sidx >= ws.cnt->small_count) return;
     const ARec* R = &ws.recs[ws.small_list[sidx]];
     const LRec* L = ws.lrec + 2 * (size_t)R->ptr;
     long long off = 2 * R->S;
+    long long noff, nn, eoff;
+    tree_frame(ws, node_off, n_nodes, R->tree, &noff, &nn, &eoff);
     for (int j = lane; j < R->nlocal; j += 32) {
         LRec a = L[j];
         long long pos = (j == 0) ? R->pos : (long long)j + off;
         long long child = (a.child < 0) ? -1 : (long long)a.child + off;
-        if (pos < 0 || pos >= n_nodes || child >= n_nodes) {
+        if (pos < 0 || pos >= nn || child >= nn) {
             atomicOr(&ws.cnt->err, 0x40000000u);
             continue;
         }
-        put_node(o, pos, child, a.Lmax, a.Rmin, a.ptr, a.size, a.dim);
+        put_node(o, noff + pos, child, a.Lmax, a.Rmin, a.ptr - eoff, a.size, a.dim);
     }
 }
 
-__global__ void k_emit_indices(WS ws, int n, int64_t* bb_indices) {
+__global__ void k_emit_indices(WS ws, int n, int64_t* bb_indices, bool forest) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        bb_indices[i] = ws.final_idx[i];
+        bb_indices[i] = forest ? ws.final_idx[i] - ws.tree_off[ws.elem_tree[i]] : ws.final_idx[i];
+}
+
+// ------------------------------------------------------------------------
+// forest initialisation: one root record per tree
+// ------------------------------------------------------------------------
+
+__global__ void k_forest_reset(WS ws) {
+    Counters* c = ws.cnt;
+    c->rec_count = ws.n_roots;
+    c->tile_count = 0;
+    c->small_count = 0;
+    c->err = 0;
+    c->max_depth = 0;
+    c->lb = 0;
+    c->le = ws.n_roots;
+}
+
+__global__ void k_forest_roots(WS ws) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ws.n_roots; t += gridDim.x * blockDim.x) {
+        ARec r;
+        memset(&r, 0, sizeof(r));
+        r.ptr = (int)ws.tree_off[t];
+        r.size = (int)(ws.tree_off[t + 1] - ws.tree_off[t]);
+        r.dim = 0;
+        r.kind = (r.size > SMALL) ? K_PENDING : K_SUBTREE;
+        r.child = -1;
+        r.level = 0;
+        r.split_dim = -1;
+        r.Lmax = -1.0;
+        r.Rmin = -1.0;
+        r.tree = t;
+        ws.recs[t] = r;
+        ws.tree_depth[t] = 0;
+        for (int f = 0; f < 4; f++) {
+            ws.root_key[4 * t + f] = ~0ull;
+            ws.root_zp[4 * t + f] = INT32_MAX;
+        }
+        if (r.kind == K_SUBTREE) ws.small_list[atomicAdd(&ws.cnt->small_count, 1)] = t;
+    }
+}
+
+__global__ void k_forest_elem_tree(WS ws, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int lo = 0, hi = ws.n_roots;  // tree_off[lo] <= i < tree_off[hi]
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (ws.tree_off[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        ws.elem_tree[i] = lo;
+    }
+}
+
+// First-occurrence bounds of every tree's boxes (root get_bounds, per tree).
+__global__ void k_forest_root_bounds(WS ws, int n) {
+    const unsigned FULL = 0xffffffffu;
+    int stride = gridDim.x * blockDim.x;
+    int iters = (n + stride - 1) / stride;
+    for (int it = 0; it < iters; it++) {
+        int i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool valid = i < n;
+        int t = valid ? ws.elem_tree[i] : -1;
+        unsigned same = __match_any_sync(FULL, t);
+        for (int f = 0; f < 4; f++) {
+            unsigned long long kk = ~0ull;
+            if (valid) {
+                double v = ws.f[0][f][i];
+                kk = (f & 1) ? ~fkey(v) : fkey(v);
+                if (is_zero(v)) atomicMin(&ws.root_zp[4 * t + f], i);
+            }
+            if (same == FULL) {
+                unsigned long long m = group_min_k(FULL, kk);
+                if ((threadIdx.x & 31) == 0 && t >= 0) atomicMin(&ws.root_key[4 * t + f], m);
+            } else if (valid) {
+                atomicMin(&ws.root_key[4 * t + f], kk);
+            }
+        }
+    }
+}
+
+__global__ void k_forest_root_resolve(WS ws) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ws.n_roots; t += gridDim.x * blockDim.x) {
+        if (ws.tree_off[t + 1] <= ws.tree_off[t]) continue;
+        for (int f = 0; f < 4; f++)
+            ws.recs[t].bnd[f] = resolve_key(ws.root_key[4 * t + f], f, ws.root_zp[4 * t + f], ws.f[0][f]);
+    }
 }
 
 }  // namespace ct
@@ -1075,40 +1200,27 @@ size_t ct_build_workspace_size(int64_t n, int32_t NB, int32_t factor) {
     return carve(nullptr, n, NB, factor, nullptr);
 }
 
-int ct_build_tree(const double* bb, int64_t n, int32_t NB, int64_t cpl, int32_t factor, void* workspace,
-                  size_t ws_bytes, int64_t* n_nodes_host, int32_t* max_depth_host, void* stream) {
-    cudaStream_t st = (cudaStream_t)stream;
-    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
-    if (cpl < 1) return ct_fail(CT_ERR_ARG, "cells_per_leaf must be >= 1");
-    if (n < 0 || n >= (int64_t)INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "n_elements out of range");
-    if (factor < 1) return ct_fail(CT_ERR_ARG, "capacity_factor must be >= 1");
-    size_t need = carve(nullptr, n, NB, factor, nullptr);
-    if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
-    if (n > 0 && !bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
-    WS ws;
-    carve((char*)workspace, n, NB, factor, &ws);
-    int ni = (int)n;
+}  // extern "C"
+
+namespace ct {
+
+// Phases A, B and C over the root records already in place (one per tree).
+// Returns the record count through *nrec_out; one host synchronisation per
+// phase-A level.
+static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_phase_a, int n_roots,
+                        Counters* hc_out) {
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(SUB_WARPS * sizeof(SubSmem)));
         attr_set = true;
     }
-    int root_dim = 0;
-    k_reset<<<1, 1, 0, st>>>(ws, ni, 0, root_dim);
-    if (ni > 0) {
-        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
-        k_init_elems<<<g, 256, 0, st>>>(bb, ni, ws);
-        k_root_bounds<<<g, 256, 0, st>>>(ws, ni);
-        k_root_resolve<<<1, 1, 0, st>>>(ws, ni);
-    }
-    CT_CHECK_LAUNCH("build init");
     std::vector<int> level_b, level_e;
     level_b.push_back(0);
-    level_e.push_back(1);
+    level_e.push_back(n_roots);
     int parity = 0;
     Counters hc;
-    if (ni > SMALL) {
+    if (run_phase_a) {
         while (true) {
             int lb = level_b.back(), le = level_e.back();
             int width = le - lb;
@@ -1160,16 +1272,72 @@ int ct_build_tree(const double* bb, int64_t n, int32_t NB, int64_t cpl, int32_t 
     }
     CT_CHECK_LAUNCH("numbering");
     CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-    long long root_splits = 0;
-    CT_CUDA(cudaMemcpyAsync(&root_splits, &ws.recs[0].splits, sizeof(long long), cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
     if (hc.err & CT_DEVERR_BUCKET)
         return ct_fail(CT_ERR_DEVICE, "tree construction failed: a cell centroid fell outside every bucket");
-    if (n_nodes_host) *n_nodes_host = 1 + 2 * root_splits;
-    if (max_depth_host) *max_depth_host = hc.max_depth;
-    // remember the record count for ct_build_emit
+    // remember the record count for the emit call
     CT_CUDA(cudaMemcpyAsync(&ws.cnt->pad, &hc.rec_count, sizeof(int), cudaMemcpyHostToDevice, st));
     CT_CUDA(cudaStreamSynchronize(st));
+    *hc_out = hc;
+    return CT_OK;
+}
+
+static int emit_nodes(const WS& ws, int64_t n, long long n_nodes, const int64_t* node_off, int64_t* child,
+                      double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim, int64_t* bb_indices,
+                      cudaStream_t st) {
+    Counters hc;
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    int nrec = hc.pad;
+    NodesOut o{child, Lmax, Rmin, ptr, size, dim};
+    k_emit_phaseA<<<(nrec + 255) / 256, 256, 0, st>>>(ws, nrec, n_nodes, o, node_off);
+    if (hc.small_count > 0)
+        k_emit_subtrees<<<(hc.small_count * 32 + 127) / 128, 128, 0, st>>>(ws, n_nodes, o, node_off);
+    if (n > 0) {
+        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        k_emit_indices<<<g, 256, 0, st>>>(ws, (int)n, bb_indices, node_off != nullptr);
+    }
+    CT_CHECK_LAUNCH("emit");
+    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    if (hc.err & 0x40000000u) return ct_fail(CT_ERR_DEVICE, "tree emission: node position out of range");
+    return CT_OK;
+}
+
+}  // namespace ct
+
+extern "C" {
+
+int ct_build_tree(const double* bb, int64_t n, int32_t NB, int64_t cpl, int32_t factor, void* workspace,
+                  size_t ws_bytes, int64_t* n_nodes_host, int32_t* max_depth_host, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
+    if (cpl < 1) return ct_fail(CT_ERR_ARG, "cells_per_leaf must be >= 1");
+    if (n < 0 || n >= (int64_t)INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "n_elements out of range");
+    if (factor < 1) return ct_fail(CT_ERR_ARG, "capacity_factor must be >= 1");
+    size_t need = carve(nullptr, n, NB, factor, nullptr);
+    if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
+    if (n > 0 && !bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
+    WS ws;
+    carve((char*)workspace, n, NB, factor, &ws);
+    int ni = (int)n;
+    int root_dim = 0;
+    k_reset<<<1, 1, 0, st>>>(ws, ni, 0, root_dim);
+    if (ni > 0) {
+        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+        k_init_elems<<<g, 256, 0, st>>>(bb, ni, ws);
+        k_root_bounds<<<g, 256, 0, st>>>(ws, ni);
+        k_root_resolve<<<1, 1, 0, st>>>(ws, ni);
+    }
+    CT_CHECK_LAUNCH("build init");
+    Counters hc;
+    int s = build_levels(ws, st, NB, cpl, ni > SMALL, 1, &hc);
+    if (s) return s;
+    long long root_splits = 0;
+    CT_CUDA(cudaMemcpyAsync(&root_splits, &ws.recs[0].splits, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    if (n_nodes_host) *n_nodes_host = 1 + 2 * root_splits;
+    if (max_depth_host) *max_depth_host = hc.max_depth;
     return CT_OK;
 }
 
@@ -1179,26 +1347,75 @@ int ct_build_emit(const void* workspace, int64_t n, int32_t NB, int32_t factor, 
     if (NB < 2 || NB > NBMAX || factor < 1) return ct_fail(CT_ERR_ARG, "bad n_buckets / capacity_factor");
     WS ws;
     carve((char*)workspace, n, NB, factor, &ws);
-    Counters hc;
-    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
-    CT_CUDA(cudaStreamSynchronize(st));
-    int nrec = hc.pad;
     long long root_splits = 0;
     CT_CUDA(cudaMemcpyAsync(&root_splits, &ws.recs[0].splits, sizeof(long long), cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
-    long long n_nodes = 1 + 2 * root_splits;
-    NodesOut o{child, Lmax, Rmin, ptr, size, dim};
-    k_emit_phaseA<<<(nrec + 255) / 256, 256, 0, st>>>(ws, nrec, n_nodes, o);
-    if (hc.small_count > 0) k_emit_subtrees<<<(hc.small_count * 32 + 127) / 128, 128, 0, st>>>(ws, n_nodes, o);
-    if (n > 0) {
-        int g = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
-        k_emit_indices<<<g, 256, 0, st>>>(ws, (int)n, bb_indices);
+    return emit_nodes(ws, n, 1 + 2 * root_splits, nullptr, child, Lmax, Rmin, ptr, size, dim, bb_indices, st);
+}
+
+size_t ct_build_forest_workspace_size(int64_t n_total, int32_t n_trees, int32_t NB, int32_t factor) {
+    if (NB < 2 || NB > NBMAX || n_total < 0 || factor < 1 || n_trees < 1) return 0;
+    return carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+}
+
+int ct_build_forest(const double* bb, int64_t n_total, const int64_t* tree_off_host, int32_t n_trees, int32_t NB,
+                    int64_t cpl, int32_t factor, void* workspace, size_t ws_bytes, int64_t* n_nodes_host,
+                    int32_t* max_depth_host, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
+    if (cpl < 1) return ct_fail(CT_ERR_ARG, "cells_per_leaf must be >= 1");
+    if (n_trees < 1 || !tree_off_host) return ct_fail(CT_ERR_ARG, "need at least one tree");
+    if (n_total < 0 || n_total >= (int64_t)INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "n_elements out of range");
+    if (factor < 1) return ct_fail(CT_ERR_ARG, "capacity_factor must be >= 1");
+    if (tree_off_host[0] != 0 || tree_off_host[n_trees] != n_total)
+        return ct_fail(CT_ERR_ARG, "tree offsets must start at 0 and end at n_total");
+    bool any_large = false;
+    for (int t = 0; t < n_trees; t++) {
+        int64_t m = tree_off_host[t + 1] - tree_off_host[t];
+        if (m < 1) return ct_fail(CT_ERR_ARG, "every tree needs at least one element");
+        any_large |= m > SMALL;
     }
-    CT_CHECK_LAUNCH("emit");
-    CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+    if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
+    if (!bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
+    WS ws;
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    int ni = (int)n_total;
+    CT_CUDA(cudaMemcpyAsync(ws.tree_off, tree_off_host, sizeof(int64_t) * ((size_t)n_trees + 1),
+                            cudaMemcpyHostToDevice, st));
+    int g = (int)std::min<int64_t>((n_total + 255) / 256, 152 * 8);
+    int gt = (int)std::min<int64_t>((n_trees + 255) / 256, 152 * 8);
+    k_forest_reset<<<1, 1, 0, st>>>(ws);
+    k_forest_roots<<<gt, 256, 0, st>>>(ws);
+    k_init_elems<<<g, 256, 0, st>>>(bb, ni, ws);
+    k_forest_elem_tree<<<g, 256, 0, st>>>(ws, ni);
+    k_forest_root_bounds<<<g, 256, 0, st>>>(ws, ni);
+    k_forest_root_resolve<<<gt, 256, 0, st>>>(ws);
+    CT_CHECK_LAUNCH("forest init");
+    Counters hc;
+    int s = build_levels(ws, st, NB, cpl, any_large, n_trees, &hc);
+    if (s) return s;
+    std::vector<ARec> roots(n_trees);
+    std::vector<int> depth(n_trees);
+    CT_CUDA(cudaMemcpyAsync(roots.data(), ws.recs, sizeof(ARec) * n_trees, cudaMemcpyDeviceToHost, st));
+    CT_CUDA(cudaMemcpyAsync(depth.data(), ws.tree_depth, sizeof(int) * n_trees, cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
-    if (hc.err & 0x40000000u) return ct_fail(CT_ERR_DEVICE, "tree emission: node position out of range");
+    for (int t = 0; t < n_trees; t++) {
+        if (n_nodes_host) n_nodes_host[t] = 1 + 2 * roots[t].splits;
+        if (max_depth_host) max_depth_host[t] = depth[t];
+    }
     return CT_OK;
+}
+
+int ct_build_forest_emit(const void* workspace, int64_t n_total, int32_t n_trees, int32_t NB, int32_t factor,
+                         const int64_t* node_off, int64_t* child, double* Lmax, double* Rmin, int64_t* ptr,
+                         int64_t* size, uint8_t* dim, int64_t* bb_indices, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX || factor < 1 || n_trees < 1) return ct_fail(CT_ERR_ARG, "bad arguments");
+    if (!node_off) return ct_fail(CT_ERR_ARG, "node_off is null");
+    WS ws;
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    return emit_nodes(ws, n_total, 0, node_off, child, Lmax, Rmin, ptr, size, dim, bb_indices, st);
 }
 
 }  // extern "C"

@@ -27,6 +27,8 @@
 // binning is safe.  The traversal stack lives in shared memory.
 #include <cfloat>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "ct_common.cuh"
 #include "ct_internal.h"
@@ -64,7 +66,19 @@ struct TreeL {
     const int64_t* coff;  // candidate lists (null: off)
     const int* cidx;
     const float4* cbox;   // widened box of each list entry
+    double tol;           // query tolerance
+    float tolf;           // tol rounded up to float32
+    float ohx, olx, ohy, oly;  // float32 frame origin, split hi + lo
 };
+
+// The tree of a query: the kernel's own (one tree) or the query's entry of a
+// device array of trees (a batch of meshes, tree index per query).
+template <bool MULTI>
+__device__ __forceinline__ const TreeL& tree_of(const TreeL& T0, const TreeL* __restrict__ forest,
+                                                const int* __restrict__ qtree, int oi) {
+    if (MULTI) return forest[qtree[oi]];
+    return T0;
+}
 
 struct Recs {
     int* orig;                 // query index in the caller's order
@@ -222,12 +236,12 @@ __device__ __forceinline__ int node_next(const TreeL& T, int* s, int B, int& sp,
 
 // Stage 2b: float32 traversal with candidate collection, over every query
 // (qlist null) or over the queries stage 2a left open (qlist, *qcount).
-template <int KT>
-__global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __restrict__ pts,
-                                                      const int* __restrict__ order, int64_t n, float tolf, float ohx,
-                                                      float olx, float ohy, float oly, int64_t* __restrict__ out,
-                                                      Recs R, int* __restrict__ counters, int* __restrict__ ovf,
-                                                      const int* __restrict__ qlist, const int* __restrict__ qcount) {
+template <int KT, bool MULTI>
+__global__ void __launch_bounds__(LOC_THREADS)
+    k_fast(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
+           const double2* __restrict__ pts, const int* __restrict__ order, int64_t n, int64_t* __restrict__ out, Recs R,
+           int* __restrict__ counters, int* __restrict__ ovf, const int* __restrict__ qlist,
+           const int* __restrict__ qcount) {
     extern __shared__ int stk[];
     const int64_t nq = qlist ? (int64_t)min(*qcount, (int)min(n, (int64_t)INT32_MAX)) : n;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nq; base += (int64_t)gridDim.x * blockDim.x) {
@@ -241,11 +255,12 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
         // queries are taken in the sorted order; oi is the query's own index
         const int oi = active ? (order ? order[i] : (int)i) : 0;
         if (active) {
+            const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
             double2 pp = pts[oi];
             float px, py, dpx, dpy;
             PtSplit P;
-            to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
-            to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+            to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
+            to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
             dpx += T.bandG;
             dpy += T.bandG;
             const int B = blockDim.x;
@@ -283,9 +298,9 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
                     int ptr = na(q);
                     bool done = false;
                     for (int j = ptr; j < ptr + b; j++) {
-                        int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
-                                                                               (int)T.plen32[j])
-                                          : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                        int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(
+                                                P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j])
+                                          : leaf_filter_local<KT>(P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4,
                                                                   (int)T.plen32[j]);
                         if (r == LF_INSIDE) {
                             res = T.bbi[j];
@@ -337,24 +352,25 @@ __global__ void __launch_bounds__(LOC_THREADS) k_fast(TreeL T, const double2* __
 // a float32 bbox reject, then the float32 leaf filter.  Exactly one sure hit
 // with sure misses elsewhere, or sure misses only, is final; otherwise the
 // query's sorted position goes to the list of stage 2b.
-template <int KT>
-__global__ void __launch_bounds__(LOC_THREADS) k_cells(TreeL T, const double2* __restrict__ pts,
-                                                       const int* __restrict__ order, int64_t n, float tolf, float ohx,
-                                                       float olx, float ohy, float oly, int64_t* __restrict__ out,
-                                                       int* __restrict__ qlist, int* __restrict__ qcount) {
+template <int KT, bool MULTI>
+__global__ void __launch_bounds__(LOC_THREADS)
+    k_cells(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
+            const double2* __restrict__ pts, const int* __restrict__ order, int64_t n, int64_t* __restrict__ out,
+            int* __restrict__ qlist, int* __restrict__ qcount) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < n;
     bool open = false;
     if (active) {
         const int oi = order ? order[i] : (int)i;
+        const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
         double2 pp = pts[oi];
         float px, py, dpx, dpy;
         PtSplit P;
-        to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
-        to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+        to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
+        to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
         float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
         float gn = (float)T.gn;
-        if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) {
+        if (T.coff && fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) {
             const int64_t g = (int64_t)(int)fy * T.gn + (int)fx;
             const int64_t s0 = T.coff[g], s1 = T.coff[g + 1];
             // the point's float32 interval
@@ -376,9 +392,9 @@ __global__ void __launch_bounds__(LOC_THREADS) k_cells(TreeL T, const double2* _
                     bn = T.cbox[k + 1];
                 }
                 if (xh < b.x || xl > b.y || yh < b.z || yl > b.w) continue;  // outside: predicate false
-                int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
-                                                                       (int)T.plen32[j])
-                                  : leaf_filter_local<KT>(P, T.dabs, tolf, T.polyf + (size_t)j * T.S4,
+                int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(
+                                        P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j])
+                                  : leaf_filter_local<KT>(P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4,
                                                           (int)T.plen32[j]);
                 if (r == LF_UNSURE) {
                     open = true;
@@ -409,48 +425,59 @@ __global__ void __launch_bounds__(LOC_THREADS) k_cells(TreeL T, const double2* _
 }
 
 // Stage 3: exact float64 test of every candidate pair.
-__global__ void __launch_bounds__(LOC_THREADS) k_pip(TreeL T, const double2* __restrict__ pts, Recs R,
-                                                     const int* __restrict__ counters, double tol) {
+template <bool MULTI>
+__global__ void __launch_bounds__(LOC_THREADS)
+    k_pip(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
+          const double2* __restrict__ pts, Recs R, const int* __restrict__ counters) {
     int npairs = counters[2];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npairs; t += gridDim.x * blockDim.x) {
         int4 pr = R.pairs[t];
-        double2 pp = pts[R.orig[pr.x]];
+        const int oi = R.orig[pr.x];
+        const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
+        double2 pp = pts[oi];
         int j = pr.z;
         const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
         int len = T.plen ? (int)T.plen[j] : T.K;
-        if (pip_or_edge(mkp(pp.x, pp.y), poly, len, tol))
+        if (pip_or_edge(mkp(pp.x, pp.y), poly, len, T.tol))
             atomicMin(&R.first[pr.x], ((unsigned long long)(unsigned)pr.y << 32) | (unsigned)j);
     }
 }
 
 // Stage 4: first true candidate, else the fast pass's hit.
-__global__ void k_resolve(TreeL T, Recs R, const int* __restrict__ counters, int64_t* __restrict__ out) {
+template <bool MULTI>
+__global__ void k_resolve(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest,
+                          const int* __restrict__ qtree, Recs R, const int* __restrict__ counters,
+                          int64_t* __restrict__ out) {
     int nrec = min(counters[1], R.cap);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
         unsigned long long f = R.first[r];
-        out[R.orig[r]] = (f != ~0ull) ? T.bbi[(int)(f & 0xffffffffull)] : R.res[r];
+        const int oi = R.orig[r];
+        const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
+        out[oi] = (f != ~0ull) ? T.bbi[(int)(f & 0xffffffffull)] : R.res[r];
     }
 }
 
 // Stage 5: overflow queries, float32 bands with float64 re-decisions.
-template <int KT>
-__global__ void __launch_bounds__(LOC_THREADS) k_exact(TreeL T, const double2* __restrict__ pts,
-                                                       const int* __restrict__ list,
-                                                       const int* __restrict__ counters, double tol, float tolf,
-                                                       float ohx, float olx, float ohy, float oly,
-                                                       int64_t* __restrict__ out) {
+template <int KT, bool MULTI>
+__global__ void __launch_bounds__(LOC_THREADS)
+    k_exact(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
+            const double2* __restrict__ pts, const int* __restrict__ list, const int* __restrict__ counters,
+            int64_t* __restrict__ out) {
     extern __shared__ int stk[];
     const int B = blockDim.x;
     int* s = stk + threadIdx.x;
     int cnt = counters[0];
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt; t += gridDim.x * blockDim.x) {
         int i = list[t];
+        const TreeL& T = tree_of<MULTI>(T0, forest, qtree, i);
+        const double tol = T.tol;
+        const float tolf = T.tolf;
         double2 pp = pts[i];
         dpt p = mkp(pp.x, pp.y);
         float px, py, dpx, dpy;
         PtSplit P;
-        to_frame(pp.x, ohx, olx, &px, &dpx, &P.xh, &P.xl);
-        to_frame(pp.y, ohy, oly, &py, &dpy, &P.yh, &P.yl);
+        to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
+        to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
         dpx += T.bandG;
         dpy += T.bandG;
         int sp = 1;
@@ -544,6 +571,39 @@ __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, 
         key[i] = k;
         idx[i] = (int)i;
         atomicAdd(&h[w][(k >> shift) & 255u], 1);
+    }
+    __syncthreads();
+    int c = 0;
+    for (int k = 0; k < RS_T / 32; k++) c += h[k][t];
+    hist[(int64_t)t * gridDim.x + blockIdx.x] = c;
+}
+
+// Keys of a batch of trees: the point's tree (binary search of the point
+// offsets) in the high bits, the top `mbits` bits of its Morton key over its
+// own tree's bbox below; histogram of the lowest digit.
+__global__ void __launch_bounds__(RS_T) k_keys_forest(const double2* __restrict__ pts, int64_t n, int64_t chunk,
+                                                       const Grid* __restrict__ grids,
+                                                       const int64_t* __restrict__ poff, int n_trees, int mbits,
+                                                       unsigned* __restrict__ key, int* __restrict__ idx,
+                                                       int* __restrict__ qtree, int64_t* __restrict__ hist) {
+    __shared__ int h[RS_T / 32][256];
+    const int t = threadIdx.x, w = t >> 5;
+    for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
+    __syncthreads();
+    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    for (int64_t i = s + t; i < e; i += RS_T) {
+        int lo = 0, hi = n_trees;  // poff[lo] <= i < poff[hi]
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (poff[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        unsigned m = morton24(grids[lo], pts[i]) >> (24 - mbits);
+        unsigned k = ((unsigned)lo << mbits) | m;
+        key[i] = k;
+        idx[i] = (int)i;
+        qtree[i] = lo;
+        atomicAdd(&h[w][k & 255u], 1);
     }
     __syncthreads();
     int c = 0;
@@ -781,13 +841,16 @@ static size_t carve_loc(void* ws, int64_t n, int32_t sort_bits, LocWS* L) {
     return off;
 }
 
-static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws_bytes, TreeL* T) {
+static void origin_split(double o, float* hi, float* lo) {
+    *hi = (float)o;
+    *lo = (float)(o - (double)*hi);
+}
+
+// Device-side view of one packed tree for queries at tolerance `tol`.
+static int fill_tree(const ct_tree* t, double tol, TreeL* T) {
     if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
-    if (n >= INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "at most 2^30 points per call");
     if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
-    if (G != 0 && G != 8 && G != 16 && G != 24) return ct_fail(CT_ERR_ARG, "sort_bits must be 0, 8, 16 or 24");
-    if (!ws || ws_bytes < carve_loc(nullptr, n, G, nullptr))
-        return ct_fail(CT_ERR_WORKSPACE, "locate workspace too small");
+    memset(T, 0, sizeof(*T));
     T->nf = (const float4*)t->nodes_f32;
     T->nd = (const double2*)t->nodes_f64;
     T->poly = (const double2*)t->poly_f64;
@@ -808,7 +871,10 @@ static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws
     }
     T->gstart = (t->grid_start && t->grid_n > 0) ? t->grid_start : nullptr;
     T->gn = T->gstart ? t->grid_n : 0;
-    T->coff = (T->gstart && t->cand_off && t->cand_idx && t->cand_lbox && t->cand_tol > 0.0) ? t->cand_off : nullptr;
+    // candidate lists only when they cover this tolerance
+    T->coff = (T->gstart && t->cand_off && t->cand_idx && t->cand_lbox && t->cand_tol > 0.0 && tol <= t->cand_tol)
+                  ? t->cand_off
+                  : nullptr;
     T->cidx = t->cand_idx;
     T->cbox = (const float4*)t->cand_lbox;
     T->gx0 = t->grid_x0;
@@ -818,21 +884,66 @@ static int make_tree(const ct_tree* t, int64_t n, int32_t G, void* ws, size_t ws
     T->K = t->n_max_vert;
     T->S4 = poly32_stride(t->n_max_vert);
     T->stack = t->max_depth + 2;
+    T->tol = tol;
+    T->tolf = (float)tol;
+    if ((double)T->tolf < tol) T->tolf = nextafterf(T->tolf, INFINITY);
+    origin_split(T->ox, &T->ohx, &T->olx);
+    origin_split(T->oy, &T->ohy, &T->oly);
     if (T->stack > 128) return ct_fail(CT_ERR_ARG, "tree deeper than 126 levels for the batched form");
     return CT_OK;
 }
 
-template <int KT>
+static int make_tree(const ct_tree* t, int64_t n, int32_t G, double tol, void* ws, size_t ws_bytes, TreeL* T) {
+    if (n >= INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "at most 2^30 points per call");
+    if (G != 0 && G != 8 && G != 16 && G != 24) return ct_fail(CT_ERR_ARG, "sort_bits must be 0, 8, 16 or 24");
+    if (!ws || ws_bytes < carve_loc(nullptr, n, G, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "locate workspace too small");
+    return fill_tree(t, tol, T);
+}
+
+template <int KT, bool MULTI>
 static void smem_attr(size_t smem) {
     if (smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_fast<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_exact<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_fast<KT, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_exact<KT, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
 }
 
-static void origin_split(double o, float* hi, float* lo) {
-    *hi = (float)o;
-    *lo = (float)(o - (double)*hi);
+static Grid morton_grid(const ct_tree* t) {
+    Grid g;
+    double xmin = t->bbox[0], xmax = t->bbox[1], ymin = t->bbox[2], ymax = t->bbox[3];
+    double wx = xmax - xmin, wy = ymax - ymin;
+    g.x0 = (float)xmin;
+    g.y0 = (float)ymin;
+    g.sx = (wx > 0) ? (float)(4096.0 / wx) : 0.0f;
+    g.sy = (wy > 0) ? (float)(4096.0 / wy) : 0.0f;
+    return g;
+}
+
+// Batch of trees: device array of the trees, their Morton grids, the point
+// offsets of every tree and the tree of every point, after the LocWS part.
+struct ForestWS {
+    TreeL* trees;
+    Grid* grids;
+    int64_t* poff;
+    int* qtree;
+};
+
+static size_t carve_forest(void* ws, int64_t n, int n_trees, LocWS* L, ForestWS* F) {
+    size_t off = carve_loc(ws, n, 32, L);
+    char* base = (char*)ws;
+    auto take = [&](size_t b) {
+        char* p = base ? base + off : nullptr;
+        off += a256(b);
+        return p;
+    };
+    ForestWS f;
+    f.trees = (TreeL*)take(sizeof(TreeL) * (size_t)n_trees);
+    f.grids = (Grid*)take(sizeof(Grid) * (size_t)n_trees);
+    f.poff = (int64_t*)take(sizeof(int64_t) * ((size_t)n_trees + 1));
+    f.qtree = (int*)take(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (F) *F = f;
+    return off;
 }
 
 }  // namespace ctl
@@ -971,18 +1082,12 @@ int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sor
                   void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     TreeL T;
-    int s = make_tree(t, n, sort_bits, ws, ws_bytes, &T);
+    int s = make_tree(t, n, sort_bits, 0.0, ws, ws_bytes, &T);
     if (s) return s;
     if (n == 0 || sort_bits == 0) return CT_OK;
     LocWS L;
     carve_loc(ws, n, sort_bits, &L);
-    Grid g;
-    double xmin = t->bbox[0], xmax = t->bbox[1], ymin = t->bbox[2], ymax = t->bbox[3];
-    double wx = xmax - xmin, wy = ymax - ymin;
-    g.x0 = (float)xmin;
-    g.y0 = (float)ymin;
-    g.sx = (wx > 0) ? (float)(4096.0 / wx) : 0.0f;
-    g.sy = (wy > 0) ? (float)(4096.0 / wy) : 0.0f;
+    Grid g = morton_grid(t);
     int passes = sort_bits / 8;
     // ping-pong so that the last pass writes the permutation into L.order
     unsigned* kin = (passes & 1) ? L.keyB : L.keyA;
@@ -1012,7 +1117,7 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
                    size_t ws_bytes, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     TreeL T;
-    int s = make_tree(t, n, G, ws, ws_bytes, &T);
+    int s = make_tree(t, n, G, tol, ws, ws_bytes, &T);
     if (s) return s;
     LocWS L;
     carve_loc(ws, n, G, &L);
@@ -1020,26 +1125,21 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     if (n == 0) return CT_OK;
     const double2* P = (const double2*)points;
     const int* ord = G > 0 ? L.order : nullptr;
-    float ohx, olx, ohy, oly;
-    origin_split(T.ox, &ohx, &olx);
-    origin_split(T.oy, &ohy, &oly);
-    float tolf = (float)tol;
-    if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
     size_t smem = (size_t)T.stack * LOC_THREADS * sizeof(int);
     unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
     // stage 2a (candidate lists) when they cover this tolerance; stage 2b
     // then traverses only the queries left open
-    const bool lists = T.coff && tol <= t->cand_tol;
+    const bool lists = T.coff != nullptr;
     const int* qlist = lists ? L.open : nullptr;
     const int* qcount = lists ? &L.counters[3] : nullptr;
     unsigned grid_b = lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16) : grid;
-#define CT_FAST_STAGES(KT)                                                                                       \
-    if (lists)                                                                                                    \
-        k_cells<KT><<<grid, LOC_THREADS, 0, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.open,            \
-                                                  &L.counters[3]);                                                \
-    smem_attr<KT>(smem);                                                                                          \
-    k_fast<KT><<<grid_b, LOC_THREADS, smem, st>>>(T, P, ord, n, tolf, ohx, olx, ohy, oly, out, L.R, L.counters,  \
-                                                  L.ovf, qlist, qcount);
+#define CT_FAST_STAGES(KT)                                                                                        \
+    if (lists)                                                                                                     \
+        k_cells<KT, false><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, L.open,              \
+                                                         &L.counters[3]);                                          \
+    smem_attr<KT, false>(smem);                                                                                    \
+    k_fast<KT, false><<<grid_b, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, ord, n, out, L.R, L.counters,    \
+                                                         L.ovf, qlist, qcount);
     if (T.K == 3) {
         CT_FAST_STAGES(3)
     } else if (T.K == 4) {
@@ -1056,29 +1156,21 @@ int ct_locate_exact(const ct_tree* t, const double* points, int64_t n, double to
                     size_t ws_bytes, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     TreeL T;
-    int s = make_tree(t, n, G, ws, ws_bytes, &T);
+    int s = make_tree(t, n, G, tol, ws, ws_bytes, &T);
     if (s) return s;
     if (n == 0) return CT_OK;
     LocWS L;
     carve_loc(ws, n, G, &L);
     const double2* P = (const double2*)points;
-    float ohx, olx, ohy, oly;
-    origin_split(T.ox, &ohx, &olx);
-    origin_split(T.oy, &ohy, &oly);
-    float tolf = (float)tol;
-    if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
-    k_pip<<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, P, L.R, L.counters, tol);
-    k_resolve<<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, L.R, L.counters, out);
+    k_pip<false><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, L.R, L.counters);
+    k_resolve<false><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, L.R, L.counters, out);
     size_t smem = (size_t)T.stack * LOC_THREADS * sizeof(int);
     if (T.K == 3)
-        k_exact<3><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy, oly,
-                                                          out);
+        k_exact<3, false><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, L.ovf, L.counters, out);
     else if (T.K == 4)
-        k_exact<4><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy, oly,
-                                                          out);
+        k_exact<4, false><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, L.ovf, L.counters, out);
     else
-        k_exact<32><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, P, L.ovf, L.counters, tol, tolf, ohx, olx, ohy,
-                                                           oly, out);
+        k_exact<32, false><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, L.ovf, L.counters, out);
     CT_CHECK_LAUNCH("locate exact");
     return CT_OK;
 }
@@ -1101,6 +1193,123 @@ int ct_locate_points_batched(const ct_tree* t, const double* points, int64_t n, 
     s = ct_locate_fast(t, points, n, tol, G, out, ws, ws_bytes, stream);
     if (s) return s;
     return ct_locate_exact(t, points, n, tol, G, out, ws, ws_bytes, stream);
+}
+
+// ---------------------------------------------------------------------------
+// a batch of trees: one pipeline for the points of every tree
+// ---------------------------------------------------------------------------
+
+size_t ct_forest_locate_workspace_size(int64_t n_points, int32_t n_trees) {
+    if (n_points < 0 || n_trees < 1) return 0;
+    return carve_forest(nullptr, n_points, n_trees, nullptr, nullptr);
+}
+
+int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double* tolerances,
+                             const int64_t* point_off, int64_t n_points, ct_forest_plan* plan, void* ws,
+                             size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!trees || !tolerances || !point_off || !plan || n_trees < 1) return ct_fail(CT_ERR_ARG, "null argument");
+    if (n_points < 0 || n_points >= INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "at most 2^30 points per call");
+    if (point_off[0] != 0 || point_off[n_trees] != n_points)
+        return ct_fail(CT_ERR_ARG, "point offsets must start at 0 and end at n_points");
+    for (int i = 0; i < n_trees; i++)
+        if (point_off[i + 1] < point_off[i]) return ct_fail(CT_ERR_ARG, "point offsets must not decrease");
+    if (!ws || ws_bytes < carve_forest(nullptr, n_points, n_trees, nullptr, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "forest locate workspace too small");
+    LocWS L;
+    ForestWS F;
+    carve_forest(ws, n_points, n_trees, &L, &F);
+    std::vector<TreeL> tl((size_t)n_trees);
+    std::vector<Grid> gr((size_t)n_trees);
+    int kmax = 0, stack = 0;
+    for (int i = 0; i < n_trees; i++) {
+        int s = fill_tree(&trees[i], tolerances[i], &tl[i]);
+        if (s) return s;
+        gr[i] = morton_grid(&trees[i]);
+        kmax = std::max(kmax, tl[i].K);
+        stack = std::max(stack, tl[i].stack);
+    }
+    int tree_bits = 0;
+    while ((1 << tree_bits) < n_trees) tree_bits++;
+    if (tree_bits > 24) return ct_fail(CT_ERR_ARG, "at most 2^24 trees per batch");
+    int mbits = std::min(24, 32 - tree_bits) & ~1;
+    plan->n_points = n_points;
+    plan->n_trees = n_trees;
+    plan->kt = (kmax <= 3) ? 3 : (kmax <= 4 ? 4 : 32);
+    plan->stack = stack;
+    plan->morton_bits = mbits;
+    CT_CUDA(cudaMemcpyAsync(F.trees, tl.data(), sizeof(TreeL) * tl.size(), cudaMemcpyHostToDevice, st));
+    CT_CUDA(cudaMemcpyAsync(F.grids, gr.data(), sizeof(Grid) * gr.size(), cudaMemcpyHostToDevice, st));
+    CT_CUDA(cudaMemcpyAsync(F.poff, point_off, sizeof(int64_t) * ((size_t)n_trees + 1), cudaMemcpyHostToDevice, st));
+    CT_CUDA(cudaStreamSynchronize(st));  // the host vectors go out of scope
+    size_t smem = (size_t)stack * LOC_THREADS * sizeof(int);
+    if (plan->kt == 3) smem_attr<3, true>(smem);
+    else if (plan->kt == 4) smem_attr<4, true>(smem);
+    else smem_attr<32, true>(smem);
+    return CT_OK;
+}
+
+// Kernel launches only (no host synchronisation, no host copies): can be
+// captured in a CUDA graph once prepared.
+int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* out, void* ws, size_t ws_bytes,
+                     void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!plan || plan->n_trees < 1) return ct_fail(CT_ERR_ARG, "plan not prepared");
+    const int64_t n = plan->n_points;
+    if (!ws || ws_bytes < carve_forest(nullptr, n, plan->n_trees, nullptr, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "forest locate workspace too small");
+    LocWS L;
+    ForestWS F;
+    carve_forest(ws, n, plan->n_trees, &L, &F);
+    CT_CUDA(cudaMemsetAsync(L.counters, 0, 64, st));
+    if (n == 0) return CT_OK;
+    const double2* P = (const double2*)points;
+    // stage 1: sort by (tree, Morton key), 4 passes of 8 bits; the last pass
+    // writes the permutation into L.order
+    unsigned* kin = L.keyA;
+    int* iin = L.order;
+    unsigned* kout = L.keyB;
+    int* iout = L.idxB;
+    int64_t chunk = (n + RS_BLOCKS - 1) / RS_BLOCKS;
+    chunk = (chunk + RS_TILE - 1) / RS_TILE * RS_TILE;
+    const int64_t nh = (int64_t)256 * RS_BLOCKS;
+    for (int pss = 0; pss < 4; pss++) {
+        int shift = 8 * pss;
+        if (pss == 0)
+            k_keys_forest<<<RS_BLOCKS, RS_T, 0, st>>>(P, n, chunk, F.grids, F.poff, plan->n_trees, plan->morton_bits,
+                                                      kin, iin, F.qtree, L.hist);
+        else
+            k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
+        int s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
+        if (s) return s;
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, L.hist, kout, iout);
+        std::swap(kin, kout);
+        std::swap(iin, iout);
+    }
+    // 4 passes: the permutation is back in L.order
+    TreeL T0;
+    memset(&T0, 0, sizeof(T0));
+    size_t smem = (size_t)plan->stack * LOC_THREADS * sizeof(int);
+    unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
+    unsigned grid_b = (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16);
+#define CT_FOREST_STAGES(KT)                                                                                      \
+    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.open,            \
+                                                    &L.counters[3]);                                             \
+    k_fast<KT, true><<<grid_b, LOC_THREADS, smem, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.R,          \
+                                                        L.counters, L.ovf, L.open, &L.counters[3]);              \
+    k_pip<true><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.R, L.counters);                  \
+    k_resolve<true><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, L.R, L.counters, out);            \
+    k_exact<KT, true><<<GRID_STRIDE, LOC_THREADS, smem, st>>>(T0, F.trees, F.qtree, P, L.ovf, L.counters, out);
+    if (plan->kt == 3) {
+        CT_FOREST_STAGES(3)
+    } else if (plan->kt == 4) {
+        CT_FOREST_STAGES(4)
+    } else {
+        CT_FOREST_STAGES(32)
+    }
+#undef CT_FOREST_STAGES
+    CT_CHECK_LAUNCH("forest locate");
+    return CT_OK;
 }
 
 }  // extern "C"

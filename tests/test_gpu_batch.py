@@ -1,0 +1,110 @@
+"""Batched build and locate of many meshes (CellTreeBatch): every mesh's tree
+and every query result equal those of the mesh built and queried alone (and
+the oracle's); the batched locate replays from a CUDA graph."""
+
+import numpy as np
+import pytest
+
+from numba_celltree_gb300 import synthetic as syn
+
+
+def _meshes():
+    out = []
+    rng = np.random.default_rng(0)
+    sizes = [(1, 1), (5, 4), (8, 8), (30, 20), (70, 50), (150, 110), (3, 2), (200, 120)]
+    for k, (nx, ny) in enumerate(sizes):
+        off = (rng.uniform(-1e3, 1e3), rng.uniform(-1e3, 1e3))
+        if k % 3 == 0:
+            xy, f = syn.triangle_mesh(nx, ny, seed=k, extent=(float(nx), float(ny)), offset=off)
+        elif k % 3 == 1:
+            xy, f = syn.quad_mesh(nx, ny, seed=k, extent=(float(nx), float(ny)), offset=off)
+        else:
+            xy, f = syn.mixed_mesh(nx, ny, seed=k, extent=(float(nx), float(ny)))
+            xy = xy + np.array(off)
+        out.append((xy, f))
+    return out
+
+
+def _points(meshes, seed=1):
+    pts = []
+    for k, (xy, f) in enumerate(meshes):
+        lo, hi = xy.min(0), xy.max(0)
+        m = 500 + 300 * k
+        pts.append(np.concatenate([
+            syn.uniform_points(m, lo - 0.5, hi + 0.5, seed=seed + k),
+            syn.near_edge_points(xy, f, m // 5, dist=0.0, seed=seed + 100 + k),
+            xy[np.random.default_rng(k).integers(0, len(xy), 20)],
+        ]))
+    return pts
+
+
+@pytest.mark.gpu
+def test_forest_build_matches_single_builds(oracle):
+    from numba_celltree_gb300 import CellTree2d, CellTreeBatch
+
+    meshes = _meshes()
+    batch = CellTreeBatch(meshes, -1)
+    assert len(batch) == len(meshes)
+    for k, (xy, f) in enumerate(meshes):
+        alone = CellTree2d(xy, f, -1)
+        t = batch[k]
+        assert np.array_equal(t.bb_indices, alone.bb_indices), k
+        assert t.nodes.tobytes() == alone.nodes.tobytes(), k
+        assert np.array_equal(t.faces, alone.faces), k
+        if k in (0, 3, 5):
+            o = oracle.OracleCellTree2d(xy, f, -1)
+            assert np.array_equal(t.bb_indices, o.bb_indices)
+            assert t.nodes.tobytes() == o.nodes.tobytes()
+
+
+@pytest.mark.gpu
+def test_forest_locate_matches_single_locate(oracle):
+    from numba_celltree_gb300 import CellTreeBatch
+
+    meshes = _meshes()
+    batch = CellTreeBatch(meshes, -1)
+    pts = _points(meshes)
+    got = batch.locate_points(pts)
+    for k, (xy, f) in enumerate(meshes):
+        ref = oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])
+        assert np.array_equal(got[k], ref), k
+        assert np.array_equal(batch[k].locate_points(pts[k]), ref), k
+    # one tolerance for all meshes, above the candidate lists' cover
+    got = batch.locate_points(pts, tolerance=1e-3)
+    for k, (xy, f) in enumerate(meshes):
+        ref = oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k], 1e-3)
+        assert np.array_equal(got[k], ref), k
+
+
+@pytest.mark.gpu
+def test_forest_locate_cuda_graph():
+    import torch
+    from numba_celltree_gb300 import CellTreeBatch
+
+    meshes = _meshes()
+    batch = CellTreeBatch(meshes, -1)
+    pts = _points(meshes, seed=7)
+    counts = [len(p) for p in pts]
+    plan = batch.plan_locate(counts)
+    pts_d = torch.as_tensor(np.concatenate(pts), device="cuda")
+    out = torch.empty(plan.n_points, dtype=torch.int64, device="cuda")
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.launch(pts_d, out)  # warm-up outside capture
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.launch(pts_d, out)
+    for seed in (11, 12):
+        new = _points(meshes, seed=seed)
+        new = [p[:c] if len(p) >= c else np.resize(p, (c, 2)) for p, c in zip(new, counts)]
+        pts_d.copy_(torch.as_tensor(np.concatenate(new)))
+        out.fill_(-7)
+        g.replay()
+        torch.cuda.synchronize()
+        res = out.cpu().numpy()
+        for k in range(len(meshes)):
+            a, b = int(plan.offsets[k]), int(plan.offsets[k + 1])
+            assert np.array_equal(res[a:b], batch[k].locate_points(new[k])), (seed, k)
