@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small fixed run for ncu captures")
+    ap.add_argument("--workload", default="single", choices=["single", "batch"],
+                    help="batch: 512 meshes built and queried together (a side measurement)")
+    ap.add_argument("--meshes", type=int, default=512)
     return ap.parse_args()
 
 
@@ -244,8 +247,124 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def batch_workload(n_meshes, seed=3):
+    """512 triangulated jittered grids, cells log-uniform in [1k, 500k]; per
+    mesh points log-uniform in [10k, 5M], 95 % in the mesh bbox, 5 % outside."""
+    from numba_celltree_gb300 import synthetic as syn
+
+    rng = np.random.default_rng(seed)
+    cells = np.exp(rng.uniform(np.log(1e3), np.log(5e5), n_meshes)).astype(np.int64)
+    npts = np.exp(rng.uniform(np.log(1e4), np.log(5e6), n_meshes)).astype(np.int64)
+    meshes, points = [], []
+    for k in range(n_meshes):
+        nq = max(1, int(cells[k] // 2))
+        nx = max(1, int(np.sqrt(2.0 * nq)))
+        ny = max(1, nq // nx)
+        off = rng.uniform(-1e4, 1e4, 2)
+        xy, f = syn.triangle_mesh(nx, ny, seed=seed * 1000 + k, extent=(float(nx), float(ny)), offset=tuple(off))
+        lo, hi = xy.min(0), xy.max(0)
+        m = int(npts[k])
+        inside = rng.uniform(lo, hi, size=(m, 2))
+        out = rng.uniform(lo - 0.5 * (hi - lo), hi + 0.5 * (hi - lo), size=(m, 2))
+        pick = rng.random(m) < 0.05
+        inside[pick] = out[pick]
+        meshes.append((xy, f))
+        points.append(inside)
+    return meshes, points
+
+
+def run_batch(args):
+    """Side measurement: many meshes built and located together."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, CellTreeBatch
+
+    meshes, points = batch_workload(args.meshes)
+    dev = torch.device("cuda", 0)
+    md = [(torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)) for xy, f in meshes]
+    counts = [len(p) for p in points]
+    pts_d = torch.as_tensor(np.concatenate(points), device=dev)
+    n = int(pts_d.shape[0])
+    n_cells = int(sum(f.shape[0] for _, f in meshes))
+    torch.cuda.synchronize()
+
+    def wall(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    batch = CellTreeBatch(md, -1)  # warm-up (allocator, module load)
+    del batch
+    batch, t_build = wall(lambda: CellTreeBatch(md, -1))
+    singles, t_build1 = wall(lambda: [CellTree2d(v, f, -1) for v, f in md])
+    plan = batch.plan_locate(counts)
+    out = torch.empty(n, dtype=torch.int64, device=dev)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        plan.launch(pts_d, out)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        plan.launch(pts_d, out)
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # the same points mesh by mesh (each mesh's own batched float32 pipeline)
+    off = plan.offsets
+    outs = torch.empty_like(out)
+
+    def per_mesh():
+        for k, t in enumerate(singles):
+            a, b = int(off[k]), int(off[k + 1])
+            t.launch_locate(pts_d[a:b], outs[a:b], t.default_tolerance(), "fp32")
+
+    per_mesh()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(max(1, args.steps // 4)):
+        per_mesh()
+    e1.record()
+    torch.cuda.synchronize()
+    ms1 = e0.elapsed_time(e1) / max(1, args.steps // 4)
+    identical = bool(torch.equal(out, outs))
+    res = {
+        "metric": "Mpoints/s batched locate_points, 512 meshes in one graph-replayed pipeline",
+        "value": round(n / (ms * 1e-3) / 1e6, 3),
+        "unit": "Mpoints/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": True,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{args.meshes} triangulated jittered grids, cells log-uniform in [1k, 500k] "
+                               f"({n_cells} cells), points log-uniform in [10k, 5M] per mesh ({n} points, "
+                               f"5% outside the mesh bbox)", "meshes": args.meshes, "cells": n_cells, "points": n},
+        "per_mesh_loop": {"value": round(n / (ms1 * 1e-3) / 1e6, 3), "unit": "Mpoints/s", "ms_per_step": round(ms1, 3)},
+        "build_batched_s": round(t_build, 3),
+        "build_per_mesh_loop_s": round(t_build1, 3),
+        "indices_identical_batched_vs_per_mesh": identical,
+    }
+    print(json.dumps(res))
+
+
 def main():
     args = parse()
+    if args.workload == "batch":
+        run_batch(args)
+        return
     if args.profile:
         args.nx, args.ny, args.points, args.steps, args.warmup = 1000, 500, 16 * 1024 * 1024, 2, 1
         args.no_e2e = True

@@ -565,7 +565,9 @@ __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, 
     const int t = threadIdx.x, w = t >> 5;
     for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
     __syncthreads();
-    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    // chunks past the end are empty (e = s): a negative length would make the
+    // vector loop bound below round down into the next chunk
+    int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
     for (int64_t i = s + t; i < e; i += RS_T) {
         unsigned k = morton24(g, pts[i]);
         key[i] = k;
@@ -590,7 +592,9 @@ __global__ void __launch_bounds__(RS_T) k_keys_forest(const double2* __restrict_
     const int t = threadIdx.x, w = t >> 5;
     for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
     __syncthreads();
-    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    // chunks past the end are empty (e = s): a negative length would make the
+    // vector loop bound below round down into the next chunk
+    int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
     for (int64_t i = s + t; i < e; i += RS_T) {
         int lo = 0, hi = n_trees;  // poff[lo] <= i < poff[hi]
         while (hi - lo > 1) {
@@ -618,7 +622,9 @@ __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* __restrict__ k
     const int t = threadIdx.x, w = t >> 5;
     for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
     __syncthreads();
-    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    // chunks past the end are empty (e = s): a negative length would make the
+    // vector loop bound below round down into the next chunk
+    int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
     int64_t ev = s + ((e - s) & ~(int64_t)3);  // end of the whole uint4 groups
     for (int64_t i = s + 4 * t; i < ev; i += 4 * RS_T) {
         uint4 k4 = *reinterpret_cast<const uint4*>(key + i);
@@ -652,7 +658,9 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
     __shared__ int si[RS_TILE];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     cur[t] = (int)offs[(int64_t)t * gridDim.x + blockIdx.x];
-    int64_t s = (int64_t)blockIdx.x * chunk, e = min(s + chunk, n);
+    // chunks past the end are empty (e = s): a negative length would make the
+    // vector loop bound below round down into the next chunk
+    int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
     for (int64_t base = s; base < e; base += RS_TILE) {
         cnt[t] = 0;
         __syncthreads();

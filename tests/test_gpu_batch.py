@@ -108,3 +108,23 @@ def test_forest_locate_cuda_graph():
         for k in range(len(meshes)):
             a, b = int(plan.offsets[k]), int(plan.offsets[k + 1])
             assert np.array_equal(res[a:b], batch[k].locate_points(new[k])), (seed, k)
+
+
+@pytest.mark.gpu
+def test_forest_locate_odd_total(oracle):
+    """Batched locate with a sorted total that is not a multiple of 4 and
+    meshes with many queries per cell."""
+    from numba_celltree_gb300 import CellTreeBatch
+
+    meshes = [syn.triangle_mesh(41, 20, seed=3, extent=(41.0, 20.0), offset=(-4765.3, 1431.0)),
+              syn.quad_mesh(7, 5, seed=4, extent=(7.0, 5.0), offset=(30.0, -40.0)),
+              syn.triangle_mesh(90, 60, seed=5, extent=(90.0, 60.0))]
+    counts = [70001, 3, 100002]
+    pts = []
+    for (xy, f), m in zip(meshes, counts):
+        lo, hi = xy.min(0), xy.max(0)
+        pts.append(syn.uniform_points(m, lo - 0.5 * (hi - lo), hi + 0.5 * (hi - lo), seed=m))
+    batch = CellTreeBatch(meshes, -1)
+    got = batch.locate_points(pts)
+    for k, (xy, f) in enumerate(meshes):
+        assert np.array_equal(got[k], oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])), k

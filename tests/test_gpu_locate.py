@@ -270,3 +270,19 @@ def test_locate_candidate_lists_and_overlaps(oracle):
     g2 = CellTree2d(xy2, f2, -1)
     o2 = oracle.OracleCellTree2d(xy2, f2, -1)
     assert np.array_equal(g2.locate_points(pts), o2.locate_points(pts))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [65537, 70001, 100002, 1_000_003, 3_061_726])
+def test_locate_sorted_batch_sizes_not_multiple_of_4(oracle, n):
+    """Sorted batches (>= 2^16 queries) of every residue mod 4, including many
+    queries per cell: the radix sort's per-block histograms must match its
+    scatter exactly."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(41, 20, seed=3, extent=(41.0, 20.0), offset=(-4765.3, 1431.0))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    lo, hi = xy.min(0), xy.max(0)
+    pts = syn.uniform_points(n, lo - 0.5 * (hi - lo), hi + 0.5 * (hi - lo), seed=n)
+    assert np.array_equal(g.locate_points(pts), o.locate_points(pts))
