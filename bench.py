@@ -51,8 +51,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true", help="small fixed run for ncu captures")
-    ap.add_argument("--workload", default="single", choices=["single", "batch"],
-                    help="batch: 512 meshes built and queried together (a side measurement)")
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "queries"],
+                    help="batch: 512 meshes built and queried together; queries: every query on the "
+                         "survey configurations against the oracle (side measurements)")
     ap.add_argument("--meshes", type=int, default=512)
     return ap.parse_args()
 
@@ -360,8 +361,147 @@ def run_batch(args):
     print(json.dumps(res))
 
 
+def run_queries(args):
+    """Side measurement: build and every query on the C1 / C2 / C4 shapes, GPU
+    (device-resident inputs, wall time around synchronised calls) against the
+    oracle (C restatement, OpenMP, all host cores) on a bounded sample, with
+    the GPU result checked on that sample."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d
+    from numba_celltree_gb300 import synthetic as syn
+    from oracle import oracle as O
+
+    O.build()
+    dev = torch.device("cuda", 0)
+    lines = []
+
+    def wall(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) / reps
+
+    def cpu(fn):
+        t0 = time.perf_counter()
+        r = fn()
+        return r, time.perf_counter() - t0
+
+    def host(x):
+        if isinstance(x, tuple):
+            return tuple(host(y) for y in x)
+        return x.cpu().numpy() if hasattr(x, "cpu") else x
+
+    def record(cfg, query, n, unit, gpu_s, m, cpu_s, same):
+        line = {"config": cfg, "query": query, "n": n, "unit": unit,
+                "gpu_ms": round(gpu_s * 1e3, 3), "gpu_rate_per_s": round(n / gpu_s, 1),
+                "cpu_sample": m, "cpu_rate_per_s": round(m / cpu_s, 1),
+                "speedup": round((n / gpu_s) / (m / cpu_s), 1), "identical_on_sample": bool(same)}
+        lines.append(line)
+        print(json.dumps(line), flush=True)
+
+    def first_queries(res, m, nq_col=0):
+        # pairs of multi-result queries whose query index < m (results are query-major)
+        ii = res[nq_col]
+        keep = ii < m
+        return tuple(r[keep] for r in res)
+
+    def same_multi(a, b):
+        return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+    cores = O.num_threads()
+    rng = np.random.default_rng(0)
+    # ---- C1: 80k triangles on [0, 1]^2, 1M points, 10k boxes
+    xy, f = syn.triangle_mesh(200, 200, seed=0, extent=(1.0, 1.0))
+    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
+    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
+    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
+    record("C1", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    pts = rng.uniform(-0.05, 1.05, (1_000_000, 2))
+    pd = torch.as_tensor(pts, device=dev)
+    r, tg = wall(lambda: tree.locate_points(pd))
+    ro, tc = cpu(lambda: ot.locate_points(pts))
+    record("C1", "locate_points", len(pts), "points", tg, len(pts), tc, np.array_equal(host(r), ro))
+    boxes = syn.random_boxes(10_000, (0.0, 0.0), (1.0, 1.0), 0.001, 0.02, seed=1)
+    bd = torch.as_tensor(boxes, device=dev)
+    r, tg = wall(lambda: tree.locate_boxes(bd))
+    ro, tc = cpu(lambda: ot.locate_boxes(boxes))
+    record("C1", "locate_boxes", len(boxes), "boxes", tg, len(boxes), tc, same_multi(host(r), ro))
+    r, tg = wall(lambda: tree.intersect_boxes(bd))
+    ro, tc = cpu(lambda: ot.intersect_boxes(boxes))
+    record("C1", "intersect_boxes", len(boxes), "boxes", tg, len(boxes), tc, same_multi(host(r), ro))
+    del tree, ot
+    # ---- C2: ~4M mixed cells (K=6) on [0, 1e3]^2; 64M points, 1M boxes, 1M segments
+    xy, f = syn.mixed_mesh(2000, 2000, seed=1, extent=(1000.0, 1000.0))
+    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
+    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
+    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
+    record("C2", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    n = 64 * 1024 * 1024
+    pd = torch.rand((n, 2), dtype=torch.float64, device=dev) * 1000.0
+    r, tg = wall(lambda: tree.locate_points(pd))
+    m = 2_000_000
+    sample = pd[:m].cpu().numpy()
+    ro, tc = cpu(lambda: ot.locate_points(sample))
+    record("C2", "locate_points", n, "points", tg, m, tc, np.array_equal(host(r[:m]), ro))
+    del pd, r
+    boxes = syn.random_boxes(1_000_000, (0.0, 0.0), (1000.0, 1000.0), 0.1, 50.0, seed=2, log_uniform=True)
+    bd = torch.as_tensor(boxes, device=dev)
+    r, tg = wall(lambda: tree.locate_boxes(bd))
+    m = 100_000
+    ro, tc = cpu(lambda: ot.locate_boxes(boxes[:m]))
+    record("C2", "locate_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    r, tg = wall(lambda: tree.intersect_boxes(bd))
+    ro, tc = cpu(lambda: ot.intersect_boxes(boxes[:m]))
+    record("C2", "intersect_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    # segments: uniform start, uniform direction, length U(0, 20) m (about 40
+    # cells each); uniform endpoints over the whole domain would give ~1.4e9
+    # (segment, cell) pairs for 1M segments
+    srng = np.random.default_rng(3)
+    a0 = srng.uniform(0.0, 1000.0, (1_000_000, 2))
+    ang = srng.uniform(0.0, 2 * np.pi, 1_000_000)
+    ln = srng.uniform(0.0, 20.0, 1_000_000)
+    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
+    sd = torch.as_tensor(segs, device=dev)
+    r, tg = wall(lambda: tree.intersect_edges(sd), reps=1)
+    m = 20_000
+    ro, tc = cpu(lambda: ot.intersect_edges(segs[:m]))
+    record("C2", "intersect_edges", len(segs), "segments", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    del tree, ot, r
+    # ---- C4: tree of 500k quads (rotated 7 degrees, offset 0.37 cell); 1M query triangles; 1M points
+    txy, tf = syn.quad_mesh(1000, 500, seed=4, extent=(100.0, 50.0), offset=(0.037, 0.037), rotate_deg=7.0)
+    qxy, qf = syn.triangle_mesh(1000, 500, seed=5, extent=(100.0, 50.0))
+    txy_d, tf_d = torch.as_tensor(txy, device=dev), torch.as_tensor(tf, device=dev)
+    tree, tb = wall(lambda: CellTree2d(txy_d, tf_d, -1), reps=2)
+    ot, cb = cpu(lambda: O.OracleCellTree2d(txy, tf, -1))
+    record("C4", "build", len(tf), "cells", tb, len(tf), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    qv, qfd = torch.as_tensor(qxy, device=dev), torch.as_tensor(qf, device=dev)
+    r, tg = wall(lambda: tree.locate_faces(qv, qfd.clone()), reps=2)
+    m = 50_000
+    ro, tc = cpu(lambda: ot.locate_faces(qxy, qf[:m].copy()))
+    record("C4", "locate_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    r, tg = wall(lambda: tree.intersect_faces(qv, qfd, -1), reps=2)
+    ro, tc = cpu(lambda: ot.intersect_faces(qxy, qf[:m], -1))
+    record("C4", "intersect_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    bp = syn.uniform_points(1_000_000, txy.min(0), txy.max(0), seed=6)
+    bpd = torch.as_tensor(bp, device=dev)
+    r, tg = wall(lambda: tree.compute_barycentric_weights(bpd))
+    m = 1_000_000
+    ro, tc = cpu(lambda: ot.compute_barycentric_weights(bp))
+    record("C4", "compute_barycentric_weights", len(bp), "points", tg, m, tc, same_multi(host(r), ro))
+    print(json.dumps({"summary": "queries vs oracle", "host_cores": cores,
+                      "min_speedup": min(x["speedup"] for x in lines),
+                      "all_identical": all(x["identical_on_sample"] for x in lines)}))
+
+
 def main():
     args = parse()
+    if args.workload == "queries":
+        run_queries(args)
+        return
     if args.workload == "batch":
         run_batch(args)
         return
