@@ -399,6 +399,38 @@ int ct_barycentric_weights_grad(const double* points, const int64_t* face_indice
                                 void* stream);
 
 /* ---------------------------------------------------------------------- */
+/* Exported helpers and the regridding step                                */
+/* ---------------------------------------------------------------------- */
+
+/* liang_barsky_line_box_clip algorithms/liang_barsky.py:10-64, one segment
+ * per row: a, b (n x 2), boxes (n x 4: xmin, xmax, ymin, ymax) -> ok (n),
+ * clipped c, d (n x 2; NaN when not ok). */
+int ct_liang_barsky_line_box_clip(const double* a, const double* b, const double* boxes, int64_t n, uint8_t* ok,
+                                  double* c, double* d, void* stream);
+
+/* points_in_triangles geometry_utils.py:273-289: out[i] = point_in_triangle
+ * (241-270) of point i in triangle face_indices[i] (first three vertices of
+ * the face).  A face index outside [0, n_faces) sets bit 1 of *error_word
+ * (upstream indexes without a check) and gives 0. */
+int ct_points_in_triangles(const double* points, const int64_t* face_indices, int64_t n, const int64_t* faces,
+                           int32_t n_max_vert, int64_t n_faces, const double* vertices, double tolerance,
+                           uint8_t* out, unsigned int* error_word, void* stream);
+
+/* Regridding step after intersect_faces / intersect_boxes (no upstream
+ * counterpart; the upstream example builds a dense weight matrix,
+ * examples/spatial_indexing_2d_grids.py:245-313).  The query-major pairs
+ * (rows non-decreasing, checked: bit 2 of *error_word) are a CSR matrix once
+ * row_ptr (n_rows + 1) is known: ct_csr_row_ptr.  ct_csr_weighted_mean:
+ * mean[r] = sum(w x[col]) / sum(w) over row r (NaN without weight),
+ * weight_sum[r] = sum(w) (may be NULL). */
+size_t ct_csr_workspace_size(int64_t n_rows);
+int ct_csr_row_ptr(const int64_t* rows, int64_t n_pairs, int64_t n_rows, int64_t* row_ptr, void* workspace,
+                   size_t workspace_bytes, unsigned int* error_word, void* stream);
+int ct_csr_weighted_mean(const int64_t* row_ptr, const int64_t* cols, const double* weights, int64_t n_rows,
+                         int64_t n_cols, const double* x, double* mean, double* weight_sum, unsigned int* error_word,
+                         void* stream);
+
+/* ---------------------------------------------------------------------- */
 /* Node-bound diagnostics                                                  */
 /* ---------------------------------------------------------------------- */
 

@@ -148,6 +148,11 @@ SIGNATURES = {
     "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),
     "ct_area_of_intersection": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
     "ct_box_area_of_intersection": (ctypes.c_int, [_P, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "ct_liang_barsky_line_box_clip": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P]),
+    "ct_points_in_triangles": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _I64, _P, _D, _P, _P, _P]),
+    "ct_csr_workspace_size": (_SZ, [_I64]),
+    "ct_csr_row_ptr": (ctypes.c_int, [_P, _I64, _I64, _P, _P, _SZ, _P, _P]),
+    "ct_csr_weighted_mean": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _P, _P, _P, _P, _P]),
     "ct_area_of_intersection_grad": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),
     "ct_barycentric_weights_grad": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I32, _I32, _D, _P, _P, _P, _P]),
     "ct_compact_workspace_size": (_SZ, [_I64]),

@@ -73,6 +73,85 @@ class CellTree2d(CellTree2dBase):
         self.cells_per_leaf = cells_per_leaf
         self.precision = "fp32"
 
+    # -- serialisation (no upstream counterpart) -------------------------------
+    def save(self, path) -> None:
+        """Write the tree to an ``.npz`` file: vertices, oriented faces, nodes
+        (NodeDType), bb_indices and the build parameters.  ``load`` restores
+        it without rebuilding."""
+        np.savez(path, format="numba_celltree_gb300.CellTree2d", version=1, vertices=self.vertices,
+                 faces=self.faces, nodes=self.nodes, bb_indices=self.bb_indices,
+                 n_buckets=self.n_buckets, cells_per_leaf=self.cells_per_leaf)
+
+    @classmethod
+    def load(cls, path) -> "CellTree2d":
+        """A tree written by ``save``."""
+        with np.load(path, allow_pickle=False) as z:
+            if str(z["format"]) != "numba_celltree_gb300.CellTree2d":
+                raise ValueError("not a CellTree2d file")
+            return cls._from_arrays(z["vertices"], z["faces"], z["nodes"], z["bb_indices"], int(z["n_buckets"]),
+                                    int(z["cells_per_leaf"]))
+
+    @classmethod
+    def from_celltree_data(cls, data, n_buckets: int = 4) -> "CellTree2d":
+        """A tree from upstream's ``CellTreeData`` (constants.py:82-89: elements,
+        vertices, nodes, bb_indices, bb_coords, bbox, cells_per_leaf), e.g.
+        ``numba_celltree.CellTree2d(...).celltree_data``, without rebuilding.
+        ``n_buckets`` is not part of ``CellTreeData``; it only matters for
+        ``n_buckets`` of the returned object."""
+        return cls._from_arrays(data.vertices, data.elements, data.nodes, data.bb_indices, n_buckets,
+                                int(data.cells_per_leaf))
+
+    @classmethod
+    def _from_arrays(cls, vertices, faces, nodes, bb_indices, n_buckets: int, cells_per_leaf: int):
+        _validate_params(n_buckets, cells_per_leaf)
+        device = _device.require_cuda()
+        torch = _device.torch()
+        vertices = cast_vertices(vertices, copy=True)
+        faces = np.ascontiguousarray(faces, dtype=np.int64)
+        nodes = np.asarray(nodes)
+        bb_indices = np.ascontiguousarray(bb_indices, dtype=np.int64)
+        if faces.ndim != 2 or faces.shape[0] == 0 or faces.shape[1] < 3:
+            raise ValueError("faces must have shape (n_face >= 1, n_max_vert >= 3)")
+        for name in ("child", "Lmax", "Rmin", "ptr", "size", "dim"):
+            if nodes.dtype.names is None or name not in nodes.dtype.names:
+                raise ValueError(f"nodes must be a NodeDType array (missing {name})")
+        n = faces.shape[0]
+        if bb_indices.shape != (n,) or not np.array_equal(np.sort(bb_indices), np.arange(n)):
+            raise ValueError("bb_indices must be a permutation of the face indices")
+        nn = nodes.shape[0]
+        child = np.ascontiguousarray(nodes["child"], dtype=np.int64)
+        # depth of every node (children are numbered after their parent)
+        internal = child >= 0
+        if np.any(child[internal] <= np.nonzero(internal)[0]) or np.any(child[internal] + 1 >= nn):
+            raise ValueError("nodes: children must follow their parent and lie inside the array")
+        depth = np.zeros(nn, dtype=np.int64)
+        frontier, level = np.array([0], dtype=np.int64), 0
+        while frontier.size and level <= nn:
+            c = child[frontier]
+            c = c[c >= 0]
+            frontier = np.concatenate([c, c + 1])
+            level += 1
+            depth[frontier] = level
+        v_d = _device.to_device(vertices, torch.float64, device)
+        f_d = _device.to_device(faces, torch.int64, device)
+        validate_elements(f_d, int(v_d.shape[0]), 3, "faces")
+        lib = _lib.load()
+        st = _device.stream()
+        K = int(f_d.shape[1])
+        bb = _device.empty((n, 4), torch.float64, device)
+        _lib.check(lib.ct_face_bboxes(_device.ptr(v_d), _device.ptr(f_d), n, K, _device.ptr(bb), st), "face_bboxes")
+        dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), device=device).to(dt)
+        pre = (dev(child, torch.int64), dev(nodes["Lmax"], torch.float64), dev(nodes["Rmin"], torch.float64),
+               dev(nodes["ptr"], torch.int64), dev(nodes["size"], torch.int64),
+               dev(nodes["dim"].astype(np.uint8), torch.uint8), dev(bb_indices, torch.int64), int(depth.max()))
+        tree = cls.__new__(cls)
+        tree._tree = _GpuTree(device, f_d, v_d, bb, n_buckets, cells_per_leaf, prebuilt=pre)
+        tree._host = {}
+        tree.n_buckets = n_buckets
+        tree.cells_per_leaf = cells_per_leaf
+        tree.precision = "fp32"
+        return tree
+
     @property
     def faces(self) -> np.ndarray:
         return self._cached("faces", lambda: self._tree.elements.cpu().numpy())
