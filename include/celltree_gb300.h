@@ -292,22 +292,39 @@ size_t ct_scan_workspace_size(int64_t n);
 int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* workspace, size_t workspace_bytes,
                       int64_t* total_host, void* stream);
 
+/* Work order of box (kind 0) or segment (kind 1) queries (no upstream
+ * counterpart): a permutation grouping queries of similar size (box area /
+ * segment length with a cell-size margin, 8-bit log classes, stable), so one
+ * warp's queries take similar time.  Passing it as `order` below changes no
+ * result: counts and pairs stay indexed and ordered by query. */
+size_t ct_work_order_workspace_size(int64_t n);
+int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_size, int32_t* order, void* workspace,
+                  size_t workspace_bytes, void* stream);
+/* One stable LSD pass on 8 bits of 32-bit keys (bits shift .. shift + 7):
+ * kin/iin -> kout/iout.  Workspace: ct_radix_pass_workspace_size() bytes. */
+size_t ct_radix_pass_workspace_size(void);
+int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
 /* locate_box query.py:177-244: per box (xmin, xmax, ymin, ymax) the number of
- * cells whose bbox overlaps it (strict, boxes_intersect geometry_utils.py:292-300). */
-int ct_count_boxes(const ct_tree* tree, const double* boxes, int64_t n, int64_t* counts, void* stream);
+ * cells whose bbox overlaps it (strict, boxes_intersect geometry_utils.py:292-300).
+ * order: NULL or a permutation of the boxes (processing order only). */
+int ct_count_boxes(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order, int64_t* counts,
+                   void* stream);
 /* Writes (box index, cell index) pairs at the scanned offsets, box-major and
  * in traversal order -- upstream's locate_boxes output order. */
-int ct_write_boxes(const ct_tree* tree, const double* boxes, int64_t n, const int64_t* offsets, int64_t* ii,
-                   int64_t* jj, void* stream);
+int ct_write_boxes(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order, const int64_t* offsets,
+                   int64_t* ii, int64_t* jj, void* stream);
 
 /* locate_edge query.py:357-455 over segments (n x 2 x 2).  mode 1: edge vs
  * face (Cohen-Sutherland + Cyrus-Beck, compute_edge_face_intersect
  * query.py:309-328); mode 0: edge vs edge (lines_intersect,
  * compute_edge_edge_intersect query.py:292-306, edge trees only). */
-int ct_count_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, int64_t* counts, void* stream);
+int ct_count_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                   int64_t* counts, void* stream);
 /* Writes (segment, cell) pairs and the clipped segment / point (xy: R x 2 x 2). */
-int ct_write_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int64_t* offsets,
-                   int64_t* ii, int64_t* jj, double* xy, void* stream);
+int ct_write_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                   const int64_t* offsets, int64_t* ii, int64_t* jj, double* xy, void* stream);
 
 /* sort_intersections_by_edge geometry_utils.py:564-574: stable sort of each
  * segment's results by t = (c - a) . (b - a), NaN last; writes the permuted

@@ -139,10 +139,10 @@ SIGNATURES = {
     "ct_locate_deferred_count": (ctypes.c_int, [_P, _I64, _I32, ctypes.POINTER(_I64), _P]),
     "ct_scan_workspace_size": (_SZ, [_I64]),
     "ct_exclusive_scan": (ctypes.c_int, [_P, _I64, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
-    "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P]),
-    "ct_write_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P]),
-    "ct_count_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P]),
-    "ct_write_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P]),
+    "ct_write_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_count_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P]),
+    "ct_write_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "ct_sort_workspace_size": (_SZ, [_I64]),
     "ct_sort_intersections": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
     "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),
@@ -151,6 +151,10 @@ SIGNATURES = {
     "ct_liang_barsky_line_box_clip": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P]),
     "ct_points_in_triangles": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _I64, _P, _D, _P, _P, _P]),
     "ct_csr_workspace_size": (_SZ, [_I64]),
+    "ct_work_order_workspace_size": (_SZ, [_I64]),
+    "ct_work_order": (ctypes.c_int, [_P, _I64, _I32, _D, _P, _P, _SZ, _P]),
+    "ct_radix_pass_workspace_size": (_SZ, []),
+    "ct_radix_pass": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P, _P, _SZ, _P]),
     "ct_csr_row_ptr": (ctypes.c_int, [_P, _I64, _I64, _P, _P, _SZ, _P, _P]),
     "ct_csr_weighted_mean": (ctypes.c_int, [_P, _P, _P, _I64, _I64, _P, _P, _P, _P, _P]),
     "ct_area_of_intersection_grad": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _P, _P]),

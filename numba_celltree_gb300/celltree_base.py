@@ -197,8 +197,10 @@ class _GpuTree:
     def auto_sort_bits(n_points: int) -> int:
         """Bits of the 24-bit Morton key the batched float32 form sorts the
         queries by: none for small batches (the sort costs more than the
-        divergence it removes), else all 24 (a 4096 x 4096 grid)."""
-        return 0 if n_points < (1 << 16) else 24
+        divergence it removes), else 16 (a 256 x 256 grid: with the candidate
+        lists a finer order saves less in the query kernels than its third
+        radix pass costs)."""
+        return 0 if n_points < (1 << 16) else 16
 
     def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None) -> None:
         """Enqueue point location on the current stream (no synchronisation)."""
@@ -243,6 +245,25 @@ class _GpuTree:
         )
         return offsets, int(total.value)
 
+    # queries per batch above which box / segment queries run in work order
+    WORK_ORDER_MIN = 4096
+
+    def work_order(self, q_d, kind: int):
+        """Permutation grouping box (kind 0) / segment (kind 1) queries of
+        similar size, or None for small batches."""
+        n = int(q_d.shape[0])
+        if n < self.WORK_ORDER_MIN:
+            return None
+        torch = _device.torch()
+        lib = _lib.load()
+        nbytes = int(lib.ct_work_order_workspace_size(n))
+        ws = _device.empty((nbytes,), torch.uint8, self.device)
+        order = _device.empty((n,), torch.int32, self.device)
+        cell = max(self.max_diagonal, 1e-300)
+        _lib.check(lib.ct_work_order(_device.ptr(q_d), n, kind, cell, _device.ptr(order), _device.ptr(ws), nbytes,
+                                     _device.stream()), "work order")
+        return order
+
     def locate_boxes(self, boxes_d):
         torch = _device.torch()
         lib = _lib.load()
@@ -250,14 +271,15 @@ class _GpuTree:
         n = int(boxes_d.shape[0])
         counts = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
-        _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(counts), st),
-                   "locate_boxes")
+        order = self.work_order(boxes_d, 0)
+        _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                      _device.ptr(counts), st), "locate_boxes")
         offsets, total = self.scan(counts)
         ii = _device.empty((total,), torch.int64, self.device)
         jj = _device.empty((total,), torch.int64, self.device)
         _lib.check(
-            lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(offsets),
-                               _device.ptr(ii), _device.ptr(jj), st),
+            lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                               _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), st),
             "locate_boxes",
         )
         self.raise_on_device_error()
@@ -271,8 +293,10 @@ class _GpuTree:
         n = int(segs_d.shape[0])
         counts = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
+        order = self.work_order(segs_d, 1)
         _lib.check(
-            lib.ct_count_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(counts), st),
+            lib.ct_count_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(order),
+                               _device.ptr(counts), st),
             "intersect_edges",
         )
         offsets, total = self.scan(counts)
@@ -280,8 +304,8 @@ class _GpuTree:
         jj = _device.empty((total,), torch.int64, self.device)
         xy = _device.empty((total, 2, 2), torch.float64, self.device)
         _lib.check(
-            lib.ct_write_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(offsets),
-                               _device.ptr(ii), _device.ptr(jj), _device.ptr(xy), st),
+            lib.ct_write_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(order),
+                               _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), _device.ptr(xy), st),
             "intersect_edges",
         )
         if total > 0:

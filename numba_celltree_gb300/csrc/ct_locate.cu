@@ -1320,4 +1320,31 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
     return CT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// one stable 8-bit radix pass, shared with the multi-result queries
+// ---------------------------------------------------------------------------
+size_t ct_radix_pass_workspace_size(void) {
+    return a256(8 * (size_t)256 * RS_BLOCKS) + a256(ct_scan_workspace_size((int64_t)256 * RS_BLOCKS));
+}
+
+int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout, void* ws,
+                  size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 0 || shift < 0 || shift > 24) return ct_fail(CT_ERR_ARG, "bad radix pass");
+    if (!ws || ws_bytes < ct_radix_pass_workspace_size()) return ct_fail(CT_ERR_WORKSPACE, "radix workspace too small");
+    if (n == 0) return CT_OK;
+    int64_t* hist = (int64_t*)ws;
+    const int64_t nh = (int64_t)256 * RS_BLOCKS;
+    void* scan_ws = (char*)ws + a256(8 * (size_t)nh);
+    size_t scan_bytes = ws_bytes - a256(8 * (size_t)nh);
+    int64_t chunk = (n + RS_BLOCKS - 1) / RS_BLOCKS;
+    chunk = (chunk + RS_TILE - 1) / RS_TILE * RS_TILE;
+    k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, hist);
+    int s = ct_exclusive_scan(hist, nh, hist, scan_ws, scan_bytes, nullptr, stream);
+    if (s) return s;
+    k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, hist, kout, iout);
+    CT_CHECK_LAUNCH("radix pass");
+    return CT_OK;
+}
+
 }  // extern "C"

@@ -13,6 +13,10 @@
 #include "ct_geom.cuh"
 #include "ct_internal.h"
 
+extern "C" size_t ct_radix_pass_workspace_size(void);
+extern "C" int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout,
+                             void* ws, size_t ws_bytes, void* stream);
+
 namespace ctm {
 
 struct TreeQ {
@@ -38,10 +42,12 @@ constexpr int STK = 128;  // traversal stack (tree depth + 2 must fit; checked o
 // ---------------------------------------------------------------------------
 template <bool WRITE>
 __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restrict__ boxes, int64_t n,
-                                               int64_t* __restrict__ cnt_or_off, int64_t* __restrict__ ii,
-                                               int64_t* __restrict__ jj) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                                               const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
+                                               int64_t* __restrict__ ii, int64_t* __restrict__ jj) {
+    int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tq >= n) return;
+    // queries in work order (similar work in one warp); results by query index
+    int64_t i = order ? (int64_t)order[tq] : tq;
     double4 q4 = boxes[i];
     dbox box;
     box.xmin = q4.x;
@@ -106,10 +112,12 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
 // ---------------------------------------------------------------------------
 template <bool WRITE, int MODE>
 __global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restrict__ segs, int64_t n,
-                                               int64_t* __restrict__ cnt_or_off, int64_t* __restrict__ ii,
-                                               int64_t* __restrict__ jj, double4* __restrict__ xy) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                                               const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
+                                               int64_t* __restrict__ ii, int64_t* __restrict__ jj,
+                                               double4* __restrict__ xy) {
+    int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tq >= n) return;
+    int64_t i = order ? (int64_t)order[tq] : tq;
     double4 s4 = segs[i];
     dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
     int64_t count = 0;
@@ -585,6 +593,26 @@ __global__ void k_validate_bounds(const int64_t* __restrict__ child, const int64
     valid[v] = (uint8_t)ok;
 }
 
+// 8-bit work class of a box (kind 0: area with a cell-size margin) or a
+// segment (kind 1: length plus a cell size): 4 * log2(work) + 128, clamped.
+__global__ void k_work_keys(const double4* __restrict__ q, int64_t n, int kind, float cell, unsigned* __restrict__ key,
+                            int* __restrict__ idx) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double4 v = q[i];
+        float w;
+        if (kind == 0) {
+            float dx = (float)(v.y - v.x), dy = (float)(v.w - v.z);
+            w = (fabsf(dx) + cell) * (fabsf(dy) + cell);
+        } else {
+            float dx = (float)(v.z - v.x), dy = (float)(v.w - v.y);
+            w = sqrtf(dx * dx + dy * dy) + cell;
+        }
+        int k = (w > 0.0f) ? (int)floorf(4.0f * log2f(w)) + 128 : 0;  // NaN -> 0
+        key[i] = (unsigned)min(max(k, 0), 255);
+        idx[i] = (int)i;
+    }
+}
+
 TreeQ make_q(const ct_tree* t) {
     TreeQ T;
     T.nf = (const float4*)t->nodes_f32;
@@ -645,53 +673,57 @@ static int check_tree(const ct_tree* t) {
     return CT_OK;
 }
 
-int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, int64_t* counts, void* stream) {
+int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order, int64_t* counts,
+                   void* stream) {
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
-    k_boxes<false><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, counts,
-                                                                       nullptr, nullptr);
+    k_boxes<false><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
+                                                                       counts, nullptr, nullptr);
     CT_CHECK_LAUNCH("count_boxes");
     return CT_OK;
 }
 
-int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int64_t* offsets, int64_t* ii,
-                   int64_t* jj, void* stream) {
+int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order, const int64_t* offsets,
+                   int64_t* ii, int64_t* jj, void* stream) {
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
-    k_boxes<true><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+    k_boxes<true><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
                                                                       (int64_t*)offsets, ii, jj);
     CT_CHECK_LAUNCH("write_boxes");
     return CT_OK;
 }
 
-int ct_count_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, int64_t* counts, void* stream) {
+int ct_count_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order, int64_t* counts,
+                   void* stream) {
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
     if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
-    if (mode == 0) k_edges<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, counts, 0, 0, 0);
-    else k_edges<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, counts, 0, 0, 0);
+    if (mode == 0)
+        k_edges<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0, 0);
+    else
+        k_edges<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0, 0);
     CT_CHECK_LAUNCH("count_edges");
     return CT_OK;
 }
 
-int ct_write_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int64_t* offsets, int64_t* ii,
-                   int64_t* jj, double* xy, void* stream) {
+int ct_write_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                   const int64_t* offsets, int64_t* ii, int64_t* jj, double* xy, void* stream) {
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
     if (mode == 0)
-        k_edges<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, (int64_t*)offsets, ii, jj,
-                                                          (double4*)xy);
+        k_edges<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets, ii,
+                                                          jj, (double4*)xy);
     else
-        k_edges<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, (int64_t*)offsets, ii, jj,
-                                                          (double4*)xy);
+        k_edges<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets, ii,
+                                                          jj, (double4*)xy);
     CT_CHECK_LAUNCH("write_edges");
     return CT_OK;
 }
@@ -806,6 +838,27 @@ int ct_validate_node_bounds(const int64_t* child, const int64_t* ptr, const int6
         child, ptr, size, bb_indices, bb_coords, (const double4*)node_bounds, n_nodes, valid);
     CT_CHECK_LAUNCH("validate_node_bounds");
     return CT_OK;
+}
+
+size_t ct_work_order_workspace_size(int64_t n) {
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    return 3 * ((4 * nn + 255) / 256 * 256) + ct_radix_pass_workspace_size();
+}
+
+int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_size, int32_t* order, void* ws,
+                  size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 0 || (kind != 0 && kind != 1)) return ct_fail(CT_ERR_ARG, "bad work-order arguments");
+    if (!ws || ws_bytes < ct_work_order_workspace_size(n)) return ct_fail(CT_ERR_WORKSPACE, "workspace too small");
+    if (n == 0) return CT_OK;
+    size_t part = (4 * (size_t)n + 255) / 256 * 256;
+    unsigned* kin = (unsigned*)ws;
+    int* iin = (int*)((char*)ws + part);
+    unsigned* kout = (unsigned*)((char*)ws + 2 * part);
+    unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    k_work_keys<<<blocks, 256, 0, st>>>((const double4*)queries, n, kind, (float)cell_size, kin, iin);
+    CT_CHECK_LAUNCH("work keys");
+    return ct_radix_pass(kin, iin, n, 0, kout, order, (char*)ws + 3 * part, ws_bytes - 3 * part, stream);
 }
 
 }  // extern "C"

@@ -249,3 +249,26 @@ def test_errors_and_casting():
         t.intersect_boxes(np.array([0.0, 1.0, 2.0, 3.0]))
     with pytest.raises(ValueError):
         t.intersect_edges(np.array([[0.0, 1.0], [2.0, 3.0]]))
+
+
+@pytest.mark.gpu
+def test_work_ordered_boxes_and_segments_match_oracle(oracle):
+    """Batches large enough to run in work order (heavy-tailed box sizes and
+    segment lengths): same pairs, same order as the oracle."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.mixed_mesh(60, 50, seed=8, extent=(60.0, 50.0))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    boxes = syn.random_boxes(20000, (0.0, 0.0), (60.0, 50.0), 0.01, 20.0, seed=2, log_uniform=True)
+    for a, b in zip(g.locate_boxes(boxes), o.locate_boxes(boxes)):
+        assert np.array_equal(a, b)
+    for a, b in zip(g.intersect_boxes(boxes[:6000]), o.intersect_boxes(boxes[:6000])):
+        assert np.array_equal(a, b)
+    rng = np.random.default_rng(4)
+    a0 = rng.uniform(0, 60, (9000, 2))
+    ang = rng.uniform(0, 2 * np.pi, 9000)
+    ln = np.exp(rng.uniform(np.log(0.01), np.log(40.0), 9000))
+    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
+    for a, b in zip(g.intersect_edges(segs), o.intersect_edges(segs)):
+        assert np.array_equal(a, b, equal_nan=True)
