@@ -163,34 +163,21 @@ def traffic_per_point():
 
 
 def dist_setup():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
+    from numba_celltree_gb300 import _dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    return ws, rank, local
+    return _dist.setup()
 
 
 def barrier(ws):
-    if ws > 1:
-        import torch.distributed as dist
+    from numba_celltree_gb300 import _dist
 
-        dist.barrier()
+    _dist.barrier()
 
 
 def max_over_ranks(ws, v):
-    if ws == 1:
-        return v
-    import torch
-    import torch.distributed as dist
+    from numba_celltree_gb300 import _dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    return _dist.max_over_ranks(v)
 
 
 def cpu_threads():
