@@ -47,7 +47,11 @@ __device__ __forceinline__ float split_hi(double x, float* lo) {
     unsigned m = (unsigned)(b & 0x1fffffffull);
     float l = 0.0f;
     if (m) {
-        l = ldexpf(__uint2float_rn(m), e - 1075);
+        // m * 2^(e - 1075): the power of two built from its exponent bits when
+        // it is a normal float (the product is then exact), else ldexpf
+        int pe = e - 1075 + 127;
+        l = (pe >= 1 && pe <= 254) ? __uint2float_rn(m) * __int_as_float(pe << 23)
+                                   : ldexpf(__uint2float_rn(m), e - 1075);
         if (sign) l = -l;
     }
     *lo = l;
