@@ -95,6 +95,7 @@ typedef struct ct_tree {
                                  float32 frame, leaf order */
     int64_t cand_n;           /* host: entries of cand_idx */
     double cand_tol;          /* host: largest query tolerance the lists cover */
+    int32_t bounds_finite;    /* host (ct_pack_tree): every node bound and bb_coords value is finite */
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */
@@ -325,6 +326,24 @@ int ct_count_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_
 /* Writes (segment, cell) pairs and the clipped segment / point (xy: R x 2 x 2). */
 int ct_write_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
                    const int64_t* offsets, int64_t* ii, int64_t* jj, double* xy, void* stream);
+
+/* The same query in two phases (what intersect_edges uses): the traversal
+ * writes candidate (segment, leaf position) pairs in traversal order --
+ * every visited cell, minus (mode 1) those Cohen-Sutherland rejects by a
+ * shared outcode -- then one thread per candidate runs the float64 cell test
+ * (keep = 0/1, xy: n_cand x 2 x 2), and the hits are compacted in candidate
+ * order (pos = exclusive scan of keep) with each segment's offset / count.
+ * Same pairs, same order, same coordinates as ct_write_edges. */
+int ct_count_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                              int64_t* counts, void* stream);
+int ct_write_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                              const int64_t* offsets, int32_t* cand_seg, int32_t* cand_pos, void* stream);
+int ct_test_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, const int32_t* cand_seg,
+                            const int32_t* cand_pos, int64_t n_cand, int64_t* keep, double* xy, void* stream);
+int ct_compact_edge_hits(const ct_tree* tree, const int64_t* keep, const int64_t* pos, int64_t n_cand,
+                         const int32_t* cand_seg, const int32_t* cand_pos, const double* xy_cand,
+                         const int64_t* cand_off, const int64_t* cand_cnt, int64_t n, int64_t* ii, int64_t* jj,
+                         double* xy, int64_t* offsets, int64_t* counts, void* stream);
 
 /* sort_intersections_by_edge geometry_utils.py:564-574: stable sort of each
  * segment's results by t = (c - a) . (b - a), NaN last; writes the permuted

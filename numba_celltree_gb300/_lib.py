@@ -78,6 +78,7 @@ class CtTree(ctypes.Structure):
         ("cand_box", _P),
         ("cand_n", _I64),
         ("cand_tol", _D),
+        ("bounds_finite", _I32),
     ]
 
 
@@ -152,6 +153,11 @@ SIGNATURES = {
     "ct_points_in_triangles": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _I64, _P, _D, _P, _P, _P]),
     "ct_csr_workspace_size": (_SZ, [_I64]),
     "ct_work_order_workspace_size": (_SZ, [_I64]),
+    "ct_count_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P]),
+    "ct_write_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_test_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P, _P]),
+    "ct_compact_edge_hits": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P,
+                                            _P, _P, _P, _P]),
     "ct_work_order": (ctypes.c_int, [_P, _I64, _I32, _D, _P, _P, _SZ, _P]),
     "ct_radix_pass_workspace_size": (_SZ, []),
     "ct_radix_pass": (ctypes.c_int, [_P, _P, _I64, _I32, _P, _P, _P, _SZ, _P]),

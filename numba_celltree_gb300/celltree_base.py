@@ -286,28 +286,37 @@ class _GpuTree:
         return ii, jj
 
     def locate_edges(self, segs_d, mode: int):
-        """count -> scan -> write -> per-segment sort by t; returns ii, jj, xy (R, 2, 2)."""
+        """Candidates (traversal) -> float64 cell test per candidate -> hits
+        in candidate order -> per-segment sort by t; returns ii, jj, xy (R, 2, 2)."""
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
         n = int(segs_d.shape[0])
-        counts = _device.empty((n,), torch.int64, self.device)
+        ccnt = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
         order = self.work_order(segs_d, 1)
-        _lib.check(
-            lib.ct_count_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(order),
-                               _device.ptr(counts), st),
-            "intersect_edges",
-        )
-        offsets, total = self.scan(counts)
+        P = _device.ptr
+        _lib.check(lib.ct_count_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(ccnt), st),
+                   "intersect_edges")
+        coff, nc = self.scan(ccnt)
+        cseg = _device.empty((max(nc, 1),), torch.int32, self.device)
+        cpos = _device.empty((max(nc, 1),), torch.int32, self.device)
+        _lib.check(lib.ct_write_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(coff),
+                                                P(cseg), P(cpos), st), "intersect_edges")
+        keep = _device.empty((max(nc, 1),), torch.int64, self.device)
+        xy_c = _device.empty((max(nc, 1), 2, 2), torch.float64, self.device)
+        _lib.check(lib.ct_test_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), P(cseg), P(cpos), nc,
+                                               P(keep), P(xy_c), st), "intersect_edges")
+        pos, total = self.scan(keep[:nc]) if nc > 0 else (keep[:0], 0)
         ii = _device.empty((total,), torch.int64, self.device)
         jj = _device.empty((total,), torch.int64, self.device)
         xy = _device.empty((total, 2, 2), torch.float64, self.device)
-        _lib.check(
-            lib.ct_write_edges(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, _device.ptr(order),
-                               _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), _device.ptr(xy), st),
-            "intersect_edges",
-        )
+        offsets = _device.empty((n,), torch.int64, self.device)
+        counts = _device.empty((n,), torch.int64, self.device)
+        _lib.check(lib.ct_compact_edge_hits(ctypes.byref(self.desc), P(keep), P(pos), nc, P(cseg), P(cpos), P(xy_c),
+                                            P(coff), P(ccnt), n, P(ii), P(jj), P(xy), P(offsets), P(counts), st),
+                   "intersect_edges")
+        del cseg, cpos, keep, xy_c, pos
         if total > 0:
             jj2 = _device.empty((total,), torch.int64, self.device)
             xy2 = _device.empty((total, 2, 2), torch.float64, self.device)
@@ -315,9 +324,7 @@ class _GpuTree:
             ws = _device.empty((int(wsz),), torch.uint8, self.device)
             _lib.check(
                 lib.ct_sort_intersections(
-                    _device.ptr(segs_d), n, _device.ptr(offsets), _device.ptr(counts), _device.ptr(ii),
-                    _device.ptr(jj), _device.ptr(xy), total, _device.ptr(jj2), _device.ptr(xy2),
-                    _device.ptr(ws), wsz, st,
+                    P(segs_d), n, P(offsets), P(counts), P(ii), P(jj), P(xy), total, P(jj2), P(xy2), P(ws), wsz, st,
                 ),
                 "sort_intersections",
             )

@@ -30,7 +30,19 @@ struct TreeQ {
     int64_t n_nodes;
     dbox bbox;
     int K;
+    bool finite;  // all node bounds and cell boxes finite: order comparisons on integer keys
 };
+
+// x < y for finite (or infinite, non-NaN) doubles as one 64-bit integer
+// comparison of order-preserving keys (-0.0 and +0.0 share a key, as they
+// compare equal): the comparisons of the box and segment traversals run on
+// the integer pipes instead of GB300's narrow float64 pipe.
+__device__ __forceinline__ bool not_nan(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool is_fin(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) < 0x7ff0000000000000ull;
+}
 
 __device__ __forceinline__ int na(const float4& q) { return __float_as_int(q.z); }
 __device__ __forceinline__ int nb(const float4& q) { return __float_as_int(q.w); }
@@ -56,6 +68,10 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
     box.ymax = q4.w;
     int64_t count = 0;
     int64_t base = WRITE ? cnt_or_off[i] : 0;
+    // key path: every value non-NaN, so the order comparisons equal the
+    // float64 ones (NaN boxes keep the float64 comparisons)
+    const bool keys = T.finite && not_nan(box.xmin) && not_nan(box.xmax) && not_nan(box.ymin) && not_nan(box.ymax);
+    const unsigned long long kx0 = fkey(box.xmin), kx1 = fkey(box.xmax), ky0 = fkey(box.ymin), ky1 = fkey(box.ymax);
     if (boxes_intersect(box, T.bbox)) {
         int st[STK];
         int sp = 1;
@@ -74,7 +90,11 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                 for (int j = ptr; j < ptr + b; j++) {
                     int64_t cell = T.bbi[j];
                     dbox lb = load_box(T.bb + 4 * cell);
-                    if (boxes_intersect(box, lb)) {
+                    // boxes_intersect geometry_utils.py:292-300
+                    bool hit = keys ? (kx0 < fkey(lb.xmax) && fkey(lb.xmin) < kx1 && ky0 < fkey(lb.ymax) &&
+                                       fkey(lb.ymin) < ky1)
+                                    : boxes_intersect(box, lb);
+                    if (hit) {
                         if (WRITE) {
                             ii[base + count] = i;
                             jj[base + count] = cell;
@@ -86,8 +106,15 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
             }
             int dim = -1 - b;
             double2 d = T.nd[v];
-            double bmin = dim ? box.ymin : box.xmin, bmax = dim ? box.ymax : box.xmax;
-            bool left = bmin <= d.x, right = bmax >= d.y;
+            bool left, right;
+            if (keys) {
+                left = (dim ? ky0 : kx0) <= fkey(d.x);
+                right = (dim ? ky1 : kx1) >= fkey(d.y);
+            } else {
+                double bmin = dim ? box.ymin : box.xmin, bmax = dim ? box.ymax : box.xmax;
+                left = bmin <= d.x;
+                right = bmax >= d.y;
+            }
             int child = na(q);
             if (sp + 2 > STK) {
                 set_error(T.err, CT_DEVERR_STACK);
@@ -127,6 +154,14 @@ __global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restric
     if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
     if (r == 1) {
         dpt V = vsub(b, a);
+        // key path for finite values: the upstream divisions below cannot
+        // change a decision then (for dx > 0, dx_left >= 0 gives a quotient
+        // >= 0 and dx_right <= 0 one <= 0 <= 1; for dx < 0 the quotients have
+        // the opposite signs and 1 - q stays on the right side of 0 and 1),
+        // and dx_left >= 0 <=> Lmax >= a_dim, dx_right <= 0 <=> Rmin <= b_dim
+        const bool keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) &&
+                          is_fin(V.y);
+        const unsigned long long kax = fkey(a.x), kay = fkey(a.y), kbx = fkey(b.x), kby = fkey(b.y);
         int st[STK];
         int sp = 1;
         st[0] = 0;
@@ -177,22 +212,31 @@ __global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restric
             int dim = -1 - bq;
             double2 nd = T.nd[v];
             double dx = dim ? V.y : V.x;
-            double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
-            double dx_left, dx_right;
-            if (dx > 0.0) {
-                dx_left = nd.x - an;
-                dx_right = nd.y - bn;
+            bool left, right;
+            if (keys) {
+                unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
+                bool pos = dx > 0.0;
+                left = fkey(nd.x) >= (pos ? ka : kb);
+                right = fkey(nd.y) <= (pos ? kb : ka);
             } else {
-                dx_left = nd.x - bn;
-                dx_right = nd.y - an;
-            }
-            bool left = dx_left >= 0.0, right = dx_right <= 0.0;
-            if (dx > 0.0) {
-                if (left) left = (dx_left / dx) >= 0.0;
-                if (right) right = (dx_right / dx) <= 1.0;
-            } else if (dx < 0.0) {
-                if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
-                if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+                double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
+                double dx_left, dx_right;
+                if (dx > 0.0) {
+                    dx_left = nd.x - an;
+                    dx_right = nd.y - bn;
+                } else {
+                    dx_left = nd.x - bn;
+                    dx_right = nd.y - an;
+                }
+                left = dx_left >= 0.0;
+                right = dx_right <= 0.0;
+                if (dx > 0.0) {
+                    if (left) left = (dx_left / dx) >= 0.0;
+                    if (right) right = (dx_right / dx) <= 1.0;
+                } else if (dx < 0.0) {
+                    if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
+                    if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+                }
             }
             int child = na(q);
             if (sp + 2 > STK) {
@@ -210,6 +254,193 @@ __global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restric
         }
     }
     if (!WRITE) cnt_or_off[i] = count;
+}
+
+// ---------------------------------------------------------------------------
+// locate_edge in two phases: the traversal collects candidate (segment, cell)
+// pairs in upstream traversal order; one thread per candidate then runs the
+// float64 cell test.  The float64 clipping of the one-pass kernel above runs
+// with a few lanes of a warp active (every segment's traversal differs); per
+// candidate it runs with full warps.  Phase 1 drops only the cells that the
+// cell test's own first step (Cohen-Sutherland's shared-outcode reject, an
+// exact order comparison) rejects.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cs_code_keys(unsigned long long kx, unsigned long long ky, unsigned long long x0,
+                                            unsigned long long x1, unsigned long long y0, unsigned long long y1) {
+    int p = CS_INSIDE;
+    if (kx < x0) p |= CS_LEFT;
+    else if (kx > x1) p |= CS_RIGHT;
+    if (ky < y0) p |= CS_LOWER;
+    else if (ky > y1) p |= CS_UPPER;
+    return p;
+}
+
+template <bool WRITE, int MODE>
+__global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __restrict__ segs, int64_t n,
+                                                    const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
+                                                    int* __restrict__ cseg, int* __restrict__ cj) {
+    int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tq >= n) return;
+    int64_t i = order ? (int64_t)order[tq] : tq;
+    double4 s4 = segs[i];
+    dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+    int64_t count = 0;
+    int64_t base = WRITE ? cnt_or_off[i] : 0;
+    dpt c, d;
+    int r = cohen_sutherland(a, b, T.bbox, &c, &d);
+    if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
+    if (r == 1) {
+        dpt V = vsub(b, a);
+        const bool keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) &&
+                          is_fin(V.y);
+        const unsigned long long kax = fkey(a.x), kay = fkey(a.y), kbx = fkey(b.x), kby = fkey(b.y);
+        int st[STK];
+        int sp = 1;
+        st[0] = 0;
+        int64_t budget = T.n_nodes;
+        while (sp > 0) {
+            if (--budget < 0) {
+                set_error(T.err, CT_DEVERR_LOOP);
+                break;
+            }
+            int v = st[--sp];
+            float4 q = T.nf[v];
+            int bq = nb(q);
+            if (bq >= 0) {
+                int ptr = na(q);
+                for (int j = ptr; j < ptr + bq; j++) {
+                    bool cand = true;
+                    if (MODE == 1) {
+                        dbox bx = load_box(T.bb + 4 * T.bbi[j]);
+                        int k1, k2;
+                        if (keys) {
+                            unsigned long long x0 = fkey(bx.xmin), x1 = fkey(bx.xmax), y0 = fkey(bx.ymin),
+                                               y1 = fkey(bx.ymax);
+                            k1 = cs_code_keys(kax, kay, x0, x1, y0, y1);
+                            k2 = cs_code_keys(kbx, kby, x0, x1, y0, y1);
+                        } else {
+                            k1 = cs_code(a, bx);
+                            k2 = cs_code(b, bx);
+                        }
+                        cand = (k1 & k2) == 0;
+                    }
+                    if (cand) {
+                        if (WRITE) {
+                            cseg[base + count] = (int)i;
+                            cj[base + count] = j;
+                        }
+                        count++;
+                    }
+                }
+                continue;
+            }
+            int dim = -1 - bq;
+            double2 nd = T.nd[v];
+            double dx = dim ? V.y : V.x;
+            bool left, right;
+            if (keys) {
+                unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
+                bool pos = dx > 0.0;
+                left = fkey(nd.x) >= (pos ? ka : kb);
+                right = fkey(nd.y) <= (pos ? kb : ka);
+            } else {
+                double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
+                double dx_left, dx_right;
+                if (dx > 0.0) {
+                    dx_left = nd.x - an;
+                    dx_right = nd.y - bn;
+                } else {
+                    dx_left = nd.x - bn;
+                    dx_right = nd.y - an;
+                }
+                left = dx_left >= 0.0;
+                right = dx_right <= 0.0;
+                if (dx > 0.0) {
+                    if (left) left = (dx_left / dx) >= 0.0;
+                    if (right) right = (dx_right / dx) <= 1.0;
+                } else if (dx < 0.0) {
+                    if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
+                    if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+                }
+            }
+            int child = na(q);
+            if (sp + 2 > STK) {
+                set_error(T.err, CT_DEVERR_STACK);
+                break;
+            }
+            if (left && right) {
+                st[sp++] = child;
+                st[sp++] = child + 1;
+            } else if (left) {
+                st[sp++] = child;
+            } else if (right) {
+                st[sp++] = child + 1;
+            }
+        }
+    }
+    if (!WRITE) cnt_or_off[i] = count;
+}
+
+// The float64 cell test of every candidate (compute_edge_face_intersect
+// query.py:309-328 / compute_edge_edge_intersect 292-306).
+template <int MODE>
+__global__ void __launch_bounds__(128) k_edge_test(TreeQ T, const double4* __restrict__ segs,
+                                                   const int* __restrict__ cseg, const int* __restrict__ cj,
+                                                   int64_t nc, int64_t* __restrict__ keep, double4* __restrict__ xy) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nc; t += (int64_t)gridDim.x * blockDim.x) {
+        double4 s4 = segs[cseg[t]];
+        dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+        int j = cj[t];
+        dpt c, d;
+        bool hit;
+        if (MODE == 0) {
+            double2 p0 = T.poly[(size_t)j * 2], p1 = T.poly[(size_t)j * 2 + 1];
+            double x, y;
+            hit = lines_intersect(a, b, mkp(p0.x, p0.y), mkp(p1.x, p1.y), &x, &y);
+            c = mkp(x, y);
+            d = c;
+        } else {
+            dbox bx = load_box(T.bb + 4 * T.bbi[j]);
+            int rr = cohen_sutherland(a, b, bx, &c, &d);
+            if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
+            hit = rr == 1;
+            if (hit) {
+                const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
+                int len = T.plen ? (int)T.plen[j] : T.K;
+                double tol = pmax(CT_MIN_TOLERANCE, CT_TOLERANCE_FACTOR * pmax(bx.xmax - bx.xmin, bx.ymax - bx.ymin));
+                hit = cyrus_beck(a, b, poly, len, tol, &c, &d);
+            }
+        }
+        keep[t] = hit ? 1 : 0;
+        xy[t] = make_double4(c.x, c.y, d.x, d.y);
+    }
+}
+
+// Hits in candidate order (segment-major, traversal order within a segment),
+// and every segment's hit offset and count.
+__global__ void k_edge_compact(const int64_t* __restrict__ keep, const int64_t* __restrict__ pos, int64_t nc,
+                               const int* __restrict__ cseg, const int* __restrict__ cj,
+                               const int64_t* __restrict__ bbi, const double4* __restrict__ xy_c,
+                               int64_t* __restrict__ ii, int64_t* __restrict__ jj, double4* __restrict__ xy) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nc; t += (int64_t)gridDim.x * blockDim.x) {
+        if (!keep[t]) continue;
+        int64_t p = pos[t];
+        ii[p] = cseg[t];
+        jj[p] = bbi[cj[t]];
+        xy[p] = xy_c[t];
+    }
+}
+
+__global__ void k_edge_seg_counts(const int64_t* __restrict__ coff, const int64_t* __restrict__ ccnt,
+                                  const int64_t* __restrict__ keep, const int64_t* __restrict__ pos, int64_t nc,
+                                  int64_t n, int64_t* __restrict__ off, int64_t* __restrict__ cnt) {
+    const int64_t total = nc > 0 ? pos[nc - 1] + keep[nc - 1] : 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c0 = coff[i], c1 = c0 + ccnt[i];
+        int64_t p0 = c0 < nc ? pos[c0] : total, p1 = c1 < nc ? pos[c1] : total;
+        off[i] = p0;
+        cnt[i] = p1 - p0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -628,6 +859,7 @@ TreeQ make_q(const ct_tree* t) {
     T.bbox.ymin = t->bbox[2];
     T.bbox.ymax = t->bbox[3];
     T.K = t->n_max_vert;
+    T.finite = t->bounds_finite != 0;
     return T;
 }
 
@@ -859,6 +1091,72 @@ int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_si
     k_work_keys<<<blocks, 256, 0, st>>>((const double4*)queries, n, kind, (float)cell_size, kin, iin);
     CT_CHECK_LAUNCH("work keys");
     return ct_radix_pass(kin, iin, n, 0, kout, order, (char*)ws + 3 * part, ws_bytes - 3 * part, stream);
+}
+
+int ct_count_edge_candidates(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                              int64_t* counts, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    if (mode == 0)
+        k_edge_cands<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
+    else
+        k_edge_cands<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
+    CT_CHECK_LAUNCH("count_edge_candidates");
+    return CT_OK;
+}
+
+int ct_write_edge_candidates(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                              const int64_t* offsets, int32_t* cand_seg, int32_t* cand_pos, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (n > INT32_MAX) return ct_fail(CT_ERR_ARG, "at most 2^31 - 1 segments");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    if (mode == 0)
+        k_edge_cands<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
+                                                               cand_seg, cand_pos);
+    else
+        k_edge_cands<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
+                                                               cand_seg, cand_pos);
+    CT_CHECK_LAUNCH("write_edge_candidates");
+    return CT_OK;
+}
+
+int ct_test_edge_candidates(const ct_tree* t, int32_t mode, const double* segs, const int32_t* cand_seg,
+                            const int32_t* cand_pos, int64_t n_cand, int64_t* keep, double* xy, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n_cand == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    unsigned g = (unsigned)std::min<int64_t>(grid_of(n_cand, 128), 152 * 64);
+    if (mode == 0)
+        k_edge_test<0><<<g, 128, 0, st>>>(T, (const double4*)segs, cand_seg, cand_pos, n_cand, keep, (double4*)xy);
+    else
+        k_edge_test<1><<<g, 128, 0, st>>>(T, (const double4*)segs, cand_seg, cand_pos, n_cand, keep, (double4*)xy);
+    CT_CHECK_LAUNCH("test_edge_candidates");
+    return CT_OK;
+}
+
+int ct_compact_edge_hits(const ct_tree* t, const int64_t* keep, const int64_t* pos, int64_t n_cand,
+                         const int32_t* cand_seg, const int32_t* cand_pos, const double* xy_cand,
+                         const int64_t* cand_off, const int64_t* cand_cnt, int64_t n, int64_t* ii, int64_t* jj,
+                         double* xy, int64_t* offsets, int64_t* counts, void* stream) {
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_cand > 0)
+        k_edge_compact<<<(unsigned)std::min<int64_t>(grid_of(n_cand, 256), 152 * 32), 256, 0, st>>>(
+            keep, pos, n_cand, cand_seg, cand_pos, t->bb_indices, (const double4*)xy_cand, ii, jj, (double4*)xy);
+    if (n > 0)
+        k_edge_seg_counts<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 32), 256, 0, st>>>(
+            cand_off, cand_cnt, keep, pos, n_cand, n, offsets, counts);
+    CT_CHECK_LAUNCH("compact_edge_hits");
+    return CT_OK;
 }
 
 }  // extern "C"

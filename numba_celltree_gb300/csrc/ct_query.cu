@@ -381,6 +381,11 @@ __global__ void k_vertex_extent(const double* __restrict__ v, int64_t n, unsigne
 // packing
 // ------------------------------------------------------------------------
 
+__global__ void k_check_finite(const double* __restrict__ x, int64_t n, unsigned int* __restrict__ flag) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (!isfinite(x[i])) atomicOr(flag, 2u);
+}
+
 __global__ void k_pack_nodes(int64_t n_nodes, const int64_t* __restrict__ child, const double* __restrict__ Lmax,
                              const double* __restrict__ Rmin, const int64_t* __restrict__ ptr,
                              const int64_t* __restrict__ size, const uint8_t* __restrict__ dim, double ox, double oy,
@@ -394,6 +399,7 @@ __global__ void k_pack_nodes(int64_t n_nodes, const int64_t* __restrict__ child,
     if (c != -1 && (c <= v || c + 1 >= n_nodes)) atomicOr(bad, 1u);
     if (c == -1 && (ptr[v] < 0 || size[v] < 0 || ptr[v] + size[v] > n_elem)) atomicOr(bad, 1u);
     double L = Lmax[v], R = Rmin[v];
+    if (!isfinite(L) || !isfinite(R)) atomicOr(bad, 2u);  // not an error: queries keep the literal float64 path
     nd[v] = make_double2(L, R);
     float4 q;
     if (child[v] == -1) {
@@ -611,10 +617,14 @@ int ct_pack_tree(ct_tree* t, void* stream) {
             (float4*)t->poly_f32, t->poly_len, t->poly_len32);
         CT_CHECK_LAUNCH("pack_polys");
     }
+    if (t->n_elements > 0 && t->bb_coords)
+        k_check_finite<<<(unsigned)std::min<int64_t>(grid_for(4 * t->n_elements, 256), 152 * 8), 256, 0, st>>>(
+            t->bb_coords, 4 * t->n_elements, red + 1);
     unsigned int hv[2] = {0, 0};
     CT_CUDA(cudaMemcpyAsync(hv, red, sizeof(hv), cudaMemcpyDeviceToHost, st));
     CT_CUDA(cudaStreamSynchronize(st));
-    if (hv[1]) return ct_fail(CT_ERR_DEVICE, "tree structure check failed (child or leaf range out of order)");
+    if (hv[1] & 1u) return ct_fail(CT_ERR_DEVICE, "tree structure check failed (child or leaf range out of order)");
+    t->bounds_finite = (hv[1] & 2u) ? 0 : 1;
     t->vmax = 0.0f;  // unused by the local-frame float32 cells
     // float64 rounding of absolute vertex coordinates (the float64 predicate
     // rounds relative to them): 2^-50 * max |coordinate|
