@@ -245,8 +245,9 @@ class _GpuTree:
         )
         return offsets, int(total.value)
 
-    # queries per batch above which box / segment queries run in work order
-    WORK_ORDER_MIN = 4096
+    # queries per batch from which box / segment queries run in work order
+    # (below it the ordering's fixed cost outweighs the better warp balance)
+    WORK_ORDER_MIN = 65536
 
     def work_order(self, q_d, kind: int):
         """Permutation grouping box (kind 0) / segment (kind 1) queries of
