@@ -142,8 +142,6 @@ SIGNATURES = {
     "ct_exclusive_scan": (ctypes.c_int, [_P, _I64, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
     "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P]),
     "ct_write_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P, _P]),
-    "ct_count_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P]),
-    "ct_write_edges": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "ct_sort_workspace_size": (_SZ, [_I64]),
     "ct_sort_intersections": (ctypes.c_int, [_P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P, _P, _SZ, _P]),
     "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),

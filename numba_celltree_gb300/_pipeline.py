@@ -17,7 +17,42 @@ import numpy as np
 
 from . import _device
 
-CHUNK_POINTS = 1 << 25  # points per chunk (512 MiB of float64 pairs)
+CHUNK_POINTS = 1 << 25  # largest chunk (512 MiB of float64 pairs)
+FIRST_CHUNK = 1 << 22   # the first (and the last) chunks are small: the GPU starts
+                        # after a short upload and the last download is short
+
+
+def chunk_bounds(n: int, chunk: int, first: int = None):
+    """Chunk boundaries [(s, e), ...]: sizes ramp up by doubling from `first`
+    to `chunk`, stay at `chunk`, and ramp down by halving at the end."""
+    first = min(FIRST_CHUNK if first is None else first, chunk)
+    if n <= 0:
+        return []
+    sizes = []
+    m = first
+    rest = n
+    while rest > 0 and m < chunk:
+        take = min(m, rest)
+        sizes.append(take)
+        rest -= take
+        m *= 2
+    tail = []
+    while rest > 2 * chunk:
+        sizes.append(chunk)
+        rest -= chunk
+    # the last <= 2 chunks: halve down to `first`
+    while rest > first:
+        half = rest // 2
+        tail.append(rest - half)
+        rest = half
+    if rest > 0:
+        tail.append(rest)
+    return_sizes = sizes + tail
+    out, s = [], 0
+    for k in return_sizes:
+        out.append((s, s + k))
+        s += k
+    return out
 
 
 def pinned_empty(shape, dtype):
@@ -41,15 +76,15 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
     compute = torch.cuda.current_stream(device)
     up = torch.cuda.Stream(device)
     down = torch.cuda.Stream(device)
-    m = min(chunk, n)
-    nbuf = 2 if n > m else 1
+    bounds = chunk_bounds(n, chunk)
+    m = max(e - s for s, e in bounds)
+    nbuf = 2 if len(bounds) > 1 else 1
     pin_in = src.is_pinned()
     p_d = [torch.empty((m, 2), dtype=torch.float64, device=device) for _ in range(nbuf)]
     o_d = [torch.empty((m,), dtype=out_dtype, device=device) for _ in range(nbuf)]
     done = [None] * nbuf  # query of the chunk that last used buffer b
     fetched = [None] * nbuf  # download of the chunk that last used buffer b
-    for c, s in enumerate(range(0, n, m)):
-        e = min(s + m, n)
+    for c, (s, e) in enumerate(bounds):
         b = c % nbuf
         k = e - s
         with torch.cuda.stream(up):

@@ -137,133 +137,14 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
 // locate_edge query.py:357-455 with compute_edge_edge_intersect (292-306,
 // mode 0) or compute_edge_face_intersect (309-328, mode 1)
 // ---------------------------------------------------------------------------
-template <bool WRITE, int MODE>
-__global__ void __launch_bounds__(128) k_edges(TreeQ T, const double4* __restrict__ segs, int64_t n,
-                                               const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
-                                               int64_t* __restrict__ ii, int64_t* __restrict__ jj,
-                                               double4* __restrict__ xy) {
-    int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (tq >= n) return;
-    int64_t i = order ? (int64_t)order[tq] : tq;
-    double4 s4 = segs[i];
-    dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
-    int64_t count = 0;
-    int64_t base = WRITE ? cnt_or_off[i] : 0;
-    dpt c, d;
-    int r = cohen_sutherland(a, b, T.bbox, &c, &d);
-    if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
-    if (r == 1) {
-        dpt V = vsub(b, a);
-        // key path for finite values: the upstream divisions below cannot
-        // change a decision then (for dx > 0, dx_left >= 0 gives a quotient
-        // >= 0 and dx_right <= 0 one <= 0 <= 1; for dx < 0 the quotients have
-        // the opposite signs and 1 - q stays on the right side of 0 and 1),
-        // and dx_left >= 0 <=> Lmax >= a_dim, dx_right <= 0 <=> Rmin <= b_dim
-        const bool keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) &&
-                          is_fin(V.y);
-        const unsigned long long kax = fkey(a.x), kay = fkey(a.y), kbx = fkey(b.x), kby = fkey(b.y);
-        int st[STK];
-        int sp = 1;
-        st[0] = 0;
-        int64_t budget = T.n_nodes;
-        while (sp > 0) {
-            if (--budget < 0) {
-                set_error(T.err, CT_DEVERR_LOOP);
-                break;
-            }
-            int v = st[--sp];
-            float4 q = T.nf[v];
-            int bq = nb(q);
-            if (bq >= 0) {
-                int ptr = na(q);
-                for (int j = ptr; j < ptr + bq; j++) {
-                    int64_t cell = T.bbi[j];
-                    bool hit;
-                    if (MODE == 0) {
-                        double2 p0 = T.poly[(size_t)j * 2], p1 = T.poly[(size_t)j * 2 + 1];
-                        double x, y;
-                        hit = lines_intersect(a, b, mkp(p0.x, p0.y), mkp(p1.x, p1.y), &x, &y);
-                        c = mkp(x, y);
-                        d = c;
-                    } else {
-                        dbox bx = load_box(T.bb + 4 * cell);
-                        int rr = cohen_sutherland(a, b, bx, &c, &d);
-                        if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
-                        hit = rr == 1;
-                        if (hit) {
-                            const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
-                            int len = T.plen ? (int)T.plen[j] : T.K;
-                            double tol = pmax(CT_MIN_TOLERANCE,
-                                              CT_TOLERANCE_FACTOR * pmax(bx.xmax - bx.xmin, bx.ymax - bx.ymin));
-                            hit = cyrus_beck(a, b, poly, len, tol, &c, &d);
-                        }
-                    }
-                    if (hit) {
-                        if (WRITE) {
-                            ii[base + count] = i;
-                            jj[base + count] = cell;
-                            xy[base + count] = make_double4(c.x, c.y, d.x, d.y);
-                        }
-                        count++;
-                    }
-                }
-                continue;
-            }
-            int dim = -1 - bq;
-            double2 nd = T.nd[v];
-            double dx = dim ? V.y : V.x;
-            bool left, right;
-            if (keys) {
-                unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
-                bool pos = dx > 0.0;
-                left = fkey(nd.x) >= (pos ? ka : kb);
-                right = fkey(nd.y) <= (pos ? kb : ka);
-            } else {
-                double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
-                double dx_left, dx_right;
-                if (dx > 0.0) {
-                    dx_left = nd.x - an;
-                    dx_right = nd.y - bn;
-                } else {
-                    dx_left = nd.x - bn;
-                    dx_right = nd.y - an;
-                }
-                left = dx_left >= 0.0;
-                right = dx_right <= 0.0;
-                if (dx > 0.0) {
-                    if (left) left = (dx_left / dx) >= 0.0;
-                    if (right) right = (dx_right / dx) <= 1.0;
-                } else if (dx < 0.0) {
-                    if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
-                    if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
-                }
-            }
-            int child = na(q);
-            if (sp + 2 > STK) {
-                set_error(T.err, CT_DEVERR_STACK);
-                break;
-            }
-            if (left && right) {
-                st[sp++] = child;
-                st[sp++] = child + 1;
-            } else if (left) {
-                st[sp++] = child;
-            } else if (right) {
-                st[sp++] = child + 1;
-            }
-        }
-    }
-    if (!WRITE) cnt_or_off[i] = count;
-}
-
 // ---------------------------------------------------------------------------
-// locate_edge in two phases: the traversal collects candidate (segment, cell)
-// pairs in upstream traversal order; one thread per candidate then runs the
-// float64 cell test.  The float64 clipping of the one-pass kernel above runs
-// with a few lanes of a warp active (every segment's traversal differs); per
-// candidate it runs with full warps.  Phase 1 drops only the cells that the
-// cell test's own first step (Cohen-Sutherland's shared-outcode reject, an
-// exact order comparison) rejects.
+// locate_edge (query.py:357-455) in two phases: the traversal collects
+// candidate (segment, cell) pairs in upstream traversal order; one thread per
+// candidate then runs the float64 cell test.  Clipping inside the traversal
+// would run with a few lanes of a warp active (every segment's traversal
+// differs); per candidate it runs with full warps.  Phase 1 drops only the
+// cells that the cell test's own first step (Cohen-Sutherland's
+// shared-outcode reject, an exact order comparison) rejects.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int cs_code_keys(unsigned long long kx, unsigned long long ky, unsigned long long x0,
                                             unsigned long long x1, unsigned long long y0, unsigned long long y1) {
@@ -924,39 +805,6 @@ int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     k_boxes<true><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
                                                                       (int64_t*)offsets, ii, jj);
     CT_CHECK_LAUNCH("write_boxes");
-    return CT_OK;
-}
-
-int ct_count_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order, int64_t* counts,
-                   void* stream) {
-    int s = check_tree(t);
-    if (s) return s;
-    if (n == 0) return CT_OK;
-    if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
-    cudaStream_t st = (cudaStream_t)stream;
-    TreeQ T = make_q(t);
-    if (mode == 0)
-        k_edges<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0, 0);
-    else
-        k_edges<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0, 0);
-    CT_CHECK_LAUNCH("count_edges");
-    return CT_OK;
-}
-
-int ct_write_edges(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
-                   const int64_t* offsets, int64_t* ii, int64_t* jj, double* xy, void* stream) {
-    int s = check_tree(t);
-    if (s) return s;
-    if (n == 0) return CT_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    TreeQ T = make_q(t);
-    if (mode == 0)
-        k_edges<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets, ii,
-                                                          jj, (double4*)xy);
-    else
-        k_edges<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets, ii,
-                                                          jj, (double4*)xy);
-    CT_CHECK_LAUNCH("write_edges");
     return CT_OK;
 }
 
