@@ -202,10 +202,19 @@ class _GpuTree:
         radix pass costs)."""
         return 0 if n_points < (1 << 16) else 16
 
+    # largest batch one library call takes (the entry points index queries
+    # with 32-bit integers); larger batches are located slice by slice
+    MAX_CALL_POINTS = 1 << 29
+
     def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None) -> None:
         """Enqueue point location on the current stream (no synchronisation)."""
         lib = _lib.load()
         n = int(points_d.shape[0])
+        if n > self.MAX_CALL_POINTS:
+            for s in range(0, n, self.MAX_CALL_POINTS):
+                e = min(s + self.MAX_CALL_POINTS, n)
+                self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits)
+            return
         if precision == "fp32":
             g = self.auto_sort_bits(n) if sort_bits is None else int(sort_bits)
             need = int(lib.ct_locate_workspace_size(n, g))
