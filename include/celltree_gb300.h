@@ -320,20 +320,14 @@ int ct_write_boxes(const ct_tree* tree, const double* boxes, int64_t n, const in
 /* locate_edge query.py:357-455 over segments (n x 2 x 2).  mode 1: edge vs
  * face (Cohen-Sutherland + Cyrus-Beck, compute_edge_face_intersect
  * query.py:309-328); mode 0: edge vs edge (lines_intersect,
- * compute_edge_edge_intersect query.py:292-306, edge trees only). */
-int ct_count_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
-                   int64_t* counts, void* stream);
-/* Writes (segment, cell) pairs and the clipped segment / point (xy: R x 2 x 2). */
-int ct_write_edges(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
-                   const int64_t* offsets, int64_t* ii, int64_t* jj, double* xy, void* stream);
-
-/* The same query in two phases (what intersect_edges uses): the traversal
- * writes candidate (segment, leaf position) pairs in traversal order --
- * every visited cell, minus (mode 1) those Cohen-Sutherland rejects by a
- * shared outcode -- then one thread per candidate runs the float64 cell test
- * (keep = 0/1, xy: n_cand x 2 x 2), and the hits are compacted in candidate
- * order (pos = exclusive scan of keep) with each segment's offset / count.
- * Same pairs, same order, same coordinates as ct_write_edges. */
+ * compute_edge_edge_intersect query.py:292-306, edge trees only).  In two
+ * phases: the traversal writes candidate (segment, leaf position) pairs in
+ * traversal order -- every visited cell, minus (mode 1) those
+ * Cohen-Sutherland rejects by a shared outcode -- then one thread per
+ * candidate runs the float64 cell test (keep = 0/1, xy: n_cand x 2 x 2), and
+ * the hits are compacted in candidate order (pos = exclusive scan of keep)
+ * with each segment's offset / count: upstream's pairs, order and clipped
+ * coordinates (before sort_intersections_by_edge). */
 int ct_count_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
                               int64_t* counts, void* stream);
 int ct_write_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
