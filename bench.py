@@ -565,7 +565,7 @@ def main():
     with ClockSampler(local) as clk:
         ms32 = timed(lambda: run("fp32", out32), args.steps, args.warmup)
     clocks = clk.summary()
-    # the dominant kernel alone: the float32 pass over the binned queries
+    # the dominant kernels alone: the float32 pass over the sorted queries
     wsb = t._locate_ws
     lib.ct_locate_bin(ctypes.byref(t.desc), _device.ptr(pts_d), n, bins, _device.ptr(wsb), int(wsb.numel()),
                       _device.stream())

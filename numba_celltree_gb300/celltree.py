@@ -39,10 +39,11 @@ class CellTree2d(CellTree2dBase):
     ``bb_indices`` arrays, the same cells for every query.  Queries given numpy
     arrays return numpy arrays; queries given CUDA tensors return CUDA tensors.
     ``precision`` selects the point-location form, all returning identical
-    indices: ``"fp32"`` (default: queries binned for coherent traversal, a
-    float32 pass that defers ambiguous leaf tests, a float64-exact pass over
-    the deferred ones), ``"fp32-inline"`` (one float32 kernel with in-line
-    float64 fallbacks) or ``"fp64"`` (plain float64).
+    indices: ``"fp32"`` (default: queries sorted for coherence, per-grid-cell
+    candidate lists and a float32 traversal with exact float32 filters, a
+    float64 pass over the queries the filters could not decide),
+    ``"fp32-inline"`` (one float32 kernel with in-line float64 fallbacks) or
+    ``"fp64"`` (plain float64).
     """
 
     _elements_name = "faces"

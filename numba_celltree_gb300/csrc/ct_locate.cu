@@ -1,21 +1,25 @@
 // ct_locate.cu -- the batched point-location pipeline (locate_points
-// query.py:63-117), float32 form.
+// query.py:63-117), float32 form, for one tree or a batch of trees.
 //
 //   1. order    queries are sorted along a Morton curve over the tree bbox
-//               (LSD radix sort of 24-bit keys with 8-bit digits: per-block
-//               shared-memory histograms, one scan, stable block-local
-//               scatter), so consecutive threads traverse nearly the same path;
-//   2. fast     float32 traversal (node bounds inside their error band are
-//               re-decided in-line with one float64 compare) and the float32
-//               leaf filter in each cell's local frame.  A polygon the filter
-//               cannot decide (UNSURE) becomes a candidate and the traversal
-//               continues, in upstream order, until a polygon is surely hit or
-//               the traversal ends.  Queries without candidates are final;
-//               the others get a record and their candidates are appended to
-//               a dense (record, ordinal, polygon) list;
+//               (LSD radix sort with 8-bit digits: per-block shared-memory
+//               histograms, one scan, shared-memory-staged scatter), so
+//               neighbouring threads take nearly the same paths;
+//   2a. cells   per query the candidate list of its grid cell (cells whose
+//               widened bbox meets the grid cell): a float32 bbox reject,
+//               then the float32 leaf filter in each cell's local frame.
+//               One sure hit and sure misses elsewhere, or sure misses only,
+//               is final; anything else leaves the query open;
+//   2b. fast    open queries: float32 traversal from the start-node grid
+//               (bounds inside their error band re-decided out of line in
+//               float64).  A polygon the filter cannot decide (UNSURE)
+//               becomes a candidate and the traversal continues, in upstream
+//               order, until a polygon is surely hit or it ends.  Queries
+//               without candidates are final; the others get a record and a
+//               dense (record, ordinal, polygon) list of candidates;
 //   3. pip      the exact float64 point_in_polygon_or_on_edge of every
-//               candidate pair, one pair per thread (full warps);
-//               a true result lowers the record's first-true ordinal;
+//               candidate pair, one pair per thread (full warps); a true
+//               result lowers the record's first-true ordinal;
 //   4. resolve  per record: the first candidate whose exact test is true,
 //               else the surely-hit cell of the fast pass, else -1 -- which is
 //               exactly upstream's first hit, since node decisions do not
@@ -23,8 +27,9 @@
 //   5. exact    queries with more than CMAX candidates (or beyond the record
 //               capacity) run the float32-with-float64-fallback traversal.
 //
-// Query order does not affect any result (queries are independent), so the
-// binning is safe.  The traversal stack lives in shared memory.
+// Query order does not affect any result (queries are independent and every
+// result is written to the query's own index), so the sort is safe.  The
+// traversal stacks live in shared memory.
 #include <cfloat>
 #include <cmath>
 #include <cstring>
