@@ -349,7 +349,8 @@ def run_batch(args):
 
 
 def run_queries(args):
-    """Side measurement: build and every query on the C1 / C2 / C4 shapes, GPU
+    """Side measurement: build and every query on the C1 / C2 / C4 shapes and the
+    segments on the 16M-triangle mesh, GPU
     (device-resident inputs, wall time around synchronised calls) against the
     oracle (C restatement, OpenMP, all host cores) on a bounded sample, with
     the GPU result checked on that sample."""
@@ -479,6 +480,25 @@ def run_queries(args):
     m = 1_000_000
     ro, tc = cpu(lambda: ot.compute_barycentric_weights(bp))
     record("C4", "compute_barycentric_weights", len(bp), "points", tg, m, tc, same_multi(host(r), ro))
+    del tree, ot, r
+    # ---- C5: 16M triangles (1 m cells, offset 5.0e5 / 4.2e6 m); 4M segments,
+    # uniform start over the mesh, uniform direction, length U(0, 20) m
+    xy, f = workload(args)
+    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
+    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
+    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
+    record("C5", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    srng = np.random.default_rng(7)
+    ns = 4_000_000
+    a0 = srng.uniform(xy.min(0), xy.max(0), (ns, 2))
+    ang = srng.uniform(0.0, 2 * np.pi, ns)
+    ln = srng.uniform(0.0, 20.0, ns)
+    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
+    sd = torch.as_tensor(segs, device=dev)
+    r, tg = wall(lambda: tree.intersect_edges(sd), reps=1)
+    m = 20_000
+    ro, tc = cpu(lambda: ot.intersect_edges(segs[:m]))
+    record("C5", "intersect_edges", ns, "segments", tg, m, tc, same_multi(first_queries(host(r), m), ro))
     print(json.dumps({"summary": "queries vs oracle", "host_cores": cores,
                       "min_speedup": min(x["speedup"] for x in lines),
                       "all_identical": all(x["identical_on_sample"] for x in lines)}))

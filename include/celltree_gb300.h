@@ -295,14 +295,17 @@ int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* workspac
 
 /* Work order of box (kind 0) or segment (kind 1) queries (no upstream
  * counterpart): a permutation grouping queries of similar size (box area /
- * segment length with a cell-size margin, 8-bit log classes, stable), so one
+ * segment length with a cell-size margin, 8-bit log classes), so one
  * warp's queries take similar time.  Passing it as `order` below changes no
  * result: counts and pairs stay indexed and ordered by query. */
 size_t ct_work_order_workspace_size(int64_t n);
 int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_size, int32_t* order, void* workspace,
                   size_t workspace_bytes, void* stream);
-/* One stable LSD pass on 8 bits of 32-bit keys (bits shift .. shift + 7):
- * kin/iin -> kout/iout.  Workspace: ct_radix_pass_workspace_size() bytes. */
+/* One LSD pass on 8 bits of 32-bit keys (bits shift .. shift + 7):
+ * kin/iin -> kout/iout, iin null for the indices 0 .. n-1.  Keys of one digit
+ * keep the order of the 4096-key tiles they come from but may be permuted
+ * within a tile (callers need grouping, not stability).  Workspace:
+ * ct_radix_pass_workspace_size() bytes. */
 size_t ct_radix_pass_workspace_size(void);
 int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout,
                   void* workspace, size_t workspace_bytes, void* stream);

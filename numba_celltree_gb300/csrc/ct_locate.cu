@@ -562,10 +562,10 @@ __device__ __forceinline__ unsigned morton24(const Grid& g, double2 p) {
 // counts digit d in block b's chunk; its exclusive scan is where block b
 // writes its keys of digit d.
 
-// Keys of the queries and the histogram of the first digit.
+// Keys of the queries and the histogram of the first digit (the indices of
+// the first pass are implicit: the scatter takes a null index input as i).
 __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, int64_t n, int64_t chunk, Grid g,
-                                                int shift, unsigned* __restrict__ key, int* __restrict__ idx,
-                                                int64_t* __restrict__ hist) {
+                                                int shift, unsigned* __restrict__ key, int64_t* __restrict__ hist) {
     __shared__ int h[RS_T / 32][256];
     const int t = threadIdx.x, w = t >> 5;
     for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
@@ -576,7 +576,6 @@ __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, 
     for (int64_t i = s + t; i < e; i += RS_T) {
         unsigned k = morton24(g, pts[i]);
         key[i] = k;
-        idx[i] = (int)i;
         atomicAdd(&h[w][(k >> shift) & 255u], 1);
     }
     __syncthreads();
@@ -591,8 +590,8 @@ __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, 
 __global__ void __launch_bounds__(RS_T) k_keys_forest(const double2* __restrict__ pts, int64_t n, int64_t chunk,
                                                        const Grid* __restrict__ grids,
                                                        const int64_t* __restrict__ poff, int n_trees, int mbits,
-                                                       unsigned* __restrict__ key, int* __restrict__ idx,
-                                                       int* __restrict__ qtree, int64_t* __restrict__ hist) {
+                                                       unsigned* __restrict__ key, int* __restrict__ qtree,
+                                                       int64_t* __restrict__ hist) {
     __shared__ int h[RS_T / 32][256];
     const int t = threadIdx.x, w = t >> 5;
     for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
@@ -610,7 +609,6 @@ __global__ void __launch_bounds__(RS_T) k_keys_forest(const double2* __restrict_
         unsigned m = morton24(grids[lo], pts[i]) >> (24 - mbits);
         unsigned k = ((unsigned)lo << mbits) | m;
         key[i] = k;
-        idx[i] = (int)i;
         qtree[i] = lo;
         atomicAdd(&h[w][k & 255u], 1);
     }
@@ -650,7 +648,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* __restrict__ k
 // atomic (so equal digits of one tile may be permuted -- the order of the
 // queries only has to be coherent, every result is written by the query's
 // own index), the tile is regrouped by digit in shared memory and written
-// out in runs.
+// out in runs.  A null `iin` stands for the indices 0 .. n-1.
 __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ iin,
                                                       int64_t n, int64_t chunk, int shift,
                                                       const int64_t* __restrict__ offs, unsigned* __restrict__ kout,
@@ -676,7 +674,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
             int64_t i = base + k * RS_T + t;
             bool v = i < e;
             key[k] = v ? kin[i] : 0u;
-            id[k] = v ? iin[i] : -1;
+            id[k] = v ? (iin ? iin[i] : (int)i) : -1;
         }
 #pragma unroll
         for (int k = 0; k < RS_IPT; k++) rk[k] = (id[k] >= 0) ? atomicAdd(&cnt[(key[k] >> shift) & 255u], 1) : 0;
@@ -1090,7 +1088,8 @@ size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits) {
 
 // Stage 1: order the queries along a Morton curve over the tree bbox (4096 x
 // 4096 grid): the top `sort_bits` bits of the 24-bit key, LSD radix sort with
-// 8-bit digits, then one gather of the points.  No-op when sort_bits == 0.
+// 8-bit digits; the last pass writes the permutation (the points stay where
+// they are).  No-op when sort_bits == 0.
 int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sort_bits, void* ws, size_t ws_bytes,
                   void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
@@ -1113,12 +1112,12 @@ int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sor
     for (int pss = 0; pss < passes; pss++) {
         int shift = 24 - sort_bits + 8 * pss;
         if (pss == 0)
-            k_keys<<<RS_BLOCKS, RS_T, 0, st>>>((const double2*)points, n, chunk, g, shift, kin, iin, L.hist);
+            k_keys<<<RS_BLOCKS, RS_T, 0, st>>>((const double2*)points, n, chunk, g, shift, kin, L.hist);
         else
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, L.hist, kout, iout);
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist, kout, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1290,12 +1289,12 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
         int shift = 8 * pss;
         if (pss == 0)
             k_keys_forest<<<RS_BLOCKS, RS_T, 0, st>>>(P, n, chunk, F.grids, F.poff, plan->n_trees, plan->morton_bits,
-                                                      kin, iin, F.qtree, L.hist);
+                                                      kin, F.qtree, L.hist);
         else
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         int s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, L.hist, kout, iout);
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist, kout, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1326,7 +1325,7 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
 }
 
 // ---------------------------------------------------------------------------
-// one stable 8-bit radix pass, shared with the multi-result queries
+// one 8-bit radix pass, shared with the multi-result queries
 // ---------------------------------------------------------------------------
 size_t ct_radix_pass_workspace_size(void) {
     return a256(8 * (size_t)256 * RS_BLOCKS) + a256(ct_scan_workspace_size((int64_t)256 * RS_BLOCKS));

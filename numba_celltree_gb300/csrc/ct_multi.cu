@@ -707,8 +707,8 @@ __global__ void k_validate_bounds(const int64_t* __restrict__ child, const int64
 
 // 8-bit work class of a box (kind 0: area with a cell-size margin) or a
 // segment (kind 1: length plus a cell size): 4 * log2(work) + 128, clamped.
-__global__ void k_work_keys(const double4* __restrict__ q, int64_t n, int kind, float cell, unsigned* __restrict__ key,
-                            int* __restrict__ idx) {
+__global__ void k_work_keys(const double4* __restrict__ q, int64_t n, int kind, float cell,
+                            unsigned* __restrict__ key) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double4 v = q[i];
         float w;
@@ -721,7 +721,6 @@ __global__ void k_work_keys(const double4* __restrict__ q, int64_t n, int kind, 
         }
         int k = (w > 0.0f) ? (int)floorf(4.0f * log2f(w)) + 128 : 0;  // NaN -> 0
         key[i] = (unsigned)min(max(k, 0), 255);
-        idx[i] = (int)i;
     }
 }
 
@@ -922,7 +921,7 @@ int ct_validate_node_bounds(const int64_t* child, const int64_t* ptr, const int6
 
 size_t ct_work_order_workspace_size(int64_t n) {
     size_t nn = (size_t)(n > 0 ? n : 1);
-    return 3 * ((4 * nn + 255) / 256 * 256) + ct_radix_pass_workspace_size();
+    return 2 * ((4 * nn + 255) / 256 * 256) + ct_radix_pass_workspace_size();
 }
 
 int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_size, int32_t* order, void* ws,
@@ -933,12 +932,11 @@ int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_si
     if (n == 0) return CT_OK;
     size_t part = (4 * (size_t)n + 255) / 256 * 256;
     unsigned* kin = (unsigned*)ws;
-    int* iin = (int*)((char*)ws + part);
-    unsigned* kout = (unsigned*)((char*)ws + 2 * part);
+    unsigned* kout = (unsigned*)((char*)ws + part);
     unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
-    k_work_keys<<<blocks, 256, 0, st>>>((const double4*)queries, n, kind, (float)cell_size, kin, iin);
+    k_work_keys<<<blocks, 256, 0, st>>>((const double4*)queries, n, kind, (float)cell_size, kin);
     CT_CHECK_LAUNCH("work keys");
-    return ct_radix_pass(kin, iin, n, 0, kout, order, (char*)ws + 3 * part, ws_bytes - 3 * part, stream);
+    return ct_radix_pass(kin, nullptr, n, 0, kout, order, (char*)ws + 2 * part, ws_bytes - 2 * part, stream);
 }
 
 int ct_count_edge_candidates(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
