@@ -608,10 +608,13 @@ def main():
 
     # kernels per batched step: radix sort (key+hist, scan x3, scatter for the
     # first 8-bit digit; hist, scan x3, scatter for each further digit),
-    # candidate lists + open-query traversal, pair tests, resolve, overflow
+    # candidate lists (+ the two-pass bucketed scatter of their results when
+    # the queries are sorted) + open-query traversal, pair tests, resolve,
+    # overflow
     passes = bins // 8
     lists = t.cand_idx is not None and tol <= float(t.desc.cand_tol)
-    launches_per_step = (5 * passes if bins else 0) + (2 if lists else 1) + 3
+    stage2 = (4 if bins else 2) if lists else 1
+    launches_per_step = (5 * passes if bins else 0) + stage2 + 3
     value = ws * n / (ms32 * 1e-3) / 1e6
     value64 = ws * n / (ms64 * 1e-3) / 1e6
 
@@ -667,7 +670,8 @@ def main():
     roof = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "traffic": (round(tpp * n) if tpp is not None else None),
-            "kernel": "float32 pass: ctl::k_cells<3> (candidate lists) + ctl::k_fast<3> over the open queries",
+            "kernel": "float32 pass: ctl::k_cells<3> (candidate lists, results by sorted position) + "
+                      "ctl::k_res_bucket + ctl::k_res_unbucket (their scatter) + ctl::k_fast<3> (open queries)",
             "kernel_ms": round(ms_fast, 3)}
     result = {
         "metric": METRIC,

@@ -81,16 +81,17 @@ typedef struct ct_tree {
     float abs_eps;            /* host: float64 rounding scale of absolute coordinates */
     unsigned int* error_word; /* device: one uint32, OR-ed CT_DEVERR_* bits */
     /* start-node grid of the batched float32 locate (filled by ct_pack_grid;
-     * grid_n = 0 disables it) */
-    int32_t* grid_start;      /* device: grid_n x grid_n node ids (-1: no cell), row = y */
-    int32_t grid_n;           /* cells per axis */
+     * grid_nx = 0 disables it) */
+    int32_t* grid_start;      /* device: grid_ny rows of grid_nx node ids (-1: no cell) */
+    int32_t grid_nx, grid_ny; /* cells along x and y */
     float grid_x0, grid_y0;   /* host: grid origin in the float32 frame */
     float grid_sx, grid_sy;   /* host: cells per unit length */
     /* per-grid-cell candidate lists of the batched float32 locate (filled by
      * ct_cand_count + ct_cand_fill; cand_tol = 0 disables them) */
-    int64_t* cand_off;        /* device: grid_n * grid_n + 1 offsets into cand_idx */
+    int64_t* cand_off;        /* device: grid_nx * grid_ny + 1 offsets into cand_idx */
     int32_t* cand_idx;        /* device: leaf-order cell ids of each grid cell */
-    void* cand_lbox;          /* device: cand_n x float4, the widened box of each cand_idx entry */
+    void* cand_lbox;          /* device: cand_n x float4, per entry the box where the cell's predicate
+                                 can be true for a point of the grid cell */
     void* cand_box;           /* device: n_elements x float4 widened bbox (xmin, xmax, ymin, ymax),
                                  float32 frame, leaf order */
     int64_t cand_n;           /* host: entries of cand_idx */
@@ -192,31 +193,38 @@ int ct_pack_tree(ct_tree* tree, void* stream);
 #define CT_MODE_FP32 1 /* float32 traversal + float32 leaf filter, exact float64 fallback */
 
 /* Start-node grid (no upstream counterpart; an index over the tree that
- * shortens the batched float32 locate).  For each cell of a grid_n x grid_n
+ * shortens the batched float32 locate).  For each cell of a grid_nx x grid_ny
  * grid over the tree bbox it stores the first node of the root path of
  * locate_point (query.py:63-107) at which the points of that cell (plus a
  * rounding margin) stop taking one and the same single child -- a leaf, a
  * node with a bound inside the cell, or a node whose two children are both
  * taken -- or -1 when the path ends without a child.  Every traversal of the
  * reference from the root reaches that node with an empty stack, so starting
- * there gives the same result.  ct_grid_resolution: grid_n for n_elements
- * (smallest power of two >= sqrt(n_elements), in [16, 4096]).
- * ct_pack_grid needs the packed tree (ct_pack_tree) and tree->grid_start /
- * grid_n set by the caller; it sets grid_n = 0 for a degenerate bbox. */
-int32_t ct_grid_resolution(int64_t n_elements);
+ * there gives the same result.  ct_grid_shape: grid_nx, grid_ny for
+ * n_elements cells in a width x height bbox -- nearly square grid cells,
+ * about cells_per_element grid cells per mesh cell, at least 16 per axis,
+ * at most 2^26 in all.  ct_pack_grid needs the packed tree (ct_pack_tree) and
+ * tree->grid_start / grid_nx / grid_ny set by the caller; it sets
+ * grid_nx = grid_ny = 0 for a degenerate bbox. */
+int ct_grid_shape(int64_t n_elements, double width, double height, double cells_per_element, int32_t* grid_nx,
+                  int32_t* grid_ny);
 int ct_pack_grid(ct_tree* tree, void* stream);
 
 /* Candidate lists (no upstream counterpart; an index that lets most batched
- * float32 queries skip the traversal).  For grid cell g the list holds every
- * cell whose bbox, widened by 2 * cover_tol plus the float64 rounding of the
- * coordinates, meets g widened by the cell-assignment margin: every cell for
- * which point_in_polygon_or_on_edge (geometry_utils.py:195-223) can be true
- * for a point of g.  A query tests its list with the float32 leaf filter; one
- * sure hit and sure misses elsewhere is locate_point's answer (a sure hit is
- * an interior point, inside the cell's bbox, so the reference reaches that
- * leaf), all sure misses is -1, anything else goes through the traversal.
- * Needs ct_pack_grid first and the caller's arrays cand_off
- * (grid_n^2 + 1 int64) and cand_box (n_elements float4).  ct_cand_count
+ * float32 queries skip the traversal).  The region where
+ * point_in_polygon_or_on_edge (geometry_utils.py:195-223) can be true for a
+ * cell lies within M = 2 * cover_tol plus the float64 rounding of the
+ * coordinates of the cell.  For grid cell g (widened by the cell-assignment
+ * margin m) the list holds every cell that meets g widened by m + M, each
+ * with the box of that part of the cell widened by M (and by the rounding of
+ * the float32 clipping that computes it): every cell whose predicate can be
+ * true for a point of g, and a box that holds every such point.  A query
+ * tests the boxes of its list and the float32 leaf filter of the cells whose
+ * box holds it; one sure hit and sure misses elsewhere is locate_point's
+ * answer (a sure hit is an interior point, inside the cell's bbox, so the
+ * reference reaches that leaf), all sure misses is -1, anything else goes
+ * through the traversal.  Needs ct_pack_grid first and the caller's arrays
+ * cand_off (grid_nx * grid_ny + 1 int64) and cand_box (n_elements float4).  ct_cand_count
  * fills the boxes and offsets and returns the number of entries (sets
  * cand_n, cand_tol; synchronises); the caller then allocates cand_idx and
  * cand_lbox (cand_n entries each) and calls ct_cand_fill.  scratch: ct_cand_scratch_size bytes. */
@@ -270,6 +278,7 @@ typedef struct ct_forest_plan {
     int32_t kt;           /* leaf-filter width: 3, 4 or 32 (largest n_max_vert) */
     int32_t stack;        /* traversal stack entries per query (deepest tree + 2) */
     int32_t morton_bits;  /* Morton bits of the sort key below the tree bits */
+    unsigned int* error_word; /* device: error bits of the batch-wide stages (the first tree's word) */
 } ct_forest_plan;
 size_t ct_forest_locate_workspace_size(int64_t n_points, int32_t n_trees);
 int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double* tolerances,

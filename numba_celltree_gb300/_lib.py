@@ -67,7 +67,8 @@ class CtTree(ctypes.Structure):
         ("abs_eps", ctypes.c_float),
         ("error_word", _P),
         ("grid_start", _P),
-        ("grid_n", _I32),
+        ("grid_nx", _I32),
+        ("grid_ny", _I32),
         ("grid_x0", ctypes.c_float),
         ("grid_y0", ctypes.c_float),
         ("grid_sx", ctypes.c_float),
@@ -91,6 +92,7 @@ class CtForestPlan(ctypes.Structure):
         ("kt", _I32),
         ("stack", _I32),
         ("morton_bits", _I32),
+        ("error_word", _P),
     ]
 
 
@@ -105,7 +107,7 @@ SIGNATURES = {
     "ct_bbox_summary": (ctypes.c_int, [_P, _I64, _P, ctypes.POINTER(_D), _P]),
     "ct_vertex_extent": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_D), _P]),
     "ct_pessimistic_n_nodes": (_I64, [_I64]),
-    "ct_grid_resolution": (_I32, [_I64]),
+    "ct_grid_shape": (ctypes.c_int, [_I64, _D, _D, _D, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
     "ct_build_forest_workspace_size": (_SZ, [_I64, _I32, _I32, _I32]),
     "ct_build_forest": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), _I32, _I32, _I64, _I32, _P, _SZ,
                                        ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P]),

@@ -30,6 +30,8 @@ class _GpuTree:
     # query tolerances up to this multiple of the default one use the
     # candidate lists (widening 2 * 1e-6 of the largest cell diagonal)
     CAND_TOL_FACTOR = 1.0e6
+    # grid cells (start-node grid and candidate lists) per mesh cell
+    GRID_CELLS_PER_ELEMENT = 1.0
 
     def __init__(self, device, elements, vertices, bb_coords, n_buckets: int, cells_per_leaf: int,
                  candidate_lists: bool = True, prebuilt=None):
@@ -66,15 +68,20 @@ class _GpuTree:
         self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
         self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
         self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
-        gn = int(lib.ct_grid_resolution(n))
-        self.grid_start = _device.empty((gn * gn,), torch.int32, device)
+        self.grid_start = None
         self.desc = _lib.CtTree()
         self._fill_desc()
-        self.desc.grid_n = gn
         _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
+        bb = self.desc.bbox
+        gx, gy = ctypes.c_int32(0), ctypes.c_int32(0)
+        _lib.check(lib.ct_grid_shape(n, bb[1] - bb[0], bb[3] - bb[2], self.GRID_CELLS_PER_ELEMENT,
+                                     ctypes.byref(gx), ctypes.byref(gy)), "grid shape")
+        self.grid_start = _device.empty((gx.value * gy.value,), torch.int32, device)
+        self.desc.grid_start = _device.ptr(self.grid_start)
+        self.desc.grid_nx, self.desc.grid_ny = gx.value, gy.value
         _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
         self.cand_off = self.cand_box = self.cand_idx = self.cand_lbox = None
-        if candidate_lists and int(self.desc.grid_n) > 0 and n > 0:
+        if candidate_lists and int(self.desc.grid_nx) > 0 and n > 0:
             self._build_candidate_lists(lib, st)
 
     def _build(self, lib, st, device, bb_coords, n, n_buckets, cells_per_leaf) -> int:
@@ -122,8 +129,8 @@ class _GpuTree:
         """Per-grid-cell candidate lists of the batched float32 locate."""
         torch = _device.torch()
         d = self.desc
-        gn = int(d.grid_n)
-        self.cand_off = _device.empty((gn * gn + 1,), torch.int64, self.device)
+        cells = int(d.grid_nx) * int(d.grid_ny)
+        self.cand_off = _device.empty((cells + 1,), torch.int64, self.device)
         self.cand_box = _device.empty((self.n, 4), torch.float32, self.device)
         d.cand_off = _device.ptr(self.cand_off)
         d.cand_box = _device.ptr(self.cand_box)
@@ -143,6 +150,7 @@ class _GpuTree:
         d.cand_idx = _device.ptr(self.cand_idx)
         d.cand_lbox = _device.ptr(self.cand_lbox)
         _lib.check(lib.ct_cand_fill(ctypes.byref(d), _device.ptr(scratch), nbytes, st), "candidate lists")
+        self.raise_on_device_error()  # the filling pass never writes past a grid cell's count
 
     def _fill_desc(self):
         d = self.desc
@@ -171,7 +179,7 @@ class _GpuTree:
         d.poly_len = P(self.poly_len)
         d.poly_len32 = P(self.poly_len32)
         d.error_word = P(self.error_word)
-        d.grid_start = P(self.grid_start)
+        d.grid_start = P(self.grid_start) if self.grid_start is not None else None
 
     def reset_error(self):
         self.error_word.zero_()

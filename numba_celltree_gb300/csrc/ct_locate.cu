@@ -66,7 +66,7 @@ struct TreeL {
     int S4;     // float4 units per cell in polyf
     int stack;  // stack entries per thread (>= max_depth + 2)
     const int* gstart;  // start-node grid (null: start at the root)
-    int gn;
+    int gnx, gny;
     float gx0, gy0, gsx, gsy;
     const int64_t* coff;  // candidate lists (null: off)
     const int* cidx;
@@ -275,8 +275,8 @@ __global__ void __launch_bounds__(LOC_THREADS)
             if (T.gstart) {
                 // grid cell of the point; outside the grid (or NaN): the root
                 float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
-                float gn = (float)T.gn;
-                if (fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) v = T.gstart[(int)fy * T.gn + (int)fx];
+                if (fx >= 0.0f && fx < (float)T.gnx && fy >= 0.0f && fy < (float)T.gny)
+                    v = T.gstart[(int64_t)(int)fy * T.gnx + (int)fx];
             }
             // at most n_nodes visits; v = -1: the root path ends without a child
             int budget = (v < 0) ? 0 : (int)min(T.n_nodes, (int64_t)INT32_MAX - 1) + 1;
@@ -353,15 +353,19 @@ __global__ void __launch_bounds__(LOC_THREADS)
     }
 }
 
+constexpr int RES_OPEN = INT32_MIN;  // sorted-order result of a query left open
+
 // Stage 2a: candidate lists.  Per query the cells listed for its grid cell:
 // a float32 bbox reject, then the float32 leaf filter.  Exactly one sure hit
 // with sure misses elsewhere, or sure misses only, is final; otherwise the
-// query's sorted position goes to the list of stage 2b.
+// query's sorted position goes to the list of stage 2b.  With `res_sorted`
+// the results go there by sorted position (RES_OPEN for open queries; a
+// bucketed scatter takes them to `out`), else straight to out[oi].
 template <int KT, bool MULTI>
 __global__ void __launch_bounds__(LOC_THREADS)
     k_cells(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
             const double2* __restrict__ pts, const int* __restrict__ order, int64_t n, int64_t* __restrict__ out,
-            int* __restrict__ qlist, int* __restrict__ qcount) {
+            int* __restrict__ res_sorted, int* __restrict__ qlist, int* __restrict__ qcount) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = i < n;
     bool open = false;
@@ -374,9 +378,8 @@ __global__ void __launch_bounds__(LOC_THREADS)
         to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
         to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
         float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
-        float gn = (float)T.gn;
-        if (T.coff && fx >= 0.0f && fx < gn && fy >= 0.0f && fy < gn) {
-            const int64_t g = (int64_t)(int)fy * T.gn + (int)fx;
+        if (T.coff && fx >= 0.0f && fx < (float)T.gnx && fy >= 0.0f && fy < (float)T.gny) {
+            const int64_t g = (int64_t)(int)fy * T.gnx + (int)fx;
             const int64_t s0 = T.coff[g], s1 = T.coff[g + 1];
             // the point's float32 interval
             const float xl = __fsub_rd(px, dpx), xh = __fadd_ru(px, dpx);
@@ -413,10 +416,15 @@ __global__ void __launch_bounds__(LOC_THREADS)
                     }
                 }
             }
-            if (!open) out[oi] = hits ? T.bbi[hit] : -1;
+            if (!open) {
+                const int r = hits ? (int)T.bbi[hit] : -1;
+                if (res_sorted) res_sorted[i] = r;
+                else out[oi] = r;
+            }
         } else {
             open = true;
         }
+        if (open && res_sorted) res_sorted[i] = RES_OPEN;
     }
     // warp-aggregated append of the open queries
     unsigned m = __ballot_sync(0xffffffffu, open);
@@ -426,6 +434,89 @@ __global__ void __launch_bounds__(LOC_THREADS)
         if (lane == leader) b0 = atomicAdd(qcount, __popc(m));
         b0 = __shfl_sync(0xffffffffu, b0, leader);
         if (open) qlist[b0 + __popc(m & lane_lt())] = (int)i;
+    }
+}
+
+// Results by sorted position -> out[order[i]], in two passes so that the
+// random 8-byte writes land in an L2-sized window at a time and leave the
+// cache as whole sectors: (1) regroup the (query, result) pairs by the
+// bucket (query >> shift) of their destination -- at most 256 buckets,
+// bucket d owning the range [d << shift, (d + 1) << shift) of the pair
+// arrays, filled through a per-bucket cursor; (2) walk the pair arrays in
+// order and write every result that is not RES_OPEN.  `order` is a
+// permutation of 0 .. n-1, so bucket d receives exactly the queries of its
+// range; a pair that would fall outside it is dropped with an error bit.
+constexpr int RB_T = 256, RB_IPT = 16, RB_TILE = RB_T * RB_IPT;
+
+__global__ void __launch_bounds__(RB_T)
+    k_res_bucket(const int* __restrict__ res_sorted, const int* __restrict__ order, int64_t n, int shift,
+                 unsigned long long* __restrict__ cursor, int* __restrict__ pq, int* __restrict__ pr,
+                 unsigned int* __restrict__ err) {
+    __shared__ int cnt[256];
+    __shared__ int tbase[256];
+    __shared__ int wsum[RB_T / 32];
+    __shared__ long long gbase[256];
+    __shared__ int sq[RB_TILE];
+    __shared__ int sr[RB_TILE];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t base = (int64_t)blockIdx.x * RB_TILE;
+    cnt[t] = 0;
+    __syncthreads();
+    int q[RB_IPT], r[RB_IPT], rk[RB_IPT];
+#pragma unroll
+    for (int k = 0; k < RB_IPT; k++) {
+        const int64_t i = base + k * RB_T + t;
+        const bool v = i < n;
+        q[k] = v ? order[i] : -1;
+        r[k] = v ? res_sorted[i] : 0;
+    }
+#pragma unroll
+    for (int k = 0; k < RB_IPT; k++) rk[k] = (q[k] >= 0) ? atomicAdd(&cnt[(q[k] >> shift) & 255], 1) : 0;
+    __syncthreads();
+    const int c = cnt[t];
+    int x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    int pre = 0;
+    for (int ww = 0; ww < w; ww++) pre += wsum[ww];
+    tbase[t] = pre + x - c;
+    gbase[t] = c ? (long long)atomicAdd(&cursor[t], (unsigned long long)c) : 0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RB_IPT; k++)
+        if (q[k] >= 0) {
+            const int pos = tbase[(q[k] >> shift) & 255] + rk[k];
+            sq[pos] = q[k];
+            sr[pos] = r[k];
+        }
+    __syncthreads();
+    const int m = (int)min((int64_t)RB_TILE, n - base);
+    for (int j = t; j < m; j += RB_T) {
+        const int qq = sq[j];
+        const int d = (qq >> shift) & 255;
+        const int64_t lo = (int64_t)d << shift, hi = min(n, (int64_t)(d + 1) << shift);
+        const int64_t dst = lo + gbase[d] + (j - tbase[d]);
+        if (dst >= hi) {
+            set_error(err, CT_DEVERR_CAPACITY);
+            continue;
+        }
+        pq[dst] = qq;
+        pr[dst] = sr[j];
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    k_res_unbucket(const int* __restrict__ pq, const int* __restrict__ pr, int64_t n, int64_t* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {
+        const int r = pr[t];
+        const int q = pq[t];
+        if (r != RES_OPEN && q >= 0 && q < n) out[q] = r;
     }
 }
 
@@ -720,11 +811,11 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
 // cell (its range widened by `m`) takes one and the same single child.  The
 // float32 node bounds are within `band` of the float64 bounds, so a decision
 // is certain when the cell range clears bound -/+ band (directed rounding).
-__global__ void k_grid_start(const float4* __restrict__ nf, int gn, float x0, float y0, float sx, float sy, double m,
-                             float band, int max_steps, int* __restrict__ start) {
-    int64_t total = (int64_t)gn * gn;
+__global__ void k_grid_start(const float4* __restrict__ nf, int gnx, int gny, float x0, float y0, float sx, float sy,
+                             double m, float band, int max_steps, int* __restrict__ start) {
+    int64_t total = (int64_t)gnx * gny;
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
-        int gx = (int)(c % gn), gy = (int)(c / gn);
+        int gx = (int)(c % gnx), gy = (int)(c / gnx);
         float xlo = __double2float_rd((double)x0 + (double)gx / (double)sx - m);
         float xhi = __double2float_ru((double)x0 + (double)(gx + 1) / (double)sx + m);
         float ylo = __double2float_rd((double)y0 + (double)gy / (double)sy - m);
@@ -767,35 +858,266 @@ __global__ void k_cand_box(const double* __restrict__ bb, const int64_t* __restr
 
 // Grid cells met by a widened box: cell gx spans [x0 + gx / sx, x0 + (gx + 1) / sx]
 // widened by m.
-__device__ __forceinline__ bool cand_range(float4 b, int gn, double x0, double y0, double sx, double sy, double m,
-                                           int* gx0, int* gx1, int* gy0, int* gy1) {
+__device__ __forceinline__ bool cand_range(float4 b, int gnx, int gny, double x0, double y0, double sx, double sy,
+                                           double m, int* gx0, int* gx1, int* gy0, int* gy1) {
     double ax = ((double)b.x - m - x0) * sx, bx = ((double)b.y + m - x0) * sx;
     double ay = ((double)b.z - m - y0) * sy, by = ((double)b.w + m - y0) * sy;
-    if (!(bx >= 0.0 && ax < (double)gn && by >= 0.0 && ay < (double)gn)) return false;  // also NaN
+    if (!(bx >= 0.0 && ax < (double)gnx && by >= 0.0 && ay < (double)gny)) return false;  // also NaN
     *gx0 = (int)fmax(floor(ax - 1e-9), 0.0);
-    *gx1 = (int)fmin(floor(bx + 1e-9), (double)(gn - 1));
+    *gx1 = (int)fmin(floor(bx + 1e-9), (double)(gnx - 1));
     *gy0 = (int)fmax(floor(ay - 1e-9), 0.0);
-    *gy1 = (int)fmin(floor(by + 1e-9), (double)(gn - 1));
+    *gy1 = (int)fmin(floor(by + 1e-9), (double)(gny - 1));
     return true;
 }
 
-template <bool FILL>
-__global__ void k_cand_lists(const float4* __restrict__ box, int64_t n, int gn, double x0, double y0, double sx,
-                             double sy, double m, unsigned long long* __restrict__ count,
-                             const int64_t* __restrict__ off, int* __restrict__ idx, float4* __restrict__ lbox) {
+// Box of polygon L (len vertices, float32, frame of the grid cell) clipped
+// to the rectangle [X0, X1] x [Y0, Y1], enlarged by the rounding of this
+// float32 computation (callers add a slack much larger than it): the union of
+// the edges' pieces inside the rectangle (Liang-Barsky, the parameter range
+// widened by its rounding bound, so a piece is never cut short) and of the
+// rectangle corners the crossing-parity test does not certainly place outside
+// (each edge's cross product with the corner beyond its error bound -- the
+// parity is then that of the exact polygon).  Extreme points of the
+// polygon's inside (crossing-parity) region within the rectangle lie on such
+// pieces or corners.  False when the box is empty.
+// S bounds every |coordinate|; each vertex of L is within u S + ea of the
+// exact vertex (float32 and float64 rounding).
+template <int KMAX>
+__device__ bool clip_box(const float2* L, int len, float X0, float X1, float Y0, float Y1, float S, float ea,
+                         float4* out) {
+    const float u = 5.9604644775390625e-08f;
+    float bx0 = FLT_MAX, bx1 = -FLT_MAX, by0 = FLT_MAX, by1 = -FLT_MAX;
+    for (int k = 0; k < len; k++) {
+        const float2 P = L[k], Q = L[(k + 1 == len) ? 0 : k + 1];
+        const float dx = Q.x - P.x, dy = Q.y - P.y;
+        float t0 = 0.0f, t1 = 1.0f;
+        bool ok = true;
+        if (dx == 0.0f) {
+            ok = P.x >= X0 && P.x <= X1;
+        } else {
+            float ta = (X0 - P.x) / dx, tb = (X1 - P.x) / dx;
+            float e = 4.0f * u * (fabsf(ta) + fabsf(tb));
+            t0 = fmaxf(t0, fminf(ta, tb) - e);
+            t1 = fminf(t1, fmaxf(ta, tb) + e);
+        }
+        if (dy == 0.0f) {
+            ok = ok && P.y >= Y0 && P.y <= Y1;
+        } else {
+            float ta = (Y0 - P.y) / dy, tb = (Y1 - P.y) / dy;
+            float e = 4.0f * u * (fabsf(ta) + fabsf(tb));
+            t0 = fmaxf(t0, fminf(ta, tb) - e);
+            t1 = fminf(t1, fmaxf(ta, tb) + e);
+        }
+        if (!ok || !(t0 <= t1)) continue;
+        const float ex0 = P.x + t0 * dx, ex1 = P.x + t1 * dx;
+        const float ey0 = P.y + t0 * dy, ey1 = P.y + t1 * dy;
+        bx0 = fminf(bx0, fminf(ex0, ex1));
+        bx1 = fmaxf(bx1, fmaxf(ex0, ex1));
+        by0 = fminf(by0, fminf(ey0, ey1));
+        by1 = fmaxf(by1, fmaxf(ey0, ey1));
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const float cx = (c & 1) ? X1 : X0, cy = (c & 2) ? Y1 : Y0;
+        int parity = 0;
+        bool unsure = false;
+        float2 U = make_float2(L[len - 1].x - cx, L[len - 1].y - cy);
+        for (int k = 0; k < len; k++) {
+            const float2 V = make_float2(L[k].x - cx, L[k].y - cy);
+            if (V.x == U.x && V.y == U.y) continue;  // repeated vertex: no edge (geometry_utils.py:203-204)
+            const float A = U.x * V.y - U.y * V.x;
+            const float m = fmaxf(fmaxf(fabsf(U.x), fabsf(U.y)), fmaxf(fabsf(V.x), fabsf(V.y)));
+            // rounding of U, V and A, and the rounding of the vertices
+            // themselves (below u S + ea each)
+            const float thr = 16.0f * u * m * m + 8.0f * (u * S + ea) * m + 1e-30f;
+            unsure |= !(fabsf(A) > thr);
+            if ((U.y > 0.0f) != (V.y > 0.0f)) parity ^= (int)((V.y > U.y) ? (A > 0.0f) : (A < 0.0f));
+            U = V;
+        }
+        if (unsure || parity) {
+            bx0 = fminf(bx0, cx);
+            bx1 = fmaxf(bx1, cx);
+            by0 = fminf(by0, cy);
+            by1 = fmaxf(by1, cy);
+        }
+    }
+    *out = make_float4(bx0, bx1, by0, by1);
+    return bx0 <= bx1 && by0 <= by1;
+}
+
+// Box of a surely counter-clockwise triangle V clipped to [X0, X1] x [Y0, Y1]
+// (same contract as clip_box, registers only): edge k runs from V[k] with
+// direction D[k] (reciprocals rx, ry; 0 where the component is 0) and
+// constant cc[k] = V[k] x V[k + 1], so that the cross product of
+// (V[k] - C, V[k + 1] - C) is cc[k] - C x D[k].  A corner is left out only
+// when one edge puts it surely on its outer side (the triangle is convex).
+// Lm, Dm: largest |component| of the vertices and of the edges; each vertex
+// is within d = u Lm + ea of the exact one.
+__device__ __forceinline__ bool tri_box(const float2 (&V)[3], const float2 (&D)[3], const float (&rx)[3],
+                                        const float (&ry)[3], const float (&cc)[3], float Lm, float Dm, float d,
+                                        float X0, float X1, float Y0, float Y1, float4* out) {
+    const float u = 5.9604644775390625e-08f;
+    float bx0 = FLT_MAX, bx1 = -FLT_MAX, by0 = FLT_MAX, by1 = -FLT_MAX;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float2 P = V[k];
+        float t0 = 0.0f, t1 = 1.0f;
+        bool ok = true;
+        if (D[k].x == 0.0f) {
+            ok = P.x >= X0 && P.x <= X1;
+        } else {
+            // the reciprocal, the differences and the products are each
+            // rounded once: 8 u of the parameter covers them
+            const float ta = (X0 - P.x) * rx[k], tb = (X1 - P.x) * rx[k];
+            const float e = 8.0f * u * (fabsf(ta) + fabsf(tb));
+            t0 = fmaxf(t0, fminf(ta, tb) - e);
+            t1 = fminf(t1, fmaxf(ta, tb) + e);
+        }
+        if (D[k].y == 0.0f) {
+            ok = ok && P.y >= Y0 && P.y <= Y1;
+        } else {
+            const float ta = (Y0 - P.y) * ry[k], tb = (Y1 - P.y) * ry[k];
+            const float e = 8.0f * u * (fabsf(ta) + fabsf(tb));
+            t0 = fmaxf(t0, fminf(ta, tb) - e);
+            t1 = fminf(t1, fmaxf(ta, tb) + e);
+        }
+        if (ok && t0 <= t1) {
+            const float ex0 = P.x + t0 * D[k].x, ex1 = P.x + t1 * D[k].x;
+            const float ey0 = P.y + t0 * D[k].y, ey1 = P.y + t1 * D[k].y;
+            bx0 = fminf(bx0, fminf(ex0, ex1));
+            bx1 = fmaxf(bx1, fmaxf(ex0, ex1));
+            by0 = fminf(by0, fminf(ey0, ey1));
+            by1 = fmaxf(by1, fmaxf(ey0, ey1));
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const float cx = (c & 1) ? X1 : X0, cy = (c & 2) ? Y1 : Y0;
+        const float c1 = fabsf(cx) + fabsf(cy);
+        // rounding of cc, D, the products and the difference; then the
+        // vertices' own rounding (d each)
+        const float thr = 8.0f * u * (Lm * Lm + c1 * Dm) + 8.0f * d * (2.0f * c1 + 2.0f * Lm) + 1e-30f;
+        bool outside = false;
+#pragma unroll
+        for (int k = 0; k < 3; k++) outside |= (cc[k] - (cx * D[k].y - cy * D[k].x)) < -thr;
+        if (!outside) {
+            bx0 = fminf(bx0, cx);
+            bx1 = fmaxf(bx1, cx);
+            by0 = fminf(by0, cy);
+            by1 = fmaxf(by1, cy);
+        }
+    }
+    *out = make_float4(bx0, bx1, by0, by1);
+    return bx0 <= bx1 && by0 <= by1;
+}
+
+// Per cell (leaf order j) and grid cell g of its widened bbox's range: the
+// part of the cell within g widened by e2 = m + M (cell-assignment margin
+// plus the predicate's reach), its box widened by M and by the float32
+// slack, intersected with the cell's widened bbox.  Counted (FILL = false)
+// or written to g's list (FILL = true); both passes take the same decisions.
+// The vertices are taken once per cell, in float32 relative to the cell's
+// first vertex (the anchor, float64); a grid cell's rectangle is placed
+// relative to the anchor in float32 with an error far below the slack.
+// Triangles that are surely counter-clockwise take tri_box; other cells
+// clip_box; cells with fewer than 3 vertices, more than KMAX or non-finite
+// coordinates keep the widened bbox in every grid cell of its range.
+template <bool FILL, int KMAX>
+__global__ void k_cand_lists(const float4* __restrict__ box, const double2* __restrict__ poly,
+                             const uint8_t* __restrict__ plen, int K, int64_t n, double ox, double oy, int gnx,
+                             int gny, double x0, double y0, double sx, double sy, double m, float Mf, float e2f,
+                             float ea, unsigned long long* __restrict__ count, const int64_t* __restrict__ off,
+                             int* __restrict__ idx, float4* __restrict__ lbox, unsigned int* __restrict__ err) {
+    const float u = 5.9604644775390625e-08f;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
         int a0, a1, b0, b1;
         const float4 b = box[j];
-        if (!cand_range(b, gn, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) continue;
-        for (int gy = b0; gy <= b1; gy++)
+        if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) continue;
+        const int len = plen ? (int)plen[j] : K;
+        const double2* pv = poly + (size_t)j * K;
+        bool clip = len >= 3 && len <= KMAX;
+        for (int k = 0; k < len && clip; k++) clip = isfinite(pv[k].x) && isfinite(pv[k].y);
+        double ax = 0.0, ay = 0.0;
+        float2 L[KMAX];
+        float Lm = 0.0f;
+        if (clip) {
+            ax = pv[0].x - ox;
+            ay = pv[0].y - oy;
+            for (int k = 0; k < len; k++) {
+                L[k] = make_float2((float)((pv[k].x - ox) - ax), (float)((pv[k].y - oy) - ay));
+                Lm = fmaxf(Lm, fmaxf(fabsf(L[k].x), fabsf(L[k].y)));
+            }
+        }
+        const float d = u * Lm + ea;
+        // triangle fast path: edges, reciprocals, constants, orientation
+        float2 V[3], D[3];
+        float rx[3], ry[3], cc[3];
+        bool tri = clip && len == 3;
+        float Dm = 0.0f;
+        if (tri) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) V[k] = L[k];
+            float area2 = 0.0f, csum = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const float2 P = V[k], Q = V[(k + 1) % 3];
+                D[k] = make_float2(Q.x - P.x, Q.y - P.y);
+                rx[k] = (D[k].x != 0.0f) ? __frcp_rn(D[k].x) : 0.0f;
+                ry[k] = (D[k].y != 0.0f) ? __frcp_rn(D[k].y) : 0.0f;
+                cc[k] = P.x * Q.y - P.y * Q.x;
+                area2 += cc[k];
+                csum += fabsf(cc[k]);
+                Dm = fmaxf(Dm, fmaxf(fabsf(D[k].x), fabsf(D[k].y)));
+            }
+            // twice the signed area, beyond its rounding and the vertices' own
+            tri = area2 > 4.0f * u * csum + 32.0f * u * Lm * Lm + 16.0f * d * Lm;
+        }
+        const double cw = 1.0 / sx, ch = 1.0 / sy;
+        const float fcw = (float)cw, fch = (float)ch;
+        // lower-left corner of the range's first grid cell relative to the anchor
+        const float fbx0 = (float)((x0 + (double)a0 * cw) - ax), fby0 = (float)((y0 + (double)b0 * ch) - ay);
+        const float axf = (float)ax, ayf = (float)ay;
+        for (int gy = b0; gy <= b1; gy++) {
+            const float ry0 = fby0 + (float)(gy - b0) * fch;
             for (int gx = a0; gx <= a1; gx++) {
-                int64_t g = (int64_t)gy * gn + gx;
+                float4 r = b;
+                bool keep = true;
+                if (clip) {
+                    const float rx0 = fbx0 + (float)(gx - a0) * fcw;
+                    const float S = Lm + fabsf(rx0) + fabsf(ry0) + fcw + fch + 2.0f * e2f;
+                    // slack: far above every rounding of the rectangle's
+                    // placement, of the clip and of the vertices
+                    const float w = ldexpf(S, -14) + 4.0f * ea;
+                    const float X0 = rx0 - e2f - w, X1 = rx0 + fcw + e2f + w;
+                    const float Y0 = ry0 - e2f - w, Y1 = ry0 + fch + e2f + w;
+                    float4 c;
+                    keep = tri ? tri_box(V, D, rx, ry, cc, Lm, Dm, d, X0, X1, Y0, Y1, &c)
+                               : clip_box<KMAX>(L, len, X0, X1, Y0, Y1, S, ea, &c);
+                    if (keep) {
+                        // back to the frame: the anchor's float32 rounding,
+                        // then M and the slack; rounded outward
+                        const float px = Mf + 2.0f * w + 2.0f * u * (fabsf(axf) + fabsf(c.x) + fabsf(c.y)) + 1e-30f;
+                        const float py = Mf + 2.0f * w + 2.0f * u * (fabsf(ayf) + fabsf(c.z) + fabsf(c.w)) + 1e-30f;
+                        r.x = fmaxf(b.x, __fsub_rd(__fadd_rd(axf, c.x), px));
+                        r.y = fminf(b.y, __fadd_ru(__fadd_ru(axf, c.y), px));
+                        r.z = fmaxf(b.z, __fsub_rd(__fadd_rd(ayf, c.z), py));
+                        r.w = fminf(b.w, __fadd_ru(__fadd_ru(ayf, c.w), py));
+                    }
+                }
+                if (!keep) continue;
+                int64_t g = (int64_t)gy * gnx + gx;
                 unsigned long long k = atomicAdd(&count[g], 1ull);
                 if (FILL) {
-                    idx[off[g] + (int64_t)k] = (int)j;
-                    lbox[off[g] + (int64_t)k] = b;
+                    const int64_t e = off[g] + (int64_t)k;
+                    if (e >= off[g + 1]) {  // the counting pass decided otherwise: never write past g
+                        set_error(err, CT_DEVERR_CAPACITY);
+                        continue;
+                    }
+                    idx[e] = (int)j;
+                    lbox[e] = r;
                 }
             }
+        }
     }
 }
 
@@ -880,8 +1202,9 @@ static int fill_tree(const ct_tree* t, double tol, TreeL* T) {
         if (!(F >= 0.0) || !std::isfinite(F)) F = 0.0;
         T->bandG = (float)(F * 2.384185791015625e-07 * 1.0001) + 1e-30f;  // bounds are inside the bbox
     }
-    T->gstart = (t->grid_start && t->grid_n > 0) ? t->grid_start : nullptr;
-    T->gn = T->gstart ? t->grid_n : 0;
+    T->gstart = (t->grid_start && t->grid_nx > 0 && t->grid_ny > 0) ? t->grid_start : nullptr;
+    T->gnx = T->gstart ? t->grid_nx : 0;
+    T->gny = T->gstart ? t->grid_ny : 0;
     // candidate lists only when they cover this tolerance
     T->coff = (T->gstart && t->cand_off && t->cand_idx && t->cand_lbox && t->cand_tol > 0.0 && tol <= t->cand_tol)
                   ? t->cand_off
@@ -957,6 +1280,22 @@ static size_t carve_forest(void* ws, int64_t n, int n_trees, LocWS* L, ForestWS*
     return off;
 }
 
+// Results of the candidate-list stage, written by sorted position into the
+// sort's key buffer A (free once the permutation is in L.order), scattered to
+// out[order[i]] through the sort's key buffer B and index buffer B; the
+// bucket cursors reuse the radix histogram.  Needs a sorted workspace.
+static int* sorted_results(const LocWS& L) { return (int*)L.keyA; }
+
+static int scatter_results(const LocWS& L, int64_t n, unsigned int* err, int64_t* out, cudaStream_t st) {
+    int shift = 0;
+    while (((n - 1) >> shift) >= 256) shift++;
+    CT_CUDA(cudaMemsetAsync(L.hist, 0, 256 * sizeof(int64_t), st));
+    k_res_bucket<<<(unsigned)((n + RB_TILE - 1) / RB_TILE), RB_T, 0, st>>>(
+        sorted_results(L), L.order, n, shift, (unsigned long long*)L.hist, (int*)L.keyB, L.idxB, err);
+    k_res_unbucket<<<(unsigned)((n + 255) / 256), 256, 0, st>>>((const int*)L.keyB, L.idxB, n, out);
+    return CT_OK;
+}
+
 }  // namespace ctl
 
 using namespace ctl;
@@ -965,45 +1304,63 @@ extern "C" {
 
 int ct_poly32_stride(int32_t K) { return poly32_stride(K); }
 
-int32_t ct_grid_resolution(int64_t n_elements) {
-    int32_t g = 16;
-    while (g < 4096 && (int64_t)g * g < n_elements) g *= 2;
-    return g;
+int ct_grid_shape(int64_t n_elements, double width, double height, double cells_per_element, int32_t* nx,
+                  int32_t* ny) {
+    if (!nx || !ny) return ct_fail(CT_ERR_ARG, "null argument");
+    if (!(cells_per_element > 0.0) || !std::isfinite(cells_per_element))
+        return ct_fail(CT_ERR_ARG, "cells_per_element must be finite and > 0");
+    double target = std::min(std::max((double)std::max<int64_t>(n_elements, 0) * cells_per_element, 256.0),
+                             (double)(1 << 26));
+    double a = width / height;  // aspect; 1 for a degenerate bbox (the grid is then switched off)
+    if (!(a > 0.0) || !std::isfinite(a)) a = 1.0;
+    a = std::min(std::max(a, 1.0 / 4096.0), 4096.0);
+    int64_t gx = std::max<int64_t>(16, (int64_t)std::llround(std::sqrt(target * a)));
+    int64_t gy = std::max<int64_t>(16, (int64_t)std::llround(std::sqrt(target / a)));
+    gx = std::min<int64_t>(gx, 65536);
+    gy = std::min<int64_t>(gy, 65536);
+    while (gx * gy > ((int64_t)1 << 26)) {  // the minimum of 16 on one axis can push the product up
+        if (gx >= gy) gx = std::max<int64_t>(16, gx * 15 / 16);
+        else gy = std::max<int64_t>(16, gy * 15 / 16);
+    }
+    *nx = (int32_t)gx;
+    *ny = (int32_t)gy;
+    return CT_OK;
 }
 
 int ct_pack_grid(ct_tree* t, void* stream) {
     if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
-    if (!t->grid_start || t->grid_n <= 0) {
-        t->grid_n = 0;
+    if (!t->grid_start || t->grid_nx <= 0 || t->grid_ny <= 0) {
+        t->grid_nx = t->grid_ny = 0;
         return CT_OK;
     }
-    if (t->grid_n > 8192) return ct_fail(CT_ERR_ARG, "grid_n above 8192");
+    if (t->grid_nx > 65536 || t->grid_ny > 65536 || (int64_t)t->grid_nx * t->grid_ny > ((int64_t)1 << 28))
+        return ct_fail(CT_ERR_ARG, "grid too large");
     if (t->n_nodes <= 0 || !t->nodes_f32) return ct_fail(CT_ERR_ARG, "tree is not packed");
     double ex = t->bbox[1] - t->bbox[0], ey = t->bbox[3] - t->bbox[2];
     double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
                         std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
     if (!(ex > 0.0 && ey > 0.0) || !std::isfinite(ex) || !std::isfinite(ey) || !std::isfinite(F)) {
-        t->grid_n = 0;  // degenerate bbox: every query starts at the root
+        t->grid_nx = t->grid_ny = 0;  // degenerate bbox: every query starts at the root
         return CT_OK;
     }
-    const int gn = t->grid_n;
+    const int gnx = t->grid_nx, gny = t->grid_ny;
     t->grid_x0 = (float)(t->bbox[0] - t->origin[0]);
     t->grid_y0 = (float)(t->bbox[2] - t->origin[1]);
-    t->grid_sx = (float)(gn / ex);
-    t->grid_sy = (float)(gn / ey);
+    t->grid_sx = (float)(gnx / ex);
+    t->grid_sy = (float)(gny / ey);
     if (!(t->grid_sx > 0.0f && t->grid_sy > 0.0f && std::isfinite(t->grid_sx) && std::isfinite(t->grid_sy))) {
-        t->grid_n = 0;
+        t->grid_nx = t->grid_ny = 0;
         return CT_OK;
     }
     // margin over the cell of a point: float32 rounding of the point in the
     // frame and of (p - x0) * s is below 2^-21 (extent + F); 4x that
     double m = std::ldexp(std::max(ex, ey) + F, -19);
     float band = (float)(F * 2.384185791015625e-07 * 1.0001) + 1e-30f;
-    int64_t total = (int64_t)gn * gn;
+    int64_t total = (int64_t)gnx * gny;
     unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
-    k_grid_start<<<blocks, 256, 0, (cudaStream_t)stream>>>((const float4*)t->nodes_f32, gn, t->grid_x0, t->grid_y0,
-                                                          t->grid_sx, t->grid_sy, m, band, t->max_depth + 2,
-                                                          t->grid_start);
+    k_grid_start<<<blocks, 256, 0, (cudaStream_t)stream>>>((const float4*)t->nodes_f32, gnx, gny, t->grid_x0,
+                                                          t->grid_y0, t->grid_sx, t->grid_sy, m, band,
+                                                          t->max_depth + 2, t->grid_start);
     CT_CHECK_LAUNCH("pack grid");
     return CT_OK;
 }
@@ -1017,9 +1374,47 @@ static double grid_margin(const ct_tree* t) {
 }
 
 size_t ct_cand_scratch_size(const ct_tree* t) {
-    if (!t || t->grid_n <= 0) return 256;
-    int64_t cells = (int64_t)t->grid_n * t->grid_n;
+    if (!t || t->grid_nx <= 0 || t->grid_ny <= 0) return 256;
+    int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
     return a256(8 * (size_t)(cells + 1)) + a256(ct_scan_workspace_size(cells + 1)) + 256;
+}
+
+// widening of the region where a cell's predicate can be true: the on-edge
+// test reaches 2 tol beyond an edge's bbox; float64 rounding of the
+// coordinates (abs_eps each) moves the tests by a few ulp
+static double cand_reach(const ct_tree* t, double cover_tol) {
+    double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
+                        std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
+    return 2.0 * cover_tol * (1.0 + 1e-6) + 16.0 * (double)t->abs_eps + std::ldexp(F, -48);
+}
+
+// v rounded up to float32
+static float float_up(double v) {
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+// counting (fill = false) or filling pass of the candidate lists
+static void launch_cand_lists(const ct_tree* t, bool fill, double M, unsigned long long* count, cudaStream_t st) {
+    int64_t n = t->n_elements;
+    unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    const uint8_t* plen = (t->n_max_vert == 3) ? nullptr : t->poly_len;
+#define CT_CAND_LISTS(FILL, KMAX)                                                                                  \
+    k_cand_lists<FILL, KMAX><<<blocks, 256, 0, st>>>(                                                              \
+        (const float4*)t->cand_box, (const double2*)t->poly_f64, plen, t->n_max_vert, n, t->origin[0],             \
+        t->origin[1], t->grid_nx, t->grid_ny, t->grid_x0, t->grid_y0, t->grid_sx, t->grid_sy, grid_margin(t),     \
+        float_up(M), float_up(grid_margin(t) + M), (float)(4.0 * (double)t->abs_eps),                             \
+        count, FILL ? t->cand_off : nullptr, FILL ? t->cand_idx : nullptr, FILL ? (float4*)t->cand_lbox : nullptr, \
+        t->error_word)
+    if (t->n_max_vert <= 4) {
+        if (fill) CT_CAND_LISTS(true, 4);
+        else CT_CAND_LISTS(false, 4);
+    } else {
+        if (fill) CT_CAND_LISTS(true, 32);
+        else CT_CAND_LISTS(false, 32);
+    }
+#undef CT_CAND_LISTS
 }
 
 int ct_cand_count(ct_tree* t, double cover_tol, void* scratch, size_t scratch_bytes, int64_t* total_host,
@@ -1029,28 +1424,22 @@ int ct_cand_count(ct_tree* t, double cover_tol, void* scratch, size_t scratch_by
     *total_host = 0;
     t->cand_n = 0;
     t->cand_tol = 0.0;
-    if (t->grid_n <= 0 || !t->grid_start) return CT_OK;  // no grid: lists off
+    if (t->grid_nx <= 0 || t->grid_ny <= 0 || !t->grid_start) return CT_OK;  // no grid: lists off
     if (!t->cand_off || !t->cand_box) return ct_fail(CT_ERR_ARG, "cand_off / cand_box not set");
+    if (!t->poly_f64) return ct_fail(CT_ERR_ARG, "tree is not packed");
     if (!(cover_tol >= 0.0) || !std::isfinite(cover_tol)) return ct_fail(CT_ERR_ARG, "cover_tol must be finite and >= 0");
     if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
-    const int gn = t->grid_n;
-    const int64_t cells = (int64_t)gn * gn;
+    const int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
     unsigned long long* count = (unsigned long long*)scratch;  // cells + 1 entries, the last stays 0
     void* scan_ws = (char*)scratch + a256(8 * (size_t)(cells + 1));
     size_t scan_bytes = scratch_bytes - a256(8 * (size_t)(cells + 1));
-    // widening: the on-edge test reaches 2 tol beyond an edge's bbox; float64
-    // rounding of the coordinates (abs_eps each) moves the tests by a few ulp
-    double F = std::max(std::max(t->bbox[1] - t->origin[0], t->origin[0] - t->bbox[0]),
-                        std::max(t->bbox[3] - t->origin[1], t->origin[1] - t->bbox[2]));
-    double M = 2.0 * cover_tol * (1.0 + 1e-6) + 16.0 * (double)t->abs_eps + std::ldexp(F, -48);
+    const double M = cand_reach(t, cover_tol);
     int64_t n = t->n_elements;
     unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
     k_cand_box<<<blocks, 256, 0, st>>>(t->bb_coords, t->bb_indices, n, t->origin[0], t->origin[1], M,
                                        (float4*)t->cand_box);
     CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)(cells + 1), st));
-    double m = grid_margin(t);
-    k_cand_lists<false><<<blocks, 256, 0, st>>>((const float4*)t->cand_box, n, gn, t->grid_x0, t->grid_y0,
-                                                t->grid_sx, t->grid_sy, m, count, nullptr, nullptr, nullptr);
+    launch_cand_lists(t, false, M, count, st);
     CT_CHECK_LAUNCH("candidate counts");
     int64_t total = 0;
     int s = ct_exclusive_scan((const int64_t*)count, cells + 1, t->cand_off, scan_ws, scan_bytes, &total, stream);
@@ -1065,18 +1454,14 @@ int ct_cand_count(ct_tree* t, double cover_tol, void* scratch, size_t scratch_by
 int ct_cand_fill(ct_tree* t, void* scratch, size_t scratch_bytes, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
-    if (t->cand_tol <= 0.0 || t->grid_n <= 0) return CT_OK;
+    if (t->cand_tol <= 0.0 || t->grid_nx <= 0 || t->grid_ny <= 0) return CT_OK;
     if ((!t->cand_idx || !t->cand_lbox) && t->cand_n > 0) return ct_fail(CT_ERR_ARG, "cand_idx / cand_lbox not set");
     if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
-    const int gn = t->grid_n;
-    const int64_t cells = (int64_t)gn * gn;
+    const int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
     unsigned long long* count = (unsigned long long*)scratch;
     CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)cells, st));
-    int64_t n = t->n_elements;
-    unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
-    k_cand_lists<true><<<blocks, 256, 0, st>>>((const float4*)t->cand_box, n, gn, t->grid_x0, t->grid_y0,
-                                               t->grid_sx, t->grid_sy, grid_margin(t), count, t->cand_off,
-                                               t->cand_idx, (float4*)t->cand_lbox);
+    const double cover = (t->cand_tol == 1e-300) ? 0.0 : t->cand_tol;  // the count's cover_tol
+    launch_cand_lists(t, true, cand_reach(t, cover), count, st);
     CT_CHECK_LAUNCH("candidate lists");
     return CT_OK;
 }
@@ -1145,10 +1530,12 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     const int* qlist = lists ? L.open : nullptr;
     const int* qcount = lists ? &L.counters[3] : nullptr;
     unsigned grid_b = lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16) : grid;
+    // sorted queries: list results by sorted position, then one bucketed scatter
+    int* res_sorted = (lists && ord) ? sorted_results(L) : nullptr;
 #define CT_FAST_STAGES(KT)                                                                                        \
     if (lists)                                                                                                     \
-        k_cells<KT, false><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, L.open,              \
-                                                         &L.counters[3]);                                          \
+        k_cells<KT, false><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,          \
+                                                         L.open, &L.counters[3]);                                  \
     smem_attr<KT, false>(smem);                                                                                    \
     k_fast<KT, false><<<grid_b, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, ord, n, out, L.R, L.counters,    \
                                                          L.ovf, qlist, qcount);
@@ -1160,6 +1547,7 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
         CT_FAST_STAGES(32)
     }
 #undef CT_FAST_STAGES
+    if (res_sorted) scatter_results(L, n, T.err, out, st);
     CT_CHECK_LAUNCH("locate fast");
     return CT_OK;
 }
@@ -1250,6 +1638,7 @@ int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double
     plan->kt = (kmax <= 3) ? 3 : (kmax <= 4 ? 4 : 32);
     plan->stack = stack;
     plan->morton_bits = mbits;
+    plan->error_word = trees[0].error_word;
     CT_CUDA(cudaMemcpyAsync(F.trees, tl.data(), sizeof(TreeL) * tl.size(), cudaMemcpyHostToDevice, st));
     CT_CUDA(cudaMemcpyAsync(F.grids, gr.data(), sizeof(Grid) * gr.size(), cudaMemcpyHostToDevice, st));
     CT_CUDA(cudaMemcpyAsync(F.poff, point_off, sizeof(int64_t) * ((size_t)n_trees + 1), cudaMemcpyHostToDevice, st));
@@ -1305,8 +1694,8 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
     unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
     unsigned grid_b = (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16);
 #define CT_FOREST_STAGES(KT)                                                                                      \
-    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.open,            \
-                                                    &L.counters[3]);                                             \
+    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out,                    \
+                                                    sorted_results(L), L.open, &L.counters[3]);                  \
     k_fast<KT, true><<<grid_b, LOC_THREADS, smem, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.R,          \
                                                         L.counters, L.ovf, L.open, &L.counters[3]);              \
     k_pip<true><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.R, L.counters);                  \
@@ -1320,6 +1709,7 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
         CT_FOREST_STAGES(32)
     }
 #undef CT_FOREST_STAGES
+    scatter_results(L, n, plan->error_word, out, st);
     CT_CHECK_LAUNCH("forest locate");
     return CT_OK;
 }

@@ -161,13 +161,14 @@ def test_locate_start_grid_edges(oracle):
     g = CellTree2d(xy, f, -1)
     o = oracle.OracleCellTree2d(xy, f, -1)
     t = g._tree
-    gn = int(t.desc.grid_n)
-    assert gn == 128
+    gnx, gny = int(t.desc.grid_nx), int(t.desc.grid_ny)
+    # about one grid cell per mesh cell (14,400 triangles), nearly square
+    assert 13_000 < gnx * gny < 16_000 and abs(gnx - 2 * gny) <= 2
     starts = t.grid_start.cpu().numpy()
     assert (starts > 0).mean() > 0.5
     xmin, xmax, ymin, ymax = [float(v) for v in g.bbox]
-    gx = np.linspace(xmin, xmax, gn + 1)
-    gy = np.linspace(ymin, ymax, gn + 1)
+    gx = np.linspace(xmin, xmax, gnx + 1)
+    gy = np.linspace(ymin, ymax, gny + 1)
     rng = np.random.default_rng(9)
     line_pts = np.concatenate([
         np.stack([rng.choice(gx, 4000), rng.uniform(ymin, ymax, 4000)], 1),
@@ -196,8 +197,8 @@ def test_locate_start_grid_edges(oracle):
 
 @pytest.mark.gpu
 def test_locate_without_start_grid(oracle):
-    """grid_n = 0 (the state for a degenerate bbox): every query starts at the
-    root, same results."""
+    """grid_nx = grid_ny = 0 (the state for a degenerate bbox): every query
+    starts at the root, same results."""
     from numba_celltree_gb300 import CellTree2d
 
     xy, f = syn.quad_mesh(50, 30, seed=4)
@@ -206,7 +207,8 @@ def test_locate_without_start_grid(oracle):
     pts = np.concatenate([syn.uniform_points(20000, xy.min(0) - 0.5, xy.max(0) + 0.5, seed=1),
                           syn.near_edge_points(xy, f, 3000, dist=0.0, seed=2)])
     ref = o.locate_points(pts)
-    g._tree.desc.grid_n = 0
+    g._tree.desc.grid_nx = 0
+    g._tree.desc.grid_ny = 0
     for prec in ("fp32", "fp64"):
         g.precision = prec
         assert np.array_equal(g.locate_points(pts), ref), prec
