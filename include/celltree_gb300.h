@@ -279,6 +279,7 @@ typedef struct ct_forest_plan {
     int32_t stack;        /* traversal stack entries per query (deepest tree + 2) */
     int32_t morton_bits;  /* Morton bits of the sort key below the tree bits */
     unsigned int* error_word; /* device: error bits of the batch-wide stages (the first tree's word) */
+    int64_t max_tree_points;  /* most points of one tree */
 } ct_forest_plan;
 size_t ct_forest_locate_workspace_size(int64_t n_points, int32_t n_trees);
 int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double* tolerances,

@@ -93,6 +93,7 @@ class CtForestPlan(ctypes.Structure):
         ("stack", _I32),
         ("morton_bits", _I32),
         ("error_word", _P),
+        ("max_tree_points", _I64),
     ]
 
 

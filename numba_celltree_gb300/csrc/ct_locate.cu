@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(LOC_THREADS)
 // ---------------------------------------------------------------------------
 // query ordering: LSD radix sort of (Morton key, index) pairs
 // ---------------------------------------------------------------------------
-constexpr int RS_BLOCKS = 152 * 4;  // fixed grid (4 resident blocks per SM); each block owns a contiguous chunk
+constexpr int RS_BLOCKS = 152 * 8;  // fixed grid (8 blocks per SM); each block owns a contiguous chunk
 constexpr int RS_T = 256;
 constexpr int RS_IPT = 16;  // keys per thread per tile of the scatter
 constexpr int RS_TILE = RS_T * RS_IPT;
@@ -739,7 +739,8 @@ __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* __restrict__ k
 // atomic (so equal digits of one tile may be permuted -- the order of the
 // queries only has to be coherent, every result is written by the query's
 // own index), the tile is regrouped by digit in shared memory and written
-// out in runs.  A null `iin` stands for the indices 0 .. n-1.
+// out in runs.  A null `iin` stands for the indices 0 .. n-1; a null `kout`
+// (the last pass) writes the indices only.
 __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ iin,
                                                       int64_t n, int64_t chunk, int shift,
                                                       const int64_t* __restrict__ offs, unsigned* __restrict__ kout,
@@ -796,7 +797,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
             unsigned kk = sk[j];
             int dd = (int)((kk >> shift) & 255u);
             int dst = cur[dd] + (j - tbase[dd]);
-            kout[dst] = kk;
+            if (kout) kout[dst] = kk;
             iout[dst] = si[j];
         }
         __syncthreads();
@@ -1286,6 +1287,11 @@ static size_t carve_forest(void* ws, int64_t n, int n_trees, LocWS* L, ForestWS*
 // bucket cursors reuse the radix histogram.  Needs a sorted workspace.
 static int* sorted_results(const LocWS& L) { return (int*)L.keyA; }
 
+// The scatter pays off once one tree's queries span more output than L2
+// holds comfortably (2^23 int64 = 64 MB): below that, direct writes from
+// k_cells already land in a cache-resident window.
+constexpr int64_t RES_SCATTER_MIN = (int64_t)1 << 23;
+
 static int scatter_results(const LocWS& L, int64_t n, unsigned int* err, int64_t* out, cudaStream_t st) {
     int shift = 0;
     while (((n - 1) >> shift) >= 256) shift++;
@@ -1502,7 +1508,8 @@ int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sor
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist, kout, iout);
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist,
+                                                 pss + 1 < passes ? kout : nullptr, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1530,8 +1537,8 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     const int* qlist = lists ? L.open : nullptr;
     const int* qcount = lists ? &L.counters[3] : nullptr;
     unsigned grid_b = lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16) : grid;
-    // sorted queries: list results by sorted position, then one bucketed scatter
-    int* res_sorted = (lists && ord) ? sorted_results(L) : nullptr;
+    // many sorted queries: list results by sorted position, then one bucketed scatter
+    int* res_sorted = (lists && ord && n > RES_SCATTER_MIN) ? sorted_results(L) : nullptr;
 #define CT_FAST_STAGES(KT)                                                                                        \
     if (lists)                                                                                                     \
         k_cells<KT, false><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,          \
@@ -1639,6 +1646,9 @@ int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double
     plan->stack = stack;
     plan->morton_bits = mbits;
     plan->error_word = trees[0].error_word;
+    plan->max_tree_points = 0;
+    for (int32_t i = 0; i < n_trees; i++)
+        plan->max_tree_points = std::max<int64_t>(plan->max_tree_points, point_off[i + 1] - point_off[i]);
     CT_CUDA(cudaMemcpyAsync(F.trees, tl.data(), sizeof(TreeL) * tl.size(), cudaMemcpyHostToDevice, st));
     CT_CUDA(cudaMemcpyAsync(F.grids, gr.data(), sizeof(Grid) * gr.size(), cudaMemcpyHostToDevice, st));
     CT_CUDA(cudaMemcpyAsync(F.poff, point_off, sizeof(int64_t) * ((size_t)n_trees + 1), cudaMemcpyHostToDevice, st));
@@ -1683,7 +1693,8 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         int s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist, kout, iout);
+        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist,
+                                                 pss < 3 ? kout : nullptr, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1693,9 +1704,12 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
     size_t smem = (size_t)plan->stack * LOC_THREADS * sizeof(int);
     unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
     unsigned grid_b = (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16);
+    // queries are sorted by tree first: one tree's results land in its own
+    // range of `out`, so only a tree with many queries needs the scatter
+    int* res_sorted = plan->max_tree_points > RES_SCATTER_MIN ? sorted_results(L) : nullptr;
 #define CT_FOREST_STAGES(KT)                                                                                      \
-    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out,                    \
-                                                    sorted_results(L), L.open, &L.counters[3]);                  \
+    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, res_sorted,        \
+                                                    L.open, &L.counters[3]);                                     \
     k_fast<KT, true><<<grid_b, LOC_THREADS, smem, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.R,          \
                                                         L.counters, L.ovf, L.open, &L.counters[3]);              \
     k_pip<true><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.R, L.counters);                  \
@@ -1709,7 +1723,7 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
         CT_FOREST_STAGES(32)
     }
 #undef CT_FOREST_STAGES
-    scatter_results(L, n, plan->error_word, out, st);
+    if (res_sorted) scatter_results(L, n, plan->error_word, out, st);
     CT_CHECK_LAUNCH("forest locate");
     return CT_OK;
 }

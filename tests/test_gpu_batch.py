@@ -128,3 +128,38 @@ def test_forest_locate_odd_total(oracle):
     got = batch.locate_points(pts)
     for k, (xy, f) in enumerate(meshes):
         assert np.array_equal(got[k], oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])), k
+
+
+@pytest.mark.gpu
+def test_result_scatter_above_threshold(oracle):
+    """More than 2^23 queries on one tree take the sorted-result path with the
+    bucketed scatter (single tree and batch): identical to the float64 form
+    on every point and to the oracle on a sample; the batch's large mesh
+    gives the same indices as the mesh queried alone."""
+    import torch
+    from numba_celltree_gb300 import CellTree2d, CellTreeBatch
+
+    n = (1 << 23) + 12345
+    xy, f = syn.triangle_mesh(300, 200, seed=3, extent=(300.0, 200.0), offset=(2.5e5, 6.1e6))
+    lo, hi = xy.min(0), xy.max(0)
+    pts = np.concatenate([syn.uniform_points(n - 40000, lo - 1.0, hi + 1.0, seed=5),
+                          syn.near_edge_points(xy, f, 40000, dist=0.0, seed=6)])
+    p_d = torch.as_tensor(pts, device="cuda")
+    g = CellTree2d(xy, f, -1)
+    r32 = g.locate_points(p_d)
+    g.precision = "fp64"
+    r64 = g.locate_points(p_d)
+    assert torch.equal(r32, r64)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    sample = np.random.default_rng(7).integers(0, n, 200_000)
+    assert np.array_equal(r32.cpu().numpy()[sample], o.locate_points(pts[sample]))
+    # batch: the large mesh plus two small ones
+    small = _meshes()[:2]
+    meshes = [(xy, f)] + small
+    qs = [pts] + _points(small)
+    batch = CellTreeBatch(meshes)
+    res = batch.locate_points(qs)
+    assert np.array_equal(res[0], r32.cpu().numpy())
+    for k in (1, 2):
+        alone = CellTree2d(*meshes[k], -1)
+        assert np.array_equal(res[k], alone.locate_points(qs[k]))
