@@ -217,8 +217,9 @@ int ct_pack_grid(ct_tree* tree, void* stream);
  * coordinates of the cell.  For grid cell g (widened by the cell-assignment
  * margin m) the list holds every cell that meets g widened by m + M, each
  * with the box of that part of the cell widened by M (and by the rounding of
- * the float32 clipping that computes it): every cell whose predicate can be
- * true for a point of g, and a box that holds every such point.  A query
+ * the float32 clipping that computes it; cells of more than 4 vertices keep
+ * their widened bbox): every cell whose predicate can be true for a point of
+ * g, and a box that holds every such point.  A query
  * tests the boxes of its list and the float32 leaf filter of the cells whose
  * box holds it; one sure hit and sure misses elsewhere is locate_point's
  * answer (a sure hit is an interior point, inside the cell's bbox, so the

@@ -1020,9 +1020,11 @@ __device__ __forceinline__ bool tri_box(const float2 (&V)[3], const float2 (&D)[
 // The vertices are taken once per cell, in float32 relative to the cell's
 // first vertex (the anchor, float64); a grid cell's rectangle is placed
 // relative to the anchor in float32 with an error far below the slack.
-// Triangles that are surely counter-clockwise take tri_box; other cells
-// clip_box; cells with fewer than 3 vertices, more than KMAX or non-finite
-// coordinates keep the widened bbox in every grid cell of its range.
+// Triangles that are surely counter-clockwise take tri_box; other cells of
+// up to 4 vertices clip_box; cells with fewer than 3 vertices, more than 4
+// (clipping them cost more build time than it saved queries in measurements
+// on mixed meshes) or non-finite coordinates keep the widened bbox in every
+// grid cell of its range.
 template <bool FILL, int KMAX>
 __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __restrict__ poly,
                              const uint8_t* __restrict__ plen, int K, int64_t n, double ox, double oy, int gnx,
@@ -1036,7 +1038,7 @@ __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __re
         if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) continue;
         const int len = plen ? (int)plen[j] : K;
         const double2* pv = poly + (size_t)j * K;
-        bool clip = len >= 3 && len <= KMAX;
+        bool clip = KMAX <= 4 && len >= 3 && len <= KMAX;
         for (int k = 0; k < len && clip; k++) clip = isfinite(pv[k].x) && isfinite(pv[k].y);
         double ax = 0.0, ay = 0.0;
         float2 L[KMAX];

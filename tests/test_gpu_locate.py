@@ -288,3 +288,80 @@ def test_locate_sorted_batch_sizes_not_multiple_of_4(oracle, n):
     lo, hi = xy.min(0), xy.max(0)
     pts = syn.uniform_points(n, lo - 0.5 * (hi - lo), hi + 0.5 * (hi - lo), seed=n)
     assert np.array_equal(g.locate_points(pts), o.locate_points(pts))
+
+
+def _awkward_cells(kind, seed=21):
+    """A jittered mesh plus awkward cells on top of it: collinear cells,
+    repeated vertices, slivers 1e-7 m thin, cells much larger and much
+    smaller than a grid cell, and (quads) non-convex darts."""
+    rng = np.random.default_rng(seed)
+    off = np.array([3.1e5, 5.2e6])
+    if kind == "tri":
+        xy, f = syn.triangle_mesh(60, 40, seed=11, extent=(60.0, 40.0), offset=tuple(off))
+    else:
+        xy, f = syn.quad_mesh(60, 40, seed=11, extent=(60.0, 40.0), offset=tuple(off))
+    K = f.shape[1]
+    verts, faces = [xy], [f]
+    base = len(xy)
+
+    def add(polys):
+        nonlocal base
+        polys = np.asarray(polys, dtype=np.float64)  # (m, k, 2)
+        m, k = polys.shape[:2]
+        idx = base + np.arange(m * k).reshape(m, k)
+        row = np.full((m, K), -1, dtype=np.int64)
+        row[:, :k] = idx
+        verts.append(polys.reshape(-1, 2))
+        faces.append(row)
+        base += m * k
+
+    def pts(m, lo=(0.0, 0.0), hi=(60.0, 40.0)):
+        return off + rng.uniform(lo, hi, (m, 2))
+
+    p, d = pts(150), rng.normal(0.0, 1.0, (150, 2))
+    add(np.stack([p, p + d, p + 2.0 * d], 1))                  # collinear
+    a, b = pts(150), pts(150, (-1.0, -1.0), (1.0, 1.0)) - off
+    add(np.stack([a, a, a + b], 1))                           # repeated vertex
+    n_ = np.stack([-b[:, 1], b[:, 0]], 1) / np.linalg.norm(b, axis=1)[:, None]
+    add(np.stack([a, a + b, a + 0.5 * b + 1e-7 * n_], 1))     # sliver
+    c = pts(12, (10.0, 10.0), (50.0, 30.0))
+    add(np.stack([c, c + [25.0, 3.0], c + [-4.0, 18.0]], 1))  # large, over many grid cells
+    c = pts(150)
+    add(np.stack([c, c + [1e-3, 0.0], c + [0.0, 1e-3]], 1))   # tiny
+    if kind == "quad":
+        c = pts(150)
+        add(np.stack([c, c + [2.0, 0.0], c + [0.4, 0.4], c + [0.0, 2.0]], 1))  # non-convex darts
+        c = pts(100)
+        add(np.stack([c, c + [1.0, 0.2], c + [1.0, 0.2], c + [0.3, 1.1]], 1))  # repeated vertex
+    return np.concatenate(verts), np.concatenate(faces)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["tri", "quad"])
+def test_locate_clipped_lists_awkward_cells(oracle, kind):
+    """Candidate entries clipped to their grid cell: degenerate, thin, large,
+    tiny and non-convex cells over a regular mesh, queries on edges (at 0 and
+    1e-12 m), vertices and grid lines -- the batched float32 form gives the
+    oracle's indices."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = _awkward_cells(kind)
+    g = CellTree2d(xy, f, -1)
+    d = g._tree.desc
+    assert d.cand_tol > 0 and int(d.grid_nx) > 0
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    xmin, xmax, ymin, ymax = [float(v) for v in g.bbox]
+    rng = np.random.default_rng(3)
+    gx = xmin + (xmax - xmin) * np.arange(int(d.grid_nx) + 1) / int(d.grid_nx)
+    gy = ymin + (ymax - ymin) * np.arange(int(d.grid_ny) + 1) / int(d.grid_ny)
+    tri_rows = np.where((f[:, :3] >= 0).all(1))[0]
+    fe = f[tri_rows][:, :3]
+    pts = np.concatenate([
+        syn.uniform_points(120_000, (xmin - 1.0, ymin - 1.0), (xmax + 1.0, ymax + 1.0), seed=4),
+        syn.near_edge_points(xy, fe, 20_000, dist=0.0, seed=5),
+        syn.near_edge_points(xy, fe, 20_000, dist=1e-12, seed=6),
+        xy[rng.integers(0, len(xy), 5000)],
+        np.stack([rng.choice(gx, 5000), rng.uniform(ymin, ymax, 5000)], 1),
+        np.stack([rng.uniform(xmin, xmax, 5000), rng.choice(gy, 5000)], 1),
+    ])
+    assert np.array_equal(g.locate_points(pts), o.locate_points(pts))
