@@ -734,17 +734,44 @@ __global__ void __launch_bounds__(RS_T) k_rs_hist(const unsigned* __restrict__ k
     hist[(int64_t)t * gridDim.x + blockIdx.x] = c;
 }
 
+// The same for one-byte digits (written by the previous pass).
+__global__ void __launch_bounds__(RS_T) k_rs_hist8(const uint8_t* __restrict__ key, int64_t n, int64_t chunk,
+                                                    int64_t* __restrict__ hist) {
+    __shared__ int h[RS_T / 32][256];
+    const int t = threadIdx.x, w = t >> 5;
+    for (int k = 0; k < RS_T / 32; k++) h[k][t] = 0;
+    __syncthreads();
+    int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
+    int64_t ev = s + ((e - s) & ~(int64_t)15);  // end of the whole 16-byte groups
+    for (int64_t i = s + 16 * t; i < ev; i += 16 * RS_T) {
+        const uint4 k4 = *reinterpret_cast<const uint4*>(key + i);
+        const unsigned wd[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) atomicAdd(&h[w][(wd[q] >> (8 * b)) & 255u], 1);
+    }
+    for (int64_t i = ev + t; i < e; i += RS_T) atomicAdd(&h[w][key[i]], 1);
+    __syncthreads();
+    int c = 0;
+    for (int k = 0; k < RS_T / 32; k++) c += h[k][t];
+    hist[(int64_t)t * gridDim.x + blockIdx.x] = c;
+}
+
 // Scatter of one digit.  The block walks its chunk in tiles of RS_TILE
 // keys; a key's rank within its digit in the tile comes from a shared-memory
 // atomic (so equal digits of one tile may be permuted -- the order of the
 // queries only has to be coherent, every result is written by the query's
 // own index), the tile is regrouped by digit in shared memory and written
 // out in runs.  A null `iin` stands for the indices 0 .. n-1; a null `kout`
-// (the last pass) writes the indices only.
-__global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ iin,
+// (the last pass) writes the indices only.  Keys are read as KI and written
+// as KO after a right shift by `oshift`: a pass whose successor sorts the
+// last 8 bits writes just that byte.
+template <typename KI, typename KO>
+__global__ void __launch_bounds__(RS_T) k_rs_scatter(const KI* __restrict__ kin, const int* __restrict__ iin,
                                                       int64_t n, int64_t chunk, int shift,
-                                                      const int64_t* __restrict__ offs, unsigned* __restrict__ kout,
-                                                      int* __restrict__ iout) {
+                                                      const int64_t* __restrict__ offs, KO* __restrict__ kout,
+                                                      int oshift, int* __restrict__ iout) {
     __shared__ int cur[256];    // output position of the digit's next key
     __shared__ int cnt[256];    // digit counts of the tile
     __shared__ int tbase[256];  // exclusive scan of cnt
@@ -765,7 +792,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
         for (int k = 0; k < RS_IPT; k++) {
             int64_t i = base + k * RS_T + t;
             bool v = i < e;
-            key[k] = v ? kin[i] : 0u;
+            key[k] = v ? (unsigned)kin[i] : 0u;
             id[k] = v ? (iin ? iin[i] : (int)i) : -1;
         }
 #pragma unroll
@@ -797,7 +824,7 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const unsigned* __restrict_
             unsigned kk = sk[j];
             int dd = (int)((kk >> shift) & 255u);
             int dst = cur[dd] + (j - tbase[dd]);
-            if (kout) kout[dst] = kk;
+            if (kout) kout[dst] = (KO)(kk >> oshift);
             iout[dst] = si[j];
         }
         __syncthreads();
@@ -1504,14 +1531,26 @@ int ct_locate_bin(const ct_tree* t, const double* points, int64_t n, int32_t sor
     const int64_t nh = (int64_t)256 * RS_BLOCKS;
     for (int pss = 0; pss < passes; pss++) {
         int shift = 24 - sort_bits + 8 * pss;
+        // the pass before the last writes the last digit as one byte
+        const bool byte_in = pss > 0 && pss + 1 == passes, byte_out = pss + 2 == passes;
         if (pss == 0)
             k_keys<<<RS_BLOCKS, RS_T, 0, st>>>((const double2*)points, n, chunk, g, shift, kin, L.hist);
+        else if (byte_in)
+            k_rs_hist8<<<RS_BLOCKS, RS_T, 0, st>>>((const uint8_t*)kin, n, chunk, L.hist);
         else
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist,
-                                                 pss + 1 < passes ? kout : nullptr, iout);
+        const int* ii = pss ? iin : nullptr;
+        if (byte_in)  // last pass: indices only
+            k_rs_scatter<uint8_t, uint8_t><<<RS_BLOCKS, RS_T, 0, st>>>((const uint8_t*)kin, ii, n, chunk, 0, L.hist,
+                                                                       nullptr, 0, iout);
+        else if (byte_out)
+            k_rs_scatter<unsigned, uint8_t><<<RS_BLOCKS, RS_T, 0, st>>>(kin, ii, n, chunk, shift, L.hist,
+                                                                        (uint8_t*)kout, shift + 8, iout);
+        else
+            k_rs_scatter<unsigned, unsigned><<<RS_BLOCKS, RS_T, 0, st>>>(
+                kin, ii, n, chunk, shift, L.hist, pss + 1 < passes ? kout : nullptr, 0, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1695,8 +1734,8 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
             k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, L.hist);
         int s = ct_exclusive_scan(L.hist, nh, L.hist, L.scan_ws, L.scan_bytes, nullptr, stream);
         if (s) return s;
-        k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift, L.hist,
-                                                 pss < 3 ? kout : nullptr, iout);
+        k_rs_scatter<unsigned, unsigned><<<RS_BLOCKS, RS_T, 0, st>>>(kin, pss ? iin : nullptr, n, chunk, shift,
+                                                                     L.hist, pss < 3 ? kout : nullptr, 0, iout);
         std::swap(kin, kout);
         std::swap(iin, iout);
     }
@@ -1752,7 +1791,7 @@ int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift,
     k_rs_hist<<<RS_BLOCKS, RS_T, 0, st>>>(kin, n, chunk, shift, hist);
     int s = ct_exclusive_scan(hist, nh, hist, scan_ws, scan_bytes, nullptr, stream);
     if (s) return s;
-    k_rs_scatter<<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, hist, kout, iout);
+    k_rs_scatter<unsigned, unsigned><<<RS_BLOCKS, RS_T, 0, st>>>(kin, iin, n, chunk, shift, hist, kout, 0, iout);
     CT_CHECK_LAUNCH("radix pass");
     return CT_OK;
 }

@@ -190,7 +190,7 @@ def test_locate_start_grid_edges(oracle):
         assert np.array_equal(g.locate_points(pts), ref), prec
     p_d = torch.as_tensor(pts, device="cuda")
     o_d = torch.empty(len(pts), dtype=torch.int64, device="cuda")
-    for bits in (0, 24):
+    for bits in (0, 8, 16, 24):
         t.locate(p_d, o_d, g.default_tolerance(), "fp32", sort_bits=bits)
         assert np.array_equal(o_d.cpu().numpy(), ref), bits
 
