@@ -150,6 +150,9 @@ def test_result_scatter_above_threshold(oracle):
     g.precision = "fp64"
     r64 = g.locate_points(p_d)
     assert torch.equal(r32, r64)
+    g.precision = "fp32"
+    # numpy input: the host pipeline (one chunk above the threshold)
+    assert np.array_equal(g.locate_points(pts), r32.cpu().numpy())
     o = oracle.OracleCellTree2d(xy, f, -1)
     sample = np.random.default_rng(7).integers(0, n, 200_000)
     assert np.array_equal(r32.cpu().numpy()[sample], o.locate_points(pts[sample]))
