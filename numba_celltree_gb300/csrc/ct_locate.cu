@@ -1372,13 +1372,14 @@ int ct_grid_shape(int64_t n_elements, double width, double height, double cells_
     double a = width / height;  // aspect; 1 for a degenerate bbox (the grid is then switched off)
     if (!(a > 0.0) || !std::isfinite(a)) a = 1.0;
     a = std::min(std::max(a, 1.0 / 4096.0), 4096.0);
-    int64_t gx = std::max<int64_t>(16, (int64_t)std::llround(std::sqrt(target * a)));
-    int64_t gy = std::max<int64_t>(16, (int64_t)std::llround(std::sqrt(target / a)));
-    gx = std::min<int64_t>(gx, 65536);
-    gy = std::min<int64_t>(gy, 65536);
-    while (gx * gy > ((int64_t)1 << 26)) {  // the minimum of 16 on one axis can push the product up
-        if (gx >= gy) gx = std::max<int64_t>(16, gx * 15 / 16);
-        else gy = std::max<int64_t>(16, gy * 15 / 16);
+    const double sx = std::sqrt(target * a), sy = std::sqrt(target / a);  // ideal cells per axis
+    int64_t gx = std::min<int64_t>(65536, std::max<int64_t>(16, (int64_t)std::llround(sx)));
+    int64_t gy = std::min<int64_t>(65536, std::max<int64_t>(16, (int64_t)std::llround(sy)));
+    // rounding (or the minimum of 16 on one axis) can step over the cap:
+    // drop a row or column of the axis furthest above its ideal count
+    while (gx * gy > ((int64_t)1 << 26) && (gx > 16 || gy > 16)) {
+        if (gy <= 16 || (gx > 16 && (double)gx * sy >= (double)gy * sx)) gx--;
+        else gy--;
     }
     *nx = (int32_t)gx;
     *ny = (int32_t)gy;

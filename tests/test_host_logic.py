@@ -17,3 +17,35 @@ def test_chunk_bounds_cover_in_order_and_ramp():
             assert all(0 < k <= chunk for k in sizes)
     sizes = [e - s for s, e in chunk_bounds(268_435_456, 1 << 25)]
     assert sizes[0] == 1 << 22 and sizes[-1] <= 1 << 22 and max(sizes) == 1 << 25
+
+
+def test_grid_shape_is_near_square_and_bounded():
+    """ct_grid_shape (host code of the C-ABI library, no GPU needed): about
+    cells_per_element grid cells per mesh cell, nearly square grid cells,
+    at least 16 per axis, at most 2^26 in all; degenerate extents fall back
+    to a square grid; bad densities are rejected."""
+    import ctypes
+
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    gx, gy = ctypes.c_int32(0), ctypes.c_int32(0)
+
+    def shape(n, w, h, d=1.0):
+        assert lib.ct_grid_shape(n, w, h, d, ctypes.byref(gx), ctypes.byref(gy)) == 0
+        return gx.value, gy.value
+
+    x, y = shape(16_000_000, 4000.0, 2000.0)
+    assert (x, y) == (5657, 2828)
+    x, y = shape(16_000_000, 4000.0, 2000.0, 4.0)
+    assert abs(x * y - 64_000_000) < 64_000_000 * 0.001 and abs(x - 2 * y) <= 2
+    for n, w, h in [(1, 1.0, 1.0), (100, 10.0, 1.0), (10**6, 1.0, 1000.0), (10**9, 3.0, 1.0)]:
+        x, y = shape(n, w, h)
+        assert x >= 16 and y >= 16 and x * y <= 1 << 26
+        if 16 < x and 16 < y and x * y < 1 << 26:
+            # nearly square cells: the grid's aspect follows the bbox's
+            assert abs((w / x) / (h / y) - 1.0) < 0.05
+    assert shape(10**9, 1.0, 1.0)[0] * shape(10**9, 1.0, 1.0)[1] <= 1 << 26
+    assert shape(1000, 0.0, 0.0) == shape(1000, 1.0, 1.0)
+    assert lib.ct_grid_shape(10, 1.0, 1.0, 0.0, ctypes.byref(gx), ctypes.byref(gy)) != 0
+    assert lib.ct_grid_shape(10, 1.0, 1.0, float("nan"), ctypes.byref(gx), ctypes.byref(gy)) != 0
