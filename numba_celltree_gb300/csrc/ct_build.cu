@@ -254,10 +254,44 @@ __device__ Decision warp_decide(const int* cnt, const double* bRmin, const doubl
     }
     int nL = pre - ck;  // cells of the first `lane` non-empty buckets
     int bprev = __shfl_up_sync(FULL, bk, 1);
-    int plane;
+    int plane = -1;
     if (m == 2) {
         plane = 1;
     } else {
+        // Float32 screening of split_plane's costs: the numerators are the
+        // upstream float64 differences; the volumes and the cost are then
+        // within 6u (u = 2^-24) of the exact real cost, all terms being
+        // non-negative, and the float64 costs within a few 2^-53.  A
+        // minimum below every other cost by more than 32u relative is
+        // therefore the float64 argmin as well; anything else (ties, zero
+        // or non-finite values, costs near FLOAT_MAX) takes the float64
+        // path below.
+        float c32 = FLT_MAX;
+        bool ok = true;
+        if (lane >= 1 && lane < m) {
+            const double dl = bLmax[bprev] - R, dr = L - bRmin[bk];
+            const float fbl = (float)bl;
+            ok = dl >= 0.0 && dr >= 0.0 && dl < 1e30 && dr < 1e30 && fbl > 1e-30f && fbl < 1e30f;
+            if (ok) {
+                const float vl = (float)dl / fbl, vr = (float)dr / fbl;
+                // no float32 denormals (their relative error is unbounded)
+                ok = (dl == 0.0 || ((float)dl >= 1e-30f && vl >= 1e-30f)) &&
+                     (dr == 0.0 || ((float)dr >= 1e-30f && vr >= 1e-30f));
+                c32 = vl * (float)nL + vr * (float)(size - nL);
+                ok = ok && c32 < 1e30f;
+            }
+        }
+        if (__all_sync(FULL, ok)) {
+            float cmin = c32;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) cmin = fminf(cmin, __shfl_xor_sync(FULL, cmin, o));
+            const float u = 5.9604644775390625e-08f;
+            const bool near = c32 <= cmin * (1.0f + 32.0f * u) + 1e-37f;
+            const unsigned nm = __ballot_sync(FULL, near && lane >= 1 && lane < m);
+            if (__popc(nm) == 1) plane = __ffs(nm) - 1;
+        }
+    }
+    if (plane < 0) {
         unsigned long long key = ~0ull;
         if (lane >= 1 && lane < m) {
             double left_volume = (bLmax[bprev] - R) / bl;
