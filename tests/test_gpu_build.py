@@ -104,3 +104,22 @@ def test_build_large_levels(oracle):
     g = CellTree2d(xy, f, -1, 6, 3)
     o = oracle.OracleCellTree2d(xy, f, -1, 6, 3)
     _same_tree(g, o)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nb, cpl", [(4, 2), (3, 1), (8, 4)])
+def test_build_regular_grids_tied_split_costs(oracle, nb, cpl):
+    """Unjittered grids: many nodes whose split_plane costs tie exactly (the
+    float32 cost screening must leave those to the float64 comparison and
+    its first-minimum rule), at integer and at large offset coordinates."""
+    from numba_celltree_gb300 import CellTree2d
+
+    for nx, ny, extent, offset in [(32, 16, (64.0, 32.0), (0.0, 0.0)), (150, 150, (300.0, 300.0), (5.0e5, 4.2e6))]:
+        xy, f = syn.triangle_mesh(nx, ny, seed=1, extent=extent, offset=offset, jitter=0.0)
+        g = CellTree2d(xy, f, -1, nb, cpl)
+        o = oracle.OracleCellTree2d(xy, f, -1, nb, cpl)
+        _same_tree(g, o)
+        xy, f = syn.quad_mesh(nx, ny, seed=1, extent=extent, offset=offset, jitter=0.0)
+        g = CellTree2d(xy, f, -1, nb, cpl)
+        o = oracle.OracleCellTree2d(xy, f, -1, nb, cpl)
+        _same_tree(g, o)
