@@ -626,7 +626,7 @@ def main():
     # overflow
     passes = bins // 8
     lists = t.cand_idx is not None and tol <= float(t.desc.cand_tol)
-    stage2 = (4 if bins else 2) if lists else 1
+    stage2 = (4 if bins and n > (1 << 23) else 2) if lists else 1
     launches_per_step = (5 * passes if bins else 0) + stage2 + 3
     value = ws * n / (ms32 * 1e-3) / 1e6
     value64 = ws * n / (ms64 * 1e-3) / 1e6
@@ -654,12 +654,28 @@ def main():
             step_s.append(time.perf_counter() - t0)
         e2e_s = max_over_ranks(ws, statistics.median(step_s))
         assert np.array_equal(res, out32.cpu().numpy()), "end-to-end result differs from the device-resident run"
+        # the host link's own bound for one step: the upload and the download
+        # of the same bytes, both at once, nothing else
+        res_t = torch.empty((n,), dtype=torch.int64, pin_memory=True)
+        up_s, down_s = torch.cuda.Stream(), torch.cuda.Stream()
+        link_s = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(up_s):
+                pts_d.copy_(pin, non_blocking=True)
+            with torch.cuda.stream(down_s):
+                res_t.copy_(out32, non_blocking=True)
+            torch.cuda.synchronize()
+            link_s.append(time.perf_counter() - t0)
+        link_ms = statistics.median(link_s) * 1e3
         e2e = {"value": round(ws * n / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(pts_pin.nbytes),
                "d2h_bytes_per_step": int(n * 8), "ms_per_step": round(e2e_s * 1e3, 3),
                "ms_steps": [round(x * 1e3, 2) for x in step_s], "statistic": "median of the timed steps",
+               "link_ms": round(link_ms, 3), "frac_of_link_bound": round(link_ms / (e2e_s * 1e3), 3),
                "path": "CellTree2d.locate_points(numpy in pinned memory) -> numpy; "
                        "chunks of 2^25 points, upload / query / download overlapped on three streams"}
-        del res, pts_pin, pin
+        del res, res_t, pts_pin, pin
 
     # ---- CPU baseline: the oracle on a bounded sample of the same workload
     cpu = None
