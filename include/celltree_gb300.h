@@ -219,16 +219,19 @@ int ct_pack_grid(ct_tree* tree, void* stream);
  * with the box of that part of the cell widened by M (and by the rounding of
  * the float32 clipping that computes it; cells of more than 4 vertices keep
  * their widened bbox): every cell whose predicate can be true for a point of
- * g, and a box that holds every such point.  A query
- * tests the boxes of its list and the float32 leaf filter of the cells whose
- * box holds it; one sure hit and sure misses elsewhere is locate_point's
- * answer (a sure hit is an interior point, inside the cell's bbox, so the
- * reference reaches that leaf), all sure misses is -1, anything else goes
- * through the traversal.  Needs ct_pack_grid first and the caller's arrays
- * cand_off (grid_nx * grid_ny + 1 int64) and cand_box (n_elements float4).  ct_cand_count
- * fills the boxes and offsets and returns the number of entries (sets
- * cand_n, cand_tol; synchronises); the caller then allocates cand_idx and
- * cand_lbox (cand_n entries each) and calls ct_cand_fill.  scratch: ct_cand_scratch_size bytes. */
+ * g, and a box that holds every such point.  A query tests the boxes of its
+ * list and the float32 leaf filter of the cells whose box holds it; one sure
+ * hit and sure misses elsewhere is locate_point's answer (a sure hit is an
+ * interior point, inside the cell's bbox, so the reference reaches that
+ * leaf), all sure misses is -1, anything else goes through the traversal.
+ * Needs ct_pack_grid first and the caller's arrays cand_off
+ * (grid_nx * grid_ny + 1 int64) and cand_box (n_elements float4).
+ * ct_cand_count fills the boxes and offsets and returns the number of
+ * entries (sets cand_n, cand_tol; synchronises); the caller then allocates
+ * cand_idx and cand_lbox (cand_n entries each) and calls ct_cand_fill, which
+ * sets CT_DEVERR_CAPACITY in the tree's error word should its decisions
+ * differ from the count's (no write goes past a grid cell's range).
+ * scratch: ct_cand_scratch_size bytes. */
 size_t ct_cand_scratch_size(const ct_tree* tree);
 int ct_cand_count(ct_tree* tree, double cover_tol, void* scratch, size_t scratch_bytes, int64_t* total_host,
                   void* stream);
@@ -241,10 +244,13 @@ int ct_locate_points(const ct_tree* tree, const double* points, int64_t n, doubl
 /* Batched float32 form of locate_points (query.py:110-117): queries are
  * ordered along a Morton curve over the tree bbox (radix sort by the top
  * sort_bits of a 24-bit key, 4096 x 4096 grid; sort_bits 0 = input order,
- * else 8, 16 or 24), located by a float32 pass that collects candidate cells
- * for queries whose float32 leaf test is ambiguous, then finished by float64
- * tests of those candidates (and a float64 traversal for the rare query with
- * too many candidates).  Output identical to ct_locate_points.
+ * else 8, 16 or 24), located through the candidate lists (a float32 pass that
+ * settles most queries) and a float32 traversal of the rest that collects
+ * candidate cells for queries whose float32 leaf test is ambiguous, then
+ * finished by float64 tests of those candidates (and a float64 traversal for
+ * the rare query with too many candidates).  Above 2^23 queries the list
+ * results go out through a bucketed scatter (the workspace's sort buffers).
+ * Output identical to ct_locate_points.
  * Workspace: ct_locate_workspace_size(n, sort_bits) bytes. */
 size_t ct_locate_workspace_size(int64_t n, int32_t sort_bits);
 int ct_locate_points_batched(const ct_tree* tree, const double* points, int64_t n, double tolerance, int32_t sort_bits,
