@@ -179,6 +179,9 @@ int ct_build_tree_noalloc(const double* bb_coords, int64_t n_elements, int32_t n
 /* float4 units of one cell in ct_tree.poly_f32: the cell's first vertex as
  * float hi/lo pairs, then the other vertices relative to it (float2). */
 int ct_poly32_stride(int32_t n_max_vert);
+/* sizeof(ct_tree) (which = 0) or sizeof(ct_forest_plan) (which = 1), else 0:
+ * lets a binding check its mirror of the structures against the library. */
+size_t ct_abi_sizeof(int32_t which);
 
 /* Fills the packed traversal arrays of `tree` (nodes_f32, nodes_f64,
  * poly_f64, poly_f32, poly_len, poly_len32) and its origin / vmax / abs_eps.

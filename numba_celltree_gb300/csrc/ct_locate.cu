@@ -1362,6 +1362,14 @@ extern "C" {
 
 int ct_poly32_stride(int32_t K) { return poly32_stride(K); }
 
+size_t ct_abi_sizeof(int32_t which) {
+    switch (which) {
+        case 0: return sizeof(ct_tree);
+        case 1: return sizeof(ct_forest_plan);
+        default: return 0;
+    }
+}
+
 int ct_grid_shape(int64_t n_elements, double width, double height, double cells_per_element, int32_t* nx,
                   int32_t* ny) {
     if (!nx || !ny) return ct_fail(CT_ERR_ARG, "null argument");

@@ -49,3 +49,16 @@ def test_grid_shape_is_near_square_and_bounded():
     assert shape(1000, 0.0, 0.0) == shape(1000, 1.0, 1.0)
     assert lib.ct_grid_shape(10, 1.0, 1.0, 0.0, ctypes.byref(gx), ctypes.byref(gy)) != 0
     assert lib.ct_grid_shape(10, 1.0, 1.0, float("nan"), ctypes.byref(gx), ctypes.byref(gy)) != 0
+
+
+def test_ctypes_mirrors_match_the_library_structs():
+    """The Python mirrors of ct_tree and ct_forest_plan have the C layouts'
+    sizes (and the library rejects unknown structure ids)."""
+    import ctypes
+
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    assert lib.ct_abi_sizeof(0) == ctypes.sizeof(_lib.CtTree)
+    assert lib.ct_abi_sizeof(1) == ctypes.sizeof(_lib.CtForestPlan)
+    assert lib.ct_abi_sizeof(7) == 0
