@@ -103,6 +103,12 @@ typedef struct ct_tree {
 /* Geometry preparation                                                    */
 /* ---------------------------------------------------------------------- */
 
+/* ct_validate_elements, ct_bbox_summary, ct_vertex_extent and ct_pack_tree
+ * share one small reduction array inside the library.  Each holds a
+ * process-wide lock from clearing it to reading its result back (all four
+ * synchronise their stream), so concurrent calls from several host threads
+ * or streams are safe and run one after another. */
+
 /* Input check for faces / edges (no upstream counterpart: upstream indexes
  * without checks).  *bad_host = 1 when an element's first min_len entries, or
  * any entry before its first fill value (-1), is not a vertex index in
@@ -165,9 +171,11 @@ int ct_build_emit(const void* workspace, int64_t n_elements, int32_t n_buckets, 
  * every GPU that loads the library holds the array until the process exits.
  * The outputs are the caller's: node arrays of node_capacity >=
  * ct_pessimistic_n_nodes(n_elements) entries and bb_indices of n_elements.
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture.  All calls share the one array:
- * calls that overlap on the GPU (other streams, other host threads) race.
+ * The first call on each device looks up the array's device address (and so
+ * does the first call after that device's context is re-created, e.g. by
+ * cudaDeviceReset); make that first call before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU (other streams,
+ * other host threads) race.
  * Extremely unbalanced trees that exceed the builder's record capacity return
  * CT_ERR_WORKSPACE; use ct_build_tree with a larger capacity_factor.
  * Synchronises the stream. */

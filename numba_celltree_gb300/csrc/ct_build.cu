@@ -1243,12 +1243,10 @@ namespace ct {
 // phase-A level.
 static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_phase_a, int n_roots,
                         Counters* hc_out) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(SUB_WARPS * sizeof(SubSmem)));
-        attr_set = true;
-    }
+    // a function attribute belongs to the current device (and context): set
+    // it on every call rather than once per process
+    CT_CUDA(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(SUB_WARPS * sizeof(SubSmem))));
     std::vector<int> level_b, level_e;
     level_b.push_back(0);
     level_e.push_back(n_roots);
@@ -1465,7 +1463,8 @@ int ct_build_forest_emit(const void* workspace, int64_t n_total, int32_t n_trees
 // workspace.  The array is 8 MiB, enough for 16384 cells with any n_buckets
 // <= 32; every GPU that loads the library holds it until the process exits.
 // Host code only sees a stand-in for the array's name, so the device address
-// is looked up once per device (with that device current) and cached.
+// is looked up once per device (with that device current) and cached; a
+// device whose context was re-created (cudaDeviceReset) is looked up again.
 // ------------------------------------------------------------------------
 
 namespace ct {
@@ -1476,21 +1475,67 @@ constexpr size_t NOALLOC_SCRATCH_BYTES = size_t(8) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 
 static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[256] = {nullptr};
 
-// Device address of g_noalloc_scratch on the current device.
+// One cached address per device, valid for the context it was looked up in.
+// A symbol's device address belongs to a CUDA context: after cudaDeviceReset
+// (or after the primary context is released and created again) the module is
+// loaded anew, so the cache is keyed by the context's unique id as well.
+struct NoallocSlot {
+    unsigned long long ctx_id;
+    void* ptr;
+};
+static NoallocSlot g_noalloc_slot[256] = {};
+
+typedef int (*pfn_ctx_get_current)(void**);
+typedef int (*pfn_ctx_get_id)(void*, unsigned long long*);
+
+// Unique id of the context current on this thread (0 when none is current).
+static int current_context_id(unsigned long long* id) {
+    static pfn_ctx_get_current get_current = nullptr;
+    static pfn_ctx_get_id get_id = nullptr;
+    if (!get_current || !get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return ct_fail(CT_ERR_CUDA, "driver entry points cuCtxGetCurrent / cuCtxGetId unavailable");
+        get_current = (pfn_ctx_get_current)f1;
+        get_id = (pfn_ctx_get_id)f2;
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0) return ct_fail(CT_ERR_CUDA, "cuCtxGetCurrent failed");
+    *id = 0;
+    if (ctx && get_id(ctx, id) != 0) return ct_fail(CT_ERR_CUDA, "cuCtxGetId failed");
+    return CT_OK;
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up once
+// per device and context (with that device current), then reused.
 static int noalloc_scratch(void** out) {
     int dev = 0;
     CT_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) return ct_fail(CT_ERR_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    int s = current_context_id(&id);
+    if (s != CT_OK) return s;
+    NoallocSlot& slot = g_noalloc_slot[dev];
+    if (id == 0 || slot.ptr == nullptr || slot.ctx_id != id) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return ct_fail(CT_ERR_CUDA, cudaGetErrorString(e));
-        g_noalloc_ptr[dev] = p;
+        // the lookup makes the runtime's context current if none was
+        if (id == 0) {
+            s = current_context_id(&id);
+            if (s != CT_OK) return s;
+        }
+        slot.ctx_id = id;
+        slot.ptr = p;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return CT_OK;
 }
 

@@ -15,6 +15,7 @@
 //                faster than float64, which is what this form exploits.
 #include <cfloat>
 #include <cmath>
+#include <mutex>
 
 #include "ct_common.cuh"
 #include "ct_internal.h"
@@ -488,8 +489,14 @@ static inline int grid_for(int64_t n, int threads) { return (int)((n + threads -
 using namespace ctq;
 
 // Reduction scratch for the summaries and checks lives in a small static
-// device array; the calls that use it synchronise before returning.
+// device array shared by ct_validate_elements, ct_bbox_summary,
+// ct_vertex_extent and ct_pack_tree.  Each of them holds g_red_mutex from
+// the reset of the array to the read-back of its result (all four
+// synchronise their stream before returning), so calls from several host
+// threads or on several streams run one after another instead of clearing
+// or overwriting each other's counters.
 static __device__ unsigned long long g_red[8];
+static std::mutex g_red_mutex;
 
 extern "C" {
 
@@ -497,6 +504,7 @@ int ct_validate_elements(const int64_t* elements, int64_t n, int32_t K, int32_t 
                          int32_t* bad_host, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     unsigned int* red = nullptr;
+    std::lock_guard<std::mutex> red_lock(g_red_mutex);
     CT_CUDA(cudaGetSymbolAddress((void**)&red, g_red));
     CT_CUDA(cudaMemsetAsync(red, 0, sizeof(unsigned int), st));
     if (n > 0) {
@@ -537,6 +545,7 @@ int ct_edge_bboxes(const double* vertices, const int64_t* edges, int64_t n, doub
 int ct_bbox_summary(const double* bb, int64_t n, double* dist, double* out5, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long* red = nullptr;
+    std::lock_guard<std::mutex> red_lock(g_red_mutex);
     CT_CUDA(cudaGetSymbolAddress((void**)&red, g_red));
     unsigned long long init[5] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
     CT_CUDA(cudaMemcpyAsync(red, init, sizeof(init), cudaMemcpyHostToDevice, st));
@@ -565,6 +574,7 @@ int ct_bbox_summary(const double* bb, int64_t n, double* dist, double* out5, voi
 int ct_vertex_extent(const double* v, int64_t n, double* out4, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     unsigned long long* red = nullptr;
+    std::lock_guard<std::mutex> red_lock(g_red_mutex);
     CT_CUDA(cudaGetSymbolAddress((void**)&red, g_red));
     unsigned long long init[4] = {~0ull, ~0ull, ~0ull, ~0ull};
     CT_CUDA(cudaMemcpyAsync(red, init, sizeof(init), cudaMemcpyHostToDevice, st));
@@ -601,6 +611,7 @@ int ct_pack_tree(ct_tree* t, void* stream) {
     }
     bool is_edge = t->n_max_vert == 2;
     unsigned int* red = nullptr;
+    std::lock_guard<std::mutex> red_lock(g_red_mutex);
     CT_CUDA(cudaGetSymbolAddress((void**)&red, g_red));
     CT_CUDA(cudaMemsetAsync(red, 0, 2 * sizeof(unsigned int), st));
     t->origin[0] = ox;

@@ -128,3 +128,41 @@ def test_regrid_weighted_mean_matches_dense():
     np.testing.assert_allclose(W2.mean(z), r2, rtol=1e-12, equal_nan=True)
     with pytest.raises(ValueError):
         WeightMatrix.from_intersections(i[::-1], j, a, len(qf), len(f))
+
+
+@pytest.mark.gpu
+def test_shared_reduction_calls_from_two_threads():
+    """ct_validate_elements (like ct_bbox_summary, ct_vertex_extent and
+    ct_pack_tree) uses a small reduction array inside the library: two host
+    threads calling it at once on their own streams, one with an index out of
+    range and one with valid faces, must each get their own verdict."""
+    import ctypes
+    import threading
+
+    import torch
+
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    xy, f = syn.triangle_mesh(300, seed=7)  # 180,000 faces
+    good = torch.as_tensor(f, device="cuda")
+    bad = good.clone()
+    bad[-1, 2] = xy.shape[0]  # one index past the vertex array
+    results = {"good": [], "bad": []}
+
+    def worker(name, faces):
+        torch.cuda.set_device(0)
+        s = torch.cuda.Stream()
+        flag = ctypes.c_int32(-1)
+        for _ in range(40):
+            assert lib.ct_validate_elements(faces.data_ptr(), faces.shape[0], 3, 3, xy.shape[0],
+                                            ctypes.byref(flag), s.cuda_stream) == 0
+            results[name].append(flag.value)
+
+    th = [threading.Thread(target=worker, args=(k, t)) for k, t in (("good", good), ("bad", bad))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert results["good"] == [0] * 40
+    assert results["bad"] == [1] * 40

@@ -62,3 +62,15 @@ def test_ctypes_mirrors_match_the_library_structs():
     assert lib.ct_abi_sizeof(0) == ctypes.sizeof(_lib.CtTree)
     assert lib.ct_abi_sizeof(1) == ctypes.sizeof(_lib.CtForestPlan)
     assert lib.ct_abi_sizeof(7) == 0
+
+
+def test_noalloc_scratch_holds_the_largest_accepted_build():
+    """ct_build_tree_noalloc accepts up to 16,384 cells with any n_buckets in
+    [2, 32] on an 8 MiB static scratch: the allocating builder's workspace for
+    the largest such case (n_buckets = 32, capacity factor 1) must fit."""
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    for nb in (2, 4, 8, 16, 32):
+        need = lib.ct_build_workspace_size(16384, nb, 1)
+        assert 0 < need <= 8 << 20, (nb, need)
