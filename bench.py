@@ -148,18 +148,17 @@ def peaks():
 
 
 def traffic_per_point():
-    """DRAM bytes per point of the float32 locate kernel from the committed ncu
-    summary (a smaller capture, scaled per point), or None."""
-    f = ROOT / "profiles" / "locate_points_fp32.md"
+    """DRAM bytes per point of the float32 locate kernels from the committed
+    ncu summary (profiles/locate_points_fp32.json: a smaller capture, scaled
+    per point), or None."""
+    f = ROOT / "profiles" / "locate_points_fp32.json"
     if not f.exists():
         return None
-    for line in f.read_text().splitlines():
-        if line.startswith("dram_bytes_per_point:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+    try:
+        d = json.loads(f.read_text())
+        return float(d["dram_bytes_per_point"])
+    except (ValueError, KeyError, TypeError):
+        return None
 
 
 def dist_setup():
@@ -679,11 +678,20 @@ def main():
 
     # ---- CPU baseline: the oracle on a bounded sample of the same workload
     cpu = None
+    build_identical = None
     if not args.no_cpu and rank == 0:
         from oracle import oracle as O
 
         O.build()
         h = tree
+        # the oracle builds the same tree: nodes and bb_indices must be identical
+        t0 = time.perf_counter()
+        otree = O.OracleCellTree2d(xy, faces, -1)
+        cpu_build_s = time.perf_counter() - t0
+        build_identical = bool(np.array_equal(otree.bb_indices, h.bb_indices) and
+                               all(np.array_equal(otree.nodes[f], h.nodes[f])
+                                   for f in ("child", "Lmax", "Rmin", "ptr", "size", "dim")))
+        del otree
         arrs = O._TreeArrays(h.faces, h.vertices, h.nodes, h.bb_indices, h.bb_coords, h.bbox)
         m = min(args.cpu_sample, n)
         sample = np.ascontiguousarray(pts_h[:m])
@@ -697,7 +705,8 @@ def main():
         cpu_s = time.perf_counter() - t0
         assert np.array_equal(outc, out32[:m].cpu().numpy()), "GPU result differs from the oracle"
         cpu = {"value": round(m / cpu_s / 1e6, 3), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
-               "sample": f"first {m} of the {n} points on the same tree (oracle = C restatement, OpenMP)"}
+               "sample": f"first {m} of the {n} points on the same tree (oracle = C restatement, OpenMP)",
+               "build_s": round(cpu_build_s, 3)}
 
     peak, peak_kind = peaks()
     achieved = BYTES_PER_POINT * n / (ms_fast * 1e-3) / 1e9
@@ -730,6 +739,7 @@ def main():
             "sort_bits": bins,
         },
         "build_ms": round(build_ms_val, 3),
+        "build_identical_to_oracle": build_identical,
         "fp64_plain": {"value": round(value64, 3), "unit": UNIT, "ms_per_step": round(ms64, 3)},
         "fp32_vs_fp64": round(value / value64, 3),
         "fp32_inline": {"value": round(ws * n / (ms_inline * 1e-3) / 1e6, 3), "unit": UNIT,

@@ -303,6 +303,45 @@ __device__ __forceinline__ bool sh_intersection(dpt a, dpt V, dpt r, dpt N, dpt*
     return false;
 }
 
+// One clip edge of polygon_polygon_clip_area (sutherland_hodgman.py:104-138):
+// `subject` (length vertices) clipped by the line through r with direction U
+// (normal N) into `output`.  Returns the output length, or -1 when the output
+// would exceed CT_CLIP_MAX vertices (upstream writes past its stack arrays).
+__device__ __forceinline__ int sh_clip_edge_seq(const dpt* subject, int length, dpt* output, dpt r, dpt U, dpt N) {
+    int n_output = 0;
+    dpt a = subject[length - 1];
+    bool a_inside = sh_inside(a, r, U);
+    for (int j = 0; j < length; j++) {
+        dpt b = subject[j];
+        dpt V = mkp(b.x - a.x, b.y - a.y);
+        if (V.x == 0 && V.y == 0) continue;
+        bool b_inside = sh_inside(b, r, U);
+        dpt pnt;
+        if (b_inside) {
+            if (!a_inside) {
+                if (sh_intersection(a, V, r, N, &pnt)) {
+                    if (n_output >= CT_CLIP_MAX) return -1;
+                    output[n_output++] = pnt;
+                }
+            }
+            if (n_output >= CT_CLIP_MAX) return -1;
+            output[n_output++] = b;
+        } else if (a_inside) {
+            if (sh_intersection(a, V, r, N, &pnt)) {
+                if (n_output >= CT_CLIP_MAX) return -1;
+                output[n_output++] = pnt;
+            } else {
+                b_inside = true;
+                if (n_output >= CT_CLIP_MAX) return -1;
+                output[n_output++] = b;
+            }
+        }
+        a = b;
+        a_inside = b_inside;
+    }
+    return n_output;
+}
+
 // polygon_polygon_clip_area: `subject` is clipped by `clipper`.  Uses two
 // CT_CLIP_MAX-vertex scratch polygons; returns NaN and sets *overflow if the
 // clipped polygon would exceed them (upstream writes past its stack arrays).
@@ -322,53 +361,136 @@ __device__ __forceinline__ double clip_area(const dpt* polygon, int n_poly, cons
         dpt* t = subject;  // swap roles instead of copying output into subject
         subject = output;
         output = t;
-        n_output = 0;
-        dpt a = subject[length - 1];
-        bool a_inside = sh_inside(a, r, U);
-        for (int j = 0; j < length; j++) {
-            dpt b = subject[j];
-            dpt V = mkp(b.x - a.x, b.y - a.y);
-            if (V.x == 0 && V.y == 0) continue;
-            bool b_inside = sh_inside(b, r, U);
-            dpt pnt;
-            if (b_inside) {
-                if (!a_inside) {
-                    if (sh_intersection(a, V, r, N, &pnt)) {
-                        if (n_output >= CT_CLIP_MAX) {
-                            *overflow = true;
-                            return dnan();
-                        }
-                        output[n_output++] = pnt;
-                    }
-                }
-                if (n_output >= CT_CLIP_MAX) {
-                    *overflow = true;
-                    return dnan();
-                }
-                output[n_output++] = b;
-            } else if (a_inside) {
-                if (sh_intersection(a, V, r, N, &pnt)) {
-                    if (n_output >= CT_CLIP_MAX) {
-                        *overflow = true;
-                        return dnan();
-                    }
-                    output[n_output++] = pnt;
-                } else {
-                    b_inside = true;
-                    if (n_output >= CT_CLIP_MAX) {
-                        *overflow = true;
-                        return dnan();
-                    }
-                    output[n_output++] = b;
-                }
-            }
-            a = b;
-            a_inside = b_inside;
+        n_output = sh_clip_edge_seq(subject, length, output, r, U, N);
+        if (n_output < 0) {
+            *overflow = true;
+            return dnan();
         }
         if (n_output < 3) return 0.0;
         r = s;
     }
     return polygon_area(output, n_output);
+}
+
+// ---------------------------------------------------------------------------
+// The same clip with each clip edge's float64 work in converged passes.
+//
+// The sequential walk computes an intersection wherever it crosses the clip
+// line.  The lanes of a warp cross at different steps, so on a GPU the
+// intersection code runs at almost every step with a few lanes active, and
+// the float64 pipe -- the bound of these kernels on GB300 -- spends most of
+// its issue slots on idle lanes.  Here each clip edge runs
+//   1. the inside test of every subject vertex, all lanes in step;
+//   2. integer bookkeeping: the skipped steps (zero-length edges, b - a == 0
+//      <=> finite and equal coordinates), the crossings and the output slot
+//      of every pushed vertex, copying the vertices that stay;
+//   3. one pass per crossing (usually two per clip edge, all lanes in step)
+//      computing the intersection into its slot.
+// The output polygon, its order and every value are those of the walk.  A
+// crossing whose intersection fails (N.V == 0, where the walk pushes a
+// vertex instead and flips its inside flag) sends the lane through the walk
+// for that clip edge.  Order comparisons and zero tests run on integer keys.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool g_notnan(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool g_finite(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) < 0x7ff0000000000000ull;
+}
+// x == 0.0 (either sign)
+__device__ __forceinline__ bool g_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull; }
+// x > y, false when either is NaN (the float64 comparison)
+__device__ __forceinline__ bool g_gt(double x, double y) { return g_notnan(x) && g_notnan(y) && fkey(x) > fkey(y); }
+// x == y as values for finite x, y (bit patterns equal, or both zeros)
+__device__ __forceinline__ bool g_eq_finite(double x, double y) {
+    unsigned long long a = (unsigned long long)__double_as_longlong(x), b = (unsigned long long)__double_as_longlong(y);
+    return a == b || ((a | b) << 1) == 0ull;
+}
+// b - a == (0, 0): both coordinates finite and equal
+__device__ __forceinline__ bool g_zero_edge(dpt a, dpt b) {
+    return g_finite(a.x) && g_finite(b.x) && g_finite(a.y) && g_finite(b.y) && g_eq_finite(a.x, b.x) &&
+           g_eq_finite(a.y, b.y);
+}
+
+__device__ __forceinline__ double clip_area_conv(const dpt* polygon, int n_poly, const dpt* clipper, int n_clip,
+                                                 dpt* bufA, dpt* bufB, bool* overflow) {
+    static_assert(CT_CLIP_MAX <= 64, "vertex masks are 64-bit");
+    dpt* output = bufA;
+    const dpt* subject = polygon;  // the first clip edge reads the polygon in place
+    int n_output = n_poly;
+    unsigned short xs[CT_CLIP_MAX];  // crossings: step j | last kept step << 6 (slot in xslot)
+    unsigned char xslot[CT_CLIP_MAX];
+    dpt r = clipper[n_clip - 1];
+    for (int i = 0; i < n_clip; i++) {
+        dpt s = clipper[i];
+        dpt U = mkp(s.x - r.x, s.y - r.y);
+        if (g_zero(U.x) && g_zero(U.y)) continue;
+        dpt N = mkp(-U.y, U.x);
+        int length = n_output;
+        // 1. inside flags and zero-length steps
+        unsigned long long inside = 0ull, skip = 0ull;
+        dpt prev = subject[length - 1];
+        for (int j = 0; j < length; j++) {
+            dpt b = subject[j];
+            double lhs = U.x * (b.y - r.y);
+            double rhs = U.y * (b.x - r.x);
+            if (g_gt(lhs, rhs)) inside |= 1ull << j;
+            if (g_zero_edge(prev, b)) skip |= 1ull << j;
+            prev = b;
+        }
+        // 2. walk on the flags: slots of the kept vertices and of the crossings
+        bool a_in = (inside >> (length - 1)) & 1ull;
+        int a_idx = length - 1;
+        int n_out = 0, n_x = 0;
+        for (int j = 0; j < length; j++) {
+            if ((skip >> j) & 1ull) continue;
+            bool b_in = (inside >> j) & 1ull;
+            if (b_in != a_in) {
+                xs[n_x] = (unsigned short)(j | (a_idx << 6));
+                xslot[n_x] = (unsigned char)(n_out < 255 ? n_out : 255);
+                n_x++;
+                n_out++;
+            }
+            if (b_in) {
+                if (n_out < CT_CLIP_MAX) output[n_out] = subject[j];
+                n_out++;
+            }
+            a_in = b_in;
+            a_idx = j;
+        }
+        // 3. intersections (sh_intersection), all lanes in step
+        bool fail = false;
+        for (int k = 0; k < n_x; k++) {
+            int j = xs[k] & 63, ai = xs[k] >> 6;
+            dpt a = subject[ai], b = subject[j];
+            dpt V = mkp(b.x - a.x, b.y - a.y);
+            dpt W = mkp(r.x - a.x, r.y - a.y);
+            double nw = dotp(N, W), nv = dotp(N, V);
+            if (!g_zero(nv)) {
+                double t = nw / nv;
+                int slot = xslot[k];
+                if (slot < CT_CLIP_MAX) output[slot] = mkp(a.x + t * V.x, a.y + t * V.y);
+            } else {
+                fail = true;
+            }
+        }
+        if (fail) {
+            n_out = sh_clip_edge_seq(subject, length, output, r, U, N);
+        } else if (n_out > CT_CLIP_MAX) {
+            n_out = -1;
+        }
+        if (n_out < 0) {
+            *overflow = true;
+            return dnan();
+        }
+        n_output = n_out;
+        if (n_output < 3) return 0.0;
+        // the output becomes the next subject
+        subject = output;
+        output = (output == bufA) ? bufB : bufA;
+        r = s;
+    }
+    return polygon_area(subject, n_output);
 }
 
 // ---------------------------------------------------------------------------

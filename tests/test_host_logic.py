@@ -74,3 +74,20 @@ def test_noalloc_scratch_holds_the_largest_accepted_build():
     for nb in (2, 4, 8, 16, 32):
         need = lib.ct_build_workspace_size(16384, nb, 1)
         assert 0 < need <= 8 << 20, (nb, need)
+
+
+def test_library_exports_every_declared_entry_point():
+    """Every function include/celltree_gb300.h declares is exported by the
+    built library, and the ctypes binding declares no name the header lacks."""
+    import pathlib
+    import re
+
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    hdr = (pathlib.Path(__file__).resolve().parents[1] / "include" / "celltree_gb300.h").read_text()
+    names = set(re.findall(r"^\s*(?:const\s+)?(?:int|size_t|int64_t|char)\s*\*?\s*(ct_\w+)\s*\(", hdr, re.M))
+    assert len(names) > 50
+    missing = sorted(n for n in names if not hasattr(lib, n))
+    assert not missing, missing
+    assert set(_lib.SIGNATURES) <= names, sorted(set(_lib.SIGNATURES) - names)
