@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CT_ABI_VERSION 1
+#define CT_ABI_VERSION 2
 
 typedef enum ct_status {
     CT_OK = 0,
@@ -97,6 +97,19 @@ typedef struct ct_tree {
     int64_t cand_n;           /* host: entries of cand_idx */
     double cand_tol;          /* host: largest query tolerance the lists cover */
     int32_t bounds_finite;    /* host (ct_pack_tree): every node bound and bb_coords value is finite */
+    /* box index of the multi-result queries (filled by ct_pack_box_index;
+     * all three NULL disables it) */
+    void* bb_leaf;            /* device: n_elements x 4 doubles, bb_coords in leaf (bb_indices) order */
+    void* node_box;           /* device: n_nodes x 32 B: float32 bbox of the node's cells (frame of origin,
+                                 rounded outward), int32 leaf ptr, int32 size, 8 B padding */
+    int32_t* leaf_start;      /* device: n_elements: first leaf position of the leaf holding each position */
+    /* launch shapes (host; 0 = the library default).  They change speed,
+     * never results; an autotuner picks them per GPU and problem size. */
+    int32_t tune_cells_bpsm;  /* candidate-list pass compiled for 4, 6 or 8 resident blocks per SM (default 6) */
+    int32_t tune_fast_bpsm;   /* grid of the open-query traversal in blocks per SM, 1 .. 32 (default 16) */
+    int32_t tune_query_threads; /* block size of the box and segment traversals: 64, 128 or 256
+                                   (default 256 boxes, 128 segments; segments take at most 128) */
+    int32_t tune_fp64_stack;  /* stack entries of the plain float64 locate: 0 = smallest that fits, 64 or 512 */
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */
@@ -298,6 +311,8 @@ typedef struct ct_forest_plan {
     int32_t morton_bits;  /* Morton bits of the sort key below the tree bits */
     unsigned int* error_word; /* device: error bits of the batch-wide stages (the first tree's word) */
     int64_t max_tree_points;  /* most points of one tree */
+    int32_t tune_cells_bpsm;  /* as ct_tree.tune_cells_bpsm (set before ct_forest_locate; 0 = default) */
+    int32_t tune_fast_bpsm;   /* as ct_tree.tune_fast_bpsm */
 } ct_forest_plan;
 size_t ct_forest_locate_workspace_size(int64_t n_points, int32_t n_trees);
 int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double* tolerances,
@@ -337,6 +352,19 @@ int ct_work_order(const double* queries, int64_t n, int32_t kind, double cell_si
 size_t ct_radix_pass_workspace_size(void);
 int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout,
                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* Box index of a packed face or edge tree (no upstream counterpart): the
+ * cell boxes in leaf order, every node's bounding box and leaf range, and
+ * every leaf position's leaf start, in caller-allocated arrays set in the
+ * descriptor (bb_leaf, node_box, leaf_start).  With it the box queries
+ * stop descending at nodes whose cells' bounding box lies strictly inside
+ * the query box -- every cell below overlaps it -- and count or write that
+ * subtree's cells in the upstream visiting order directly.  Results are
+ * unchanged.  scratch: ct_box_index_scratch_size(tree) bytes; the call only
+ * enqueues work, so the scratch must stay allocated until that work has run
+ * (stream order). */
+size_t ct_box_index_scratch_size(const ct_tree* tree);
+int ct_pack_box_index(ct_tree* tree, void* scratch, size_t scratch_bytes, void* stream);
 
 /* locate_box query.py:177-244: per box (xmin, xmax, ymin, ymax) the number of
  * cells whose bbox overlaps it (strict, boxes_intersect geometry_utils.py:292-300).
@@ -397,6 +425,28 @@ int ct_area_of_intersection(const double* vertices_a, const int64_t* faces_a, in
 int ct_box_area_of_intersection(const double* boxes, const double* vertices, const int64_t* faces,
                                 int32_t n_max_vert, const int64_t* indices_box, const int64_t* indices_face,
                                 int64_t n, double* out, unsigned int* error_word, void* stream);
+
+/* The two above with the pairs processed in `order` (a permutation of 0 ..
+ * n-1, e.g. from ct_pair_order; NULL = index order).  Results are written
+ * at each pair's own index, so they do not depend on the order. */
+int ct_area_of_intersection_ordered(const double* vertices_a, const int64_t* faces_a, int32_t n_max_vert_a,
+                                    const double* vertices_b, const int64_t* faces_b, int32_t n_max_vert_b,
+                                    const int64_t* indices_a, const int64_t* indices_b, int64_t n,
+                                    const int32_t* order, double* out, unsigned int* error_word, void* stream);
+int ct_box_area_of_intersection_ordered(const double* boxes, const double* vertices, const int64_t* faces,
+                                        int32_t n_max_vert, const int64_t* indices_box, const int64_t* indices_face,
+                                        int64_t n, const int32_t* order, double* out, unsigned int* error_word,
+                                        void* stream);
+
+/* Processing order for the per-pair kernels (no upstream counterpart): the
+ * pairs grouped by the polygon lengths of their two faces (faces_a NULL:
+ * the pairs' first members are boxes), so that the lanes of a warp clip
+ * polygons of the same lengths.  order: n int32.  Workspace:
+ * ct_pair_order_workspace_size(n) bytes. */
+size_t ct_pair_order_workspace_size(int64_t n);
+int ct_pair_order(const int64_t* faces_a, int32_t n_max_vert_a, const int64_t* indices_a, const int64_t* faces_b,
+                  int32_t n_max_vert_b, const int64_t* indices_b, int64_t n, int32_t* order, void* workspace,
+                  size_t workspace_bytes, void* stream);
 
 /* Keeps the pairs with area > 0 (area != NULL) or flag != 0 (celltree.py:183,
  * 226, 268); outputs have capacity n; *total_host = kept count (synchronises). */

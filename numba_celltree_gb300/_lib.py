@@ -12,7 +12,7 @@ import pathlib
 from . import build as _build
 
 LIB_PATH = _build.LIB_PATH
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 CT_OK = 0
 CT_ERR_CUDA = 1
@@ -80,6 +80,13 @@ class CtTree(ctypes.Structure):
         ("cand_n", _I64),
         ("cand_tol", _D),
         ("bounds_finite", _I32),
+        ("bb_leaf", _P),
+        ("node_box", _P),
+        ("leaf_start", _P),
+        ("tune_cells_bpsm", _I32),
+        ("tune_fast_bpsm", _I32),
+        ("tune_query_threads", _I32),
+        ("tune_fp64_stack", _I32),
     ]
 
 
@@ -94,6 +101,8 @@ class CtForestPlan(ctypes.Structure):
         ("morton_bits", _I32),
         ("error_word", _P),
         ("max_tree_points", _I64),
+        ("tune_cells_bpsm", _I32),
+        ("tune_fast_bpsm", _I32),
     ]
 
 
@@ -144,6 +153,8 @@ SIGNATURES = {
     "ct_locate_deferred_count": (ctypes.c_int, [_P, _I64, _I32, ctypes.POINTER(_I64), _P]),
     "ct_scan_workspace_size": (_SZ, [_I64]),
     "ct_exclusive_scan": (ctypes.c_int, [_P, _I64, _P, _P, _SZ, ctypes.POINTER(_I64), _P]),
+    "ct_box_index_scratch_size": (_SZ, [ctypes.POINTER(CtTree)]),
+    "ct_pack_box_index": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _SZ, _P]),
     "ct_count_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P]),
     "ct_write_boxes": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P, _P]),
     "ct_sort_workspace_size": (_SZ, [_I64]),
@@ -151,6 +162,10 @@ SIGNATURES = {
     "ct_polygons_intersect": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P]),
     "ct_area_of_intersection": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
     "ct_box_area_of_intersection": (ctypes.c_int, [_P, _P, _P, _I32, _P, _P, _I64, _P, _P, _P]),
+    "ct_area_of_intersection_ordered": (ctypes.c_int, [_P, _P, _I32, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _P]),
+    "ct_box_area_of_intersection_ordered": (ctypes.c_int, [_P, _P, _P, _I32, _P, _P, _I64, _P, _P, _P, _P]),
+    "ct_pair_order_workspace_size": (_SZ, [_I64]),
+    "ct_pair_order": (ctypes.c_int, [_P, _I32, _P, _P, _I32, _P, _I64, _P, _P, _SZ, _P]),
     "ct_liang_barsky_line_box_clip": (ctypes.c_int, [_P, _P, _P, _I64, _P, _P, _P, _P]),
     "ct_points_in_triangles": (ctypes.c_int, [_P, _P, _I64, _P, _I32, _I64, _P, _D, _P, _P, _P]),
     "ct_csr_workspace_size": (_SZ, [_I64]),

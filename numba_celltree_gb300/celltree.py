@@ -179,6 +179,9 @@ class CellTree2d(CellTree2dBase):
         points = cast_vertices(points)
         t = self._tree
         torch = _device.torch()
+        n = int(points.shape[0])
+        # first use of a batch size class: tune the launch shape (autotune.py)
+        t.maybe_tune_locate(points, tol, self.precision, n if cuda_in else min(n, _pipeline.CHUNK_POINTS))
         t.reset_error()
         if not cuda_in:
             # host batch: chunked upload / query / download, result in pinned memory
@@ -191,6 +194,52 @@ class CellTree2d(CellTree2dBase):
         out = _device.empty((int(p_d.shape[0]),), torch.int64, t.device)
         t.locate(p_d, out, tol, self.precision)
         t.raise_on_device_error()
+        return out
+
+    # -- launch-shape tuning (no upstream counterpart) --------------------------
+    def autotune(self, points=None, boxes=None, edges=None, tolerance: Optional[float] = None,
+                 index: bool = False) -> dict:
+        """Time the launch shapes of this tree's kernels on sample queries and
+        keep the fastest (autotune.py: per GPU and problem size class, cached
+        on disk).  ``points``: point location for batches of that size (and,
+        with ``index=True``, the density of the start-node grid and candidate
+        lists, rebuilt for each candidate); ``boxes`` / ``edges``: the box and
+        segment traversals.  Results never change, only speed.  Returns
+        {kind: cache entry}."""
+        from . import autotune as at
+
+        t = self._tree
+        torch = _device.torch()
+        out = {}
+        tol = self._tolerance(tolerance)
+        if points is not None:
+            p_d = _device.to_device(cast_vertices(points), torch.float64, t.device)
+            n = int(p_d.shape[0])
+            if index:
+                o = _device.empty((n,), torch.int64, t.device)
+                timed = []
+                for dens in at.SPACE["index"]["grid_density"]:
+                    t.rebuild_index(dens)
+                    cfg = {"grid_density": dens}
+                    timed.append((cfg, at.time_gpu(lambda: t.locate(p_d, o, tol, "fp32"))))
+                best, ms = at.pick(timed)
+                key = t.tune_key("index", 0)
+                entry = {"config": best, "ms": round(ms, 4), "candidates": len(timed), "sample": n}
+                at.cache().put(key, entry)
+                t._tuned[key] = dict(best)
+                t.rebuild_index(best["grid_density"])
+                out["index"] = entry
+            out["locate"] = t.tune_locate(p_d, tol, "fp32")
+        if boxes is not None:
+            b_d = _device.to_device(cast_bboxes(boxes), torch.float64, t.device)
+            key = t.tune_key("boxes", int(b_d.shape[0]))
+            t._tuned[key] = t.tune("boxes", key, lambda c: t.locate_boxes(b_d, c), int(b_d.shape[0]))
+            out["boxes"] = at.cache().get(key)
+        if edges is not None:
+            e_d = _device.to_device(cast_edges(edges), torch.float64, t.device)
+            key = t.tune_key("segments", int(e_d.shape[0]))
+            t._tuned[key] = t.tune("segments", key, lambda c: t.locate_edges(e_d, 1, c), int(e_d.shape[0]))
+            out["segments"] = at.cache().get(key)
         return out
 
     # -- box queries -----------------------------------------------------------
@@ -223,13 +272,16 @@ class CellTree2d(CellTree2dBase):
         n = int(ii.shape[0])
         area = _device.empty((n,), torch.float64, t.device)
         t.reset_error()
+        order = t.pair_order(None, 4, ii, t.elements, t.K, jj)
         _lib.check(
-            _lib.load().ct_box_area_of_intersection(
+            _lib.load().ct_box_area_of_intersection_ordered(
                 _device.ptr(b_d), _device.ptr(t.vertices), _device.ptr(t.elements), t.K, _device.ptr(ii),
-                _device.ptr(jj), n, _device.ptr(area), _device.ptr(t.error_word), _device.stream(),
+                _device.ptr(jj), n, _device.ptr(order), _device.ptr(area), _device.ptr(t.error_word),
+                _device.stream(),
             ),
             "intersect_boxes",
         )
+        del order
         t.raise_on_device_error()
         i, j, a = t.compact(ii, jj, area=area)
         return _as_output(i, cuda_in), _as_output(j, cuda_in), _as_output(a, cuda_in)
@@ -310,14 +362,16 @@ class CellTree2d(CellTree2dBase):
         n = int(i.shape[0])
         area = _device.empty((n,), torch.float64, t.device)
         t.reset_error()
+        order = t.pair_order(f_d, int(f_d.shape[1]), i, t.elements, t.K, j)
         _lib.check(
-            _lib.load().ct_area_of_intersection(
+            _lib.load().ct_area_of_intersection_ordered(
                 _device.ptr(v_d), _device.ptr(f_d), int(f_d.shape[1]), _device.ptr(t.vertices),
-                _device.ptr(t.elements), t.K, _device.ptr(i), _device.ptr(j), n, _device.ptr(area),
-                _device.ptr(t.error_word), _device.stream(),
+                _device.ptr(t.elements), t.K, _device.ptr(i), _device.ptr(j), n, _device.ptr(order),
+                _device.ptr(area), _device.ptr(t.error_word), _device.stream(),
             ),
             "area_of_intersection",
         )
+        del order
         t.raise_on_device_error()
         i2, j2, a2 = t.compact(i, j, area=area)
         return _as_output(i2, cuda_in), _as_output(j2, cuda_in), _as_output(a2, cuda_in)

@@ -16,6 +16,7 @@ import numpy as np
 
 from . import _device
 from . import _lib
+from . import autotune
 from .constants import MAX_N_BUCKETS, MIN_TOLERANCE, TOLERANCE_FACTOR, CellTreeData, NodeDType
 
 
@@ -71,17 +72,37 @@ class _GpuTree:
         self.grid_start = None
         self.desc = _lib.CtTree()
         self._fill_desc()
+        self._gpu = None
+        self._tuned = {}
+        self.candidate_lists = candidate_lists
         _lib.check(lib.ct_pack_tree(ctypes.byref(self.desc), st), "pack")
+        self.grid_density = self.GRID_CELLS_PER_ELEMENT
+        if candidate_lists and n > 0:
+            # a density tuned for trees of this size class (autotune(index=True)), if any
+            self.grid_density = float(self.cached("index", 0).get("grid_density") or self.grid_density)
+        self._build_index(self.grid_density)
+
+    def _build_index(self, density: float):
+        """Start-node grid and candidate lists of the batched float32 locate,
+        about `density` grid cells per mesh cell."""
+        torch = _device.torch()
+        lib = _lib.load()
+        st = _device.stream()
+        n = self.n
         bb = self.desc.bbox
         gx, gy = ctypes.c_int32(0), ctypes.c_int32(0)
-        _lib.check(lib.ct_grid_shape(n, bb[1] - bb[0], bb[3] - bb[2], self.GRID_CELLS_PER_ELEMENT,
+        _lib.check(lib.ct_grid_shape(n, bb[1] - bb[0], bb[3] - bb[2], float(density),
                                      ctypes.byref(gx), ctypes.byref(gy)), "grid shape")
-        self.grid_start = _device.empty((gx.value * gy.value,), torch.int32, device)
+        self.grid_start = _device.empty((gx.value * gy.value,), torch.int32, self.device)
         self.desc.grid_start = _device.ptr(self.grid_start)
         self.desc.grid_nx, self.desc.grid_ny = gx.value, gy.value
         _lib.check(lib.ct_pack_grid(ctypes.byref(self.desc), st), "pack_grid")
         self.cand_off = self.cand_box = self.cand_idx = self.cand_lbox = None
-        if candidate_lists and int(self.desc.grid_nx) > 0 and n > 0:
+        d = self.desc
+        d.cand_off = d.cand_box = d.cand_idx = d.cand_lbox = None
+        d.cand_n, d.cand_tol = 0, 0.0
+        self.grid_density = float(density)
+        if self.candidate_lists and int(self.desc.grid_nx) > 0 and n > 0:
             self._build_candidate_lists(lib, st)
 
     def _build(self, lib, st, device, bb_coords, n, n_buckets, cells_per_leaf) -> int:
@@ -214,16 +235,94 @@ class _GpuTree:
     # with 32-bit integers); larger batches are located slice by slice
     MAX_CALL_POINTS = 1 << 29
 
-    def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None) -> None:
-        """Enqueue point location on the current stream (no synchronisation)."""
+    # -- launch shapes (autotune.py) ------------------------------------------
+    def gpu(self) -> str:
+        if self._gpu is None:
+            self._gpu = autotune.gpu_name(self.device)
+        return self._gpu
+
+    def tune_key(self, kind: str, n_queries: int) -> str:
+        return autotune.cache_key(kind, self.gpu(), self.n, n_queries, K=self.K)
+
+    def cached(self, kind: str, n_queries: int) -> dict:
+        """Launch shape of `kind` for a batch of n_queries: tuned in this
+        process, else from the cache file, else the library defaults."""
+        key = self.tune_key(kind, n_queries)
+        if key not in self._tuned:
+            self._tuned[key] = autotune.lookup(kind, key)
+        return self._tuned[key]
+
+    def _apply(self, kind: str, cfg: dict) -> None:
+        d = self.desc
+        if kind == "locate":
+            d.tune_cells_bpsm = int(cfg.get("cells_bpsm") or 0)
+            d.tune_fast_bpsm = int(cfg.get("fast_bpsm") or 0)
+        elif kind == "fp64":
+            d.tune_fp64_stack = int(cfg.get("stack") or 0)
+        elif kind in ("boxes", "segments"):
+            d.tune_query_threads = int(cfg.get("threads") or 0)
+
+    @staticmethod
+    def _capturing() -> bool:
+        torch = _device.torch()
+        try:
+            return bool(torch.cuda.is_current_stream_capturing())
+        except Exception:  # pragma: no cover
+            return False
+
+    def maybe_tune(self, kind: str, n_queries: int, run, sample_n: int) -> dict:
+        """The launch shape for a batch of n_queries; tunes it first (timing
+        `run(cfg)` on a sample of sample_n queries) when autotuning is on,
+        the batch is large enough, nothing is cached for its bucket and no
+        stream capture is running."""
+        key = self.tune_key(kind, n_queries)
+        if key in self._tuned:
+            return self._tuned[key]
+        cached_entry = autotune.cache().get(key)
+        if (cached_entry is None and autotune.enabled() and n_queries >= autotune.TUNE_MIN[kind]
+                and not self._capturing()):
+            self._tuned[key] = self.tune(kind, key, run, sample_n)
+        return self.cached(kind, n_queries)
+
+    def tune(self, kind: str, key: str, run, sample_n: int) -> dict:
+        """Coordinate descent over the knobs of `kind` (one knob at a time,
+        the others at their best so far), timing run(cfg) on the sample;
+        stores the best in the cache and returns it merged over the defaults."""
+        cfg = dict(autotune.DEFAULTS[kind])
+        if kind == "locate":
+            cfg["sort_bits"] = self.auto_sort_bits(sample_n)
+        default = dict(cfg)
+        entries = []
+        for knob in sorted(autotune.SPACE[kind]):
+            cands = [dict(cfg, **{knob: v}) for v in autotune.SPACE[kind][knob]]
+            e = autotune.tune(kind, key, run, cands, store=False, default=default)
+            entries.append(e)
+            cfg = dict(e["config"])
+        best_ms = min(e["ms"] for e in entries)
+        d_ms = next((e["default_ms"] for e in entries if e["default_ms"] is not None), None)
+        entry = {"config": cfg, "ms": best_ms, "default_ms": d_ms, "candidates": sum(e["candidates"] for e in entries),
+                 "sample": int(sample_n)}
+        autotune.cache().put(key, entry)
+        merged = dict(autotune.DEFAULTS[kind])
+        merged.update(cfg)
+        return merged
+
+    def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None, config=None) -> None:
+        """Enqueue point location on the current stream (no synchronisation).
+        `config`: launch shape (autotune.DEFAULTS["locate"] keys), else the
+        cached one for this batch size."""
         lib = _lib.load()
         n = int(points_d.shape[0])
         if n > self.MAX_CALL_POINTS:
             for s in range(0, n, self.MAX_CALL_POINTS):
                 e = min(s + self.MAX_CALL_POINTS, n)
-                self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits)
+                self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits, config)
             return
         if precision == "fp32":
+            cfg = config if config is not None else self.cached("locate", n)
+            self._apply("locate", cfg)
+            if sort_bits is None:
+                sort_bits = cfg.get("sort_bits")
             g = self.auto_sort_bits(n) if sort_bits is None else int(sort_bits)
             need = int(lib.ct_locate_workspace_size(n, g))
             ws = getattr(self, "_locate_ws", None)
@@ -239,11 +338,48 @@ class _GpuTree:
             )
             return
         mode = _lib.CT_MODE_FP64 if precision == "fp64" else _lib.CT_MODE_FP32
+        self._apply("fp64", config if config is not None else self.cached("fp64", n))
         _lib.check(
             lib.ct_locate_points(ctypes.byref(self.desc), _device.ptr(points_d), n, float(tolerance), mode,
                                  _device.ptr(out_d), _device.stream()),
             "locate_points",
         )
+
+    def tune_locate(self, points_d, tolerance: float, precision: str = "fp32", n_call: Optional[int] = None) -> dict:
+        """Tune the launch shape of point location now, timing calls on the
+        device points `points_d`, for batches of n_call points (default: as
+        many as points_d holds); returns the cache entry (config, ms,
+        default_ms)."""
+        torch = _device.torch()
+        n = int(points_d.shape[0])
+        out = _device.empty((n,), torch.int64, self.device)
+        kind = "locate" if precision == "fp32" else "fp64"
+        key = self.tune_key(kind, n if n_call is None else n_call)
+        self._tuned[key] = self.tune(kind, key, lambda c: self.locate(points_d, out, tolerance, precision, config=c), n)
+        return autotune.cache().get(key) or {"config": self._tuned[key]}
+
+    def maybe_tune_locate(self, points, tolerance: float, precision: str, n_call: int) -> None:
+        """First-use tuning of point location for batches of n_call points
+        (host or device `points`; a strided sample of at most one call's
+        size is timed on the device)."""
+        kind = "locate" if precision == "fp32" else "fp64"
+        key = self.tune_key(kind, n_call)
+        if (key in self._tuned or not autotune.enabled() or n_call < autotune.TUNE_MIN[kind] or self._capturing()
+                or autotune.cache().get(key) is not None):
+            return
+        torch = _device.torch()
+        m = min(int(points.shape[0]), n_call if kind == "locate" else autotune.SAMPLE_MAX[kind])
+        step = max(1, int(points.shape[0]) // max(m, 1))
+        if isinstance(points, torch.Tensor):
+            sample = points[::step][:m].contiguous()
+        else:
+            sample = torch.as_tensor(np.ascontiguousarray(points[::step][:m]), device=self.device)
+        self.tune_locate(sample, tolerance, precision, n_call=n_call)
+
+    def rebuild_index(self, density: float) -> None:
+        """Rebuild the start-node grid and candidate lists at `density` grid
+        cells per mesh cell (speed only; results never change)."""
+        self._build_index(density)
 
     # -- multi-result helpers ------------------------------------------------
     def scan(self, counts):
@@ -266,11 +402,12 @@ class _GpuTree:
     # (below it the ordering's fixed cost outweighs the better warp balance)
     WORK_ORDER_MIN = 65536
 
-    def work_order(self, q_d, kind: int):
+    def work_order(self, q_d, kind: int, force=None):
         """Permutation grouping box (kind 0) / segment (kind 1) queries of
-        similar size, or None for small batches."""
+        similar size, or None for small batches (`force` True / False
+        overrides the size rule)."""
         n = int(q_d.shape[0])
-        if n < self.WORK_ORDER_MIN:
+        if force is False or (force is None and n < self.WORK_ORDER_MIN):
             return None
         torch = _device.torch()
         lib = _lib.load()
@@ -282,14 +419,41 @@ class _GpuTree:
                                      _device.stream()), "work order")
         return order
 
-    def locate_boxes(self, boxes_d):
+    def ensure_box_index(self):
+        """Build the box index of the multi-result queries on first use (cell
+        boxes in leaf order, node bounding boxes and leaf ranges)."""
+        if self.desc.node_box or not self.desc.bounds_finite or self.n == 0:
+            return
+        torch = _device.torch()
+        lib = _lib.load()
+        self.bb_leaf = _device.empty((self.n, 4), torch.float64, self.device)
+        self.node_box = _device.empty((self.n_nodes, 8), torch.int32, self.device)
+        self.leaf_start = _device.empty((self.n,), torch.int32, self.device)
+        d = self.desc
+        d.bb_leaf = _device.ptr(self.bb_leaf)
+        d.node_box = _device.ptr(self.node_box)
+        d.leaf_start = _device.ptr(self.leaf_start)
+        nbytes = int(lib.ct_box_index_scratch_size(ctypes.byref(d)))
+        scratch = _device.empty((max(nbytes, 1),), torch.uint8, self.device)
+        status = lib.ct_pack_box_index(ctypes.byref(d), _device.ptr(scratch), nbytes, _device.stream())
+        if status != _lib.CT_OK:
+            d.bb_leaf = d.node_box = d.leaf_start = None
+            _lib.check(status, "box index")
+
+    def locate_boxes(self, boxes_d, config=None):
+        n = int(boxes_d.shape[0])
+        if config is None:
+            m = min(n, autotune.SAMPLE_MAX["boxes"])
+            step = max(1, n // max(m, 1))
+            config = self.maybe_tune("boxes", n, lambda c: self.locate_boxes(boxes_d[::step][:m].contiguous(), c), m)
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
-        n = int(boxes_d.shape[0])
         counts = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
-        order = self.work_order(boxes_d, 0)
+        self.ensure_box_index()
+        self._apply("boxes", config)
+        order = self.work_order(boxes_d, 0, config.get("work_order"))
         _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
                                       _device.ptr(counts), st), "locate_boxes")
         offsets, total = self.scan(counts)
@@ -303,16 +467,24 @@ class _GpuTree:
         self.raise_on_device_error()
         return ii, jj
 
-    def locate_edges(self, segs_d, mode: int):
+    def locate_edges(self, segs_d, mode: int, config=None):
         """Candidates (traversal) -> float64 cell test per candidate -> hits
         in candidate order -> per-segment sort by t; returns ii, jj, xy (R, 2, 2)."""
+        n = int(segs_d.shape[0])
+        if config is None:
+            m = min(n, autotune.SAMPLE_MAX["segments"])
+            step = max(1, n // max(m, 1))
+            config = self.maybe_tune("segments", n,
+                                     lambda c: self.locate_edges(segs_d[::step][:m].contiguous(), mode, c), m)
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
-        n = int(segs_d.shape[0])
         ccnt = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
-        order = self.work_order(segs_d, 1)
+        if mode == 1:
+            self.ensure_box_index()
+        self._apply("segments", config)
+        order = self.work_order(segs_d, 1, config.get("work_order"))
         P = _device.ptr
         _lib.check(lib.ct_count_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(ccnt), st),
                    "intersect_edges")
@@ -349,6 +521,26 @@ class _GpuTree:
             jj, xy = jj2, xy2
         self.raise_on_device_error()
         return ii, jj, xy
+
+    # pairs from which the per-pair kernels run grouped by polygon lengths
+    PAIR_ORDER_MIN = 65536
+
+    def pair_order(self, fa, Ka: int, ia, fb, Kb: int, ib):
+        """Processing order of the per-pair kernels (pairs of equal polygon
+        lengths side by side), or None when every pair has the same lengths
+        or the batch is small."""
+        n = int(ib.shape[0])
+        uniform = Kb <= 3 and (fa is None or Ka <= 3)  # boxes have 4 vertices, triangles 3
+        if n < self.PAIR_ORDER_MIN or uniform:
+            return None
+        torch = _device.torch()
+        lib = _lib.load()
+        nbytes = int(lib.ct_pair_order_workspace_size(n))
+        ws = _device.empty((nbytes,), torch.uint8, self.device)
+        order = _device.empty((n,), torch.int32, self.device)
+        _lib.check(lib.ct_pair_order(_device.ptr(fa), Ka, _device.ptr(ia), _device.ptr(fb), Kb, _device.ptr(ib), n,
+                                     _device.ptr(order), _device.ptr(ws), nbytes, _device.stream()), "pair order")
+        return order
 
     def compact(self, ii, jj, area=None, flag=None):
         """Keep pairs with area > 0 (or flag != 0)."""

@@ -7,6 +7,7 @@
 #include <cfloat>
 
 #include "ct_common.cuh"
+#include "ct_locf.cuh"
 
 __device__ __forceinline__ double dnan() { return __longlong_as_double(0x7ff8000000000000ll); }
 
@@ -412,29 +413,70 @@ __device__ __forceinline__ bool g_zero_edge(dpt a, dpt b) {
            g_eq_finite(a.y, b.y);
 }
 
+// Float32 local coordinates of a float64 point: v - o in a frame at the
+// point split in O (each coordinate split exactly into float hi + lo), with
+// the per-component error bound folded into *ed (a running maximum).
+__device__ __forceinline__ float2 g_local(dpt v, const PtSplit& O, float* ed) {
+    PtSplit P = split_point(v.x, v.y);
+    float dx, dy, e;
+    local_delta(P, make_float4(O.xh, O.xl, O.yh, O.yl), &dx, &dy, &e);
+    *ed = fmaxf(*ed, e);
+    return make_float2(dx, dy);
+}
+
 __device__ __forceinline__ double clip_area_conv(const dpt* polygon, int n_poly, const dpt* clipper, int n_clip,
                                                  dpt* bufA, dpt* bufB, bool* overflow) {
     static_assert(CT_CLIP_MAX <= 64, "vertex masks are 64-bit");
+    const float u24 = 5.9604644775390625e-08f;  // 2^-24
     dpt* output = bufA;
     const dpt* subject = polygon;  // the first clip edge reads the polygon in place
     int n_output = n_poly;
     unsigned short xs[CT_CLIP_MAX];  // crossings: step j | last kept step << 6 (slot in xslot)
     unsigned char xslot[CT_CLIP_MAX];
+    // float32 local coordinates (frame at the first clipper vertex) of the
+    // subject, output and clipper vertices, for the filtered inside test
+    float2 fP[CT_MAX_N_VERTEX], fA[CT_CLIP_MAX], fB[CT_CLIP_MAX], fC[CT_MAX_N_VERTEX];
+    float ed = 0.0f;
+    const PtSplit O = split_point(clipper[0].x, clipper[0].y);
+    for (int k = 0; k < n_clip; k++) fC[k] = g_local(clipper[k], O, &ed);
+    for (int k = 0; k < n_poly; k++) fP[k] = g_local(polygon[k], O, &ed);
+    const float2* fsub = fP;
+    float2* fout = fA;
     dpt r = clipper[n_clip - 1];
+    float2 fr = fC[n_clip - 1];
     for (int i = 0; i < n_clip; i++) {
         dpt s = clipper[i];
         dpt U = mkp(s.x - r.x, s.y - r.y);
         if (g_zero(U.x) && g_zero(U.y)) continue;
         dpt N = mkp(-U.y, U.x);
         int length = n_output;
-        // 1. inside flags and zero-length steps
+        // float32 U and its error against the float64 U
+        const float2 fs = fC[i];
+        const float ufx = fs.x - fr.x, ufy = fs.y - fr.y;
+        const float eU = 2.0f * ed + 2.0f * u24 * fmaxf(fabsf(ufx), fabsf(ufy));
+        const float Nu = fabsf(ufx) + fabsf(ufy) + 2.0f * eU;
+        // 1. inside flags and zero-length steps.  The inside test is decided
+        // in float32 when its margin clears the float32 error and the float64
+        // rounding of both products; otherwise in float64 as upstream.
         unsigned long long inside = 0ull, skip = 0ull;
         dpt prev = subject[length - 1];
         for (int j = 0; j < length; j++) {
             dpt b = subject[j];
-            double lhs = U.x * (b.y - r.y);
-            double rhs = U.y * (b.x - r.x);
-            if (g_gt(lhs, rhs)) inside |= 1ull << j;
+            const float2 fb = fsub[j];
+            float wx = fb.x - fr.x, wy = fb.y - fr.y;
+            float ew = 2.0f * ed + u24 * fmaxf(fabsf(wx), fabsf(wy));
+            float M = fmaxf(fabsf(wx), fabsf(wy)) + ew;
+            float est = ufx * wy - ufy * wx;
+            float thr = 1.02f * (2.0f * eU * M + Nu * ew + 4.0f * u24 * Nu * M + 2.2204461e-16f * Nu * M) + 1e-37f;
+            bool in;
+            if (fabsf(est) > thr) {
+                in = est > 0.0f;
+            } else {
+                double lhs = U.x * (b.y - r.y);
+                double rhs = U.y * (b.x - r.x);
+                in = g_gt(lhs, rhs);
+            }
+            if (in) inside |= 1ull << j;
             if (g_zero_edge(prev, b)) skip |= 1ull << j;
             prev = b;
         }
@@ -452,7 +494,10 @@ __device__ __forceinline__ double clip_area_conv(const dpt* polygon, int n_poly,
                 n_out++;
             }
             if (b_in) {
-                if (n_out < CT_CLIP_MAX) output[n_out] = subject[j];
+                if (n_out < CT_CLIP_MAX) {
+                    output[n_out] = subject[j];
+                    fout[n_out] = fsub[j];
+                }
                 n_out++;
             }
             a_in = b_in;
@@ -469,13 +514,18 @@ __device__ __forceinline__ double clip_area_conv(const dpt* polygon, int n_poly,
             if (!g_zero(nv)) {
                 double t = nw / nv;
                 int slot = xslot[k];
-                if (slot < CT_CLIP_MAX) output[slot] = mkp(a.x + t * V.x, a.y + t * V.y);
+                dpt pnt = mkp(a.x + t * V.x, a.y + t * V.y);
+                if (slot < CT_CLIP_MAX) {
+                    output[slot] = pnt;
+                    fout[slot] = g_local(pnt, O, &ed);
+                }
             } else {
                 fail = true;
             }
         }
         if (fail) {
             n_out = sh_clip_edge_seq(subject, length, output, r, U, N);
+            for (int k = 0; k < n_out; k++) fout[k] = g_local(output[k], O, &ed);
         } else if (n_out > CT_CLIP_MAX) {
             n_out = -1;
         }
@@ -487,8 +537,11 @@ __device__ __forceinline__ double clip_area_conv(const dpt* polygon, int n_poly,
         if (n_output < 3) return 0.0;
         // the output becomes the next subject
         subject = output;
+        fsub = fout;
         output = (output == bufA) ? bufB : bufA;
+        fout = (fout == fA) ? fB : fA;
         r = s;
+        fr = fs;
     }
     return polygon_area(subject, n_output);
 }

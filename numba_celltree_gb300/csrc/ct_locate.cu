@@ -363,8 +363,8 @@ constexpr int RES_OPEN = INT32_MIN;  // sorted-order result of a query left open
 // bucketed scatter takes them to `out`), else straight to out[oi].
 // 6 blocks of 256 threads per SM (40 registers): measured faster than the
 // 48-register build at 5 blocks despite a few spilled values.
-template <int KT, bool MULTI>
-__global__ void __launch_bounds__(LOC_THREADS, 6)
+template <int KT, bool MULTI, int MINB = 6>
+__global__ void __launch_bounds__(LOC_THREADS, MINB)
     k_cells(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
             const double2* __restrict__ pts, const int* __restrict__ order, int64_t n, int64_t* __restrict__ out,
             int* __restrict__ res_sorted, int* __restrict__ qlist, int* __restrict__ qcount) {
@@ -1609,13 +1609,29 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     const bool lists = T.coff != nullptr;
     const int* qlist = lists ? L.open : nullptr;
     const int* qcount = lists ? &L.counters[3] : nullptr;
-    unsigned grid_b = lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16) : grid;
+    const int cells_bpsm = t->tune_cells_bpsm;
+    int sms = 152;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int fast_bpsm = (t->tune_fast_bpsm >= 1 && t->tune_fast_bpsm <= 32) ? t->tune_fast_bpsm : 16;
+    unsigned grid_b =
+        lists ? (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, (int64_t)sms * fast_bpsm) : grid;
     // many sorted queries: list results by sorted position, then one bucketed scatter
     int* res_sorted = (lists && ord && n > RES_SCATTER_MIN) ? sorted_results(L) : nullptr;
 #define CT_FAST_STAGES(KT)                                                                                        \
-    if (lists)                                                                                                     \
-        k_cells<KT, false><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,          \
-                                                         L.open, &L.counters[3]);                                  \
+    if (lists) {                                                                                                   \
+        if (cells_bpsm == 4)                                                                                       \
+            k_cells<KT, false, 4><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,   \
+                                                                L.open, &L.counters[3]);                           \
+        else if (cells_bpsm == 8)                                                                                  \
+            k_cells<KT, false, 8><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,   \
+                                                                L.open, &L.counters[3]);                           \
+        else                                                                                                       \
+            k_cells<KT, false, 6><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,   \
+                                                                L.open, &L.counters[3]);                           \
+    }                                                                                                              \
     smem_attr<KT, false>(smem);                                                                                    \
     k_fast<KT, false><<<grid_b, LOC_THREADS, smem, st>>>(T, nullptr, nullptr, P, ord, n, out, L.R, L.counters,    \
                                                          L.ovf, qlist, qcount);
@@ -1776,13 +1792,24 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
     memset(&T0, 0, sizeof(T0));
     size_t smem = (size_t)plan->stack * LOC_THREADS * sizeof(int);
     unsigned grid = (unsigned)((n + LOC_THREADS - 1) / LOC_THREADS);
-    unsigned grid_b = (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, 152 * 16);
+    int sms = 152;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int fast_bpsm = (plan->tune_fast_bpsm >= 1 && plan->tune_fast_bpsm <= 32) ? plan->tune_fast_bpsm : 16;
+    const int cells_bpsm = plan->tune_cells_bpsm;
+    unsigned grid_b = (unsigned)std::min<int64_t>((n + LOC_THREADS - 1) / LOC_THREADS, (int64_t)sms * fast_bpsm);
     // queries are sorted by tree first: one tree's results land in its own
     // range of `out`, so only a tree with many queries needs the scatter
     int* res_sorted = plan->max_tree_points > RES_SCATTER_MIN ? sorted_results(L) : nullptr;
 #define CT_FOREST_STAGES(KT)                                                                                      \
-    k_cells<KT, true><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, res_sorted,        \
-                                                    L.open, &L.counters[3]);                                     \
+    if (cells_bpsm == 8)                                                                                          \
+        k_cells<KT, true, 8><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, res_sorted, \
+                                                           L.open, &L.counters[3]);                              \
+    else                                                                                                          \
+        k_cells<KT, true, 6><<<grid, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, res_sorted, \
+                                                           L.open, &L.counters[3]);                              \
     k_fast<KT, true><<<grid_b, LOC_THREADS, smem, st>>>(T0, F.trees, F.qtree, P, L.order, n, out, L.R,          \
                                                         L.counters, L.ovf, L.open, &L.counters[3]);              \
     k_pip<true><<<GRID_STRIDE, LOC_THREADS, 0, st>>>(T0, F.trees, F.qtree, P, L.R, L.counters);                  \

@@ -6,12 +6,14 @@
 // count and write kernels run the same traversal, so the write pass knows
 // each query's output offset.  Results come out query-major and, within a
 // query, in traversal order -- exactly upstream's concatenated order.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 
 #include "ct_common.cuh"
 #include "ct_geom.cuh"
 #include "ct_internal.h"
+#include "ct_locf.cuh"
 
 extern "C" size_t ct_radix_pass_workspace_size(void);
 extern "C" int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift, unsigned* kout, int* iout,
@@ -31,6 +33,18 @@ struct TreeQ {
     dbox bbox;
     int K;
     bool finite;  // all node bounds and cell boxes finite: order comparisons on integer keys
+    // box index (ct_pack_box_index; null when not built)
+    const double4* bbl;        // cell boxes in leaf order
+    const struct NodeBox* nbx; // per node: bounding box of its cells (float32 frame, outward) and leaf range
+    const int* lstart;         // per leaf position: first position of its leaf
+    double ox, oy;             // float32 frame origin
+};
+
+// Bounding box of a node's cells in the float32 frame of the tree (x - ox,
+// y - oy rounded outward) and the node's range of leaf positions.  32 bytes.
+struct NodeBox {
+    float xmin, xmax, ymin, ymax;
+    int ptr, size, pad0, pad1;
 };
 
 // x < y for finite (or infinite, non-NaN) doubles as one 64-bit integer
@@ -48,6 +62,21 @@ __device__ __forceinline__ int na(const float4& q) { return __float_as_int(q.z);
 __device__ __forceinline__ int nb(const float4& q) { return __float_as_int(q.w); }
 
 constexpr int STK = 128;  // traversal stack (tree depth + 2 must fit; checked on the host)
+
+// bb_coords of the cell at leaf position j: from the leaf-ordered copy of the
+// box index when it is built, else through bb_indices
+__device__ __forceinline__ dbox leaf_box(const TreeQ& T, int64_t j) {
+    if (T.bbl) {
+        double4 c4 = T.bbl[j];
+        dbox b;
+        b.xmin = c4.x;
+        b.xmax = c4.y;
+        b.ymin = c4.z;
+        b.ymax = c4.w;
+        return b;
+    }
+    return load_box(T.bb + 4 * T.bbi[j]);
+}
 
 // ---------------------------------------------------------------------------
 // locate_box query.py:177-244
@@ -72,6 +101,19 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
     // float64 ones (NaN boxes keep the float64 comparisons)
     const bool keys = T.finite && not_nan(box.xmin) && not_nan(box.xmax) && not_nan(box.ymin) && not_nan(box.ymax);
     const unsigned long long kx0 = fkey(box.xmin), kx1 = fkey(box.xmax), ky0 = fkey(box.ymin), ky1 = fkey(box.ymax);
+    // box index: a node whose cells' bounding box lies strictly inside the
+    // query box has every cell overlapping it (boxes_intersect is strict and
+    // cell.xmax >= node.xmin > box.xmin, ...); the traversal would visit all
+    // of it.  The query box in the float32 frame is rounded inward, the node
+    // boxes outward, so a float32 "strictly inside" implies the float64 one.
+    const bool idx = keys && T.nbx != nullptr;
+    float qx0 = 0.0f, qx1 = 0.0f, qy0 = 0.0f, qy1 = 0.0f;
+    if (idx) {
+        qx0 = __double2float_ru(box.xmin - T.ox);
+        qx1 = __double2float_rd(box.xmax - T.ox);
+        qy0 = __double2float_ru(box.ymin - T.oy);
+        qy1 = __double2float_rd(box.ymax - T.oy);
+    }
     if (boxes_intersect(box, T.bbox)) {
         int st[STK];
         int sp = 1;
@@ -83,13 +125,39 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                 break;
             }
             int v = st[--sp];
+            if (idx) {
+                const NodeBox nbv = T.nbx[v];
+                if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
+                    // the whole subtree, in upstream's visiting order: right
+                    // child first, i.e. leaves by decreasing position, each
+                    // leaf's cells by increasing position
+                    if (WRITE) {
+                        int q = nbv.ptr + nbv.size;
+                        int64_t c = count;
+                        while (q > nbv.ptr) {
+                            int s = T.lstart[q - 1];
+                            if (s < nbv.ptr || s >= q) {  // corrupt index: stop rather than loop
+                                set_error(T.err, CT_DEVERR_LOOP);
+                                break;
+                            }
+                            for (int j = s; j < q; j++) {
+                                ii[base + c] = i;
+                                jj[base + c] = T.bbi[j];
+                                c++;
+                            }
+                            q = s;
+                        }
+                    }
+                    count += nbv.size;
+                    continue;
+                }
+            }
             float4 q = T.nf[v];
             int b = nb(q);
             if (b >= 0) {
                 int ptr = na(q);
                 for (int j = ptr; j < ptr + b; j++) {
-                    int64_t cell = T.bbi[j];
-                    dbox lb = load_box(T.bb + 4 * cell);
+                    dbox lb = leaf_box(T, j);
                     // boxes_intersect geometry_utils.py:292-300
                     bool hit = keys ? (kx0 < fkey(lb.xmax) && fkey(lb.xmin) < kx1 && ky0 < fkey(lb.ymax) &&
                                        fkey(lb.ymin) < ky1)
@@ -97,7 +165,7 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                     if (hit) {
                         if (WRITE) {
                             ii[base + count] = i;
-                            jj[base + count] = cell;
+                            jj[base + count] = T.bbi[j];
                         }
                         count++;
                     }
@@ -192,7 +260,7 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
                 for (int j = ptr; j < ptr + bq; j++) {
                     bool cand = true;
                     if (MODE == 1) {
-                        dbox bx = load_box(T.bb + 4 * T.bbi[j]);
+                        dbox bx = leaf_box(T, j);
                         int k1, k2;
                         if (keys) {
                             unsigned long long x0 = fkey(bx.xmin), x1 = fkey(bx.xmax), y0 = fkey(bx.ymin),
@@ -281,7 +349,7 @@ __global__ void __launch_bounds__(128) k_edge_test(TreeQ T, const double4* __res
             c = mkp(x, y);
             d = c;
         } else {
-            dbox bx = load_box(T.bb + 4 * T.bbi[j]);
+            dbox bx = leaf_box(T, j);
             int rr = cohen_sutherland(a, b, bx, &c, &d);
             if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
             hit = rr == 1;
@@ -530,6 +598,90 @@ __device__ __forceinline__ int load_poly(const double* __restrict__ v, const int
     return gather_polygon(v, faces + f * K, K, out);
 }
 
+// Float32 filter of polygons_intersect (separating_axis.py:17-75).
+//
+// For the axis of edge p -> q the upstream test compares float64
+// projections v . n with n = (p.y - q.y, q.x - p.x) (both float64).  Each
+// projection is within D = 2u(1+u) |v|max (|n.x| + |n.y|) (u = 2^-53) of the
+// exact projection on that same n, so a comparison of a maximum with a
+// minimum whose exact values differ by more than 2D has the float64 outcome
+// of the exact one.  Here the projections are evaluated in float32 in a frame
+// at the first vertex of a (each coordinate split exactly into float hi + lo,
+// as the leaf filter does), within E of the exact ones (error terms of the
+// local coordinates, of n and of the float32 dot products).  An axis whose
+// two comparisons clear 2(D + E) is decided: separating or not.  Any
+// decided separating axis makes the answer false (upstream stops at the
+// first separating axis, but the answer is the same boolean); all axes
+// decided and none separating makes it true; otherwise the float64 test runs.
+// Returns 0 / 1 for a decided answer, 2 when undecided.
+template <int KA, int KB>
+__device__ __forceinline__ int sat_filter(const dpt* a, int la, const dpt* b, int lb) {
+    constexpr int KM = KA + KB;
+    const float u32 = 5.9604644775390625e-08f;  // 2^-24
+    float dx[KM], dy[KM];
+    float vmax = 0.0f, dmax = 0.0f, ed = 0.0f;
+    PtSplit O = split_point(a[0].x, a[0].y);
+    bool finite = true;
+#pragma unroll
+    for (int j = 0; j < KM; j++) {
+        if (j < KA ? j < la : (j - KA) < lb) {
+            dpt v = j < KA ? a[j] : b[j - KA];
+            finite = finite && g_finite(v.x) && g_finite(v.y);
+            PtSplit P = split_point(v.x, v.y);
+            float4 o = make_float4(O.xh, O.xl, O.yh, O.yl);
+            float e;
+            local_delta(P, o, &dx[j], &dy[j], &e);
+            ed = fmaxf(ed, e);
+            dmax = fmaxf(dmax, fmaxf(fabsf(dx[j]), fabsf(dy[j])));
+            vmax = fmaxf(vmax, fmaxf(fabsf(P.xh), fabsf(P.yh)));
+        } else {
+            dx[j] = dy[j] = 0.0f;
+        }
+    }
+    if (!finite) return 2;
+    vmax *= 1.0000003f;
+    dmax += ed;
+    bool undecided = false;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+        const int base = side ? KA : 0, len = side ? lb : la;
+        const int KS = side ? KB : KA;
+#pragma unroll
+        for (int i = 0; i < KS; i++) {
+            if (i >= len) break;
+            const int ip = (i == 0) ? base + len - 1 : base + i - 1, iq = base + i;
+            dpt p = side ? b[ip - KA] : a[ip], q = side ? b[iq - KA] : a[iq];
+            if (g_zero_edge(p, q)) continue;  // norm == (0, 0): upstream skips the axis
+            float nx = dy[ip] - dy[iq], ny = dx[iq] - dx[ip];
+            float nm = fabsf(nx) + fabsf(ny);
+            float en = 2.0f * ed + 2.0f * u32 * fmaxf(fabsf(nx), fabsf(ny));
+            float mina = 3.0e38f, maxa = -3.0e38f, minb = 3.0e38f, maxb = -3.0e38f;
+#pragma unroll
+            for (int j = 0; j < KM; j++) {
+                if (j < KA ? j < la : (j - KA) < lb) {
+                    float pr = dx[j] * nx + dy[j] * ny;
+                    if (j < KA) {
+                        mina = fminf(mina, pr);
+                        maxa = fmaxf(maxa, pr);
+                    } else {
+                        minb = fminf(minb, pr);
+                        maxb = fmaxf(maxb, pr);
+                    }
+                }
+            }
+            float E = ed * nm + 2.0f * dmax * en + 4.0f * u32 * dmax * (nm + 2.0f * en);
+            float D = 2.2204461e-16f * 1.0001f * vmax * (nm + 2.0f * en);
+            float thr = 2.03f * (E + D) + 1e-37f;
+            float d1 = maxa - minb, d2 = maxb - mina;
+            bool sure1 = fabsf(d1) * (1.0f - 4.0f * u32) > thr, sure2 = fabsf(d2) * (1.0f - 4.0f * u32) > thr;
+            // separating for sure: one comparison surely false
+            if ((sure1 && d1 < 0.0f) || (sure2 && d2 < 0.0f)) return 0;
+            if (!(sure1 && sure2)) undecided = true;
+        }
+    }
+    return undecided ? 2 : 1;
+}
+
 // polygons_intersect separating_axis.py:58-75
 __global__ void k_sat(const double* __restrict__ va, const int64_t* __restrict__ fa, int Ka,
                       const double* __restrict__ vb, const int64_t* __restrict__ fb, int Kb,
@@ -540,41 +692,62 @@ __global__ void k_sat(const double* __restrict__ va, const int64_t* __restrict__
     dpt a[CT_MAX_N_VERTEX], b[CT_MAX_N_VERTEX];
     int la = load_poly(va, fa, Ka, ia[i], a);
     int lb = load_poly(vb, fb, Kb, ib[i], b);
-    out[i] = (uint8_t)(separating_axes(a, la, b, lb) && separating_axes(b, lb, a, la));
+    int r = 2;
+    if (Ka <= 4 && Kb <= 4) r = sat_filter<4, 4>(a, la, b, lb);
+    else if (Ka <= 8 && Kb <= 8) r = sat_filter<8, 8>(a, la, b, lb);
+    if (r == 2) r = (int)(separating_axes(a, la, b, lb) && separating_axes(b, lb, a, la));
+    out[i] = (uint8_t)r;
 }
 
 // area_of_intersection sutherland_hodgman.py:151-168 (subject: face of a,
 // clipper: face of b)
+// `order`: NULL, or a permutation of the pairs (processing order only:
+// pairs of equal polygon lengths side by side, so a warp's lanes run the
+// same number of clip edges; results stay at their pair's index).
 __global__ void k_clip_area(const double* __restrict__ va, const int64_t* __restrict__ fa, int Ka,
                             const double* __restrict__ vb, const int64_t* __restrict__ fb, int Kb,
                             const int64_t* __restrict__ ia, const int64_t* __restrict__ ib, int64_t n,
-                            double* __restrict__ out, unsigned int* __restrict__ err) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                            const int* __restrict__ order, double* __restrict__ out, unsigned int* __restrict__ err) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int64_t i = order ? (int64_t)order[t] : t;
     dpt a[CT_MAX_N_VERTEX], b[CT_MAX_N_VERTEX];
     dpt A[CT_CLIP_MAX], B[CT_CLIP_MAX];
     int la = load_poly(va, fa, Ka, ia[i], a);
     int lb = load_poly(vb, fb, Kb, ib[i], b);
     bool of = false;
-    out[i] = clip_area(a, la, b, lb, A, B, &of);
+    out[i] = clip_area_conv(a, la, b, lb, A, B, &of);
     if (of) set_error(err, CT_DEVERR_CLIP);
 }
 
 // box_area_of_intersection sutherland_hodgman.py:171-187 (subject: the box)
 __global__ void k_box_area(const double4* __restrict__ boxes, const double* __restrict__ vb,
                            const int64_t* __restrict__ fb, int Kb, const int64_t* __restrict__ ibox,
-                           const int64_t* __restrict__ iface, int64_t n, double* __restrict__ out,
-                           unsigned int* __restrict__ err) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                           const int64_t* __restrict__ iface, int64_t n, const int* __restrict__ order,
+                           double* __restrict__ out, unsigned int* __restrict__ err) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int64_t i = order ? (int64_t)order[t] : t;
     double4 q = boxes[ibox[i]];
     dpt a[4] = {mkp(q.x, q.z), mkp(q.y, q.z), mkp(q.y, q.w), mkp(q.x, q.w)};
     dpt b[CT_MAX_N_VERTEX];
     dpt A[CT_CLIP_MAX], B[CT_CLIP_MAX];
     int lb = load_poly(vb, fb, Kb, iface[i], b);
     bool of = false;
-    out[i] = clip_area(a, 4, b, lb, A, B, &of);
+    out[i] = clip_area_conv(a, 4, b, lb, A, B, &of);
     if (of) set_error(err, CT_DEVERR_CLIP);
+}
+
+// 6-bit class of a pair: the polygon lengths (3 .. 10) of its two faces
+// (fa NULL: boxes, length 4)
+__global__ void k_pair_keys(const int64_t* __restrict__ fa, int Ka, const int64_t* __restrict__ ia,
+                            const int64_t* __restrict__ fb, int Kb, const int64_t* __restrict__ ib, int64_t n,
+                            unsigned* __restrict__ key) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int la = fa ? polygon_length(fa + ia[i] * Ka, Ka) : 4;
+        int lb = polygon_length(fb + ib[i] * Kb, Kb);
+        key[i] = (unsigned)(min(la - 3, 7) * 8 + min(lb - 3, 7));
+    }
 }
 
 // keep = area > 0 (celltree.py:183, 268) or keep = flag
@@ -740,7 +913,97 @@ TreeQ make_q(const ct_tree* t) {
     T.bbox.ymax = t->bbox[3];
     T.K = t->n_max_vert;
     T.finite = t->bounds_finite != 0;
+    const bool box_index = t->node_box && t->leaf_start && t->bb_leaf && T.finite;
+    T.bbl = box_index ? (const double4*)t->bb_leaf : nullptr;
+    T.nbx = box_index ? (const NodeBox*)t->node_box : nullptr;
+    T.lstart = box_index ? t->leaf_start : nullptr;
+    T.ox = t->origin[0];
+    T.oy = t->origin[1];
     return T;
+}
+
+// ---------------------------------------------------------------------------
+// Box index (no upstream counterpart), built once per tree:
+//  * bb_leaf: bb_coords in leaf order (the leaf loop reads them in sequence
+//    instead of through bb_indices);
+//  * leaf_start: for every leaf position the first position of its leaf;
+//  * node_box: per node the bounding box of the cells below it (leaves from
+//    their cells, then up the parent chain with integer-key atomics; a leaf
+//    stops climbing where its box is already covered, since whichever leaf
+//    widened that node carries the wider box further up) and its leaf range.
+// ---------------------------------------------------------------------------
+__global__ void k_bi_leaf_boxes(const int64_t* __restrict__ bbi, const double4* __restrict__ bb, int64_t n,
+                                double4* __restrict__ bbl) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+        bbl[p] = bb[bbi[p]];
+}
+
+__global__ void k_bi_parents(const int64_t* __restrict__ child, int64_t nn, int* __restrict__ parent,
+                             unsigned long long* __restrict__ keys) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn) return;
+    int64_t c = child[v];
+    if (c >= 0 && c + 1 < nn) {
+        parent[c] = (int)v;
+        parent[c + 1] = (int)v;
+    }
+    keys[4 * v + 0] = ~0ull;
+    keys[4 * v + 1] = 0ull;
+    keys[4 * v + 2] = ~0ull;
+    keys[4 * v + 3] = 0ull;
+}
+
+__global__ void k_bi_leaves(const int64_t* __restrict__ child, const int64_t* __restrict__ ptr,
+                            const int64_t* __restrict__ size, int64_t nn, const double4* __restrict__ bbl, int64_t n,
+                            const int* __restrict__ parent, unsigned long long* __restrict__ keys,
+                            int* __restrict__ lstart, unsigned int* __restrict__ err) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn || child[v] >= 0) return;
+    int64_t p0 = ptr[v], sz = size[v];
+    if (p0 < 0 || sz < 0 || p0 + sz > n) {
+        set_error(err, CT_DEVERR_CAPACITY);
+        return;
+    }
+    if (sz == 0) return;
+    unsigned long long x0 = ~0ull, x1 = 0ull, y0 = ~0ull, y1 = 0ull;
+    for (int64_t p = p0; p < p0 + sz; p++) {
+        lstart[p] = (int)p0;
+        double4 b = bbl[p];
+        x0 = min(x0, fkey(b.x));
+        x1 = max(x1, fkey(b.y));
+        y0 = min(y0, fkey(b.z));
+        y1 = max(y1, fkey(b.w));
+    }
+    int u = (int)v;
+    for (int64_t guard = nn; u >= 0 && guard > 0; guard--) {
+        unsigned long long* k = keys + 4 * (int64_t)u;
+        unsigned long long o0 = atomicMin(k + 0, x0), o1 = atomicMax(k + 1, x1);
+        unsigned long long o2 = atomicMin(k + 2, y0), o3 = atomicMax(k + 3, y1);
+        if (o0 <= x0 && o1 >= x1 && o2 <= y0 && o3 >= y1) break;
+        u = parent[u];
+    }
+}
+
+__global__ void k_bi_nodes(const int64_t* __restrict__ ptr, const int64_t* __restrict__ size, int64_t nn,
+                           const unsigned long long* __restrict__ keys, double ox, double oy,
+                           NodeBox* __restrict__ out) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nn) return;
+    NodeBox b;
+    const unsigned long long* k = keys + 4 * v;
+    if (k[0] == ~0ull) {  // no cells: never "inside" a query box
+        b.xmin = b.ymin = __int_as_float(0x7fc00000);
+        b.xmax = b.ymax = __int_as_float(0x7fc00000);
+    } else {
+        b.xmin = __double2float_rd(fkey_inv(k[0]) - ox);
+        b.xmax = __double2float_ru(fkey_inv(k[1]) - ox);
+        b.ymin = __double2float_rd(fkey_inv(k[2]) - oy);
+        b.ymax = __double2float_ru(fkey_inv(k[3]) - oy);
+    }
+    b.ptr = (int)ptr[v];
+    b.size = (int)size[v];
+    b.pad0 = b.pad1 = 0;
+    out[v] = b;
 }
 
 static inline unsigned grid_of(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -778,6 +1041,47 @@ int ct_exclusive_scan(const int64_t* in, int64_t n, int64_t* out, void* ws, size
     return CT_OK;
 }
 
+size_t ct_box_index_scratch_size(const ct_tree* t) {
+    if (!t || t->n_nodes <= 0) return 0;
+    return (size_t)t->n_nodes * (4 * sizeof(unsigned long long) + sizeof(int)) + 256;
+}
+
+int ct_pack_box_index(ct_tree* t, void* scratch, size_t scratch_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
+    if (!t->bb_leaf || !t->node_box || !t->leaf_start) return ct_fail(CT_ERR_ARG, "box index arrays not set");
+    if (t->n_nodes <= 0 || t->n_nodes >= INT32_MAX || t->n_elements >= INT32_MAX)
+        return ct_fail(CT_ERR_ARG, "tree size out of range");
+    if (!scratch || scratch_bytes < ct_box_index_scratch_size(t))
+        return ct_fail(CT_ERR_WORKSPACE, "box index scratch too small");
+    int64_t nn = t->n_nodes, n = t->n_elements;
+    unsigned long long* keys = (unsigned long long*)scratch;
+    int* parent = (int*)(keys + 4 * nn);
+    CT_CUDA(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));
+    if (n > 0) {
+        k_bi_leaf_boxes<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 8), 256, 0, st>>>(
+            t->bb_indices, (const double4*)t->bb_coords, n, (double4*)t->bb_leaf);
+    }
+    k_bi_parents<<<grid_of(nn, 256), 256, 0, st>>>(t->node_child, nn, parent, keys);
+    k_bi_leaves<<<grid_of(nn, 128), 128, 0, st>>>(t->node_child, t->node_ptr, t->node_size, nn,
+                                                  (const double4*)t->bb_leaf, n, parent, keys, t->leaf_start,
+                                                  t->error_word);
+    k_bi_nodes<<<grid_of(nn, 256), 256, 0, st>>>(t->node_ptr, t->node_size, nn, keys, t->origin[0], t->origin[1],
+                                                 (NodeBox*)t->node_box);
+    CT_CHECK_LAUNCH("pack_box_index");
+    return CT_OK;
+}
+
+// block sizes of the traversal kernels (the tree's launch shape, else the defaults)
+static int box_threads(const ct_tree* t) {
+    int b = t->tune_query_threads;
+    return (b == 64 || b == 128 || b == 256) ? b : 256;
+}
+static int seg_threads(const ct_tree* t) {
+    int b = t->tune_query_threads;
+    return (b == 64 || b == 128) ? b : 128;
+}
+
 static int check_tree(const ct_tree* t) {
     if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
     if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
@@ -790,7 +1094,8 @@ int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
-    k_boxes<false><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
+    const int bt = box_threads(t);
+    k_boxes<false><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
                                                                        counts, nullptr, nullptr);
     CT_CHECK_LAUNCH("count_boxes");
     return CT_OK;
@@ -801,7 +1106,8 @@ int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
-    k_boxes<true><<<grid_of(n, 256), 256, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
+    const int bt = box_threads(t);
+    k_boxes<true><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
                                                                       (int64_t*)offsets, ii, jj);
     CT_CHECK_LAUNCH("write_boxes");
     return CT_OK;
@@ -837,24 +1143,55 @@ int ct_polygons_intersect(const double* va, const int64_t* fa, int32_t Ka, const
     return CT_OK;
 }
 
+int ct_area_of_intersection_ordered(const double* va, const int64_t* fa, int32_t Ka, const double* vb,
+                                    const int64_t* fb, int32_t Kb, const int64_t* ia, const int64_t* ib, int64_t n,
+                                    const int32_t* order, double* out, unsigned int* error_word, void* stream) {
+    if (n == 0) return CT_OK;
+    k_clip_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>(va, fa, Ka, vb, fb, Kb, ia, ib, n, order, out,
+                                                                    error_word);
+    CT_CHECK_LAUNCH("area_of_intersection");
+    return CT_OK;
+}
+
 int ct_area_of_intersection(const double* va, const int64_t* fa, int32_t Ka, const double* vb, const int64_t* fb,
                             int32_t Kb, const int64_t* ia, const int64_t* ib, int64_t n, double* out,
                             unsigned int* error_word, void* stream) {
+    return ct_area_of_intersection_ordered(va, fa, Ka, vb, fb, Kb, ia, ib, n, nullptr, out, error_word, stream);
+}
+
+int ct_box_area_of_intersection_ordered(const double* boxes, const double* vb, const int64_t* fb, int32_t Kb,
+                                        const int64_t* ibox, const int64_t* iface, int64_t n, const int32_t* order,
+                                        double* out, unsigned int* error_word, void* stream) {
     if (n == 0) return CT_OK;
-    k_clip_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>(va, fa, Ka, vb, fb, Kb, ia, ib, n, out,
-                                                                    error_word);
-    CT_CHECK_LAUNCH("area_of_intersection");
+    k_box_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>((const double4*)boxes, vb, fb, Kb, ibox, iface, n,
+                                                                   order, out, error_word);
+    CT_CHECK_LAUNCH("box_area_of_intersection");
     return CT_OK;
 }
 
 int ct_box_area_of_intersection(const double* boxes, const double* vb, const int64_t* fb, int32_t Kb,
                                 const int64_t* ibox, const int64_t* iface, int64_t n, double* out,
                                 unsigned int* error_word, void* stream) {
+    return ct_box_area_of_intersection_ordered(boxes, vb, fb, Kb, ibox, iface, n, nullptr, out, error_word, stream);
+}
+
+size_t ct_pair_order_workspace_size(int64_t n) {
+    size_t part = ((size_t)(n > 0 ? n : 1) * sizeof(unsigned) + 255) / 256 * 256;
+    return 2 * part + ct_radix_pass_workspace_size();
+}
+
+int ct_pair_order(const int64_t* fa, int32_t Ka, const int64_t* ia, const int64_t* fb, int32_t Kb, const int64_t* ib,
+                  int64_t n, int32_t* order, void* ws, size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n < 0 || n > INT32_MAX) return ct_fail(CT_ERR_ARG, "pair count out of range");
+    if (!ws || ws_bytes < ct_pair_order_workspace_size(n)) return ct_fail(CT_ERR_WORKSPACE, "pair order workspace");
     if (n == 0) return CT_OK;
-    k_box_area<<<grid_of(n, 128), 128, 0, (cudaStream_t)stream>>>((const double4*)boxes, vb, fb, Kb, ibox, iface, n,
-                                                                   out, error_word);
-    CT_CHECK_LAUNCH("box_area_of_intersection");
-    return CT_OK;
+    size_t part = ((size_t)n * sizeof(unsigned) + 255) / 256 * 256;
+    unsigned* kin = (unsigned*)ws;
+    unsigned* kout = (unsigned*)((char*)ws + part);
+    k_pair_keys<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 8), 256, 0, st>>>(fa, Ka, ia, fb, Kb, ib, n, kin);
+    CT_CHECK_LAUNCH("pair keys");
+    return ct_radix_pass(kin, nullptr, n, 0, kout, order, (char*)ws + 2 * part, ws_bytes - 2 * part, stream);
 }
 
 int ct_compact_pairs(const double* area, const uint8_t* flag, int64_t n, const int64_t* ii, const int64_t* jj,
@@ -947,10 +1284,11 @@ int ct_count_edge_candidates(const ct_tree* t, int32_t mode, const double* segs,
     if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
+    const int et = seg_threads(t);
     if (mode == 0)
-        k_edge_cands<false, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
+        k_edge_cands<false, 0><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
     else
-        k_edge_cands<false, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
+        k_edge_cands<false, 1><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
     CT_CHECK_LAUNCH("count_edge_candidates");
     return CT_OK;
 }
@@ -963,11 +1301,12 @@ int ct_write_edge_candidates(const ct_tree* t, int32_t mode, const double* segs,
     if (n > INT32_MAX) return ct_fail(CT_ERR_ARG, "at most 2^31 - 1 segments");
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
+    const int et = seg_threads(t);
     if (mode == 0)
-        k_edge_cands<true, 0><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
+        k_edge_cands<true, 0><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
                                                                cand_seg, cand_pos);
     else
-        k_edge_cands<true, 1><<<grid_of(n, 128), 128, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
+        k_edge_cands<true, 1><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
                                                                cand_seg, cand_pos);
     CT_CHECK_LAUNCH("write_edge_candidates");
     return CT_OK;

@@ -646,11 +646,13 @@ int ct_pack_tree(ct_tree* t, void* stream) {
     return CT_OK;
 }
 
+// traversal stack of the float64 / in-line float32 forms: the tree's launch
+// shape when it fits the tree, else the smallest stack that does
 static int stack_for(const ct_tree* t) {
     int need = t->max_depth + 2;
-    if (need <= 64) return 64;
-    if (need <= 512) return 512;
-    return -1;
+    if (need > 512) return -1;
+    if (t->tune_fp64_stack == 512) return 512;
+    return need <= 64 ? 64 : 512;
 }
 
 int ct_locate_points(const ct_tree* t, const double* points, int64_t n, double tol, int32_t mode, int64_t* out,

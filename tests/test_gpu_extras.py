@@ -217,6 +217,15 @@ def test_pair_areas_on_degenerate_polygons_match_oracle(oracle):
         assert lib.ct_area_of_intersection(P(d["xy"]), P(d["fa"]), K, P(d["xy"]), P(d["fb"]), K, P(d["ia"]),
                                            P(d["ib"]), len(ia), P(got), P(err), _device.stream()) == 0
         assert np.array_equal(got.cpu().numpy(), exp, equal_nan=True), grid
+        # polygons_intersect (the float32-filtered separating-axis test):
+        # grid polygons touch exactly along edges and at vertices
+        exp_sat = np.empty(len(ia), dtype=np.uint8)
+        O.lib().cto_polygons_intersect(xy.ctypes.data, xy.ctypes.data, fa.ctypes.data, K, fb.ctypes.data, K,
+                                       ia.ctypes.data, ib.ctypes.data, len(ia), exp_sat.ctypes.data)
+        sat = torch.empty(len(ia), dtype=torch.uint8, device="cuda")
+        assert lib.ct_polygons_intersect(P(d["xy"]), P(d["fa"]), K, P(d["xy"]), P(d["fb"]), K, P(d["ia"]),
+                                         P(d["ib"]), len(ia), P(sat), _device.stream()) == 0
+        assert np.array_equal(sat.cpu().numpy(), exp_sat), grid
         # boxes as subjects
         lo = rng.integers(0, grid, size=(3000, 2)) * scale + 0.25 * scale
         hi = lo + rng.integers(0, 3, size=(3000, 2)) * scale
