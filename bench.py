@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=4 * 1024 * 1024)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-queries", action="store_true", help="skip the per-query suite of the default run")
     ap.add_argument("--profile", action="store_true", help="small fixed run for ncu captures")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "queries"],
                     help="batch: 512 meshes built and queried together; queries: every query on the "
@@ -360,12 +361,15 @@ def run_batch(args):
     print(json.dumps(res))
 
 
-def run_queries(args):
-    """Side measurement: build and every query on the C1 / C2 / C4 shapes and the
-    segments on the 16M-triangle mesh, GPU
-    (device-resident inputs, wall time around synchronised calls) against the
-    oracle (C restatement, OpenMP, all host cores) on a bounded sample, with
-    the GPU result checked on that sample."""
+def query_suite(args, c5=None, verbose=False):
+    """Build and every query on the survey shapes (C1: 80k triangles, C2: the
+    mixed 5M-cell mesh, C4: the regridding pair, C5: segments on the
+    16M-triangle mesh, `c5` = (xy, faces, tree) when already built), GPU
+    (device-resident inputs, wall time around synchronised calls, best of 3
+    after a warm-up call) against the oracle (C restatement, OpenMP, all host
+    cores) on a bounded sample, with the GPU result checked on that sample.
+    Per row: result count, ms, algorithmic bytes (per query and per result)
+    over time as a fraction of the measured HBM bandwidth, speed-up."""
     import torch
 
     from numba_celltree_gb300 import CellTree2d
@@ -374,16 +378,20 @@ def run_queries(args):
 
     O.build()
     dev = torch.device("cuda", 0)
-    lines = []
+    peak, _ = peaks()
+    rows = []
 
     def wall(fn, reps=3):
         fn()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        best = None
         for _ in range(reps):
+            t0 = time.perf_counter()
             r = fn()
-        torch.cuda.synchronize()
-        return r, (time.perf_counter() - t0) / reps
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return r, best
 
     def cpu(fn):
         t0 = time.perf_counter()
@@ -395,125 +403,137 @@ def run_queries(args):
             return tuple(host(y) for y in x)
         return x.cpu().numpy() if hasattr(x, "cpu") else x
 
-    def record(cfg, query, n, unit, gpu_s, m, cpu_s, same):
-        line = {"config": cfg, "query": query, "n": n, "unit": unit,
-                "gpu_ms": round(gpu_s * 1e3, 3), "gpu_rate_per_s": round(n / gpu_s, 1),
-                "cpu_sample": m, "cpu_rate_per_s": round(m / cpu_s, 1),
-                "speedup": round((n / gpu_s) / (m / cpu_s), 1), "identical_on_sample": bool(same)}
-        lines.append(line)
-        print(json.dumps(line), flush=True)
+    def record(cfg, query, n, unit, gpu_s, m, cpu_s, same, results=None, bytes_q=0.0, bytes_r=0.0):
+        row = {"config": cfg, "query": query, "n": n, "unit": unit, "results": results,
+               "gpu_ms": round(gpu_s * 1e3, 3), "gpu_rate_per_s": round(n / gpu_s, 1),
+               "cpu_sample": m, "cpu_rate_per_s": round(m / cpu_s, 1),
+               "speedup": round((n / gpu_s) / (m / cpu_s), 1), "identical_on_sample": bool(same)}
+        algo = bytes_q * n + bytes_r * (results or 0)
+        if algo:
+            row["roofline"] = {"bound": "hbm", "algorithmic_bytes": int(algo),
+                               "achieved": round(algo / gpu_s / 1e9, 2), "unit": "GB/s",
+                               "frac": round(algo / gpu_s / 1e9 / peak, 4)}
+        rows.append(row)
+        if verbose:
+            print(json.dumps(row), flush=True)
 
     def first_queries(res, m, nq_col=0):
         # pairs of multi-result queries whose query index < m (results are query-major)
-        ii = res[nq_col]
-        keep = ii < m
+        keep = res[nq_col] < m
         return tuple(r[keep] for r in res)
 
     def same_multi(a, b):
-        return all(np.array_equal(x, y) for x, y in zip(a, b))
+        return all(np.array_equal(x, y, equal_nan=np.asarray(x).dtype.kind == "f") for x, y in zip(a, b))
+
+    def build_row(cfg, xy, f):
+        xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
+        tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
+        ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
+        same = tree.nodes.tobytes() == ot.nodes.tobytes() and np.array_equal(tree.bb_indices, ot.bb_indices)
+        K = f.shape[1]
+        record(cfg, "build", len(f), "cells", tb, len(f), cb, same, results=len(tree.nodes),
+               bytes_q=8 * K + 40 + 16 * len(xy) / len(f), bytes_r=16)
+        return tree, ot
+
+    def boxes_rows(cfg, tree, ot, boxes, m):
+        bd = torch.as_tensor(boxes, device=dev)
+        r, tg = wall(lambda: tree.locate_boxes(bd))
+        ro, tc = cpu(lambda: ot.locate_boxes(boxes[:m]))
+        record(cfg, "locate_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro),
+               results=int(r[0].shape[0]), bytes_q=32, bytes_r=16)
+        del r
+        r, tg = wall(lambda: tree.intersect_boxes(bd))
+        ro, tc = cpu(lambda: ot.intersect_boxes(boxes[:m]))
+        record(cfg, "intersect_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro),
+               results=int(r[0].shape[0]), bytes_q=32, bytes_r=24)
+
+    def segment_row(cfg, tree, ot, segs, m, reps=3):
+        sd = torch.as_tensor(segs, device=dev)
+        r, tg = wall(lambda: tree.intersect_edges(sd), reps=reps)
+        ro, tc = cpu(lambda: ot.intersect_edges(segs[:m]))
+        record(cfg, "intersect_edges", len(segs), "segments", tg, m, tc, same_multi(first_queries(host(r), m), ro),
+               results=int(r[0].shape[0]), bytes_q=32, bytes_r=48)
+
+    def segments(rng, lo, hi, n, length):
+        a0 = rng.uniform(lo, hi, (n, 2))
+        ang = rng.uniform(0.0, 2 * np.pi, n)
+        ln = rng.uniform(0.0, length, n)
+        return np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
 
     cores = O.num_threads()
     rng = np.random.default_rng(0)
     # ---- C1: 80k triangles on [0, 1]^2, 1M points, 10k boxes
     xy, f = syn.triangle_mesh(200, 200, seed=0, extent=(1.0, 1.0))
-    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
-    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
-    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
-    record("C1", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    tree, ot = build_row("C1", xy, f)
     pts = rng.uniform(-0.05, 1.05, (1_000_000, 2))
     pd = torch.as_tensor(pts, device=dev)
     r, tg = wall(lambda: tree.locate_points(pd))
     ro, tc = cpu(lambda: ot.locate_points(pts))
-    record("C1", "locate_points", len(pts), "points", tg, len(pts), tc, np.array_equal(host(r), ro))
-    boxes = syn.random_boxes(10_000, (0.0, 0.0), (1.0, 1.0), 0.001, 0.02, seed=1)
-    bd = torch.as_tensor(boxes, device=dev)
-    r, tg = wall(lambda: tree.locate_boxes(bd))
-    ro, tc = cpu(lambda: ot.locate_boxes(boxes))
-    record("C1", "locate_boxes", len(boxes), "boxes", tg, len(boxes), tc, same_multi(host(r), ro))
-    r, tg = wall(lambda: tree.intersect_boxes(bd))
-    ro, tc = cpu(lambda: ot.intersect_boxes(boxes))
-    record("C1", "intersect_boxes", len(boxes), "boxes", tg, len(boxes), tc, same_multi(host(r), ro))
+    record("C1", "locate_points", len(pts), "points", tg, len(pts), tc, np.array_equal(host(r), ro), bytes_q=24)
+    boxes_rows("C1", tree, ot, syn.random_boxes(10_000, (0.0, 0.0), (1.0, 1.0), 0.001, 0.02, seed=1), 10_000)
     del tree, ot
-    # ---- C2: ~4M mixed cells (K=6) on [0, 1e3]^2; 64M points, 1M boxes, 1M segments
+    # ---- C2: ~5M mixed cells (K=6) on [0, 1e3]^2; 64M points, 1M boxes, 1M segments
     xy, f = syn.mixed_mesh(2000, 2000, seed=1, extent=(1000.0, 1000.0))
-    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
-    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
-    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
-    record("C2", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    tree, ot = build_row("C2", xy, f)
     n = 64 * 1024 * 1024
     pd = torch.rand((n, 2), dtype=torch.float64, device=dev) * 1000.0
     r, tg = wall(lambda: tree.locate_points(pd))
     m = 2_000_000
     sample = pd[:m].cpu().numpy()
     ro, tc = cpu(lambda: ot.locate_points(sample))
-    record("C2", "locate_points", n, "points", tg, m, tc, np.array_equal(host(r[:m]), ro))
+    record("C2", "locate_points", n, "points", tg, m, tc, np.array_equal(host(r[:m]), ro), bytes_q=24)
     del pd, r
-    boxes = syn.random_boxes(1_000_000, (0.0, 0.0), (1000.0, 1000.0), 0.1, 50.0, seed=2, log_uniform=True)
-    bd = torch.as_tensor(boxes, device=dev)
-    r, tg = wall(lambda: tree.locate_boxes(bd))
-    m = 100_000
-    ro, tc = cpu(lambda: ot.locate_boxes(boxes[:m]))
-    record("C2", "locate_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro))
-    r, tg = wall(lambda: tree.intersect_boxes(bd))
-    ro, tc = cpu(lambda: ot.intersect_boxes(boxes[:m]))
-    record("C2", "intersect_boxes", len(boxes), "boxes", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    boxes_rows("C2", tree, ot, syn.random_boxes(1_000_000, (0.0, 0.0), (1000.0, 1000.0), 0.1, 50.0, seed=2,
+                                                 log_uniform=True), 100_000)
     # segments: uniform start, uniform direction, length U(0, 20) m (about 40
-    # cells each); uniform endpoints over the whole domain would give ~1.4e9
-    # (segment, cell) pairs for 1M segments
-    srng = np.random.default_rng(3)
-    a0 = srng.uniform(0.0, 1000.0, (1_000_000, 2))
-    ang = srng.uniform(0.0, 2 * np.pi, 1_000_000)
-    ln = srng.uniform(0.0, 20.0, 1_000_000)
-    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
-    sd = torch.as_tensor(segs, device=dev)
-    r, tg = wall(lambda: tree.intersect_edges(sd), reps=1)
-    m = 20_000
-    ro, tc = cpu(lambda: ot.intersect_edges(segs[:m]))
-    record("C2", "intersect_edges", len(segs), "segments", tg, m, tc, same_multi(first_queries(host(r), m), ro))
-    del tree, ot, r
+    # cells each); uniform endpoints over the whole domain give ~1.4e9
+    # (segment, cell) pairs for 1M segments (chunked-output mode, not timed here)
+    segment_row("C2", tree, ot, segments(np.random.default_rng(3), 0.0, 1000.0, 1_000_000, 20.0), 20_000)
+    del tree, ot
     # ---- C4: tree of 500k quads (rotated 7 degrees, offset 0.37 cell); 1M query triangles; 1M points
     txy, tf = syn.quad_mesh(1000, 500, seed=4, extent=(100.0, 50.0), offset=(0.037, 0.037), rotate_deg=7.0)
     qxy, qf = syn.triangle_mesh(1000, 500, seed=5, extent=(100.0, 50.0))
-    txy_d, tf_d = torch.as_tensor(txy, device=dev), torch.as_tensor(tf, device=dev)
-    tree, tb = wall(lambda: CellTree2d(txy_d, tf_d, -1), reps=2)
-    ot, cb = cpu(lambda: O.OracleCellTree2d(txy, tf, -1))
-    record("C4", "build", len(tf), "cells", tb, len(tf), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
+    tree, ot = build_row("C4", txy, tf)
     qv, qfd = torch.as_tensor(qxy, device=dev), torch.as_tensor(qf, device=dev)
-    r, tg = wall(lambda: tree.locate_faces(qv, qfd.clone()), reps=2)
+    r, tg = wall(lambda: tree.locate_faces(qv, qfd.clone()))
     m = 50_000
     ro, tc = cpu(lambda: ot.locate_faces(qxy, qf[:m].copy()))
-    record("C4", "locate_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro))
-    r, tg = wall(lambda: tree.intersect_faces(qv, qfd, -1), reps=2)
+    record("C4", "locate_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro),
+           results=int(r[0].shape[0]), bytes_q=8 * 3 + 16 * len(qxy) / len(qf), bytes_r=16)
+    r, tg = wall(lambda: tree.intersect_faces(qv, qfd, -1))
     ro, tc = cpu(lambda: ot.intersect_faces(qxy, qf[:m], -1))
-    record("C4", "intersect_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro))
+    record("C4", "intersect_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro),
+           results=int(r[0].shape[0]), bytes_q=8 * 3 + 16 * len(qxy) / len(qf), bytes_r=24)
     bp = syn.uniform_points(1_000_000, txy.min(0), txy.max(0), seed=6)
     bpd = torch.as_tensor(bp, device=dev)
     r, tg = wall(lambda: tree.compute_barycentric_weights(bpd))
-    m = 1_000_000
     ro, tc = cpu(lambda: ot.compute_barycentric_weights(bp))
-    record("C4", "compute_barycentric_weights", len(bp), "points", tg, m, tc, same_multi(host(r), ro))
+    record("C4", "compute_barycentric_weights", len(bp), "points", tg, len(bp), tc, same_multi(host(r), ro),
+           bytes_q=24 + 8 * 4)
     del tree, ot, r
     # ---- C5: 16M triangles (1 m cells, offset 5.0e5 / 4.2e6 m); 4M segments,
     # uniform start over the mesh, uniform direction, length U(0, 20) m
-    xy, f = workload(args)
-    xy_d, f_d = torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev)
-    tree, tb = wall(lambda: CellTree2d(xy_d, f_d, -1), reps=2)
-    ot, cb = cpu(lambda: O.OracleCellTree2d(xy, f, -1))
-    record("C5", "build", len(f), "cells", tb, len(f), cb, tree.nodes.tobytes() == ot.nodes.tobytes())
-    srng = np.random.default_rng(7)
-    ns = 4_000_000
-    a0 = srng.uniform(xy.min(0), xy.max(0), (ns, 2))
-    ang = srng.uniform(0.0, 2 * np.pi, ns)
-    ln = srng.uniform(0.0, 20.0, ns)
-    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
-    sd = torch.as_tensor(segs, device=dev)
-    r, tg = wall(lambda: tree.intersect_edges(sd), reps=1)
-    m = 20_000
-    ro, tc = cpu(lambda: ot.intersect_edges(segs[:m]))
-    record("C5", "intersect_edges", ns, "segments", tg, m, tc, same_multi(first_queries(host(r), m), ro))
-    print(json.dumps({"summary": "queries vs oracle", "host_cores": cores,
-                      "min_speedup": min(x["speedup"] for x in lines),
-                      "all_identical": all(x["identical_on_sample"] for x in lines)}))
+    if c5 is None:
+        xy, f = workload(args)
+        tree = CellTree2d(torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev), -1)
+    else:
+        xy, f, tree = c5
+    ot = O.OracleCellTree2d(xy, f, -1)
+    segment_row("C5", tree, ot, segments(np.random.default_rng(7), xy.min(0), xy.max(0), 4_000_000, 20.0), 20_000,
+                reps=2)
+    del ot
+    multi = [x for x in rows if x["query"] not in ("build", "locate_points")]
+    return {"summary": "build and every query vs the oracle on the survey shapes", "host_cores": cores,
+            "min_speedup": min(x["speedup"] for x in rows),
+            "min_speedup_multi_result": min(x["speedup"] for x in multi),
+            "all_identical": all(x["identical_on_sample"] for x in rows), "rows": rows}
+
+
+def run_queries(args):
+    """Side measurement: every query against the oracle (one JSON line per row)."""
+    res = query_suite(args, verbose=True)
+    res.pop("rows")
+    print(json.dumps(res))
 
 
 def main():
@@ -528,6 +548,7 @@ def main():
         args.nx, args.ny, args.points, args.steps, args.warmup = 1000, 500, 16 * 1024 * 1024, 2, 1
         args.no_e2e = True
         args.no_cpu = True
+        args.no_queries = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -633,6 +654,7 @@ def main():
     # ---- end to end through the public API: numpy points in pinned host
     # memory in, numpy indices out (upload, query and download per step)
     e2e = None
+    e2e_pageable = None
     if not args.no_e2e:
         # the first calls set up the pipeline's pinned buffers (100-180 ms);
         # single steps on the host side occasionally stall for tens of ms, so
@@ -653,6 +675,20 @@ def main():
             step_s.append(time.perf_counter() - t0)
         e2e_s = max_over_ranks(ws, statistics.median(step_s))
         assert np.array_equal(res, out32.cpu().numpy()), "end-to-end result differs from the device-resident run"
+        # the same call on an ordinary (pageable) numpy array, as a drop-in
+        # caller passes it
+        for _ in range(2):
+            res = tree.locate_points(pts_h, tol)
+        torch.cuda.synchronize()
+        barrier(ws)
+        page_s = []
+        for _ in range(e2e_steps):
+            t0 = time.perf_counter()
+            res = tree.locate_points(pts_h, tol)
+            torch.cuda.synchronize()
+            page_s.append(time.perf_counter() - t0)
+        e2e_page_s = max_over_ranks(ws, statistics.median(page_s))
+        assert np.array_equal(res, out32.cpu().numpy()), "pageable end-to-end result differs"
         # the host link's own bound for one step: the upload and the download
         # of the same bytes, both at once, nothing else
         res_t = torch.empty((n,), dtype=torch.int64, pin_memory=True)
@@ -674,6 +710,11 @@ def main():
                "link_ms": round(link_ms, 3), "frac_of_link_bound": round(link_ms / (e2e_s * 1e3), 3),
                "path": "CellTree2d.locate_points(numpy in pinned memory) -> numpy; "
                        "chunks of 2^25 points, upload / query / download overlapped on three streams"}
+        e2e_pageable = {"value": round(ws * n / e2e_page_s / 1e6, 3), "unit": UNIT,
+                        "h2d_bytes_per_step": int(pts_h.nbytes), "d2h_bytes_per_step": int(n * 8),
+                        "ms_per_step": round(e2e_page_s * 1e3, 3), "ms_steps": [round(x * 1e3, 2) for x in page_s],
+                        "vs_pinned": round(e2e_page_s / e2e_s, 3),
+                        "path": "CellTree2d.locate_points(ordinary pageable numpy array) -> numpy"}
         del res, res_t, pts_pin, pin
 
     # ---- CPU baseline: the oracle on a bounded sample of the same workload
@@ -707,6 +748,15 @@ def main():
         cpu = {"value": round(m / cpu_s / 1e6, 3), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
                "sample": f"first {m} of the {n} points on the same tree (oracle = C restatement, OpenMP)",
                "build_s": round(cpu_build_s, 3)}
+
+    # ---- every query against the oracle on the survey shapes (outside the timed region)
+    queries = None
+    if not args.no_queries and not args.no_cpu and rank == 0 and ws == 1:
+        del out64
+        try:
+            queries = query_suite(args, c5=(xy, faces, tree))
+        except Exception as exc:  # keep the headline line if a side measurement fails
+            queries = {"error": f"{type(exc).__name__}: {exc}"}
 
     peak, peak_kind = peaks()
     achieved = BYTES_PER_POINT * n / (ms_fast * 1e-3) / 1e9
@@ -753,6 +803,8 @@ def main():
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "e2e_pageable": e2e_pageable,
+        "queries": queries,
     }
     if rank == 0:
         print(json.dumps(result))

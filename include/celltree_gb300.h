@@ -110,6 +110,12 @@ typedef struct ct_tree {
     int32_t tune_query_threads; /* block size of the box and segment traversals: 64, 128 or 256
                                    (default 256 boxes, 128 segments; segments take at most 128) */
     int32_t tune_fp64_stack;  /* stack entries of the plain float64 locate: 0 = smallest that fits, 64 or 512 */
+    /* parent of every node (device, n_nodes int32, -1 for the root; filled by
+     * ct_pack_tree when not NULL).  Trees deeper than the traversal stacks
+     * (510 levels for point location, 126 for the multi-result queries) are
+     * then traversed without a stack, in the same order; without it such
+     * trees are refused. */
+    int32_t* node_parent;
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */

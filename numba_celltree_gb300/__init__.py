@@ -5,7 +5,8 @@ CUDA kernels (libcelltree_gb300.so)."""
 from .batch import CellTreeBatch
 from .celltree import CellTree2d
 from .edge_celltree import EdgeCellTree2d
+from .sharded import MultiDeviceCellTree, ShardedCellTree
 
-__version__ = "0.1.0"
+__version__ = "0.2.0"
 
-__all__ = ("CellTree2d", "CellTreeBatch", "EdgeCellTree2d")
+__all__ = ("CellTree2d", "CellTreeBatch", "EdgeCellTree2d", "MultiDeviceCellTree", "ShardedCellTree")

@@ -87,6 +87,7 @@ class CtTree(ctypes.Structure):
         ("tune_fast_bpsm", _I32),
         ("tune_query_threads", _I32),
         ("tune_fp64_stack", _I32),
+        ("node_parent", _P),
     ]
 
 

@@ -243,32 +243,105 @@ class CellTree2d(CellTree2dBase):
         return out
 
     # -- box queries -----------------------------------------------------------
+    # bytes a result of a multi-result query occupies on the device while it
+    # is produced (pairs, temporaries of the count / write / compact passes)
+    BYTES_PER_BOX_PAIR = 64
+    BYTES_PER_EDGE_CANDIDATE = 160
+
+    def _chunks(self, q_d, count, run, budget: int, cuda_out: bool, counts=None):
+        """Ranges of the device queries q_d whose results fit `budget`, run one
+        after another; yields each range's results (global query indices) as
+        CUDA tensors or, with cuda_out False, numpy arrays (so that the device
+        holds one range's results at a time).  `counts`: the per-query counts
+        when already known."""
+        t = self._tree
+        counts = (count(q_d) if counts is None else counts).cpu().numpy()
+        for s, e in t.chunk_ranges(counts, budget):
+            res = run(q_d[s:e])
+            res = (res[0] + s,) + tuple(res[1:])
+            yield tuple(_as_output(x, cuda_out) for x in res)
+
+    def _iter(self, q, cast, count, run, per_result: int, max_results):
+        cuda_in = is_cuda_tensor(q)
+        t = self._tree
+        q_d = _device.to_device(cast(q), _device.torch().float64, t.device)
+        budget = int(max_results) if max_results is not None else t.device_budget(per_result)
+        return self._chunks(q_d, count, run, budget, cuda_in)
+
+    @staticmethod
+    def _concat(chunks):
+        chunks = list(chunks)
+        return tuple(np.concatenate([c[k] for c in chunks]) for k in range(len(chunks[0])))
+
+    def iter_locate_boxes(self, bbox_coords, max_pairs: Optional[int] = None):
+        """locate_boxes in ranges of boxes whose pairs stay within max_pairs
+        (default: what fits the free device memory): yields
+        ``(bbox_indices, tree_face_indices)`` per range, box-major; their
+        concatenation is locate_boxes' result."""
+        t = self._tree
+        return self._iter(bbox_coords, cast_bboxes, t.count_boxes, t.locate_boxes, self.BYTES_PER_BOX_PAIR,
+                          max_pairs)
+
+    def iter_intersect_boxes(self, bbox_coords, max_pairs: Optional[int] = None):
+        """intersect_boxes in ranges of boxes (see iter_locate_boxes)."""
+        t = self._tree
+        return self._iter(bbox_coords, cast_bboxes, t.count_boxes, self._intersect_boxes_dev,
+                          self.BYTES_PER_BOX_PAIR, max_pairs)
+
+    def iter_intersect_edges(self, edge_coords, max_candidates: Optional[int] = None):
+        """intersect_edges in ranges of segments whose candidate cells (an
+        upper bound of their results) stay within max_candidates (default:
+        what fits the free device memory); the concatenation of the ranges'
+        results is intersect_edges' result.  Segments crossing much of a big
+        mesh produce billions of results: this keeps the device memory
+        bounded while they stream to the host."""
+        t = self._tree
+        return self._iter(edge_coords, cast_edges, lambda q: t.count_edge_candidates(q, 1),
+                          lambda q: t.locate_edges(q, 1), self.BYTES_PER_EDGE_CANDIDATE, max_candidates)
+
     def locate_boxes(self, bbox_coords):
         """
         Find the index of a face intersecting with a bounding box
         (celltree.py:130-148, query.py:177-289).
 
         Returns ``(bbox_indices, tree_face_indices)``, box-major, in the
-        upstream order.
+        upstream order.  Host (numpy) batches whose pairs exceed the free
+        device memory run in ranges of boxes (iter_locate_boxes).
         """
         cuda_in = is_cuda_tensor(bbox_coords)
         b = cast_bboxes(bbox_coords)
         t = self._tree
         b_d = _device.to_device(b, _device.torch().float64, t.device)
-        ii, jj = t.locate_boxes(b_d)
+        budget = None if cuda_in else t.device_budget(self.BYTES_PER_BOX_PAIR)
+        res = t.locate_boxes(b_d, budget=budget)
+        if res is None:  # more pairs than the device holds: ranges of boxes
+            return self._concat(self._chunks(b_d, None, t.locate_boxes, budget, False, counts=t.last_counts))
+        ii, jj = res
         return _as_output(ii, cuda_in), _as_output(jj, cuda_in)
 
     def intersect_boxes(self, bbox_coords):
         """
         Boxes, intersecting faces and the area of intersection
-        (celltree.py:150-184); only pairs with area > 0 are kept.
+        (celltree.py:150-184); only pairs with area > 0 are kept.  Host
+        batches run in ranges when their pairs exceed the device memory.
         """
         cuda_in = is_cuda_tensor(bbox_coords)
-        b = cast_bboxes(bbox_coords)
+        t = self._tree
+        b_d = _device.to_device(cast_bboxes(bbox_coords), _device.torch().float64, t.device)
+        budget = None if cuda_in else t.device_budget(self.BYTES_PER_BOX_PAIR)
+        res = self._intersect_boxes_dev(b_d, budget)
+        if res is None:  # more pairs than the device holds: ranges of boxes
+            return self._concat(self._chunks(b_d, None, self._intersect_boxes_dev, budget, False,
+                                             counts=t.last_counts))
+        return tuple(_as_output(x, cuda_in) for x in res)
+
+    def _intersect_boxes_dev(self, b_d, budget=None):
         t = self._tree
         torch = _device.torch()
-        b_d = _device.to_device(b, torch.float64, t.device)
-        ii, jj = t.locate_boxes(b_d)
+        res = t.locate_boxes(b_d, budget=budget)
+        if res is None:
+            return None
+        ii, jj = res
         n = int(ii.shape[0])
         area = _device.empty((n,), torch.float64, t.device)
         t.reset_error()
@@ -283,8 +356,7 @@ class CellTree2d(CellTree2dBase):
         )
         del order
         t.raise_on_device_error()
-        i, j, a = t.compact(ii, jj, area=area)
-        return _as_output(i, cuda_in), _as_output(j, cuda_in), _as_output(a, cuda_in)
+        return t.compact(ii, jj, area=area)
 
     # -- face queries ----------------------------------------------------------
     def _faces_on_device(self, vertices, faces):
@@ -388,7 +460,12 @@ class CellTree2d(CellTree2dBase):
         e = cast_edges(edge_coords)
         t = self._tree
         e_d = _device.to_device(e, _device.torch().float64, t.device)
-        ii, jj, xy = t.locate_edges(e_d, 1)
+        budget = None if cuda_in else t.device_budget(self.BYTES_PER_EDGE_CANDIDATE)
+        res = t.locate_edges(e_d, 1, budget=budget)
+        if res is None:  # more candidates than the device holds: ranges of segments
+            return self._concat(self._chunks(e_d, None, lambda q: t.locate_edges(q, 1), budget, False,
+                                             counts=t.last_counts))
+        ii, jj, xy = res
         return _as_output(ii, cuda_in), _as_output(jj, cuda_in), _as_output(xy, cuda_in)
 
     # -- barycentric -----------------------------------------------------------

@@ -68,6 +68,8 @@ class _GpuTree:
         self.poly_f32 = _device.empty((max(n, 1), lib.ct_poly32_stride(K), 4), torch.float32, device)
         self.poly_len = _device.empty((max(n, 1),), torch.uint8, device)
         self.poly_len32 = _device.empty((max(n, 1),), torch.uint8, device)
+        # node parents: trees deeper than the traversal stacks are walked through them
+        self.node_parent = _device.empty((max(nn, 1),), torch.int32, device)
         self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
         self.grid_start = None
         self.desc = _lib.CtTree()
@@ -200,6 +202,7 @@ class _GpuTree:
         d.poly_len = P(self.poly_len)
         d.poly_len32 = P(self.poly_len32)
         d.error_word = P(self.error_word)
+        d.node_parent = P(self.node_parent)
         d.grid_start = P(self.grid_start) if self.grid_start is not None else None
 
     def reset_error(self):
@@ -230,6 +233,9 @@ class _GpuTree:
         lists a finer order saves less in the query kernels than its third
         radix pass costs)."""
         return 0 if n_points < (1 << 16) else 16
+
+    # deepest tree (levels + 2) the batched float32 locate takes
+    BATCHED_MAX_STACK = 128
 
     # largest batch one library call takes (the entry points index queries
     # with 32-bit integers); larger batches are located slice by slice
@@ -318,6 +324,8 @@ class _GpuTree:
                 e = min(s + self.MAX_CALL_POINTS, n)
                 self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits, config)
             return
+        if precision == "fp32" and self.max_depth + 2 > self.BATCHED_MAX_STACK:
+            precision = "fp64"  # the batched form's stacks hold 126 levels; deeper trees take the float64 walk
         if precision == "fp32":
             cfg = config if config is not None else self.cached("locate", n)
             self._apply("locate", cfg)
@@ -364,6 +372,8 @@ class _GpuTree:
         size is timed on the device)."""
         kind = "locate" if precision == "fp32" else "fp64"
         key = self.tune_key(kind, n_call)
+        if self.max_depth + 2 > self.BATCHED_MAX_STACK:
+            return
         if (key in self._tuned or not autotune.enabled() or n_call < autotune.TUNE_MIN[kind] or self._capturing()
                 or autotune.cache().get(key) is not None):
             return
@@ -440,7 +450,56 @@ class _GpuTree:
             d.bb_leaf = d.node_box = d.leaf_start = None
             _lib.check(status, "box index")
 
-    def locate_boxes(self, boxes_d, config=None):
+    # -- output-budgeted chunks of multi-result queries ------------------------
+    def count_boxes(self, boxes_d):
+        """Result pairs of every box query (device int64)."""
+        torch = _device.torch()
+        n = int(boxes_d.shape[0])
+        counts = _device.empty((n,), torch.int64, self.device)
+        self.ensure_box_index()
+        _lib.check(_lib.load().ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, None,
+                                              _device.ptr(counts), _device.stream()), "count_boxes")
+        return counts
+
+    def count_edge_candidates(self, segs_d, mode: int):
+        """Candidate cells of every segment (device int64): an upper bound of
+        its results."""
+        torch = _device.torch()
+        n = int(segs_d.shape[0])
+        counts = _device.empty((n,), torch.int64, self.device)
+        if mode == 1:
+            self.ensure_box_index()
+        _lib.check(_lib.load().ct_count_edge_candidates(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, None,
+                                                        _device.ptr(counts), _device.stream()), "count_edges")
+        return counts
+
+    @staticmethod
+    def chunk_ranges(counts: np.ndarray, max_results: int):
+        """Contiguous query ranges [s, e) whose summed counts stay within
+        max_results (a single query above it forms a range of its own)."""
+        n = int(counts.shape[0])
+        if n == 0:
+            return [(0, 0)]
+        cum = np.concatenate([[0], np.cumsum(counts, dtype=np.int64)])
+        out, s = [], 0
+        while s < n:
+            e = int(np.searchsorted(cum, cum[s] + max(int(max_results), 1), side="right")) - 1
+            e = min(max(e, s + 1), n)
+            out.append((s, e))
+            s = e
+        return out
+
+    def device_budget(self, bytes_per_result: int) -> int:
+        """Results one device pass may produce: a quarter of the free device
+        memory over the bytes a result needs in flight."""
+        torch = _device.torch()
+        free, _ = torch.cuda.mem_get_info(self.device)
+        return max(1 << 20, int(free // 4 // max(bytes_per_result, 1)))
+
+    def locate_boxes(self, boxes_d, config=None, budget=None):
+        """Pairs (box, cell) of every box query, box-major in upstream order;
+        with `budget`, returns None instead when the pairs would exceed it
+        (the per-box counts are left in self.last_counts)."""
         n = int(boxes_d.shape[0])
         if config is None:
             m = min(n, autotune.SAMPLE_MAX["boxes"])
@@ -457,6 +516,9 @@ class _GpuTree:
         _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
                                       _device.ptr(counts), st), "locate_boxes")
         offsets, total = self.scan(counts)
+        if budget is not None and total > budget:
+            self.last_counts = counts
+            return None
         ii = _device.empty((total,), torch.int64, self.device)
         jj = _device.empty((total,), torch.int64, self.device)
         _lib.check(
@@ -467,9 +529,11 @@ class _GpuTree:
         self.raise_on_device_error()
         return ii, jj
 
-    def locate_edges(self, segs_d, mode: int, config=None):
+    def locate_edges(self, segs_d, mode: int, config=None, budget=None):
         """Candidates (traversal) -> float64 cell test per candidate -> hits
-        in candidate order -> per-segment sort by t; returns ii, jj, xy (R, 2, 2)."""
+        in candidate order -> per-segment sort by t; returns ii, jj, xy (R, 2, 2).
+        With `budget`, returns None instead when the candidates would exceed
+        it (the per-segment candidate counts are left in self.last_counts)."""
         n = int(segs_d.shape[0])
         if config is None:
             m = min(n, autotune.SAMPLE_MAX["segments"])
@@ -489,6 +553,9 @@ class _GpuTree:
         _lib.check(lib.ct_count_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(ccnt), st),
                    "intersect_edges")
         coff, nc = self.scan(ccnt)
+        if budget is not None and nc > budget:
+            self.last_counts = ccnt
+            return None
         cseg = _device.empty((max(nc, 1),), torch.int32, self.device)
         cpos = _device.empty((max(nc, 1),), torch.int32, self.device)
         _lib.check(lib.ct_write_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(coff),

@@ -38,6 +38,7 @@ struct TreeQ {
     const struct NodeBox* nbx; // per node: bounding box of its cells (float32 frame, outward) and leaf range
     const int* lstart;         // per leaf position: first position of its leaf
     double ox, oy;             // float32 frame origin
+    const int* parent;         // node parents (trees deeper than the stacks are walked through them)
 };
 
 // Bounding box of a node's cells in the float32 frame of the tree (x - ox,
@@ -81,7 +82,7 @@ __device__ __forceinline__ dbox leaf_box(const TreeQ& T, int64_t j) {
 // ---------------------------------------------------------------------------
 // locate_box query.py:177-244
 // ---------------------------------------------------------------------------
-template <bool WRITE>
+template <bool WRITE, bool DEEP>
 __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restrict__ boxes, int64_t n,
                                                const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
                                                int64_t* __restrict__ ii, int64_t* __restrict__ jj) {
@@ -115,86 +116,111 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
         qy1 = __double2float_rd(box.ymax - T.oy);
     }
     if (boxes_intersect(box, T.bbox)) {
-        int st[STK];
+        // depth-first walk: a stack, or (DEEP, trees deeper than the stack)
+        // the parent links -- down to the child that would be popped first,
+        // back up to the parent to find the sibling still to visit
+        int st[DEEP ? 1 : STK];
         int sp = 1;
         st[0] = 0;
-        int64_t budget = T.n_nodes;
-        while (sp > 0) {
+        int dv = 0, from = -1;
+        bool down = true;
+        int64_t budget = DEEP ? 2 * T.n_nodes + 2 : T.n_nodes;
+        while (DEEP ? dv >= 0 : sp > 0) {
             if (--budget < 0) {
                 set_error(T.err, CT_DEVERR_LOOP);
                 break;
             }
-            int v = st[--sp];
-            if (idx) {
-                const NodeBox nbv = T.nbx[v];
-                if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
-                    // the whole subtree, in upstream's visiting order: right
-                    // child first, i.e. leaves by decreasing position, each
-                    // leaf's cells by increasing position
-                    if (WRITE) {
-                        int q = nbv.ptr + nbv.size;
-                        int64_t c = count;
-                        while (q > nbv.ptr) {
-                            int s = T.lstart[q - 1];
-                            if (s < nbv.ptr || s >= q) {  // corrupt index: stop rather than loop
-                                set_error(T.err, CT_DEVERR_LOOP);
-                                break;
-                            }
-                            for (int j = s; j < q; j++) {
-                                ii[base + c] = i;
-                                jj[base + c] = T.bbi[j];
-                                c++;
-                            }
-                            q = s;
-                        }
-                    }
-                    count += nbv.size;
-                    continue;
-                }
-            }
-            float4 q = T.nf[v];
-            int b = nb(q);
-            if (b >= 0) {
-                int ptr = na(q);
-                for (int j = ptr; j < ptr + b; j++) {
-                    dbox lb = leaf_box(T, j);
-                    // boxes_intersect geometry_utils.py:292-300
-                    bool hit = keys ? (kx0 < fkey(lb.xmax) && fkey(lb.xmin) < kx1 && ky0 < fkey(lb.ymax) &&
-                                       fkey(lb.ymin) < ky1)
-                                    : boxes_intersect(box, lb);
-                    if (hit) {
+            const int v = DEEP ? dv : st[--sp];
+            bool terminal = false;
+            float4 q;
+            if (!DEEP || down) {
+                if (idx) {
+                    const NodeBox nbv = T.nbx[v];
+                    if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
+                        // the whole subtree, in upstream's visiting order: right
+                        // child first, i.e. leaves by decreasing position, each
+                        // leaf's cells by increasing position
                         if (WRITE) {
-                            ii[base + count] = i;
-                            jj[base + count] = T.bbi[j];
+                            int qq = nbv.ptr + nbv.size;
+                            int64_t c = count;
+                            while (qq > nbv.ptr) {
+                                int s = T.lstart[qq - 1];
+                                if (s < nbv.ptr || s >= qq) {  // corrupt index: stop rather than loop
+                                    set_error(T.err, CT_DEVERR_LOOP);
+                                    break;
+                                }
+                                for (int j = s; j < qq; j++) {
+                                    ii[base + c] = i;
+                                    jj[base + c] = T.bbi[j];
+                                    c++;
+                                }
+                                qq = s;
+                            }
                         }
-                        count++;
+                        count += nbv.size;
+                        terminal = true;
                     }
                 }
-                continue;
-            }
-            int dim = -1 - b;
-            double2 d = T.nd[v];
-            bool left, right;
-            if (keys) {
-                left = (dim ? ky0 : kx0) <= fkey(d.x);
-                right = (dim ? ky1 : kx1) >= fkey(d.y);
+                if (!terminal) {
+                    q = T.nf[v];
+                    int b = nb(q);
+                    if (b >= 0) {
+                        int ptr = na(q);
+                        for (int j = ptr; j < ptr + b; j++) {
+                            dbox lb = leaf_box(T, j);
+                            // boxes_intersect geometry_utils.py:292-300
+                            bool hit = keys ? (kx0 < fkey(lb.xmax) && fkey(lb.xmin) < kx1 && ky0 < fkey(lb.ymax) &&
+                                               fkey(lb.ymin) < ky1)
+                                            : boxes_intersect(box, lb);
+                            if (hit) {
+                                if (WRITE) {
+                                    ii[base + count] = i;
+                                    jj[base + count] = T.bbi[j];
+                                }
+                                count++;
+                            }
+                        }
+                        terminal = true;
+                    }
+                }
             } else {
-                double bmin = dim ? box.ymin : box.xmin, bmax = dim ? box.ymax : box.xmax;
-                left = bmin <= d.x;
-                right = bmax >= d.y;
+                q = T.nf[v];  // back from a child: an internal node, not contained
             }
-            int child = na(q);
-            if (sp + 2 > STK) {
-                set_error(T.err, CT_DEVERR_STACK);
-                break;
+            int first = -1, second = -1;
+            if (!terminal) {
+                int dim = -1 - nb(q);
+                double2 d = T.nd[v];
+                bool left, right;
+                if (keys) {
+                    left = (dim ? ky0 : kx0) <= fkey(d.x);
+                    right = (dim ? ky1 : kx1) >= fkey(d.y);
+                } else {
+                    double bmin = dim ? box.ymin : box.xmin, bmax = dim ? box.ymax : box.xmax;
+                    left = bmin <= d.x;
+                    right = bmax >= d.y;
+                }
+                // pushed left, then right: the right child is visited first
+                int child = na(q);
+                first = right ? child + 1 : (left ? child : -1);
+                second = (left && right) ? child : -1;
             }
-            if (left && right) {
-                st[sp++] = child;
-                st[sp++] = child + 1;
-            } else if (left) {
-                st[sp++] = child;
-            } else if (right) {
-                st[sp++] = child + 1;
+            if (DEEP) {
+                int next = terminal ? -1 : (down ? first : ((from == first) ? second : -1));
+                from = dv;
+                if (next >= 0) {
+                    dv = next;
+                    down = true;
+                } else {
+                    dv = T.parent[dv];
+                    down = false;
+                }
+            } else if (!terminal) {
+                if (sp + 2 > STK) {
+                    set_error(T.err, CT_DEVERR_STACK);
+                    break;
+                }
+                if (second >= 0) st[sp++] = second;
+                if (first >= 0) st[sp++] = first;
             }
         }
     }
@@ -224,7 +250,7 @@ __device__ __forceinline__ int cs_code_keys(unsigned long long kx, unsigned long
     return p;
 }
 
-template <bool WRITE, int MODE>
+template <bool WRITE, int MODE, bool DEEP>
 __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __restrict__ segs, int64_t n,
                                                     const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
                                                     int* __restrict__ cseg, int* __restrict__ cj) {
@@ -243,19 +269,24 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
         const bool keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) &&
                           is_fin(V.y);
         const unsigned long long kax = fkey(a.x), kay = fkey(a.y), kbx = fkey(b.x), kby = fkey(b.y);
-        int st[STK];
+        // depth-first walk: a stack, or (DEEP) the parent links (see k_boxes)
+        int st[DEEP ? 1 : STK];
         int sp = 1;
         st[0] = 0;
-        int64_t budget = T.n_nodes;
-        while (sp > 0) {
+        int dv = 0, from = -1;
+        bool down = true;
+        int64_t budget = DEEP ? 2 * T.n_nodes + 2 : T.n_nodes;
+        while (DEEP ? dv >= 0 : sp > 0) {
             if (--budget < 0) {
                 set_error(T.err, CT_DEVERR_LOOP);
                 break;
             }
-            int v = st[--sp];
+            const int v = DEEP ? dv : st[--sp];
             float4 q = T.nf[v];
             int bq = nb(q);
-            if (bq >= 0) {
+            int first = -1, second = -1;
+            const bool terminal = bq >= 0;
+            if (terminal && (!DEEP || down)) {
                 int ptr = na(q);
                 for (int j = ptr; j < ptr + bq; j++) {
                     bool cand = true;
@@ -281,49 +312,59 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
                         count++;
                     }
                 }
-                continue;
             }
-            int dim = -1 - bq;
-            double2 nd = T.nd[v];
-            double dx = dim ? V.y : V.x;
-            bool left, right;
-            if (keys) {
-                unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
-                bool pos = dx > 0.0;
-                left = fkey(nd.x) >= (pos ? ka : kb);
-                right = fkey(nd.y) <= (pos ? kb : ka);
-            } else {
-                double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
-                double dx_left, dx_right;
-                if (dx > 0.0) {
-                    dx_left = nd.x - an;
-                    dx_right = nd.y - bn;
+            if (!terminal) {
+                int dim = -1 - bq;
+                double2 nd = T.nd[v];
+                double dx = dim ? V.y : V.x;
+                bool left, right;
+                if (keys) {
+                    unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
+                    bool pos = dx > 0.0;
+                    left = fkey(nd.x) >= (pos ? ka : kb);
+                    right = fkey(nd.y) <= (pos ? kb : ka);
                 } else {
-                    dx_left = nd.x - bn;
-                    dx_right = nd.y - an;
+                    double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
+                    double dx_left, dx_right;
+                    if (dx > 0.0) {
+                        dx_left = nd.x - an;
+                        dx_right = nd.y - bn;
+                    } else {
+                        dx_left = nd.x - bn;
+                        dx_right = nd.y - an;
+                    }
+                    left = dx_left >= 0.0;
+                    right = dx_right <= 0.0;
+                    if (dx > 0.0) {
+                        if (left) left = (dx_left / dx) >= 0.0;
+                        if (right) right = (dx_right / dx) <= 1.0;
+                    } else if (dx < 0.0) {
+                        if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
+                        if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+                    }
                 }
-                left = dx_left >= 0.0;
-                right = dx_right <= 0.0;
-                if (dx > 0.0) {
-                    if (left) left = (dx_left / dx) >= 0.0;
-                    if (right) right = (dx_right / dx) <= 1.0;
-                } else if (dx < 0.0) {
-                    if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
-                    if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+                // pushed left, then right: the right child is visited first
+                int child = na(q);
+                first = right ? child + 1 : (left ? child : -1);
+                second = (left && right) ? child : -1;
+            }
+            if (DEEP) {
+                int next = terminal ? -1 : (down ? first : ((from == first) ? second : -1));
+                from = dv;
+                if (next >= 0) {
+                    dv = next;
+                    down = true;
+                } else {
+                    dv = T.parent[dv];
+                    down = false;
                 }
-            }
-            int child = na(q);
-            if (sp + 2 > STK) {
-                set_error(T.err, CT_DEVERR_STACK);
-                break;
-            }
-            if (left && right) {
-                st[sp++] = child;
-                st[sp++] = child + 1;
-            } else if (left) {
-                st[sp++] = child;
-            } else if (right) {
-                st[sp++] = child + 1;
+            } else if (!terminal) {
+                if (sp + 2 > STK) {
+                    set_error(T.err, CT_DEVERR_STACK);
+                    break;
+                }
+                if (second >= 0) st[sp++] = second;
+                if (first >= 0) st[sp++] = first;
             }
         }
     }
@@ -919,6 +960,7 @@ TreeQ make_q(const ct_tree* t) {
     T.lstart = box_index ? t->leaf_start : nullptr;
     T.ox = t->origin[0];
     T.oy = t->origin[1];
+    T.parent = t->node_parent;
     return T;
 }
 
@@ -1085,9 +1127,13 @@ static int seg_threads(const ct_tree* t) {
 static int check_tree(const ct_tree* t) {
     if (!t) return ct_fail(CT_ERR_ARG, "tree is null");
     if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
-    if (t->max_depth + 2 > STK) return ct_fail(CT_ERR_ARG, "tree deeper than 126 levels for multi-result queries");
+    if (t->max_depth + 2 > STK && !t->node_parent)
+        return ct_fail(CT_ERR_ARG, "tree deeper than 126 levels for multi-result queries (no node_parent)");
     return CT_OK;
 }
+
+// trees deeper than the traversal stack are walked through the node parents
+static bool deep_tree(const ct_tree* t) { return t->max_depth + 2 > STK; }
 
 int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order, int64_t* counts,
                    void* stream) {
@@ -1095,8 +1141,12 @@ int ct_count_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     if (s) return s;
     if (n == 0) return CT_OK;
     const int bt = box_threads(t);
-    k_boxes<false><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
-                                                                       counts, nullptr, nullptr);
+    if (deep_tree(t))
+        k_boxes<false, true><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+                                                                              order, counts, nullptr, nullptr);
+    else
+        k_boxes<false, false><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+                                                                               order, counts, nullptr, nullptr);
     CT_CHECK_LAUNCH("count_boxes");
     return CT_OK;
 }
@@ -1107,8 +1157,12 @@ int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     if (s) return s;
     if (n == 0) return CT_OK;
     const int bt = box_threads(t);
-    k_boxes<true><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n, order,
-                                                                      (int64_t*)offsets, ii, jj);
+    if (deep_tree(t))
+        k_boxes<true, true><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+                                                                             order, (int64_t*)offsets, ii, jj);
+    else
+        k_boxes<true, false><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
+                                                                              order, (int64_t*)offsets, ii, jj);
     CT_CHECK_LAUNCH("write_boxes");
     return CT_OK;
 }
@@ -1285,10 +1339,15 @@ int ct_count_edge_candidates(const ct_tree* t, int32_t mode, const double* segs,
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
     const int et = seg_threads(t);
-    if (mode == 0)
-        k_edge_cands<false, 0><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
-    else
-        k_edge_cands<false, 1><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, counts, 0, 0);
+    const double4* S = (const double4*)segs;
+    const unsigned g = grid_of(n, et);
+    if (deep_tree(t)) {
+        if (mode == 0) k_edge_cands<false, 0, true><<<g, et, 0, st>>>(T, S, n, order, counts, 0, 0);
+        else k_edge_cands<false, 1, true><<<g, et, 0, st>>>(T, S, n, order, counts, 0, 0);
+    } else {
+        if (mode == 0) k_edge_cands<false, 0, false><<<g, et, 0, st>>>(T, S, n, order, counts, 0, 0);
+        else k_edge_cands<false, 1, false><<<g, et, 0, st>>>(T, S, n, order, counts, 0, 0);
+    }
     CT_CHECK_LAUNCH("count_edge_candidates");
     return CT_OK;
 }
@@ -1302,12 +1361,16 @@ int ct_write_edge_candidates(const ct_tree* t, int32_t mode, const double* segs,
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
     const int et = seg_threads(t);
-    if (mode == 0)
-        k_edge_cands<true, 0><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
-                                                               cand_seg, cand_pos);
-    else
-        k_edge_cands<true, 1><<<grid_of(n, et), et, 0, st>>>(T, (const double4*)segs, n, order, (int64_t*)offsets,
-                                                               cand_seg, cand_pos);
+    const double4* S = (const double4*)segs;
+    const unsigned g = grid_of(n, et);
+    int64_t* off = (int64_t*)offsets;
+    if (deep_tree(t)) {
+        if (mode == 0) k_edge_cands<true, 0, true><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos);
+        else k_edge_cands<true, 1, true><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos);
+    } else {
+        if (mode == 0) k_edge_cands<true, 0, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos);
+        else k_edge_cands<true, 1, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos);
+    }
     CT_CHECK_LAUNCH("write_edge_candidates");
     return CT_OK;
 }

@@ -200,6 +200,132 @@ __global__ void __launch_bounds__(256) k_locate_points(TreeDev T, const double2*
     out[i] = res;
 }
 
+// ------------------------------------------------------------------------
+// Trees deeper than the stacks: the same depth-first traversal without a
+// stack.  A node's children and their visiting order depend only on the
+// query and the node, so the walk goes down to the first child it would have
+// popped, and on the way back up (through node_parent) recomputes the order
+// at the parent to find the sibling still to visit.  Every node is entered at
+// most twice per query.
+// ------------------------------------------------------------------------
+
+// Children of internal node v in locate_point's visiting order (query.py:87-105):
+// both: the one pushed last first; *second = -1 when there is only one.
+__device__ __forceinline__ int order_fp64(const TreeDev& T, int v, const float4& q, double pd, int* second) {
+    double2 nd = T.nd[v];
+    bool left = pd <= nd.x, right = pd >= nd.y;
+    int child = node_a(q);
+    *second = -1;
+    if (left && right) {
+        if ((nd.x - pd) < (pd - nd.y)) {  // pushed left, then right
+            *second = child;
+            return child + 1;
+        }
+        *second = child + 1;
+        return child;
+    }
+    if (left) return child;
+    if (right) return child + 1;
+    return -1;
+}
+
+template <int KT>
+__global__ void __launch_bounds__(256) k_locate_points_deep(TreeDev T, const int* __restrict__ parent,
+                                                            const double2* __restrict__ pts, int64_t n, double tol,
+                                                            int64_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 pp = pts[i];
+    dpt p = mkp(pp.x, pp.y);
+    const int K = KT == 32 ? T.K : KT;
+    int64_t res = -1;
+    int v = 0, from = -1;
+    bool down = true;
+    int64_t budget = 2 * T.n_nodes + 2;
+    while (v >= 0) {
+        if (--budget < 0) {
+            set_error(T.err, CT_DEVERR_LOOP);
+            break;
+        }
+        float4 q = T.nf[v];
+        int b = node_b(q);
+        int next;
+        if (b >= 0) {  // leaf
+            if (down) {
+                int ptr = node_a(q);
+                for (int j = ptr; j < ptr + b && res < 0; j++) {
+                    const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * K);
+                    int len = (KT == 3) ? 3 : (T.plen ? (int)T.plen[j] : K);
+                    if (pip_or_edge(p, poly, len, tol)) res = T.bbi[j];
+                }
+                if (res >= 0) break;
+            }
+            next = -1;
+        } else {
+            int second;
+            int first = order_fp64(T, v, q, (-1 - b) ? p.y : p.x, &second);
+            next = down ? first : ((from == first) ? second : -1);
+        }
+        if (next >= 0) {
+            from = v;
+            v = next;
+            down = true;
+        } else {
+            from = v;
+            v = parent[v];
+            down = false;
+        }
+    }
+    out[i] = res;
+}
+
+__global__ void __launch_bounds__(256) k_locate_on_edge_deep(TreeDev T, const int* __restrict__ parent,
+                                                             const double2* __restrict__ pts, int64_t n, double tol,
+                                                             int64_t* __restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 pp = pts[i];
+    dpt p = mkp(pp.x, pp.y);
+    int64_t res = -1;
+    int v = 0, from = -1;
+    bool down = true;
+    int64_t budget = 2 * T.n_nodes + 2;
+    while (v >= 0) {
+        if (--budget < 0) {
+            set_error(T.err, CT_DEVERR_LOOP);
+            break;
+        }
+        float4 q = T.nf[v];
+        int b = node_b(q);
+        int next;
+        if (b >= 0) {
+            if (down) {
+                int ptr = node_a(q);
+                for (int j = ptr; j < ptr + b && res < 0; j++) {
+                    const double2* e = T.poly + (size_t)j * 2;
+                    if (point_on_edge(p, mkp(e[0].x, e[0].y), mkp(e[1].x, e[1].y), tol)) res = T.bbi[j];
+                }
+                if (res >= 0) break;
+            }
+            next = -1;
+        } else {
+            int second;
+            int first = order_fp64(T, v, q, (-1 - b) ? p.y : p.x, &second);
+            next = down ? first : ((from == first) ? second : -1);
+        }
+        if (next >= 0) {
+            from = v;
+            v = next;
+            down = true;
+        } else {
+            from = v;
+            v = parent[v];
+            down = false;
+        }
+    }
+    out[i] = res;
+}
+
 // locate_point_on_edge query.py:121-164 (edge trees, K == 2).
 template <int STACK>
 __global__ void __launch_bounds__(256) k_locate_on_edge(TreeDev T, const double2* __restrict__ pts, int64_t n,
@@ -391,13 +517,17 @@ __global__ void k_pack_nodes(int64_t n_nodes, const int64_t* __restrict__ child,
                              const double* __restrict__ Rmin, const int64_t* __restrict__ ptr,
                              const int64_t* __restrict__ size, const uint8_t* __restrict__ dim, double ox, double oy,
                              int64_t n_elem, float4* __restrict__ nf, double2* __restrict__ nd,
-                             unsigned int* __restrict__ bad) {
+                             int* __restrict__ parent, unsigned int* __restrict__ bad) {
     int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n_nodes) return;
     // structure check: children after their parent and in range, leaf ranges
     // inside bb_indices -- guarantees every traversal terminates in bounds
     int64_t c = child[v];
     if (c != -1 && (c <= v || c + 1 >= n_nodes)) atomicOr(bad, 1u);
+    if (parent && c > v && c + 1 < n_nodes) {
+        parent[c] = (int)v;
+        parent[c + 1] = (int)v;
+    }
     if (c == -1 && (ptr[v] < 0 || size[v] < 0 || ptr[v] + size[v] > n_elem)) atomicOr(bad, 1u);
     double L = Lmax[v], R = Rmin[v];
     if (!isfinite(L) || !isfinite(R)) atomicOr(bad, 2u);  // not an error: queries keep the literal float64 path
@@ -617,9 +747,10 @@ int ct_pack_tree(ct_tree* t, void* stream) {
     t->origin[0] = ox;
     t->origin[1] = oy;
     if (t->n_nodes > 0) {
+        if (t->node_parent) CT_CUDA(cudaMemsetAsync(t->node_parent, 0xff, (size_t)t->n_nodes * sizeof(int), st));
         k_pack_nodes<<<grid_for(t->n_nodes, 256), 256, 0, st>>>(
             t->n_nodes, t->node_child, t->node_Lmax, t->node_Rmin, t->node_ptr, t->node_size, t->node_dim, ox, oy,
-            t->n_elements, (float4*)t->nodes_f32, (double2*)t->nodes_f64, red + 1);
+            t->n_elements, (float4*)t->nodes_f32, (double2*)t->nodes_f64, t->node_parent, red + 1);
         CT_CHECK_LAUNCH("pack_nodes");
     }
     if (t->n_elements > 0) {
@@ -662,8 +793,17 @@ int ct_locate_points(const ct_tree* t, const double* points, int64_t n, double t
     if (n == 0) return CT_OK;
     if (t->n_nodes <= 0) return ct_fail(CT_ERR_ARG, "tree has no nodes");
     int S = stack_for(t);
-    if (S < 0) return ct_fail(CT_ERR_ARG, "tree deeper than 510 levels");
+    if (S < 0 && !t->node_parent) return ct_fail(CT_ERR_ARG, "tree deeper than 510 levels (no node_parent)");
     TreeDev T = make_dev(t);
+    if (S < 0) {  // deeper than the stacks: the stackless float64 traversal (same results)
+        const double2* P = (const double2*)points;
+        int g = grid_for(n, 256);
+        if (t->n_max_vert == 3) k_locate_points_deep<3><<<g, 256, 0, st>>>(T, t->node_parent, P, n, tol, out);
+        else if (t->n_max_vert == 4) k_locate_points_deep<4><<<g, 256, 0, st>>>(T, t->node_parent, P, n, tol, out);
+        else k_locate_points_deep<32><<<g, 256, 0, st>>>(T, t->node_parent, P, n, tol, out);
+        CT_CHECK_LAUNCH("locate_points (deep tree)");
+        return CT_OK;
+    }
     float tolf = __builtin_nanf("");
     {
         // float32 tolerance rounded up (conservative for the filter)
@@ -699,8 +839,14 @@ int ct_locate_points_on_edge(const ct_tree* t, const double* points, int64_t n, 
     if (n == 0) return CT_OK;
     if (t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "not an edge tree");
     int S = stack_for(t);
-    if (S < 0) return ct_fail(CT_ERR_ARG, "tree deeper than 510 levels");
+    if (S < 0 && !t->node_parent) return ct_fail(CT_ERR_ARG, "tree deeper than 510 levels (no node_parent)");
     TreeDev T = make_dev(t);
+    if (S < 0) {
+        k_locate_on_edge_deep<<<grid_for(n, 256), 256, 0, st>>>(T, t->node_parent, (const double2*)points, n, tol,
+                                                                 out);
+        CT_CHECK_LAUNCH("locate_points_on_edge (deep tree)");
+        return CT_OK;
+    }
     float f = (float)tol;
     if ((double)f < tol) f = nextafterf(f, INFINITY);
     int g = grid_for(n, 256);

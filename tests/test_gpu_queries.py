@@ -272,3 +272,42 @@ def test_work_ordered_boxes_and_segments_match_oracle(oracle):
     segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
     for a, b in zip(g.intersect_edges(segs), o.intersect_edges(segs)):
         assert np.array_equal(a, b, equal_nan=True)
+
+
+@pytest.mark.gpu
+def test_output_budgeted_chunks_reassemble_the_full_results(monkeypatch):
+    """Multi-result queries in ranges of queries whose results stay within a
+    budget (iter_locate_boxes / iter_intersect_boxes / iter_intersect_edges,
+    and the automatic ranges of numpy batches that exceed the device memory):
+    the concatenated ranges equal the one-pass results, in order."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.mixed_mesh(60, 50, seed=8, extent=(60.0, 50.0))
+    g = CellTree2d(xy, f, -1)
+    boxes = syn.random_boxes(3000, (0.0, 0.0), (60.0, 50.0), 0.01, 20.0, seed=2, log_uniform=True)
+    segs = syn.random_segments(700, (0.0, 0.0), (60.0, 50.0), seed=3)  # long segments
+    bd, sd = torch.as_tensor(boxes, device="cuda"), torch.as_tensor(segs, device="cuda")
+    full = [tuple(x.cpu().numpy() for x in g.locate_boxes(bd)), tuple(x.cpu().numpy() for x in g.intersect_boxes(bd)),
+            tuple(x.cpu().numpy() for x in g.intersect_edges(sd))]
+    assert len(full[2][0]) > 20000
+    for budget in (1, 997, 50_000):
+        parts = [list(g.iter_locate_boxes(boxes, budget)), list(g.iter_intersect_boxes(boxes, budget)),
+                 list(g.iter_intersect_edges(segs, budget))]
+        if budget == 1:
+            assert len(parts[0]) == len(boxes) and len(parts[2]) == len(segs)
+        for p, ref in zip(parts, full):
+            for k in range(len(ref)):
+                got = np.concatenate([c[k] for c in p])
+                assert np.array_equal(got, ref[k], equal_nan=True)
+    # numpy batches beyond the device budget take the ranges automatically
+    from numba_celltree_gb300 import celltree_base
+
+    monkeypatch.setattr(celltree_base._GpuTree, "device_budget", lambda self, b: 4096)
+    for got, ref in zip((g.locate_boxes(boxes), g.intersect_boxes(boxes), g.intersect_edges(segs)), full):
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b, equal_nan=True)
+    # empty batches
+    for got in (g.locate_boxes(boxes[:0]), g.intersect_edges(segs[:0])):
+        assert all(len(x) == 0 for x in got)
