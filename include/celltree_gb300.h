@@ -39,6 +39,7 @@ typedef enum ct_status {
 #define CT_DEVERR_CLIP 4u     /* clip polygon scratch (64 vertices) overflow */
 #define CT_DEVERR_CAPACITY 8u /* output capacity exceeded */
 #define CT_DEVERR_LOOP 16u    /* a bounded loop gave up (Cohen-Sutherland) */
+#define CT_DEVERR_NONFINITE 32u /* a coordinate of a batch index is not finite */
 
 int ct_abi_version(void);
 const char* ct_last_error_message(void);
@@ -327,6 +328,76 @@ int ct_forest_locate_prepare(const ct_tree* trees, int32_t n_trees, const double
 int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* out, void* workspace,
                      size_t workspace_bytes, void* stream);
 
+/* The index and query records of a batch built by ct_build_forest_async,
+ * computed on the device (no upstream counterpart).  With it a batch's
+ * build and point location run as one sequence of launches with no host
+ * synchronisation -- ct_counter_clockwise and ct_face_bboxes over the faces,
+ * ct_build_forest_async, ct_forest_index_build, ct_forest_locate -- which can
+ * be captured in one CUDA graph and replayed when the vertices and points
+ * change (the mesh topology and the point counts stay).  Per tree it computes
+ * on the device what ct_bbox_summary, ct_pack_tree and ct_pack_grid compute
+ * for a single tree (bbox, default tolerance, float32 frame, packed nodes and
+ * cells, start-node grid of a fixed shape) and writes the tree records of
+ * ct_forest_locate into its workspace.  The batch locate then runs without
+ * candidate lists (every query traverses from its start node); results equal
+ * ct_locate_points on each tree.  Errors are reported in error_word:
+ * CT_DEVERR_STACK (a tree deeper than `stack` - 2 levels), CT_DEVERR_NONFINITE
+ * (a box or node bound is not finite). */
+typedef struct ct_forest_index {
+    /* inputs (device) */
+    const double* vertices;     /* all meshes' vertices, x y */
+    const int64_t* faces;       /* tree i: n_i x K_i indices into `vertices` (-1 padded) from face_off[i] */
+    const int64_t* face_off;    /* n_trees: first int64 of tree i's faces (also its float64 cells' offset) */
+    const int64_t* poly32_off;  /* n_trees: first float4 of tree i's float32 cells */
+    const int32_t* tree_K;      /* n_trees: n_max_vert of tree i */
+    const double* bb_coords;    /* n_total x 4, the boxes the trees were built from */
+    const int64_t* tree_off;    /* n_trees + 1 face offsets of the trees */
+    const int64_t* node_off;    /* n_trees + 1 node offsets (ct_build_forest_async) */
+    const int32_t* max_depth;   /* n_trees (ct_build_forest_async) */
+    const int64_t* node_child;
+    const double* node_Lmax;
+    const double* node_Rmin;
+    const int64_t* node_ptr;
+    const int64_t* node_size;
+    const uint8_t* node_dim;
+    const int64_t* bb_indices;  /* n_total, relative to each tree */
+    /* start-node grids: tree i has grid_nx[i] x grid_ny[i] cells at
+     * grid_start + grid_off[i] (shapes fixed by the caller, e.g. from
+     * ct_grid_shape; the origin and scale follow each build's boxes) */
+    int32_t* grid_start;
+    const int64_t* grid_off;    /* n_trees + 1 */
+    const int32_t* grid_nx;
+    const int32_t* grid_ny;
+    /* sizes and settings (host) */
+    int64_t n_total;
+    int64_t node_capacity;
+    int64_t grid_cells;         /* grid_off[n_trees] */
+    int32_t n_trees;
+    int32_t k_max;              /* largest K_i */
+    int32_t stack;              /* traversal stack entries per query (deepest tree + 2, at most 128) */
+    int32_t pad_;
+    double tolerance;           /* query tolerance of every tree; <= 0: each tree's default */
+    /* outputs (device), written by ct_forest_index_build */
+    void* nodes_f32;            /* node_capacity x 16 B */
+    void* nodes_f64;            /* node_capacity x 16 B */
+    void* poly_f64;             /* 16 B per face vertex, tree i from face_off[i], leaf order */
+    void* poly_f32;             /* 16 B units, tree i from poly32_off[i] (ct_poly32_stride(K_i) per cell) */
+    uint8_t* poly_len;          /* n_total */
+    uint8_t* poly_len32;        /* n_total */
+    unsigned long long* summary; /* scratch: n_trees x 8 words */
+    unsigned int* error_word;   /* device: CT_DEVERR_* bits */
+} ct_forest_index;
+/* Fills `plan` (points per tree from point_off_host, n_trees + 1 host
+ * offsets; kt and stack from the index's k_max and stack) and uploads the
+ * point offsets into the ct_forest_locate workspace (synchronises; call once
+ * per set of sizes). */
+int ct_forest_index_prepare(const ct_forest_index* index, const int64_t* point_off_host, int64_t n_points,
+                            ct_forest_plan* plan, void* workspace, size_t workspace_bytes, void* stream);
+/* Enqueues the device-side index of the current build (kernels and memsets
+ * only). */
+int ct_forest_index_build(const ct_forest_index* index, const ct_forest_plan* plan, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
 /* locate_points_on_edge query.py:167-174 (locate_point_on_edge 121-164). */
 int ct_locate_points_on_edge(const ct_tree* tree, const double* points, int64_t n, double tolerance,
                              int64_t* out, void* stream);
@@ -482,6 +553,26 @@ size_t ct_build_forest_workspace_size(int64_t n_total, int32_t n_trees, int32_t 
 int ct_build_forest(const double* bb_coords, int64_t n_total, const int64_t* tree_off, int32_t n_trees,
                     int32_t n_buckets, int64_t cells_per_leaf, int32_t capacity_factor, void* workspace,
                     size_t workspace_bytes, int64_t* n_nodes_host, int32_t* max_depth_host, void* stream);
+/* ct_build_forest + ct_build_forest_emit with every tree level driven on
+ * the device: a fixed sequence of launches and no host synchronisation (the
+ * call only enqueues work, so it can be captured in a CUDA graph and
+ * replayed while the boxes change and the tree sizes do not).  tree_off_host
+ * and tree_off_dev hold the same n_trees + 1 offsets.  Outputs on the device:
+ * per tree its node count (n_nodes_dev), node offset into the node arrays
+ * (node_off_dev, n_trees + 1; the arrays hold node_capacity nodes -- the sum
+ * of ct_pessimistic_n_nodes over the trees always suffices), depth
+ * (max_depth_dev); status_dev = 0, or CT_DEVERR_* bits: BUCKET (a centroid
+ * outside every bucket), CAPACITY (record or node capacity exceeded: retry
+ * with a larger capacity_factor), LOOP (more than 64 tree levels above the
+ * subtree size of 128 cells: use ct_build_forest).  Nodes and bb_indices are
+ * those of ct_build_forest whenever status_dev is 0. */
+int ct_build_forest_async(const double* bb_coords, int64_t n_total, const int64_t* tree_off_host,
+                          const int64_t* tree_off_dev, int32_t n_trees, int32_t n_buckets, int64_t cells_per_leaf,
+                          int32_t capacity_factor, void* workspace, size_t workspace_bytes, int64_t node_capacity,
+                          int64_t* child, double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
+                          int64_t* bb_indices, int64_t* n_nodes_dev, int64_t* node_off_dev, int32_t* max_depth_dev,
+                          unsigned int* status_dev, void* stream);
+
 /* node_off: device, n_trees + 1 node offsets (prefix sums of n_nodes); the
  * node arrays hold every tree's nodes at its offset (child, ptr relative to
  * the tree); bb_indices (n_total) hold each tree's indices at its rows. */

@@ -28,6 +28,7 @@ DEVERR_BUCKET = 2
 DEVERR_CLIP = 4
 DEVERR_CAPACITY = 8
 DEVERR_LOOP = 16
+DEVERR_NONFINITE = 32
 
 _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -107,6 +108,25 @@ class CtForestPlan(ctypes.Structure):
     ]
 
 
+class CtForestIndex(ctypes.Structure):
+    """Mirror of ``struct ct_forest_index``."""
+
+    _fields_ = [(n, _P) for n in (
+        "vertices", "faces", "face_off", "poly32_off", "tree_K", "bb_coords", "tree_off", "node_off", "max_depth",
+        "node_child", "node_Lmax", "node_Rmin", "node_ptr", "node_size", "node_dim", "bb_indices", "grid_start",
+        "grid_off", "grid_nx", "grid_ny")] + [
+        ("n_total", _I64),
+        ("node_capacity", _I64),
+        ("grid_cells", _I64),
+        ("n_trees", _I32),
+        ("k_max", _I32),
+        ("stack", _I32),
+        ("pad_", _I32),
+        ("tolerance", _D),
+    ] + [(n, _P) for n in ("nodes_f32", "nodes_f64", "poly_f64", "poly_f32", "poly_len", "poly_len32", "summary",
+                           "error_word")]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "ct_abi_version": (ctypes.c_int, []),
@@ -122,11 +142,16 @@ SIGNATURES = {
     "ct_build_forest_workspace_size": (_SZ, [_I64, _I32, _I32, _I32]),
     "ct_build_forest": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), _I32, _I32, _I64, _I32, _P, _SZ,
                                        ctypes.POINTER(_I64), ctypes.POINTER(_I32), _P]),
+    "ct_build_forest_async": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), _P, _I32, _I32, _I64, _I32, _P, _SZ,
+                                             _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "ct_build_forest_emit": (ctypes.c_int, [_P, _I64, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "ct_forest_locate_workspace_size": (_SZ, [_I64, _I32]),
     "ct_forest_locate_prepare": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_D), ctypes.POINTER(_I64), _I64,
                                                 _P, _P, _SZ, _P]),
     "ct_forest_locate": (ctypes.c_int, [_P, _P, _P, _P, _SZ, _P]),
+    "ct_forest_index_prepare": (ctypes.c_int, [ctypes.POINTER(CtForestIndex), ctypes.POINTER(_I64), _I64, _P, _P,
+                                               _SZ, _P]),
+    "ct_forest_index_build": (ctypes.c_int, [ctypes.POINTER(CtForestIndex), _P, _P, _SZ, _P]),
     "ct_pack_grid": (ctypes.c_int, [_P, _P]),
     "ct_cand_scratch_size": (_SZ, [_P]),
     "ct_cand_count": (ctypes.c_int, [_P, _D, _P, _SZ, ctypes.POINTER(_I64), _P]),
@@ -216,6 +241,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         raise ImportError(f"libcelltree_gb300 ABI {v} != expected {ABI_VERSION}")
     _lib = lib
     return lib
+
+
+def device_error_text(err: int) -> str:
+    """The CT_DEVERR_* bits of a device error word, in words."""
+    names = [(DEVERR_STACK, "traversal stack overflow"), (DEVERR_BUCKET, "centroid outside every bucket"),
+             (DEVERR_CLIP, "clip polygon overflow"), (DEVERR_CAPACITY, "output capacity exceeded"),
+             (DEVERR_LOOP, "bounded loop gave up"), (DEVERR_NONFINITE, "non-finite coordinate")]
+    return ", ".join(text for bit, text in names if err & bit) or f"{err:#x}"
 
 
 def check(status: int, what: str = "") -> None:

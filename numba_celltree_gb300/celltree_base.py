@@ -211,18 +211,7 @@ class _GpuTree:
     def raise_on_device_error(self):
         err = int(self.error_word.item())
         if err:
-            bits = []
-            if err & _lib.DEVERR_STACK:
-                bits.append("traversal stack overflow")
-            if err & _lib.DEVERR_BUCKET:
-                bits.append("centroid outside every bucket")
-            if err & _lib.DEVERR_CLIP:
-                bits.append("clip polygon overflow")
-            if err & _lib.DEVERR_CAPACITY:
-                bits.append("output capacity exceeded")
-            if err & _lib.DEVERR_LOOP:
-                bits.append("bounded loop gave up")
-            raise _lib.CellTreeError("device error: " + ", ".join(bits))
+            raise _lib.CellTreeError("device error: " + _lib.device_error_text(err))
 
     # -- point location ---------------------------------------------------------
     @staticmethod

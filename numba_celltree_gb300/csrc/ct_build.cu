@@ -79,7 +79,13 @@ struct Counters {
     int pad;
     unsigned long long root_key[4];
     int root_zp[4];
+    int done;    // device-driven level loop: no pending record left (or an error)
+    int nlev;    // device-driven level loop: phase-A levels recorded in lvl_b / lvl_e
 };
+
+// most phase-A levels the device-driven level loop runs (a balanced tree of
+// 2^31 cells needs about 30; more sets CT_DEVERR_LOOP in the status)
+constexpr int DEV_MAX_LEVELS = 64;
 
 struct WS {
     double* f[2][6];  // lo_x, hi_x, lo_y, hi_y, c_x, c_y (two ping-pong buffers)
@@ -101,6 +107,8 @@ struct WS {
     LRec* lrec;                      // [2 * n]
     Counters* cnt;
     int* level_begin;                // [rec_cap + 1] host mirror written per level
+    int* lvl_b;                      // [DEV_MAX_LEVELS + 1] level record ranges (device-driven loop)
+    int* lvl_e;
     // per tree (a forest build has n_roots trees, root records 0 .. n_roots-1)
     int n_roots;
     int64_t* tree_off;               // [n_roots + 1] element offsets
@@ -146,6 +154,8 @@ static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_tre
     w.lrec = (LRec*)take(sizeof(LRec) * 2 * nn);
     w.cnt = (Counters*)take(sizeof(Counters));
     w.level_begin = nullptr;
+    w.lvl_b = (int*)take(sizeof(int) * (DEV_MAX_LEVELS + 1));
+    w.lvl_e = (int*)take(sizeof(int) * (DEV_MAX_LEVELS + 1));
     w.n_roots = n_trees;
     w.tree_off = (int64_t*)take(sizeof(int64_t) * ((size_t)n_trees + 1));
     w.elem_tree = (int*)take(n_trees > 1 ? sizeof(int) * nn : 16);
@@ -351,6 +361,8 @@ __global__ void k_reset(WS ws, int n, int cpl_small_root, int root_dim) {
     c->max_depth = 0;
     c->lb = 0;
     c->le = 1;
+    c->done = 0;
+    c->nlev = 1;
     for (int f = 0; f < 4; f++) {
         c->root_key[f] = ~0ull;
         c->root_zp[f] = INT32_MAX;
@@ -426,6 +438,7 @@ __device__ __forceinline__ int tile_len_for(int size) {
 // One warp per record of the current level: make tiles for pending nodes and
 // reset their stats slots.
 __global__ void k_make_tiles(WS ws, int NB) {
+    if (ws.cnt->done) return;
     int lb = ws.cnt->lb, le = ws.cnt->le;
     int lane = threadIdx.x & 31;
     int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -464,13 +477,18 @@ __global__ void k_make_tiles(WS ws, int NB) {
 // Per tile: bucket membership in both dimensions; per (dim, bucket): count,
 // first-occurrence min of lo_x / lo_y and max of hi_x / hi_y (as min-form
 // keys) and the first position of a zero value.
+// LOOP: the device-driven level loop's form -- a fixed grid walks the tiles
+// whose count the make-tiles pass left on the device.
+template <bool LOOP>
 __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int NB) {
     __shared__ unsigned long long K[2][NBMAX + 1];
     __shared__ unsigned int cnt[2][NBMAX];
     __shared__ unsigned long long key[2][NBMAX][4];
     __shared__ int zp[2][NBMAX][4];
     const unsigned FULL = 0xffffffffu;
-    int t = blockIdx.x;
+    const int nt = LOOP ? (ws.cnt->done ? 0 : ws.cnt->tile_count) : (int)gridDim.x;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    if (LOOP) __syncthreads();  // the previous tile's readers are done with the shared arrays
     int r = ws.tile_rec[t];
     int s = ws.tile_start[t], e = ws.tile_end[t];
     int lb = ws.cnt->lb;
@@ -548,10 +566,12 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
             if (zp[d][b][f] != INT32_MAX) atomicMin(&ws.st_zp[sidx * 2 * NB * 4 + j], zp[d][b][f]);
         }
     }
+    }
 }
 
 // One warp per record of the current level: the upstream split decision for
 // pending nodes, children records, bucket bases and tile prefixes.
+template <bool LOOP>
 __global__ void k_decide(WS ws, int NB, long long cpl) {
     __shared__ int s_cnt[4][2][NBMAX];
     __shared__ double s_Rmin[4][2][NBMAX];
@@ -559,11 +579,13 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int w = threadIdx.x >> 5;  // blockDim = 128
+    if (LOOP && ws.cnt->done) return;
     int lb = ws.cnt->lb, le = ws.cnt->le;
-    int r = lb + blockIdx.x * 4 + w;
-    if (r >= le) return;
+    const int step = LOOP ? (int)gridDim.x * 4 : INT32_MAX / 2;
+    for (int r = lb + blockIdx.x * 4 + w; r < le; r += step) {
+    __syncwarp();
     ARec* R = &ws.recs[r];
-    if (R->kind != K_PENDING) return;
+    if (R->kind != K_PENDING) continue;
     int parity = R->parity;
     size_t sidx = (size_t)(r - lb);
     int size = R->size, ptr = R->ptr;
@@ -628,7 +650,7 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
             R->Lmax = -1.0;
             R->Rmin = -1.0;
         }
-        return;
+        continue;
     }
     // split in ds
     int c = 0;
@@ -640,7 +662,7 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
             R->kind = K_LEAF;
             R->split_dim = -1;
         }
-        return;
+        continue;
     }
     int rb = D.rbucket;
     // child bounds: first occurrence over the child's buckets in order
@@ -722,16 +744,20 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
         }
     }
 }
+}
 
 // Per tile: stable partition of split nodes into the other buffer; leaf cells
 // go straight to their final position.
+template <bool LOOP>
 __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, int NB) {
     __shared__ unsigned long long K[NBMAX + 1];
     __shared__ int base[NBMAX];
     __shared__ int run[NBMAX];
     __shared__ int wcnt[STATS_THREADS / 32][NBMAX];
     const unsigned FULL = 0xffffffffu;
-    int t = blockIdx.x;
+    const int nt = LOOP ? (ws.cnt->done ? 0 : ws.cnt->tile_count) : (int)gridDim.x;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+    if (LOOP) __syncthreads();
     int r = ws.tile_rec[t];
     int s = ws.tile_start[t], e = ws.tile_end[t];
     int lb = ws.cnt->lb;
@@ -740,7 +766,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
     const int* idx_in = ws.idx[parity];
     if (R->kind != K_SPLIT) {
         for (int i = s + tid; i < e; i += blockDim.x) ws.final_idx[i] = idx_in[i];
-        return;
+        continue;
     }
     int ds = R->split_dim;
     size_t sidx = (size_t)(r - lb);
@@ -781,6 +807,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
             run[tid] += tot;
         }
         __syncthreads();
+    }
     }
 }
 
@@ -824,14 +851,17 @@ __device__ __forceinline__ double warp_range_extreme(const SubSmem& S, int f, bo
     return S.F[f][S.perm[p + (int)po]];
 }
 
+template <bool LOOP>
 __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long long cpl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const unsigned FULL = 0xffffffffu;
     int lane = threadIdx.x & 31;
     int w = threadIdx.x >> 5;
     SubSmem& S = reinterpret_cast<SubSmem*>(smem_raw)[w];
-    int sidx = blockIdx.x * SUB_WARPS + w;
-    if (sidx >= ws.cnt->small_count) return;
+    const int nsmall = ws.cnt->small_count;
+    const int step = LOOP ? (int)gridDim.x * SUB_WARPS : INT32_MAX / 2;
+    for (int sidx = blockIdx.x * SUB_WARPS + w; sidx < nsmall; sidx += step) {
+    __syncwarp();
     int r = ws.small_list[sidx];
     ARec* RR = &ws.recs[r];
     int p0 = RR->ptr, s = RR->size, par = RR->parity, d0 = RR->dim, lvl = RR->level;
@@ -1016,11 +1046,110 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         atomicMax(&ws.tree_depth[RR->tree], maxd);
         if (err) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
     }
+    }
 }
 
 // ------------------------------------------------------------------------
 // phase C: numbering and emission
 // ------------------------------------------------------------------------
+
+// ---- the device-driven level loop: per-level bookkeeping on the device ----
+__global__ void k_level_start(WS ws) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && !ws.cnt->done) ws.cnt->tile_count = 0;
+}
+
+// After a level's scatter: the records it created are the next level; none
+// (or a capacity error) ends the loop.
+__global__ void k_level_next(WS ws, int L) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Counters* c = ws.cnt;
+    if (c->done) return;
+    int nb = c->le, ne = c->rec_count;
+    if ((c->err & 0x80000000u) || ne == nb) {
+        c->done = 1;
+        return;
+    }
+    if (L + 1 >= DEV_MAX_LEVELS) {  // more levels than the loop runs
+        c->done = 1;
+        c->err |= CT_DEVERR_LOOP;
+        return;
+    }
+    c->lb = nb;
+    c->le = ne;
+    ws.lvl_b[L + 1] = nb;
+    ws.lvl_e[L + 1] = ne;
+    c->nlev = L + 2;
+}
+
+__global__ void k_count_up_dev(WS ws, int L) {
+    if (L >= ws.cnt->nlev) return;
+    int b = ws.lvl_b[L], e = ws.lvl_e[L];
+    for (int r = b + blockIdx.x * blockDim.x + threadIdx.x; r < e; r += gridDim.x * blockDim.x) {
+        ARec* R = &ws.recs[r];
+        if (R->kind == K_SPLIT) R->splits = 1 + ws.recs[R->child].splits + ws.recs[R->child + 1].splits;
+        else if (R->kind == K_LEAF) R->splits = 0;
+    }
+}
+
+__global__ void k_number_down_dev(WS ws, int L) {
+    if (L >= ws.cnt->nlev) return;
+    int b = ws.lvl_b[L], e = ws.lvl_e[L];
+    for (int r = b + blockIdx.x * blockDim.x + threadIdx.x; r < e; r += gridDim.x * blockDim.x) {
+        ARec* R = &ws.recs[r];
+        if (r < ws.n_roots) {
+            R->S = 0;
+            R->pos = 0;
+        }
+        if (R->kind == K_SPLIT) {
+            ARec* A = &ws.recs[R->child];
+            ARec* B = &ws.recs[R->child + 1];
+            A->S = R->S + 1;
+            B->S = R->S + 1 + A->splits;
+            A->pos = 1 + 2 * R->S;
+            B->pos = 2 + 2 * R->S;
+        }
+    }
+}
+
+// Node counts (1 + 2 splits of the root), their offsets (one block, serial
+// prefix in chunks of the block) and depths per tree; the status word gets
+// the builder's error bits and whether the node capacity holds the trees.
+__global__ void k_forest_counts(WS ws, int64_t* n_nodes, int64_t* node_off, int* depth, int64_t capacity,
+                                unsigned int* status) {
+    __shared__ long long carry;
+    __shared__ long long part[256];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ws.n_roots; base += blockDim.x) {
+        int t = base + threadIdx.x;
+        long long v = 0;
+        if (t < ws.n_roots) {
+            v = 1 + 2 * ws.recs[t].splits;
+            n_nodes[t] = v;
+            depth[t] = ws.tree_depth[t];
+        }
+        part[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+            long long y = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+            __syncthreads();
+            part[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (t < ws.n_roots) node_off[t] = carry + part[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += part[threadIdx.x];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        node_off[ws.n_roots] = carry;
+        unsigned st = ws.cnt->err & (CT_DEVERR_BUCKET | CT_DEVERR_LOOP);
+        if (ws.cnt->err & 0x80000000u) st |= CT_DEVERR_CAPACITY;
+        if (!ws.cnt->done && ws.cnt->nlev > 0 && ws.cnt->tile_count > 0) st |= CT_DEVERR_LOOP;
+        if (carry > capacity) st |= CT_DEVERR_CAPACITY;
+        *status = st;
+    }
+}
 
 __global__ void k_count_up(WS ws, int b, int e) {
     int r = b + blockIdx.x * blockDim.x + threadIdx.x;
@@ -1126,6 +1255,53 @@ __global__ void k_emit_indices(WS ws, int n, int64_t* bb_indices, bool forest) {
         bb_indices[i] = forest ? ws.final_idx[i] - ws.tree_off[ws.elem_tree[i]] : ws.final_idx[i];
 }
 
+__global__ void k_emit_phaseA_dev(WS ws, NodesOut o, const int64_t* node_off, const unsigned int* status) {
+    if (*status) return;
+    int nrec = ws.cnt->rec_count;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += gridDim.x * blockDim.x) {
+        const ARec* R = &ws.recs[r];
+        if (R->kind != K_SPLIT && R->kind != K_LEAF) continue;
+        long long noff, nn, eoff;
+        tree_frame(ws, node_off, 0, R->tree, &noff, &nn, &eoff);
+        if (R->pos < 0 || R->pos >= nn) {
+            atomicOr(&ws.cnt->err, 0x40000000u);
+            continue;
+        }
+        if (R->kind == K_SPLIT)
+            put_node(o, noff + R->pos, 1 + 2 * R->S, R->Lmax, R->Rmin, R->ptr - eoff, R->size, R->dim);
+        else put_node(o, noff + R->pos, -1, R->Lmax, R->Rmin, R->ptr - eoff, R->size, R->dim);
+    }
+}
+
+__global__ void k_emit_subtrees_dev(WS ws, NodesOut o, const int64_t* node_off, const unsigned int* status) {
+    if (*status) return;
+    int lane = threadIdx.x & 31;
+    int nsmall = ws.cnt->small_count;
+    for (int sidx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sidx < nsmall;
+         sidx += (gridDim.x * blockDim.x) >> 5) {
+        const ARec* R = &ws.recs[ws.small_list[sidx]];
+        const LRec* Lr = ws.lrec + 2 * (size_t)R->ptr;
+        long long off = 2 * R->S;
+        long long noff, nn, eoff;
+        tree_frame(ws, node_off, 0, R->tree, &noff, &nn, &eoff);
+        for (int j = lane; j < R->nlocal; j += 32) {
+            LRec a = Lr[j];
+            long long pos = (j == 0) ? R->pos : (long long)j + off;
+            long long child = (a.child < 0) ? -1 : (long long)a.child + off;
+            if (pos < 0 || pos >= nn || child >= nn) {
+                atomicOr(&ws.cnt->err, 0x40000000u);
+                continue;
+            }
+            put_node(o, noff + pos, child, a.Lmax, a.Rmin, a.ptr - eoff, a.size, a.dim);
+        }
+    }
+}
+
+// emission errors (a node position outside its tree's range) into the status
+__global__ void k_forest_status_final(WS ws, unsigned int* status) {
+    if (threadIdx.x == 0 && blockIdx.x == 0 && (ws.cnt->err & 0x40000000u)) *status |= CT_DEVERR_CAPACITY;
+}
+
 // ------------------------------------------------------------------------
 // forest initialisation: one root record per tree
 // ------------------------------------------------------------------------
@@ -1139,6 +1315,10 @@ __global__ void k_forest_reset(WS ws) {
     c->max_depth = 0;
     c->lb = 0;
     c->le = ws.n_roots;
+    c->done = 0;
+    c->nlev = 1;
+    ws.lvl_b[0] = 0;
+    ws.lvl_e[0] = ws.n_roots;
 }
 
 __global__ void k_forest_roots(WS ws) {
@@ -1245,7 +1425,7 @@ static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_p
                         Counters* hc_out) {
     // a function attribute belongs to the current device (and context): set
     // it on every call rather than once per process
-    CT_CUDA(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CT_CUDA(cudaFuncSetAttribute(k_subtree<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(SUB_WARPS * sizeof(SubSmem))));
     std::vector<int> level_b, level_e;
     level_b.push_back(0);
@@ -1266,9 +1446,9 @@ static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_p
             if (hc.err & 0x80000000u) return ct_fail(CT_ERR_WORKSPACE, "builder tile capacity exceeded");
             int ntiles = hc.tile_count;
             if (ntiles == 0) break;
-            k_stats<<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
-            k_decide<<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
-            k_scatter<<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_stats<false><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_decide<false><<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
+            k_scatter<false><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
             CT_CHECK_LAUNCH("phase A level");
             CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
             CT_CUDA(cudaStreamSynchronize(st));
@@ -1290,7 +1470,7 @@ static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_p
     int nsmall = hc.small_count;
     if (nsmall > 0) {
         int blocks = (nsmall + SUB_WARPS - 1) / SUB_WARPS;
-        k_subtree<<<blocks, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
+        k_subtree<false><<<blocks, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
         CT_CHECK_LAUNCH("subtree");
     }
     // phase C: split counts bottom-up, pre-order ranks top-down
@@ -1436,6 +1616,80 @@ int ct_build_forest(const double* bb, int64_t n_total, const int64_t* tree_off_h
         if (n_nodes_host) n_nodes_host[t] = 1 + 2 * roots[t].splits;
         if (max_depth_host) max_depth_host[t] = depth[t];
     }
+    return CT_OK;
+}
+
+// Build + emit of a forest with every level driven on the device: a fixed
+// sequence of launches (the level loop runs DEV_MAX_LEVELS times; levels past
+// the last one find nothing to do), no host synchronisation, so the whole
+// call can be captured in a CUDA graph and replayed.  The trees' sizes are
+// fixed by the host-side offsets; everything that depends on the boxes --
+// levels, node counts and offsets, depths -- stays on the device.
+int ct_build_forest_async(const double* bb, int64_t n_total, const int64_t* tree_off_host,
+                          const int64_t* tree_off_dev, int32_t n_trees, int32_t NB, int64_t cpl, int32_t factor,
+                          void* workspace, size_t ws_bytes, int64_t node_capacity, int64_t* child, double* Lmax,
+                          double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim, int64_t* bb_indices,
+                          int64_t* n_nodes_dev, int64_t* node_off_dev, int32_t* max_depth_dev,
+                          unsigned int* status_dev, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (NB < 2 || NB > NBMAX) return ct_fail(CT_ERR_ARG, "n_buckets must be in [2, 32] for the GPU builder");
+    if (cpl < 1) return ct_fail(CT_ERR_ARG, "cells_per_leaf must be >= 1");
+    if (n_trees < 1 || !tree_off_host || !tree_off_dev) return ct_fail(CT_ERR_ARG, "need at least one tree");
+    if (n_total < 1 || n_total >= (int64_t)INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "n_elements out of range");
+    if (factor < 1) return ct_fail(CT_ERR_ARG, "capacity_factor must be >= 1");
+    if (tree_off_host[0] != 0 || tree_off_host[n_trees] != n_total)
+        return ct_fail(CT_ERR_ARG, "tree offsets must start at 0 and end at n_total");
+    if (!n_nodes_dev || !node_off_dev || !max_depth_dev || !status_dev || !bb_indices || !child)
+        return ct_fail(CT_ERR_ARG, "null output");
+    bool any_large = false;
+    for (int t = 0; t < n_trees; t++) {
+        int64_t m = tree_off_host[t + 1] - tree_off_host[t];
+        if (m < 1) return ct_fail(CT_ERR_ARG, "every tree needs at least one element");
+        any_large |= m > SMALL;
+    }
+    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+    if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
+    if (!bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
+    WS ws;
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    CT_CUDA(cudaMemcpyAsync(ws.tree_off, tree_off_dev, sizeof(int64_t) * ((size_t)n_trees + 1),
+                            cudaMemcpyDeviceToDevice, st));
+    const int ni = (int)n_total;
+    const int g = (int)std::min<int64_t>((n_total + 255) / 256, 152 * 8);
+    const int gt = (int)std::min<int64_t>((n_trees + 255) / 256, 152 * 8);
+    k_forest_reset<<<1, 1, 0, st>>>(ws);
+    k_forest_roots<<<gt, 256, 0, st>>>(ws);
+    k_init_elems<<<g, 256, 0, st>>>(bb, ni, ws);
+    k_forest_elem_tree<<<g, 256, 0, st>>>(ws, ni);
+    k_forest_root_bounds<<<g, 256, 0, st>>>(ws, ni);
+    k_forest_root_resolve<<<gt, 256, 0, st>>>(ws);
+    CT_CHECK_LAUNCH("forest init");
+    CT_CUDA(cudaFuncSetAttribute(k_subtree<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(SUB_WARPS * sizeof(SubSmem))));
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int G = sms * 8;
+    if (any_large) {
+        for (int L = 0; L < DEV_MAX_LEVELS; L++) {
+            const int parity = L & 1;
+            k_level_start<<<1, 32, 0, st>>>(ws);
+            k_make_tiles<<<G, 128, 0, st>>>(ws, NB);
+            k_stats<true><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_decide<true><<<G, 128, 0, st>>>(ws, NB, (long long)cpl);
+            k_scatter<true><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_level_next<<<1, 32, 0, st>>>(ws, L);
+        }
+    }
+    k_subtree<true><<<G, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
+    for (int L = DEV_MAX_LEVELS - 1; L >= 0; L--) k_count_up_dev<<<sms * 4, 256, 0, st>>>(ws, L);
+    for (int L = 0; L < DEV_MAX_LEVELS; L++) k_number_down_dev<<<sms * 4, 256, 0, st>>>(ws, L);
+    k_forest_counts<<<1, 256, 0, st>>>(ws, n_nodes_dev, node_off_dev, max_depth_dev, node_capacity, status_dev);
+    NodesOut o{child, Lmax, Rmin, ptr, size, dim};
+    k_emit_phaseA_dev<<<G, 256, 0, st>>>(ws, o, node_off_dev, status_dev);
+    k_emit_subtrees_dev<<<G, 256, 0, st>>>(ws, o, node_off_dev, status_dev);
+    k_emit_indices<<<g, 256, 0, st>>>(ws, ni, bb_indices, true);
+    k_forest_status_final<<<1, 32, 0, st>>>(ws, status_dev);
+    CT_CHECK_LAUNCH("forest build (device-driven)");
     return CT_OK;
 }
 

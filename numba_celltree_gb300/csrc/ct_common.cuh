@@ -138,6 +138,14 @@ __device__ __forceinline__ double fkey_inv(unsigned long long k) {
     return __longlong_as_double((long long)b);
 }
 
+// Diagonal of a box of sides dx, dy as numpy evaluates sqrt(dx**2 + dy**2)
+// (bbox_distances, celltree_base.py:20-48): products and sum rounded
+// separately (no fused multiply-add), so that the default tolerance derived
+// from the largest diagonal is the same wherever it is computed.
+__device__ __forceinline__ double box_diagonal(double dx, double dy) {
+    return sqrt(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+}
+
 __device__ __forceinline__ void set_error(unsigned int* err, unsigned int bit) {
     if (err) atomicOr(err, bit);
 }

@@ -858,39 +858,44 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const KI* __restrict__ kin,
 // ---------------------------------------------------------------------------
 // start-node grid
 // ---------------------------------------------------------------------------
-// One thread per grid cell: follow the root path while every point of the
-// cell (its range widened by `m`) takes one and the same single child.  The
-// float32 node bounds are within `band` of the float64 bounds, so a decision
-// is certain when the cell range clears bound -/+ band (directed rounding).
+// Start node of grid cell (gx, gy): follow the root path while every point of
+// the cell (its range widened by `m`) takes one and the same single child.
+// The float32 node bounds are within `band` of the float64 bounds, so a
+// decision is certain when the cell range clears bound -/+ band (directed
+// rounding).
+__device__ __forceinline__ int grid_cell_start(const float4* __restrict__ nf, int gx, int gy, float x0, float y0,
+                                               float sx, float sy, double m, float band, int max_steps) {
+    float xlo = __double2float_rd((double)x0 + (double)gx / (double)sx - m);
+    float xhi = __double2float_ru((double)x0 + (double)(gx + 1) / (double)sx + m);
+    float ylo = __double2float_rd((double)y0 + (double)gy / (double)sy - m);
+    float yhi = __double2float_ru((double)y0 + (double)(gy + 1) / (double)sy + m);
+    int v = 0;
+    for (int k = 0; k < max_steps; k++) {
+        float4 q = nf[v];
+        int b = nbq(q);
+        if (b >= 0) break;  // leaf
+        int dim = -1 - b;
+        float lo = dim ? ylo : xlo, hi = dim ? yhi : xhi;
+        bool all_left = hi < __fsub_rd(q.x, band), no_left = lo > __fadd_ru(q.x, band);
+        bool all_right = lo > __fadd_ru(q.y, band), no_right = hi < __fsub_rd(q.y, band);
+        if (!((all_left || no_left) && (all_right || no_right))) break;  // a bound inside the cell
+        if (all_left && all_right) break;                                // both children taken
+        if (all_left) v = na(q);
+        else if (all_right) v = na(q) + 1;
+        else {
+            v = -1;  // no child: locate_point returns -1
+            break;
+        }
+    }
+    return v;
+}
+
+// One thread per grid cell of one tree.
 __global__ void k_grid_start(const float4* __restrict__ nf, int gnx, int gny, float x0, float y0, float sx, float sy,
                              double m, float band, int max_steps, int* __restrict__ start) {
     int64_t total = (int64_t)gnx * gny;
-    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
-        int gx = (int)(c % gnx), gy = (int)(c / gnx);
-        float xlo = __double2float_rd((double)x0 + (double)gx / (double)sx - m);
-        float xhi = __double2float_ru((double)x0 + (double)(gx + 1) / (double)sx + m);
-        float ylo = __double2float_rd((double)y0 + (double)gy / (double)sy - m);
-        float yhi = __double2float_ru((double)y0 + (double)(gy + 1) / (double)sy + m);
-        int v = 0;
-        for (int k = 0; k < max_steps; k++) {
-            float4 q = nf[v];
-            int b = nbq(q);
-            if (b >= 0) break;  // leaf
-            int dim = -1 - b;
-            float lo = dim ? ylo : xlo, hi = dim ? yhi : xhi;
-            bool all_left = hi < __fsub_rd(q.x, band), no_left = lo > __fadd_ru(q.x, band);
-            bool all_right = lo > __fadd_ru(q.y, band), no_right = hi < __fsub_rd(q.y, band);
-            if (!((all_left || no_left) && (all_right || no_right))) break;  // a bound inside the cell
-            if (all_left && all_right) break;                                // both children taken
-            if (all_left) v = na(q);
-            else if (all_right) v = na(q) + 1;
-            else {
-                v = -1;  // no child: locate_point returns -1
-                break;
-            }
-        }
-        start[c] = v;
-    }
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x)
+        start[c] = grid_cell_start(nf, (int)(c % gnx), (int)(c / gnx), x0, y0, sx, sy, m, band, max_steps);
 }
 
 // ---------------------------------------------------------------------------
@@ -1354,6 +1359,242 @@ static int scatter_results(const LocWS& L, int64_t n, unsigned int* err, int64_t
     return CT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Device-side index of a batch built by ct_build_forest_async: the per-tree
+// summaries and records that ct_bbox_summary, ct_pack_tree, ct_pack_grid and
+// ct_forest_locate_prepare derive on the host for single trees, computed
+// here so that no value has to come back to the host between the build and
+// the locate.
+// ---------------------------------------------------------------------------
+constexpr int FX_WORDS = 8;  // summary words per tree: 5 reduction keys, grid margin
+
+// Stand-in tree of a build that overflowed its node capacity (its node
+// ranges are not usable): one empty leaf, so that every query of the batch
+// ends at once with -1 while the error word reports the overflow.
+__device__ float4 g_fx_empty_leaf = {0.0f, 0.0f, 0.0f, 0.0f};
+__device__ double2 g_fx_empty_bounds = {0.0, 0.0};
+
+// std::max as the host computes it ((a < b) ? b : a)
+__device__ __forceinline__ double hmax(double a, double b) { return (a < b) ? b : a; }
+
+// Tree of row r of a batch: the largest t with off[t] <= r (trees with no
+// rows share their offset with the next tree).
+__device__ __forceinline__ int tree_of_row(const int64_t* __restrict__ off, int n_trees, int64_t r) {
+    int lo = 0, hi = n_trees - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_fx_reset(unsigned long long* __restrict__ summary, int n_trees, unsigned int* __restrict__ err) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n_trees * FX_WORDS;
+         i += (int64_t)gridDim.x * blockDim.x)
+        summary[i] = ~0ull;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && err) *err = 0u;
+}
+
+// Per-tree bbox and largest box diagonal (bbox_tree / bbox_distances,
+// celltree_base.py:20-48) as order-preserving keys reduced with atomicMin;
+// a warp whose rows all belong to one tree reduces in registers first.
+__global__ void k_fx_summary(const double* __restrict__ bb, int64_t n, const int64_t* __restrict__ tree_off,
+                             int n_trees, unsigned long long* __restrict__ summary, unsigned int* __restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        unsigned long long k[5] = {~0ull, ~0ull, ~0ull, ~0ull, ~0ull};
+        int t = -1;
+        if (valid) {
+            t = tree_of_row(tree_off, n_trees, i);
+            double4 b = reinterpret_cast<const double4*>(bb)[i];
+            if (!isfinite(b.x) || !isfinite(b.y) || !isfinite(b.z) || !isfinite(b.w))
+                set_error(err, CT_DEVERR_NONFINITE);
+            k[0] = fkey(b.x);
+            k[1] = ~fkey(b.y);
+            k[2] = fkey(b.z);
+            k[3] = ~fkey(b.w);
+            k[4] = ~fkey(box_diagonal(b.y - b.x, b.w - b.z));
+        }
+        const int t0 = __shfl_sync(0xffffffffu, t, 0);  // lane 0 is valid (base < n)
+        if (__all_sync(0xffffffffu, !valid || t == t0)) {
+            for (int j = 0; j < 5; j++) {
+                unsigned long long m = k[j];
+                for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+                if (lane == 0) atomicMin(&summary[(int64_t)t0 * FX_WORDS + j], m);
+            }
+        } else if (valid) {
+            for (int j = 0; j < 5; j++) atomicMin(&summary[(int64_t)t * FX_WORDS + j], k[j]);
+        }
+    }
+}
+
+// One thread per tree: the tree record of the batched locate (the fields
+// fill_tree takes from a packed ct_tree), its Morton grid, and the margin of
+// its start-node grid (summary word 5).
+__global__ void k_fx_records(const __grid_constant__ ct_forest_index X, TreeL* __restrict__ trees,
+                             Grid* __restrict__ grids) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= X.n_trees) return;
+    unsigned long long* S = X.summary + (int64_t)t * FX_WORDS;
+    const double b0 = fkey_inv(S[0]), b1 = fkey_inv(~S[1]), b2 = fkey_inv(S[2]), b3 = fkey_inv(~S[3]);
+    const double diag = fkey_inv(~S[4]);
+    const int64_t e0 = X.tree_off[t];
+    const int K = X.tree_K[t];
+    // origin: bbox centre (ct_pack_tree)
+    double ox = 0.5 * (b0 + b1), oy = 0.5 * (b2 + b3);
+    if (!isfinite(ox) || !isfinite(oy)) {
+        ox = 0.0;
+        oy = 0.0;
+    }
+    TreeL T;
+    memset(&T, 0, sizeof(T));
+    T.nf = (const float4*)X.nodes_f32 + X.node_off[t];
+    T.nd = (const double2*)X.nodes_f64 + X.node_off[t];
+    T.poly = (const double2*)X.poly_f64 + X.face_off[t];
+    T.polyf = (const float4*)X.poly_f32 + X.poly32_off[t];
+    T.plen = (K == 3) ? nullptr : X.poly_len + e0;
+    T.plen32 = X.poly_len32 + e0;
+    T.bbi = X.bb_indices + e0;
+    T.err = X.error_word;
+    T.n_nodes = X.node_off[t + 1] - X.node_off[t];
+    const bool over = X.node_off[X.n_trees] > X.node_capacity;
+    if (over) {
+        set_error(X.error_word, CT_DEVERR_CAPACITY);
+        T.nf = &g_fx_empty_leaf;
+        T.nd = &g_fx_empty_bounds;
+        T.n_nodes = 1;
+    }
+    T.ox = ox;
+    T.oy = oy;
+    double amax = hmax(hmax(fabs(b0), fabs(b1)), hmax(fabs(b2), fabs(b3)));
+    if (!isfinite(amax)) amax = 0.0;
+    T.dabs = __double2float_rn(amax * 8.881784197001252e-16) + 1e-30f;
+    const double F = hmax(hmax(b1 - ox, ox - b0), hmax(b3 - oy, oy - b2));
+    const double Fb = (!(F >= 0.0) || !isfinite(F)) ? 0.0 : F;
+    T.bandG = __double2float_rn(Fb * 2.384185791015625e-07 * 1.0001) + 1e-30f;
+    // start-node grid of the caller's shape over this build's bbox (ct_pack_grid)
+    const int gnx = X.grid_nx[t], gny = X.grid_ny[t];
+    const double ex = b1 - b0, ey = b3 - b2;
+    bool grid_ok = !over && gnx > 0 && gny > 0 && ex > 0.0 && ey > 0.0 && isfinite(ex) && isfinite(ey) && isfinite(F);
+    if (grid_ok) {
+        T.gx0 = __double2float_rn(b0 - ox);
+        T.gy0 = __double2float_rn(b2 - oy);
+        T.gsx = __double2float_rn((double)gnx / ex);
+        T.gsy = __double2float_rn((double)gny / ey);
+        grid_ok = T.gsx > 0.0f && T.gsy > 0.0f && isfinite(T.gsx) && isfinite(T.gsy);
+    }
+    T.gstart = grid_ok ? X.grid_start + X.grid_off[t] : nullptr;
+    T.gnx = grid_ok ? gnx : 0;
+    T.gny = grid_ok ? gny : 0;
+    S[5] = (unsigned long long)__double_as_longlong(grid_ok ? ldexp(hmax(ex, ey) + F, -19) : 0.0);
+    T.coff = nullptr;  // no candidate lists
+    T.K = K;
+    T.S4 = poly32_stride(K);
+    const int need = X.max_depth[t] + 2;
+    if (need > X.stack) set_error(X.error_word, CT_DEVERR_STACK);
+    T.stack = need < X.stack ? need : X.stack;
+    // query tolerance: the given one, or default_tolerance (celltree_base.py:51-52)
+    double tol = X.tolerance;
+    if (!(tol > 0.0)) {
+        const double d = 1e-12 * diag;
+        tol = (d > 1e-15) ? d : 1e-15;
+    }
+    T.tol = tol;
+    T.tolf = __double2float_ru(tol);
+    T.ohx = __double2float_rn(ox);
+    T.olx = __double2float_rn(ox - (double)T.ohx);
+    T.ohy = __double2float_rn(oy);
+    T.oly = __double2float_rn(oy - (double)T.ohy);
+    trees[t] = T;
+    // Morton grid of the query sort (morton_grid)
+    Grid g;
+    g.x0 = __double2float_rn(b0);
+    g.y0 = __double2float_rn(b2);
+    g.sx = (ex > 0.0) ? __double2float_rn(4096.0 / ex) : 0.0f;
+    g.sy = (ey > 0.0) ? __double2float_rn(4096.0 / ey) : 0.0f;
+    grids[t] = g;
+}
+
+// Packed nodes of every tree (k_pack_nodes over the batch): node v of the
+// batch belongs to the tree whose node range holds it; child and ptr are
+// relative to the tree.  The structure check of k_pack_nodes (children after
+// their parent and inside the tree, leaf ranges inside the tree's cells)
+// turns a bad node into an empty leaf and reports it, so that no traversal
+// leaves the tree's arrays.
+__global__ void k_fx_pack_nodes(const __grid_constant__ ct_forest_index X, const TreeL* __restrict__ trees) {
+    const int64_t total = X.node_off[X.n_trees];
+    if (total > X.node_capacity) return;  // overflowed build: the records use the stand-in tree
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < total; v += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tree_of_row(X.node_off, X.n_trees, v);
+        const int64_t local = v - X.node_off[t], nn = X.node_off[t + 1] - X.node_off[t];
+        const int64_t rows = X.tree_off[t + 1] - X.tree_off[t];
+        const double L = X.node_Lmax[v], R = X.node_Rmin[v];
+        if (!isfinite(L) || !isfinite(R)) set_error(X.error_word, CT_DEVERR_NONFINITE);
+        reinterpret_cast<double2*>(X.nodes_f64)[v] = make_double2(L, R);
+        int64_t c = X.node_child[v];
+        const bool bad = (c != -1 && (c <= local || c + 1 >= nn)) ||
+                         (c == -1 && (X.node_ptr[v] < 0 || X.node_size[v] < 0 || X.node_ptr[v] + X.node_size[v] > rows));
+        float4 q;
+        if (bad) {
+            set_error(X.error_word, CT_DEVERR_CAPACITY);
+            q = make_float4(0.f, 0.f, 0.f, 0.f);  // empty leaf
+        } else if (c == -1) {
+            q.x = 0.f;
+            q.y = 0.f;
+            q.z = __int_as_float((int)X.node_ptr[v]);
+            q.w = __int_as_float((int)X.node_size[v]);
+        } else {
+            const int d = X.node_dim[v] ? 1 : 0;
+            const double o = d ? trees[t].oy : trees[t].ox;
+            q.x = __double2float_ru(L - o);
+            q.y = __double2float_rd(R - o);
+            q.z = __int_as_float((int)c);
+            q.w = __int_as_float(-1 - d);
+        }
+        reinterpret_cast<float4*>(X.nodes_f32)[v] = q;
+    }
+}
+
+// Leaf-ordered cells of every tree (k_pack_polys over the batch).
+__global__ void k_fx_pack_cells(const __grid_constant__ ct_forest_index X) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < X.n_total;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tree_of_row(X.tree_off, X.n_trees, p);
+        const int64_t j = p - X.tree_off[t];
+        const int K = X.tree_K[t];
+        const int64_t b = X.bb_indices[p];
+        if (b < 0 || b >= X.tree_off[t + 1] - X.tree_off[t]) {  // only after an overflowed build
+            set_error(X.error_word, CT_DEVERR_CAPACITY);
+            X.poly_len[p] = 0;
+            X.poly_len32[p] = 0;
+            continue;
+        }
+        pack_cell(X.faces + X.face_off[t] + b * K, K, false, X.vertices, (double2*)X.poly_f64 + X.face_off[t] + j * K,
+                  (float4*)X.poly_f32 + X.poly32_off[t] + j * poly32_stride(K), X.poly_len + p, X.poly_len32 + p);
+    }
+}
+
+// Start nodes of every tree's grid (k_grid_start over the batch).
+__global__ void k_fx_grid_start(const __grid_constant__ ct_forest_index X, const TreeL* __restrict__ trees) {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < X.grid_cells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tree_of_row(X.grid_off, X.n_trees, c);
+        const TreeL& T = trees[t];
+        if (!T.gstart) {
+            X.grid_start[c] = 0;  // grid off for this build: queries start at the root
+            continue;
+        }
+        const int64_t local = c - X.grid_off[t];
+        const double m = __longlong_as_double((long long)X.summary[(int64_t)t * FX_WORDS + 5]);
+        X.grid_start[c] = grid_cell_start(T.nf, (int)(local % T.gnx), (int)(local / T.gnx), T.gx0, T.gy0, T.gsx,
+                                          T.gsy, m, T.bandG, X.max_depth[t] + 2);
+    }
+}
+
 }  // namespace ctl
 
 using namespace ctl;
@@ -1366,6 +1607,7 @@ size_t ct_abi_sizeof(int32_t which) {
     switch (which) {
         case 0: return sizeof(ct_tree);
         case 1: return sizeof(ct_forest_plan);
+        case 2: return sizeof(ct_forest_index);
         default: return 0;
     }
 }
@@ -1825,6 +2067,90 @@ int ct_forest_locate(const ct_forest_plan* plan, const double* points, int64_t* 
 #undef CT_FOREST_STAGES
     if (res_sorted) scatter_results(L, n, plan->error_word, out, st);
     CT_CHECK_LAUNCH("forest locate");
+    return CT_OK;
+}
+
+static int check_index(const ct_forest_index* X) {
+    if (!X) return ct_fail(CT_ERR_ARG, "index is null");
+    if (X->n_trees < 1 || X->n_total < X->n_trees) return ct_fail(CT_ERR_ARG, "index sizes out of range");
+    if (X->k_max < 3 || X->k_max > CT_MAX_N_VERTEX) return ct_fail(CT_ERR_ARG, "k_max must be in [3, 32]");
+    if (X->stack < 2 || X->stack > 128) return ct_fail(CT_ERR_ARG, "stack must be in [2, 128]");
+    if (X->grid_cells < 0 || X->node_capacity < 1) return ct_fail(CT_ERR_ARG, "index sizes out of range");
+    if (!X->vertices || !X->faces || !X->face_off || !X->poly32_off || !X->tree_K || !X->bb_coords ||
+        !X->tree_off || !X->node_off || !X->max_depth || !X->node_child || !X->node_Lmax || !X->node_Rmin ||
+        !X->node_ptr || !X->node_size || !X->node_dim || !X->bb_indices || !X->grid_off || !X->grid_nx ||
+        !X->grid_ny || (X->grid_cells > 0 && !X->grid_start) || !X->nodes_f32 || !X->nodes_f64 || !X->poly_f64 ||
+        !X->poly_f32 || !X->poly_len || !X->poly_len32 || !X->summary || !X->error_word)
+        return ct_fail(CT_ERR_ARG, "index has a null array");
+    return CT_OK;
+}
+
+int ct_forest_index_prepare(const ct_forest_index* X, const int64_t* point_off, int64_t n_points,
+                            ct_forest_plan* plan, void* ws, size_t ws_bytes, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    int s = check_index(X);
+    if (s) return s;
+    if (!point_off || !plan) return ct_fail(CT_ERR_ARG, "null argument");
+    const int32_t n_trees = X->n_trees;
+    if (n_points < 0 || n_points >= INT32_MAX / 2) return ct_fail(CT_ERR_ARG, "at most 2^30 points per call");
+    if (point_off[0] != 0 || point_off[n_trees] != n_points)
+        return ct_fail(CT_ERR_ARG, "point offsets must start at 0 and end at n_points");
+    for (int i = 0; i < n_trees; i++)
+        if (point_off[i + 1] < point_off[i]) return ct_fail(CT_ERR_ARG, "point offsets must not decrease");
+    if (!ws || ws_bytes < carve_forest(nullptr, n_points, n_trees, nullptr, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "forest locate workspace too small");
+    int tree_bits = 0;
+    while ((1 << tree_bits) < n_trees) tree_bits++;
+    if (tree_bits > 24) return ct_fail(CT_ERR_ARG, "at most 2^24 trees per batch");
+    LocWS L;
+    ForestWS F;
+    carve_forest(ws, n_points, n_trees, &L, &F);
+    plan->n_points = n_points;
+    plan->n_trees = n_trees;
+    plan->kt = (X->k_max <= 3) ? 3 : (X->k_max <= 4 ? 4 : 32);
+    plan->stack = X->stack;
+    plan->morton_bits = std::min(24, 32 - tree_bits) & ~1;
+    plan->error_word = X->error_word;
+    plan->max_tree_points = 0;
+    for (int32_t i = 0; i < n_trees; i++)
+        plan->max_tree_points = std::max<int64_t>(plan->max_tree_points, point_off[i + 1] - point_off[i]);
+    CT_CUDA(cudaMemcpyAsync(F.poff, point_off, sizeof(int64_t) * ((size_t)n_trees + 1), cudaMemcpyHostToDevice, st));
+    CT_CUDA(cudaStreamSynchronize(st));
+    size_t smem = (size_t)plan->stack * LOC_THREADS * sizeof(int);
+    if (plan->kt == 3) smem_attr<3, true>(smem);
+    else if (plan->kt == 4) smem_attr<4, true>(smem);
+    else smem_attr<32, true>(smem);
+    return CT_OK;
+}
+
+int ct_forest_index_build(const ct_forest_index* X, const ct_forest_plan* plan, void* ws, size_t ws_bytes,
+                          void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    int s = check_index(X);
+    if (s) return s;
+    if (!plan || plan->n_trees != X->n_trees || plan->stack != X->stack)
+        return ct_fail(CT_ERR_ARG, "plan not prepared for this index");
+    if (!ws || ws_bytes < carve_forest(nullptr, plan->n_points, plan->n_trees, nullptr, nullptr))
+        return ct_fail(CT_ERR_WORKSPACE, "forest locate workspace too small");
+    LocWS L;
+    ForestWS F;
+    carve_forest(ws, plan->n_points, plan->n_trees, &L, &F);
+    int sms = 152;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    auto blocks = [&](int64_t n, int per_sm) {
+        return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sms * per_sm));
+    };
+    k_fx_reset<<<blocks((int64_t)X->n_trees * FX_WORDS, 4), 256, 0, st>>>(X->summary, X->n_trees, X->error_word);
+    k_fx_summary<<<blocks(X->n_total, 8), 256, 0, st>>>(X->bb_coords, X->n_total, X->tree_off, X->n_trees,
+                                                        X->summary, X->error_word);
+    k_fx_records<<<(unsigned)((X->n_trees + 127) / 128), 128, 0, st>>>(*X, F.trees, F.grids);
+    k_fx_pack_nodes<<<blocks(X->node_capacity, 16), 256, 0, st>>>(*X, F.trees);
+    k_fx_pack_cells<<<blocks(X->n_total, 16), 256, 0, st>>>(*X);
+    if (X->grid_cells > 0) k_fx_grid_start<<<blocks(X->grid_cells, 16), 256, 0, st>>>(*X, F.trees);
+    CT_CHECK_LAUNCH("forest index");
     return CT_OK;
 }
 

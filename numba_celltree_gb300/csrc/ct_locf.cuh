@@ -210,3 +210,40 @@ __device__ __forceinline__ int leaf_filter_poly(const PtSplit& P, float dabs, fl
     if (unsure) return LF_UNSURE;
     return parity ? LF_INSIDE : LF_OUTSIDE;
 }
+
+// One cell of the leaf-ordered polygon arrays: its K float64 vertices (NaN
+// padded past its length) and its float32 local-frame record (first vertex
+// split hi + lo, the other distinct consecutive vertices as float32 offsets),
+// its length and the length without repeated consecutive vertices.
+__device__ __forceinline__ void pack_cell(const int64_t* __restrict__ e, int K, bool is_edge,
+                                          const double* __restrict__ v, double2* __restrict__ P,
+                                          float4* __restrict__ C, uint8_t* plen, uint8_t* plen32) {
+    int len = is_edge ? 2 : polygon_length(e, K);
+    const int S4 = poly32_stride(K);
+    float2* rel = reinterpret_cast<float2*>(C + 1);
+    for (int k = 0; k < len; k++) P[k] = make_double2(v[2 * e[k]], v[2 * e[k] + 1]);
+    for (int k = len; k < K; k++) P[k] = make_double2(__longlong_as_double(0x7ff8000000000000ll), 0.0);
+    int m = 0;
+    double2 v0 = make_double2(0.0, 0.0);
+    if (len > 0) {
+        double2 prev = P[len - 1];
+        for (int k = 0; k < len; k++) {
+            double2 c = P[k];
+            if (c.x == prev.x && c.y == prev.y) continue;
+            if (m == 0) {
+                v0 = c;
+                float xl, yl;
+                float xh = split_hi(c.x, &xl), yh = split_hi(c.y, &yl);
+                C[0] = make_float4(xh, xl, yh, yl);
+            } else {
+                rel[m - 1] = make_float2(__double2float_rn(c.x - v0.x), __double2float_rn(c.y - v0.y));
+            }
+            m++;
+            prev = c;
+        }
+    }
+    if (m == 0) C[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = (m > 0 ? m - 1 : 0); k < 2 * (S4 - 1); k++) rel[k] = make_float2(0.f, 0.f);
+    if (plen) *plen = (uint8_t)len;
+    *plen32 = (uint8_t)m;
+}

@@ -39,6 +39,11 @@ struct TreeQ {
     const int* lstart;         // per leaf position: first position of its leaf
     double ox, oy;             // float32 frame origin
     const int* parent;         // node parents (trees deeper than the stacks are walked through them)
+    // float32 leaf data (ct_locf.cuh) for the filters of the segment test
+    const float4* polyf;
+    const uint8_t* plen32;
+    int S4;
+    float dabs;                // float64 rounding of absolute coordinates
 };
 
 // Bounding box of a node's cells in the float32 frame of the tree (x - ox,
@@ -371,6 +376,138 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
     if (!WRITE) cnt_or_off[i] = count;
 }
 
+// Sign of the cross product (v - a) x s used by Cyrus-Beck's crossing walk
+// (cyrus_beck.py:162-180: ksi / eta) decided in float32 in the cell's local
+// frame: -1 / +1 when sure (then also nonzero), 0 when the float64 product
+// must be computed.  dv, da: float32 local coordinates of v and a (error ev
+// per component), sf: float32 s with error es.  The float64 value is
+// fl(fl(U.x * s.y) - fl(U.y * s.x)) with U = fl(v - a): within
+// 3.0001 u (|U.x||s.y| + |U.y||s.x|) (u = 2^-53) of the exact product of the
+// float64 inputs, so a float32 margin above that bound plus the float32
+// error fixes its sign.
+__device__ __forceinline__ int cb_sign32(float2 dv, float2 da, float ev, float2 sf, float es) {
+    const float u24 = 5.9604644775390625e-08f;
+    float ux = dv.x - da.x, uy = dv.y - da.y;
+    float eu = 2.0f * ev + u24 * fmaxf(fabsf(ux), fabsf(uy));
+    float M = fmaxf(fabsf(ux), fabsf(uy)) + eu;
+    float Ns = fabsf(sf.x) + fabsf(sf.y) + 2.0f * es;
+    float est = ux * sf.y - uy * sf.x;
+    float thr = 1.02f * (2.0f * es * M + Ns * eu + 4.0f * u24 * Ns * M + 3.3307e-16f * Ns * M) + 1e-37f;
+    if (!(fabsf(est) > thr)) return 0;
+    return est > 0.0f ? 1 : -1;
+}
+
+// cyrus_beck_line_polygon_clip (cyrus_beck.py:133-241) with its float64
+// decisions screened in float32: the two point_in_polygon_or_on_edge tests by
+// the certified leaf filter (ct_locf.cuh), the crossing walk's signs by
+// cb_sign32; undecided ones run in float64.  The intersection parameters and
+// clipped points are the float64 computations of cyrus_beck().
+template <int KT>
+__device__ __forceinline__ bool cyrus_beck_f32(dpt a, dpt b, const dpt* poly, int length, double tol,
+                                               const float4* __restrict__ cellf, int len32, float dabs, dpt* c,
+                                               dpt* d) {
+    *c = mkp(dnan(), dnan());
+    *d = *c;
+    dpt s = vsub(b, a);
+    if (s.x == 0 && s.y == 0) return false;
+    float tolf = (float)tol;
+    if ((double)tolf < tol) tolf = nextafterf(tolf, INFINITY);
+    PtSplit Pa = split_point(a.x, a.y), Pb = split_point(b.x, b.y);
+    int ra = leaf_filter_local<KT>(Pa, dabs, tolf, cellf, len32);
+    int rb = leaf_filter_local<KT>(Pb, dabs, tolf, cellf, len32);
+    bool a_inside = (ra == LF_UNSURE) ? pip_or_edge(a, poly, length, tol) : (ra == LF_INSIDE);
+    bool b_inside = (rb == LF_UNSURE) ? pip_or_edge(b, poly, length, tol) : (rb == LF_INSIDE);
+    if (a_inside && b_inside) {
+        *c = a;
+        *d = b;
+        return true;
+    }
+    // float32 local coordinates of a and s (frame: the cell's first vertex)
+    float da_x, da_y, ea, db_x, db_y, eb;
+    local_delta(Pa, cellf[0], &da_x, &da_y, &ea);
+    local_delta(Pb, cellf[0], &db_x, &db_y, &eb);
+    const float u24 = 5.9604644775390625e-08f;
+    const float ed = fmaxf(ea, eb) + dabs;
+    const float2 da = make_float2(da_x, da_y);
+    const float2 sf = make_float2(db_x - da_x, db_y - da_y);
+    const float es = 2.0f * ed + 2.0f * u24 * fmaxf(fabsf(sf.x), fabsf(sf.y));
+    const float2* rel = reinterpret_cast<const float2*>(cellf + 1);
+    // poly[i] in the local frame: vertex 0 at the origin, the others as their
+    // stored float32 offsets (rounded by 2^-24 of their size)
+    float vmax = 0.0f;
+    for (int i = 1; i < len32 && i < KT; i++) vmax = fmaxf(vmax, fmaxf(fabsf(rel[i - 1].x), fabsf(rel[i - 1].y)));
+    const float ev = ed + u24 * vmax + dabs;
+    // the float32 cell lists the same vertices as poly unless repeated ones were dropped
+    const bool use32 = (len32 == length);
+    int i0 = -1, i1 = -1, i = 0, k = 0;
+    int sk = use32 ? cb_sign32(make_float2(0.0f, 0.0f), da, ev, sf, es) : 0;
+    bool ksi64 = sk == 0;
+    double ksi = ksi64 ? crossp(vsub(poly[0], a), s) : 0.0;
+    while (i < length && k < 2) {
+        const int in = (i + 1) % length;
+        int se = use32 ? cb_sign32(in == 0 ? make_float2(0.0f, 0.0f) : rel[in - 1], da, ev, sf, es) : 0;
+        const bool eta64 = se == 0;
+        const double eta = eta64 ? crossp(vsub(poly[in], a), s) : 0.0;
+        const bool ksi_neg = ksi64 ? (ksi < 0.0) : (sk < 0);
+        const bool eta_neg = eta64 ? (eta < 0.0) : (se < 0);
+        if (ksi_neg != eta_neg) {
+            if (k == 0) i0 = i;
+            else i1 = i;
+            k++;
+        } else if (ksi64 && eta64 && ksi == 0.0 && eta == 0.0) {
+            bool r = cb_collinear(a, b, poly[i], poly[in], c, d);
+            if (!r) {
+                *c = mkp(dnan(), dnan());
+                *d = *c;
+            }
+            return r;
+        }
+        ksi = eta;
+        sk = se;
+        ksi64 = eta64;
+        i++;
+    }
+    if (k == 0) return false;
+    // intersections cyrus_beck.py:46-63 (Python index -1 wraps)
+    int j0 = i0 < 0 ? i0 + length : i0, j1 = i1 < 0 ? i1 + length : i1;
+    dpt v0 = poly[j0], v01 = poly[(i0 + 1) % length];
+    dpt v1 = poly[j1], v11 = poly[((i1 + 1) % length + length) % length];
+    bool e0, e1;
+    double t0 = cb_param(a, s, v0, v01, &e0);
+    double t1 = cb_param(a, s, v1, v11, &e1);
+    if (e1) {
+        double t = t0;
+        t0 = t1;
+        t1 = t;
+    }
+    if (t0 == t1) {
+        if (a_inside && t1 != 0.0) t0 = 0.0;
+        else if (b_inside && t0 != 1.0) t1 = 1.0;
+        else return false;
+    }
+    if (t1 < t0) {
+        double t = t0;
+        t0 = t1;
+        t1 = t;
+    }
+    bool valid0 = t0 >= 0 && t0 < 1;
+    bool valid1 = t1 > 0 && t1 <= 1;
+    if (valid0 && valid1) {
+        *c = mkp(a.x + t0 * s.x, a.y + t0 * s.y);
+        *d = mkp(a.x + t1 * s.x, a.y + t1 * s.y);
+        return true;
+    } else if (valid0) {
+        *c = mkp(a.x + t0 * s.x, a.y + t0 * s.y);
+        *d = b;
+        return true;
+    } else if (valid1) {
+        *c = a;
+        *d = mkp(a.x + t1 * s.x, a.y + t1 * s.y);
+        return true;
+    }
+    return false;
+}
+
 // The float64 cell test of every candidate (compute_edge_face_intersect
 // query.py:309-328 / compute_edge_edge_intersect 292-306).
 template <int MODE>
@@ -398,7 +535,11 @@ __global__ void __launch_bounds__(128) k_edge_test(TreeQ T, const double4* __res
                 const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
                 int len = T.plen ? (int)T.plen[j] : T.K;
                 double tol = pmax(CT_MIN_TOLERANCE, CT_TOLERANCE_FACTOR * pmax(bx.xmax - bx.xmin, bx.ymax - bx.ymin));
-                hit = cyrus_beck(a, b, poly, len, tol, &c, &d);
+                if (T.polyf && T.K <= 8)
+                    hit = cyrus_beck_f32<8>(a, b, poly, len, tol, T.polyf + (size_t)j * T.S4, (int)T.plen32[j],
+                                            T.dabs, &c, &d);
+                else
+                    hit = cyrus_beck(a, b, poly, len, tol, &c, &d);
             }
         }
         keep[t] = hit ? 1 : 0;
@@ -961,6 +1102,10 @@ TreeQ make_q(const ct_tree* t) {
     T.ox = t->origin[0];
     T.oy = t->origin[1];
     T.parent = t->node_parent;
+    T.polyf = (const float4*)t->poly_f32;
+    T.plen32 = t->poly_len32;
+    T.S4 = poly32_stride(t->n_max_vert);
+    T.dabs = t->abs_eps;
     return T;
 }
 

@@ -466,7 +466,7 @@ __global__ void k_bbox_summary(const double* __restrict__ bb, int64_t n, double*
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double4 b = reinterpret_cast<const double4*>(bb)[i];
         double dx = b.y - b.x, dy = b.w - b.z;
-        double dxy = sqrt(dx * dx + dy * dy);
+        double dxy = box_diagonal(dx, dy);
         if (dist) {
             dist[3 * i] = dx;
             dist[3 * i + 1] = dy;
@@ -560,37 +560,8 @@ __global__ void k_pack_polys(int64_t n, int K, bool is_edge, const int64_t* __re
                              uint8_t* __restrict__ plen32) {
     int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const int64_t* e = elems + bbi[j] * K;
-    int len = is_edge ? 2 : polygon_length(e, K);
-    double2* P = poly + j * K;
-    int S4 = poly32_stride(K);
-    float4* C = polyf + j * S4;
-    float2* rel = reinterpret_cast<float2*>(C + 1);
-    for (int k = 0; k < len; k++) P[k] = make_double2(v[2 * e[k]], v[2 * e[k] + 1]);
-    for (int k = len; k < K; k++) P[k] = make_double2(__longlong_as_double(0x7ff8000000000000ll), 0.0);
-    int m = 0;
-    double2 v0 = make_double2(0.0, 0.0);
-    if (len > 0) {
-        double2 prev = P[len - 1];
-        for (int k = 0; k < len; k++) {
-            double2 c = P[k];
-            if (c.x == prev.x && c.y == prev.y) continue;
-            if (m == 0) {
-                v0 = c;
-                float xl, yl;
-                float xh = split_hi(c.x, &xl), yh = split_hi(c.y, &yl);
-                C[0] = make_float4(xh, xl, yh, yl);
-            } else {
-                rel[m - 1] = make_float2(__double2float_rn(c.x - v0.x), __double2float_rn(c.y - v0.y));
-            }
-            m++;
-            prev = c;
-        }
-    }
-    if (m == 0) C[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int k = (m > 0 ? m - 1 : 0); k < 2 * (S4 - 1); k++) rel[k] = make_float2(0.f, 0.f);
-    if (plen) plen[j] = (uint8_t)len;
-    plen32[j] = (uint8_t)m;
+    pack_cell(elems + bbi[j] * K, K, is_edge, v, poly + j * K, polyf + j * poly32_stride(K), plen ? plen + j : nullptr,
+              plen32 + j);
 }
 
 TreeDev make_dev(const ct_tree* t) {

@@ -39,11 +39,13 @@ def _points(meshes, seed=1):
 
 
 @pytest.mark.gpu
-def test_forest_build_matches_single_builds(oracle):
+@pytest.mark.parametrize("device_levels", [True, False])
+def test_forest_build_matches_single_builds(oracle, device_levels):
     from numba_celltree_gb300 import CellTree2d, CellTreeBatch
 
     meshes = _meshes()
-    batch = CellTreeBatch(meshes, -1)
+    batch = CellTreeBatch(meshes, -1, device_levels=device_levels)
+    assert (batch.forest is not None) == device_levels
     assert len(batch) == len(meshes)
     for k, (xy, f) in enumerate(meshes):
         alone = CellTree2d(xy, f, -1)
@@ -166,3 +168,120 @@ def test_result_scatter_above_threshold(oracle):
     for k in (1, 2):
         alone = CellTree2d(*meshes[k], -1)
         assert np.array_equal(res[k], alone.locate_points(qs[k]))
+
+
+@pytest.mark.gpu
+def test_device_driven_forest_build_replays_from_a_graph():
+    """ct_build_forest_async (every level on the device, no host
+    synchronisation) captured once in a CUDA graph and replayed on moved
+    coordinates of meshes of the same sizes: each replay's trees equal the
+    meshes built alone."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, _device, _lib
+    from numba_celltree_gb300.batch import ForestBuild
+
+    def boxes(meshes):
+        lib = _lib.load()
+        parts = []
+        for xy, f in meshes:
+            v = torch.as_tensor(xy, device="cuda")
+            fd = torch.as_tensor(f, device="cuda").clone()
+            bb = torch.empty((len(f), 4), dtype=torch.float64, device="cuda")
+            assert lib.ct_counter_clockwise(v.data_ptr(), fd.data_ptr(), len(f), f.shape[1], _device.stream()) == 0
+            assert lib.ct_face_bboxes(v.data_ptr(), fd.data_ptr(), len(f), f.shape[1], bb.data_ptr(),
+                                      _device.stream()) == 0
+            parts.append(bb)
+        return torch.cat(parts)
+
+    meshes = _meshes()
+    fb = ForestBuild([len(f) for _, f in meshes], torch.device("cuda", 0))
+    bb = boxes(meshes)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        fb.launch(bb)  # warm-up outside the capture (function attributes, module load)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fb.launch(bb)
+    for seed in (11, 12):
+        moved = []
+        for k, (xy, f) in enumerate(meshes):
+            rng = np.random.default_rng(seed * 100 + k)
+            moved.append((xy + rng.uniform(-0.05, 0.05, xy.shape), f))
+        bb.copy_(boxes(moved))
+        g.replay()
+        node_off, depth = fb.result()
+        for k, (xy, f) in enumerate(moved):
+            alone = CellTree2d(xy, f, -1)
+            a, b = int(node_off[k]), int(node_off[k + 1])
+            assert b - a == len(alone.nodes), (seed, k)
+            assert np.array_equal(fb.child[a:b].cpu().numpy(), alone.nodes["child"]), (seed, k)
+            assert np.array_equal(fb.Lmax[a:b].cpu().numpy(), alone.nodes["Lmax"]), (seed, k)
+            assert np.array_equal(fb.Rmin[a:b].cpu().numpy(), alone.nodes["Rmin"]), (seed, k)
+            assert np.array_equal(fb.ptr[a:b].cpu().numpy(), alone.nodes["ptr"]), (seed, k)
+            e0, e1 = int(fb.tree_off[k]), int(fb.tree_off[k + 1])
+            assert np.array_equal(fb.bb_indices[e0:e1].cpu().numpy(), alone.bb_indices), (seed, k)
+            assert depth[k] == alone._tree.max_depth
+
+
+def test_k_runs_group_consecutive_meshes_of_one_width():
+    from numba_celltree_gb300.batch import k_runs
+
+    Ks = [3, 3, 4, 6, 6, 6, 3]
+    sizes = np.array([5, 2, 7, 1, 1, 3, 4])
+    tree_off = np.concatenate([[0], np.cumsum(sizes)])
+    face_off = np.concatenate([[0], np.cumsum(sizes * np.array(Ks))])
+    runs = k_runs(Ks, tree_off, face_off)
+    assert runs == [(0, 7, 3, 0), (7, 7, 4, 21), (14, 5, 6, 49), (19, 4, 3, 79)]
+    assert k_runs([], [0], [0]) == []
+
+
+@pytest.mark.gpu
+def test_forest_pipeline_build_and_locate_replay_from_one_graph(oracle):
+    """ForestPipeline: face boxes, tree build, device-side index and batched
+    locate of triangle, quad and mixed meshes in one CUDA graph, replayed on
+    moved vertices and new points: every mesh's results equal the mesh built
+    and queried alone (and the oracle's on the first geometry)."""
+    from numba_celltree_gb300 import CellTree2d
+    from numba_celltree_gb300.batch import ForestPipeline
+
+    meshes = _meshes()
+    pts = _points(meshes)
+    counts = [len(p) for p in pts]
+    pipe = ForestPipeline(meshes, counts)
+    res = pipe.run(np.concatenate([xy for xy, _ in meshes]), np.concatenate(pts)).cpu().numpy()
+    for k, (xy, f) in enumerate(meshes):
+        a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
+        ref = oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])
+        assert np.array_equal(res[a:b], ref), k
+    pipe.capture()
+    for seed in (11, 12):
+        moved = []
+        for k, (xy, f) in enumerate(meshes):
+            rng = np.random.default_rng(seed * 100 + k)
+            moved.append((xy + rng.uniform(-0.05, 0.05, xy.shape), f))
+        new = _points(moved, seed=seed)
+        new = [p[:c] if len(p) >= c else np.resize(p, (c, 2)) for p, c in zip(new, counts)]
+        res = pipe.run(np.concatenate([xy for xy, _ in moved]), np.concatenate(new)).cpu().numpy()
+        for k, (xy, f) in enumerate(moved):
+            a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
+            assert np.array_equal(res[a:b], CellTree2d(xy, f, -1).locate_points(new[k])), (seed, k)
+
+
+@pytest.mark.gpu
+def test_forest_pipeline_given_tolerance_and_empty_mesh_points(oracle):
+    """One tolerance for every mesh, and meshes without points."""
+    from numba_celltree_gb300.batch import ForestPipeline
+
+    meshes = _meshes()[:5]
+    pts = _points(meshes, seed=3)
+    pts[1] = pts[1][:0]
+    pts[3] = pts[3][:0]
+    pipe = ForestPipeline(meshes, [len(p) for p in pts], tolerance=1e-3)
+    res = pipe.run(None, np.concatenate(pts)).cpu().numpy()
+    for k, (xy, f) in enumerate(meshes):
+        a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
+        assert np.array_equal(res[a:b], oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k], 1e-3)), k

@@ -61,6 +61,7 @@ def test_ctypes_mirrors_match_the_library_structs():
     lib = _lib.load()
     assert lib.ct_abi_sizeof(0) == ctypes.sizeof(_lib.CtTree)
     assert lib.ct_abi_sizeof(1) == ctypes.sizeof(_lib.CtForestPlan)
+    assert lib.ct_abi_sizeof(2) == ctypes.sizeof(_lib.CtForestIndex)
     assert lib.ct_abi_sizeof(7) == 0
 
 
