@@ -550,8 +550,40 @@ def query_suite(args, c5=None, verbose=False):
             "all_identical": all(x["identical_on_sample"] for x in rows), "rows": rows}
 
 
+def query_profile(args):
+    """Small fixed run of the multi-result query kernels for ncu captures (no
+    timing, no oracle): the C2 mixed mesh at a quarter of its cells (build,
+    100k boxes intersected, 100k segments of length U(0, 20) m) and the C4
+    regridding pair at a quarter of its cells (intersect_faces)."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d
+    from numba_celltree_gb300 import synthetic as syn
+
+    dev = torch.device("cuda", 0)
+    xy, f = syn.mixed_mesh(1000, 1000, seed=1, extent=(500.0, 500.0))
+    tree = CellTree2d(torch.as_tensor(xy, device=dev), torch.as_tensor(f, device=dev), -1)
+    boxes = syn.random_boxes(100_000, (0.0, 0.0), (500.0, 500.0), 0.1, 50.0, seed=2, log_uniform=True)
+    r1 = tree.intersect_boxes(torch.as_tensor(boxes, device=dev))
+    rng = np.random.default_rng(3)
+    a0 = rng.uniform(0.0, 500.0, (100_000, 2))
+    ang, ln = rng.uniform(0.0, 2 * np.pi, 100_000), rng.uniform(0.0, 20.0, 100_000)
+    segs = np.stack([a0, a0 + np.stack([ln * np.cos(ang), ln * np.sin(ang)], 1)], 1)
+    r2 = tree.intersect_edges(torch.as_tensor(segs, device=dev))
+    txy, tf = syn.quad_mesh(500, 250, seed=4, extent=(50.0, 25.0), offset=(0.037, 0.037), rotate_deg=7.0)
+    qxy, qf = syn.triangle_mesh(500, 250, seed=5, extent=(50.0, 25.0))
+    t4 = CellTree2d(torch.as_tensor(txy, device=dev), torch.as_tensor(tf, device=dev), -1)
+    r3 = t4.intersect_faces(torch.as_tensor(qxy, device=dev), torch.as_tensor(qf, device=dev), -1)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "queries", "cells": [len(f), len(tf)],
+                      "pairs": [int(r1[0].shape[0]), int(r2[0].shape[0]), int(r3[0].shape[0])]}))
+
+
 def run_queries(args):
     """Side measurement: every query against the oracle (one JSON line per row)."""
+    if args.profile:
+        query_profile(args)
+        return
     res = query_suite(args, verbose=True)
     res.pop("rows")
     print(json.dumps(res))
