@@ -43,6 +43,14 @@ typedef enum ct_status {
 
 int ct_abi_version(void);
 const char* ct_last_error_message(void);
+/* Page-lock (register) host memory in place for direct DMA, and release it
+ * (no upstream counterpart; the chunked host-array path registers a caller's
+ * ordinary array chunk by chunk instead of copying it into a pinned staging
+ * buffer).  ptr / bytes should cover whole pages; read_only registers pages
+ * the process may only read.  A failure returns CT_ERR_CUDA and leaves no
+ * error pending in the CUDA runtime. */
+int ct_host_register(void* ptr, size_t bytes, int32_t read_only);
+int ct_host_unregister(void* ptr);
 
 /* ---------------------------------------------------------------------- */
 /* Tree descriptor                                                         */

@@ -169,6 +169,8 @@ SIGNATURES = {
     "ct_pack_tree": (ctypes.c_int, [ctypes.POINTER(CtTree), _P]),
     "ct_poly32_stride": (ctypes.c_int, [_I32]),
     "ct_abi_sizeof": (_SZ, [_I32]),
+    "ct_host_register": (ctypes.c_int, [_P, _SZ, _I32]),
+    "ct_host_unregister": (ctypes.c_int, [_P]),
     "ct_locate_points": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _I32, _P, _P]),
     "ct_locate_points_on_edge": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _D, _P, _P]),
     "ct_locate_workspace_size": (_SZ, [_I64, _I32]),

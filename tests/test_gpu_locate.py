@@ -150,6 +150,37 @@ def test_locate_host_pipeline(oracle, monkeypatch, chunk, pinned):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["writeable", "read_only", "offset_8"])
+def test_locate_host_pipeline_registers_pageable_input(oracle, monkeypatch, layout):
+    """Pageable host arrays page-locked in place chunk by chunk (every chunk
+    on its own pages), read-only arrays, and arrays whose rows cannot start
+    on a page boundary (staging copy instead): same results as the oracle;
+    the pages are released after each call (a second call registers them
+    again)."""
+    from numba_celltree_gb300 import CellTree2d, _pipeline
+    from numba_celltree_gb300 import synthetic as syn
+
+    monkeypatch.setattr(_pipeline, "CHUNK_POINTS", 5000)
+    monkeypatch.setattr(_pipeline, "REGISTER_MIN_BYTES", 0)
+    xy, f = syn.triangle_mesh(60, seed=18, extent=(60.0, 60.0), offset=(3.0e5, 6.0e6))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = syn.uniform_points(70_001, xy.min(0) - 1.0, xy.max(0) + 1.0, seed=19)
+    if layout == "offset_8":
+        raw = np.empty(2 * len(pts) + 1, dtype=np.float64)
+        view = raw[1:].reshape(-1, 2) if raw.ctypes.data % 16 == 0 else raw[:-1].reshape(-1, 2)
+        view[:] = pts
+        assert view.ctypes.data % 16 == 8
+        pts = view
+    elif layout == "read_only":
+        pts = pts.copy()
+        pts.setflags(write=False)
+    ref = o.locate_points(np.ascontiguousarray(pts))
+    for _ in range(2):
+        assert np.array_equal(g.locate_points(pts), ref)
+
+
+@pytest.mark.gpu
 def test_locate_start_grid_edges(oracle):
     """Queries on the lines of the start-node grid, on the bbox boundary and
     just outside it, and on vertices: same result as the oracle in every

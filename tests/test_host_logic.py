@@ -1,7 +1,7 @@
 """Host-side logic that needs no GPU: the chunk schedule of the host-batch
 pipeline."""
 
-from numba_celltree_gb300._pipeline import chunk_bounds
+from numba_celltree_gb300._pipeline import chunk_bounds, page_cuts
 
 
 def test_chunk_bounds_cover_in_order_and_ramp():
@@ -17,6 +17,24 @@ def test_chunk_bounds_cover_in_order_and_ramp():
             assert all(0 < k <= chunk for k in sizes)
     sizes = [e - s for s, e in chunk_bounds(268_435_456, 1 << 25)]
     assert sizes[0] == 1 << 22 and sizes[-1] <= 1 << 22 and max(sizes) == 1 << 25
+
+
+def test_page_cuts_give_every_chunk_its_own_pages():
+    page = 65536
+    for addr in (0x7F0000000000, 0x7F0000000010, 0x7F000000FFF0, 0x7F0000001230):
+        for n, chunk in ((268_435_456, 1 << 25), (10_000, 1000), (5_000_000, 1 << 22), (4096, 1000)):
+            b = page_cuts(addr, 16, chunk_bounds(n, chunk), page)
+            assert b[0][0] == 0 and b[-1][1] == n
+            assert all(b[i][1] == b[i + 1][0] and b[i][0] < b[i][1] for i in range(len(b) - 1))
+            for s, _ in b[1:]:
+                assert (addr + 16 * s) % page == 0
+            # page ranges of consecutive chunks do not overlap
+            for (s0, e0), (s1, e1) in zip(b[:-1], b[1:]):
+                last_page0 = (addr + 16 * e0 - 1) // page
+                first_page1 = (addr + 16 * s1) // page
+                assert last_page0 < first_page1
+    assert page_cuts(0x7F0000000008, 16, chunk_bounds(10_000, 1000), page) is None
+    assert page_cuts(0x7F0000000000, 16, [], page) == []
 
 
 def test_grid_shape_is_near_square_and_bounded():
