@@ -29,6 +29,7 @@ handling of pages the GPU has already read).
 from __future__ import annotations
 
 import mmap
+import warnings
 
 import numpy as np
 
@@ -138,7 +139,10 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
     out_h = pinned_empty((n,), out_dtype)
     if n == 0:
         return out_h.numpy()
-    src = torch.from_numpy(points)
+    with warnings.catch_warnings():
+        # a read-only array: the tensor over it is only ever read
+        warnings.simplefilter("ignore", UserWarning)
+        src = torch.from_numpy(points)
     compute = torch.cuda.current_stream(device)
     up = torch.cuda.Stream(device)
     down = torch.cuda.Stream(device)

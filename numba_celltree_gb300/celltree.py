@@ -355,8 +355,10 @@ class CellTree2d(CellTree2dBase):
             "intersect_boxes",
         )
         del order
-        t.raise_on_device_error()
-        return t.compact(ii, jj, area=area)
+        t.stage_error()
+        out = t.compact(ii, jj, area=area)  # synchronises (pair count)
+        t.raise_on_staged_error()
+        return out
 
     # -- face queries ----------------------------------------------------------
     def _faces_on_device(self, vertices, faces):
@@ -444,8 +446,9 @@ class CellTree2d(CellTree2dBase):
             "area_of_intersection",
         )
         del order
-        t.raise_on_device_error()
-        i2, j2, a2 = t.compact(i, j, area=area)
+        t.stage_error()
+        i2, j2, a2 = t.compact(i, j, area=area)  # synchronises (pair count)
+        t.raise_on_staged_error()
         return _as_output(i2, cuda_in), _as_output(j2, cuda_in), _as_output(a2, cuda_in)
 
     # -- segments --------------------------------------------------------------

@@ -213,6 +213,23 @@ class _GpuTree:
         if err:
             raise _lib.CellTreeError("device error: " + _lib.device_error_text(err))
 
+    def stage_error(self):
+        """Enqueue a copy of the error word into pinned host memory, to be read
+        by raise_on_staged_error after a synchronisation the query makes anyway
+        (a result count): one host round trip instead of two."""
+        torch = _device.torch()
+        if getattr(self, "_err_host", None) is None:
+            self._err_host = torch.zeros((1,), dtype=torch.int32, pin_memory=True)
+            self._err_event = torch.cuda.Event()
+        self._err_host.copy_(self.error_word, non_blocking=True)
+        self._err_event.record()
+
+    def raise_on_staged_error(self):
+        self._err_event.synchronize()  # complete already after the query's own synchronisation
+        err = int(self._err_host.numpy()[0])
+        if err:
+            raise _lib.CellTreeError("device error: " + _lib.device_error_text(err))
+
     # -- point location ---------------------------------------------------------
     @staticmethod
     def auto_sort_bits(n_points: int) -> int:
@@ -504,18 +521,21 @@ class _GpuTree:
         order = self.work_order(boxes_d, 0, config.get("work_order"))
         _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
                                       _device.ptr(counts), st), "locate_boxes")
+        self.stage_error()
         offsets, total = self.scan(counts)
+        self.raise_on_staged_error()
         if budget is not None and total > budget:
             self.last_counts = counts
             return None
         ii = _device.empty((total,), torch.int64, self.device)
         jj = _device.empty((total,), torch.int64, self.device)
+        # the writing pass repeats the counting pass's traversal: a condition
+        # it could report has been reported by the count
         _lib.check(
             lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
                                _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), st),
             "locate_boxes",
         )
-        self.raise_on_device_error()
         return ii, jj
 
     def locate_edges(self, segs_d, mode: int, config=None, budget=None):
@@ -553,7 +573,9 @@ class _GpuTree:
         xy_c = _device.empty((max(nc, 1), 2, 2), torch.float64, self.device)
         _lib.check(lib.ct_test_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), P(cseg), P(cpos), nc,
                                                P(keep), P(xy_c), st), "intersect_edges")
+        self.stage_error()
         pos, total = self.scan(keep[:nc]) if nc > 0 else (keep[:0], 0)
+        self.raise_on_staged_error()
         ii = _device.empty((total,), torch.int64, self.device)
         jj = _device.empty((total,), torch.int64, self.device)
         xy = _device.empty((total, 2, 2), torch.float64, self.device)
@@ -575,7 +597,6 @@ class _GpuTree:
                 "sort_intersections",
             )
             jj, xy = jj2, xy2
-        self.raise_on_device_error()
         return ii, jj, xy
 
     # pairs from which the per-pair kernels run grouped by polygon lengths
