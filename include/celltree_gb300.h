@@ -201,12 +201,12 @@ int ct_build_emit(const void* workspace, int64_t n_elements, int32_t n_buckets, 
  * ct_pessimistic_n_nodes(n_elements) entries and bb_indices of n_elements.
  * The first call on each device looks up the array's device address (and so
  * does the first call after that device's context is re-created, e.g. by
- * cudaDeviceReset); make that first call before any stream capture.  All
- * calls share the one array: calls that overlap on the GPU (other streams,
- * other host threads) race.
+ * cudaDeviceReset).  All calls share the one array: calls that overlap on
+ * the GPU (other streams, other host threads) race.
  * Extremely unbalanced trees that exceed the builder's record capacity return
  * CT_ERR_WORKSPACE; use ct_build_tree with a larger capacity_factor.
- * Synchronises the stream. */
+ * Not capturable in a CUDA graph: it synchronises the stream once per tree
+ * level (ct_build_forest_async is the capturable build). */
 int ct_build_tree_noalloc(const double* bb_coords, int64_t n_elements, int32_t n_buckets, int64_t cells_per_leaf,
                           int64_t* child, double* Lmax, double* Rmin, int64_t* ptr, int64_t* size, uint8_t* dim,
                           int64_t node_capacity, int64_t* bb_indices, int64_t* n_nodes_host, int32_t* max_depth_host,

@@ -128,11 +128,17 @@ def pinned_empty(shape, dtype):
     return torch.empty(shape, dtype=dtype, pin_memory=True)
 
 
+COMPUTE_STREAMS = 2  # chunks queried on alternating streams
+
+
 def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> np.ndarray:
-    """Run ``query(points_d, out_d)`` over `points` (n, 2) float64 host array
-    in chunks; returns the concatenated results as a numpy array over pinned
-    memory.  ``query`` enqueues work on the current stream and must not
-    synchronise."""
+    """Run ``query(points_d, out_d, slot)`` over `points` (n, 2) float64 host
+    array in chunks; returns the concatenated results as a numpy array over
+    pinned memory.  ``query`` enqueues work on the current stream and must
+    not synchronise; consecutive chunks run on COMPUTE_STREAMS streams in
+    turn (slot = the stream's number), so that one chunk's kernels fill the
+    tail of the previous chunk's -- calls with different slots may run at
+    the same time and must not share scratch memory."""
     torch = _device.torch()
     chunk = CHUNK_POINTS if chunk is None else int(chunk)
     n = int(points.shape[0])
@@ -146,6 +152,11 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
     compute = torch.cuda.current_stream(device)
     up = torch.cuda.Stream(device)
     down = torch.cuda.Stream(device)
+    computes = [compute]
+    for _ in range(COMPUTE_STREAMS - 1):
+        cs = torch.cuda.Stream(device)
+        cs.wait_stream(compute)  # work the caller enqueued before (e.g. the tree build)
+        computes.append(cs)
     bounds = chunk_bounds(n, chunk)
     pin_in = src.is_pinned()
     pins = None
@@ -156,7 +167,7 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
             bounds = aligned
             pins = InPlacePins(read_only=not points.flags.writeable)
     m = max(e - s for s, e in bounds)
-    nbuf = 2 if len(bounds) > 1 else 1
+    nbuf = min(max(2, COMPUTE_STREAMS), len(bounds))
     p_d = [torch.empty((m, 2), dtype=torch.float64, device=device) for _ in range(nbuf)]
     o_d = [torch.empty((m,), dtype=out_dtype, device=device) for _ in range(nbuf)]
     stage = None  # pinned staging blocks, allocated when a chunk needs them
@@ -189,12 +200,15 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
                 uploaded = torch.cuda.Event()
                 uploaded.record(up)
                 staged[b] = uploaded
-            compute.wait_event(uploaded)
+            slot = c % len(computes)
+            cs = computes[slot]
+            cs.wait_event(uploaded)
             if fetched[b] is not None:
-                compute.wait_event(fetched[b])
-            query(p_d[b][:k], o_d[b][:k])
+                cs.wait_event(fetched[b])
+            with torch.cuda.stream(cs):
+                query(p_d[b][:k], o_d[b][:k], slot)
             ev = torch.cuda.Event()
-            ev.record(compute)
+            ev.record(cs)
             done[b] = ev
             with torch.cuda.stream(down):
                 down.wait_event(ev)
@@ -203,7 +217,10 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
                 ev2.record(down)
                 fetched[b] = ev2
         down.synchronize()
-        compute.synchronize()
+        for cs in computes:
+            cs.synchronize()
+            if cs is not compute:
+                compute.wait_stream(cs)
     finally:
         if pins is not None:
             up.synchronize()  # no upload may still read a registered page

@@ -186,7 +186,8 @@ class CellTree2d(CellTree2dBase):
         if not cuda_in:
             # host batch: chunked upload / query / download, result in pinned memory
             res = _pipeline.stream_points(
-                points, t.device, lambda p_d, o_d: t.locate(p_d, o_d, tol, self.precision), torch.int64
+                points, t.device, lambda p_d, o_d, slot: t.locate(p_d, o_d, tol, self.precision, slot=slot),
+                torch.int64,
             )
             t.raise_on_device_error()
             return res

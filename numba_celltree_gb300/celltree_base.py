@@ -319,16 +319,19 @@ class _GpuTree:
         merged.update(cfg)
         return merged
 
-    def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None, config=None) -> None:
+    def locate(self, points_d, out_d, tolerance: float, precision: str, sort_bits=None, config=None,
+               slot: int = 0) -> None:
         """Enqueue point location on the current stream (no synchronisation).
         `config`: launch shape (autotune.DEFAULTS["locate"] keys), else the
-        cached one for this batch size."""
+        cached one for this batch size.  `slot`: workspace of the batched
+        form; calls that may run at the same time (other streams) use
+        different slots."""
         lib = _lib.load()
         n = int(points_d.shape[0])
         if n > self.MAX_CALL_POINTS:
             for s in range(0, n, self.MAX_CALL_POINTS):
                 e = min(s + self.MAX_CALL_POINTS, n)
-                self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits, config)
+                self.locate(points_d[s:e], out_d[s:e], tolerance, precision, sort_bits, config, slot)
             return
         if precision == "fp32" and self.max_depth + 2 > self.BATCHED_MAX_STACK:
             precision = "fp64"  # the batched form's stacks hold 126 levels; deeper trees take the float64 walk
@@ -339,10 +342,12 @@ class _GpuTree:
                 sort_bits = cfg.get("sort_bits")
             g = self.auto_sort_bits(n) if sort_bits is None else int(sort_bits)
             need = int(lib.ct_locate_workspace_size(n, g))
-            ws = getattr(self, "_locate_ws", None)
+            name = "_locate_ws" if slot == 0 else f"_locate_ws{slot}"
+            ws = getattr(self, name, None)
             if ws is None or ws.numel() < need:
                 torch = _device.torch()
-                self._locate_ws = ws = _device.empty((need,), torch.uint8, self.device)
+                ws = _device.empty((need,), torch.uint8, self.device)
+                setattr(self, name, ws)
             _lib.check(
                 lib.ct_locate_points_batched(
                     ctypes.byref(self.desc), _device.ptr(points_d), n, float(tolerance), g, _device.ptr(out_d),

@@ -43,7 +43,7 @@ constexpr int NBMAX = 32;          // maximum n_buckets
 constexpr int STATS_THREADS = 256; // threads of the stats / scatter CTAs
 constexpr int TILE_MIN = 2048;     // minimum cells per tile
 constexpr int MAX_TILES = 512;     // maximum tiles per node
-constexpr int SUB_WARPS = 4;       // warps per CTA in the subtree kernel
+constexpr int SUB_WARPS = 2;       // warps per CTA in the subtree kernel (8.1 KB of shared memory each)
 
 enum : int { K_PENDING = 0, K_SPLIT = 1, K_LEAF = 2, K_SUBTREE = 3 };
 
@@ -88,7 +88,7 @@ struct Counters {
 constexpr int DEV_MAX_LEVELS = 64;
 
 struct WS {
-    double* f[2][6];  // lo_x, hi_x, lo_y, hi_y, c_x, c_y (two ping-pong buffers)
+    double* f[2][4];  // lo_x, hi_x, lo_y, hi_y (two ping-pong buffers); centroids are recomputed (centroid_of)
     int* idx[2];
     int* final_idx;
     ARec* recs;
@@ -134,7 +134,7 @@ static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_tre
     int tile_cap = (int)std::min<int64_t>(INT32_MAX / 4, 2 * (nn / TILE_MIN) + 2 * (int64_t)rec_cap + 64);
     WS w;
     for (int b = 0; b < 2; b++) {
-        for (int k = 0; k < 6; k++) w.f[b][k] = (double*)take(sizeof(double) * nn);
+        for (int k = 0; k < 4; k++) w.f[b][k] = (double*)take(sizeof(double) * nn);
         w.idx[b] = (int*)take(sizeof(int) * nn);
     }
     w.final_idx = (int*)take(sizeof(int) * nn);
@@ -338,6 +338,13 @@ __device__ Decision warp_decide(const int* cnt, const double* bRmin, const doubl
 // initial element buffers and root bounds
 // ------------------------------------------------------------------------
 
+// centroid creation.py:50: box[2d] + 0.5 * (box[2d + 1] - box[2d]), each
+// operation rounded on its own (no fused multiply-add); recomputed wherever a
+// cell's bucket is needed instead of being stored and moved with the cell
+__device__ __forceinline__ double centroid_of(double lo, double hi) {
+    return __dadd_rn(lo, __dmul_rn(0.5, __dsub_rn(hi, lo)));
+}
+
 __global__ void k_init_elems(const double* __restrict__ bb, int n, WS ws) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double x0 = bb[4 * (size_t)i], x1 = bb[4 * (size_t)i + 1], y0 = bb[4 * (size_t)i + 2], y1 = bb[4 * (size_t)i + 3];
@@ -345,9 +352,6 @@ __global__ void k_init_elems(const double* __restrict__ bb, int n, WS ws) {
         ws.f[0][1][i] = x1;
         ws.f[0][2][i] = y0;
         ws.f[0][3][i] = y1;
-        // centroid creation.py:50: box[2d] + 0.5 * (box[2d + 1] - box[2d])
-        ws.f[0][4][i] = x0 + 0.5 * (x1 - x0);
-        ws.f[0][5][i] = y0 + 0.5 * (y1 - y0);
         ws.idx[0][i] = i;
     }
 }
@@ -509,8 +513,6 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     const double* F1 = ws.f[parity][1];
     const double* F2 = ws.f[parity][2];
     const double* F3 = ws.f[parity][3];
-    const double* C0 = ws.f[parity][4];
-    const double* C1 = ws.f[parity][5];
     for (int base = s; base < e; base += blockDim.x) {
         int i = base + tid;
         bool valid = i < e;
@@ -520,8 +522,8 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
             v1 = F1[i];
             v2 = F2[i];
             v3 = F3[i];
-            c0 = C0[i];
-            c1 = C1[i];
+            c0 = centroid_of(v0, v1);
+            c1 = centroid_of(v2, v3);
         }
         unsigned long long k0 = fkey(v0), k1 = ~fkey(v1), k2 = fkey(v2), k3 = ~fkey(v3);
 #pragma unroll
@@ -779,11 +781,12 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
         run[tid] = 0;
     }
     __syncthreads();
-    const double* Cd = ws.f[parity][4 + ds];
+    const double* Lo = ws.f[parity][2 * ds];
+    const double* Hi = ws.f[parity][2 * ds + 1];
     for (int b0 = s; b0 < e; b0 += blockDim.x) {
         int i = b0 + tid;
         bool valid = i < e;
-        int b = valid ? find_bucket(K, NB, fkey(Cd[i])) : -2;
+        int b = valid ? find_bucket(K, NB, fkey(centroid_of(Lo[i], Hi[i]))) : -2;
         if (valid && b < 0) b = -1;  // counted nowhere: flagged by k_stats
         unsigned grp = __match_any_sync(FULL, b);
         int rank = __popc(grp & lanemask_lt());
@@ -797,7 +800,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
             int dst = base[b] + run[b] + off + rank;
             int op = 1 - parity;
 #pragma unroll
-            for (int k = 0; k < 6; k++) ws.f[op][k][dst] = ws.f[parity][k][i];
+            for (int k = 0; k < 4; k++) ws.f[op][k][dst] = ws.f[parity][k][i];
             ws.idx[op][dst] = idx_in[i];
         }
         __syncthreads();
@@ -815,20 +818,42 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
 // phase B: one warp builds a subtree of <= SMALL cells in shared memory
 // ------------------------------------------------------------------------
 
+// Per-warp shared memory of a subtree: the four box fields of its cells
+// (the centroids are recomputed from them with the expression that produced
+// them, so the same bits), and the node stack as packed arrays.  8.1 KB, so
+// that more warps are resident (the kernel is bound by issue latency).
 struct SubSmem {
-    double F[6][SMALL];
-    int gid[SMALL];
-    unsigned short perm[SMALL];
-    unsigned short tmp[SMALL];
-    unsigned char bkt[SMALL];
-    int stk[SMALL + 2][5];  // node, local ptr, size, dim flag, depth
+    double F[4][SMALL];
     unsigned long long K[NBMAX + 1];
+    double bRmin[NBMAX];
+    double bLmax[NBMAX];
+    int gid[SMALL];
+    int stk_v[SMALL + 2];      // node
+    int stk_depth[SMALL + 2];  // depth
     int cnt[NBMAX];
     int bstart[NBMAX];
     int brun[NBMAX];
-    double bRmin[NBMAX];
-    double bLmax[NBMAX];
+    unsigned short perm[SMALL];
+    unsigned short tmp[SMALL];
+    unsigned short stk_p[SMALL + 2];  // local ptr
+    unsigned short stk_n[SMALL + 2];  // size
+    unsigned char bkt[SMALL];
+    signed char stk_flag[SMALL + 2];  // dim, or dim - 2 after an all-in-one-bucket flip
 };
+static_assert(SMALL <= 65535, "subtree positions are 16-bit");
+
+__device__ __forceinline__ void sub_push(SubSmem& S, int sp, int v, int p, int n, int flag, int depth) {
+    S.stk_v[sp] = v;
+    S.stk_p[sp] = (unsigned short)p;
+    S.stk_n[sp] = (unsigned short)n;
+    S.stk_flag[sp] = (signed char)flag;
+    S.stk_depth[sp] = depth;
+}
+
+// centroid of cell k along dimension d (creation.py:50), as k_init_elems computes it
+__device__ __forceinline__ double sub_centroid(const SubSmem& S, int d, int k) {
+    return centroid_of(S.F[2 * d][k], S.F[2 * d + 1][k]);
+}
 
 // First-occurrence min over perm[p .. p+n) of field f (min-form key: maxima
 // complemented when `is_max`); returns the exact value.  All lanes call.
@@ -866,7 +891,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
     ARec* RR = &ws.recs[r];
     int p0 = RR->ptr, s = RR->size, par = RR->parity, d0 = RR->dim, lvl = RR->level;
     for (int i = lane; i < s; i += 32) {
-        for (int k = 0; k < 6; k++) S.F[k][i] = ws.f[par][k][p0 + i];
+        for (int k = 0; k < 4; k++) S.F[k][i] = ws.f[par][k][p0 + i];
         S.gid[i] = ws.idx[par][p0 + i];
         S.perm[i] = (unsigned short)i;
     }
@@ -880,18 +905,14 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         z.size = s;
         z.dim = d0;
         L[0] = z;
-        S.stk[0][0] = 0;
-        S.stk[0][1] = 0;
-        S.stk[0][2] = s;
-        S.stk[0][3] = d0;
-        S.stk[0][4] = lvl;
+        sub_push(S, 0, 0, 0, s, d0, lvl);
     }
     __syncwarp();
     int sp = 1, nloc = 1, maxd = lvl;
     bool err = false;
     while (sp > 0) {
         sp--;
-        int v = S.stk[sp][0], p = S.stk[sp][1], n = S.stk[sp][2], flag = S.stk[sp][3], depth = S.stk[sp][4];
+        int v = S.stk_v[sp], p = S.stk_p[sp], n = S.stk_n[sp], flag = S.stk_flag[sp], depth = S.stk_depth[sp];
         __syncwarp();
         int d = flag < 0 ? flag + 2 : flag;
         if ((long long)n <= cpl) continue;
@@ -907,7 +928,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         __syncwarp();
         bool lbad = false;
         for (int i = lane; i < n; i += 32) {
-            int b = find_bucket(S.K, NB, fkey(S.F[4 + d][S.perm[p + i]]));
+            int b = find_bucket(S.K, NB, fkey(sub_centroid(S, d, S.perm[p + i])));
             if (b < 0) {
                 lbad = true;
                 b = 0;
@@ -985,11 +1006,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
             if (flag >= 0) {
                 if (lane == 0) {
                     L[v].dim = 1 - L[v].dim;
-                    S.stk[sp][0] = v;
-                    S.stk[sp][1] = p;
-                    S.stk[sp][2] = n;
-                    S.stk[sp][3] = (1 - d) - 2;
-                    S.stk[sp][4] = depth;
+                    sub_push(S, sp, v, p, n, (1 - d) - 2, depth);
                 }
                 sp++;
             } else if (lane == 0) {
@@ -1020,16 +1037,8 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
             a.size = n - nl;
             L[nloc + 1] = a;
             // push right, then left (creation.py:378-379)
-            S.stk[sp][0] = nloc + 1;
-            S.stk[sp][1] = p + nl;
-            S.stk[sp][2] = n - nl;
-            S.stk[sp][3] = 1 - d;
-            S.stk[sp][4] = depth + 1;
-            S.stk[sp + 1][0] = nloc;
-            S.stk[sp + 1][1] = p;
-            S.stk[sp + 1][2] = nl;
-            S.stk[sp + 1][3] = 1 - d;
-            S.stk[sp + 1][4] = depth + 1;
+            sub_push(S, sp, nloc + 1, p + nl, n - nl, 1 - d, depth + 1);
+            sub_push(S, sp + 1, nloc, p, nl, 1 - d, depth + 1);
         }
         sp += 2;
         nloc += 2;
@@ -1680,7 +1689,8 @@ int ct_build_forest_async(const double* bb, int64_t n_total, const int64_t* tree
             k_level_next<<<1, 32, 0, st>>>(ws, L);
         }
     }
-    k_subtree<true><<<G, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
+    // enough blocks to fill every SM with resident subtree warps (the grid strides over the subtrees)
+    k_subtree<true><<<sms * 16, SUB_WARPS * 32, SUB_WARPS * sizeof(SubSmem), st>>>(ws, NB, (long long)cpl);
     for (int L = DEV_MAX_LEVELS - 1; L >= 0; L--) k_count_up_dev<<<sms * 4, 256, 0, st>>>(ws, L);
     for (int L = 0; L < DEV_MAX_LEVELS; L++) k_number_down_dev<<<sms * 4, 256, 0, st>>>(ws, L);
     k_forest_counts<<<1, 256, 0, st>>>(ws, n_nodes_dev, node_off_dev, max_depth_dev, node_capacity, status_dev);

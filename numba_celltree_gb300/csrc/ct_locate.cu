@@ -1083,8 +1083,9 @@ __device__ __forceinline__ bool tri_box(const float2 (&V)[3], const float2 (&D)[
 template <bool FILL, int KMAX>
 __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __restrict__ poly,
                              const uint8_t* __restrict__ plen, int K, int64_t n, double ox, double oy, int gnx,
-                             int gny, double x0, double y0, double sx, double sy, double m, float Mf, float e2f,
-                             float ea, unsigned long long* __restrict__ count, const int64_t* __restrict__ off,
+                             int gny, double x0, double y0, double sx, double sy, double cw, double ch, double m,
+                             float Mf, float e2f, float ea, unsigned long long* __restrict__ count,
+                             const int64_t* __restrict__ off,
                              int* __restrict__ idx, float4* __restrict__ lbox, unsigned int* __restrict__ err) {
     const float u = 5.9604644775390625e-08f;
     for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
@@ -1130,7 +1131,7 @@ __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __re
             // twice the signed area, beyond its rounding and the vertices' own
             tri = area2 > 4.0f * u * csum + 32.0f * u * Lm * Lm + 16.0f * d * Lm;
         }
-        const double cw = 1.0 / sx, ch = 1.0 / sy;
+        // cw = 1 / sx, ch = 1 / sy: grid cell sizes, divided once on the host
         const float fcw = (float)cw, fch = (float)ch;
         // lower-left corner of the range's first grid cell relative to the anchor
         const float fbx0 = (float)((x0 + (double)a0 * cw) - ax), fby0 = (float)((y0 + (double)b0 * ch) - ay);
@@ -1712,7 +1713,8 @@ static void launch_cand_lists(const ct_tree* t, bool fill, double M, unsigned lo
 #define CT_CAND_LISTS(FILL, KMAX)                                                                                  \
     k_cand_lists<FILL, KMAX><<<blocks, 256, 0, st>>>(                                                              \
         (const float4*)t->cand_box, (const double2*)t->poly_f64, plen, t->n_max_vert, n, t->origin[0],             \
-        t->origin[1], t->grid_nx, t->grid_ny, t->grid_x0, t->grid_y0, t->grid_sx, t->grid_sy, grid_margin(t),     \
+        t->origin[1], t->grid_nx, t->grid_ny, t->grid_x0, t->grid_y0, t->grid_sx, t->grid_sy,                     \
+        1.0 / (double)t->grid_sx, 1.0 / (double)t->grid_sy, grid_margin(t),                                       \
         float_up(M), float_up(grid_margin(t) + M), (float)(4.0 * (double)t->abs_eps),                             \
         count, FILL ? t->cand_off : nullptr, FILL ? t->cand_idx : nullptr, FILL ? (float4*)t->cand_lbox : nullptr, \
         t->error_word)
