@@ -129,6 +129,7 @@ def pinned_empty(shape, dtype):
 
 
 COMPUTE_STREAMS = 2  # chunks queried on alternating streams
+BUFFERS = 3  # device buffers (points and results) the chunks rotate through
 
 
 def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> np.ndarray:
@@ -167,7 +168,7 @@ def stream_points(points: np.ndarray, device, query, out_dtype, chunk=None) -> n
             bounds = aligned
             pins = InPlacePins(read_only=not points.flags.writeable)
     m = max(e - s for s, e in bounds)
-    nbuf = min(max(2, COMPUTE_STREAMS), len(bounds))
+    nbuf = min(max(2, BUFFERS), len(bounds))
     p_d = [torch.empty((m, 2), dtype=torch.float64, device=device) for _ in range(nbuf)]
     o_d = [torch.empty((m,), dtype=out_dtype, device=device) for _ in range(nbuf)]
     stage = None  # pinned staging blocks, allocated when a chunk needs them

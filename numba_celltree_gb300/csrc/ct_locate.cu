@@ -355,6 +355,101 @@ __global__ void __launch_bounds__(LOC_THREADS)
 
 constexpr int RES_OPEN = INT32_MIN;  // sorted-order result of a query left open
 
+// One query of stage 2a: the cells listed for its grid cell, a float32 bbox
+// reject, then the float32 leaf filter.  Returns whether the query stays
+// open (its result is then left to stage 2b).
+template <int KT>
+__device__ __forceinline__ bool cells_one(const TreeL& T, double2 pp, int64_t i, int oi, int64_t* __restrict__ out,
+                                          int* __restrict__ res_sorted) {
+    bool open = false;
+    float px, py, dpx, dpy;
+    PtSplit P;
+    to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
+    to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
+    float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
+    if (T.coff && fx >= 0.0f && fx < (float)T.gnx && fy >= 0.0f && fy < (float)T.gny) {
+        const int64_t g = (int64_t)(int)fy * T.gnx + (int)fx;
+        const int64_t s0 = T.coff[g], s1 = T.coff[g + 1];
+        // the point's float32 interval
+        const float xl = __fsub_rd(px, dpx), xh = __fadd_ru(px, dpx);
+        const float yl = __fsub_rd(py, dpy), yh = __fadd_ru(py, dpy);
+        int hits = 0, hit = -1;
+        // entry k+1 is loaded while entry k is tested
+        int jn = 0;
+        float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (s0 < s1) {
+            jn = T.cidx[s0];
+            bn = T.cbox[s0];
+        }
+        // Rounds of two phases: (1) collect up to four entries whose box
+        // holds the point's interval, (2) filter them.  The filter then
+        // runs for the lanes that have a polygon to test, not once per
+        // iteration of a loop whose trip count is the longest list of
+        // the warp.  The decision does not depend on the order of the
+        // tests.
+        int64_t k = s0;
+        while (!open && k < s1) {
+            int np = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
+            for (; k < s1 && np < 4; k++) {
+                const int j = jn;
+                const float4 b = bn;
+                if (k + 1 < s1) {
+                    jn = T.cidx[k + 1];
+                    bn = T.cbox[k + 1];
+                }
+                if (xh < b.x || xl > b.y || yh < b.z || yl > b.w) continue;  // outside: predicate false
+                c3 = c2;
+                c2 = c1;
+                c1 = c0;
+                c0 = j;
+                np++;
+            }
+            for (int c = 0; c < np; c++) {
+                const int j = c0;
+                c0 = c1;
+                c1 = c2;
+                c2 = c3;
+                int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(
+                                        P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j])
+                                  : leaf_filter_local<KT>(P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4,
+                                                          (int)T.plen32[j]);
+                if (r == LF_UNSURE) {
+                    open = true;
+                    break;
+                }
+                if (r == LF_INSIDE) {
+                    hit = j;
+                    if (++hits > 1) {
+                        open = true;
+                        break;
+                    }
+                }
+            }
+        }
+        if (!open) {
+            const int r = hits ? (int)T.bbi[hit] : -1;
+            if (res_sorted) res_sorted[i] = r;
+            else out[oi] = r;
+        }
+    } else {
+        open = true;
+    }
+    if (open && res_sorted) res_sorted[i] = RES_OPEN;
+    return open;
+}
+
+// Warp-aggregated append of the open queries' sorted positions.
+__device__ __forceinline__ void append_open(bool open, int64_t i, int* __restrict__ qlist, int* __restrict__ qcount) {
+    unsigned m = __ballot_sync(0xffffffffu, open);
+    if (m) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        int b0 = 0;
+        if (lane == leader) b0 = atomicAdd(qcount, __popc(m));
+        b0 = __shfl_sync(0xffffffffu, b0, leader);
+        if (open) qlist[b0 + __popc(m & lane_lt())] = (int)i;
+    }
+}
+
 // Stage 2a: candidate lists.  Per query the cells listed for its grid cell:
 // a float32 bbox reject, then the float32 leaf filter.  Exactly one sure hit
 // with sure misses elsewhere, or sure misses only, is final; otherwise the
@@ -369,94 +464,51 @@ __global__ void __launch_bounds__(LOC_THREADS, MINB)
             const double2* __restrict__ pts, const int* __restrict__ order, int64_t n, int64_t* __restrict__ out,
             int* __restrict__ res_sorted, int* __restrict__ qlist, int* __restrict__ qcount) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < n;
     bool open = false;
-    if (active) {
+    if (i < n) {
         const int oi = order ? order[i] : (int)i;
         const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
-        double2 pp = pts[oi];
-        float px, py, dpx, dpy;
-        PtSplit P;
-        to_frame(pp.x, T.ohx, T.olx, &px, &dpx, &P.xh, &P.xl);
-        to_frame(pp.y, T.ohy, T.oly, &py, &dpy, &P.yh, &P.yl);
-        float fx = (px - T.gx0) * T.gsx, fy = (py - T.gy0) * T.gsy;
-        if (T.coff && fx >= 0.0f && fx < (float)T.gnx && fy >= 0.0f && fy < (float)T.gny) {
-            const int64_t g = (int64_t)(int)fy * T.gnx + (int)fx;
-            const int64_t s0 = T.coff[g], s1 = T.coff[g + 1];
-            // the point's float32 interval
-            const float xl = __fsub_rd(px, dpx), xh = __fadd_ru(px, dpx);
-            const float yl = __fsub_rd(py, dpy), yh = __fadd_ru(py, dpy);
-            int hits = 0, hit = -1;
-            // entry k+1 is loaded while entry k is tested
-            int jn = 0;
-            float4 bn = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (s0 < s1) {
-                jn = T.cidx[s0];
-                bn = T.cbox[s0];
-            }
-            // Rounds of two phases: (1) collect up to four entries whose box
-            // holds the point's interval, (2) filter them.  The filter then
-            // runs for the lanes that have a polygon to test, not once per
-            // iteration of a loop whose trip count is the longest list of
-            // the warp.  The decision does not depend on the order of the
-            // tests.
-            int64_t k = s0;
-            while (!open && k < s1) {
-                int np = 0, c0 = 0, c1 = 0, c2 = 0, c3 = 0;
-                for (; k < s1 && np < 4; k++) {
-                    const int j = jn;
-                    const float4 b = bn;
-                    if (k + 1 < s1) {
-                        jn = T.cidx[k + 1];
-                        bn = T.cbox[k + 1];
-                    }
-                    if (xh < b.x || xl > b.y || yh < b.z || yl > b.w) continue;  // outside: predicate false
-                    c3 = c2;
-                    c2 = c1;
-                    c1 = c0;
-                    c0 = j;
-                    np++;
-                }
-                for (int c = 0; c < np; c++) {
-                    const int j = c0;
-                    c0 = c1;
-                    c1 = c2;
-                    c2 = c3;
-                    int r = (KT <= 4) ? leaf_filter_poly<(KT <= 4 ? KT : 4)>(
-                                            P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4, (int)T.plen32[j])
-                                      : leaf_filter_local<KT>(P, T.dabs, T.tolf, T.polyf + (size_t)j * T.S4,
-                                                              (int)T.plen32[j]);
-                    if (r == LF_UNSURE) {
-                        open = true;
-                        break;
-                    }
-                    if (r == LF_INSIDE) {
-                        hit = j;
-                        if (++hits > 1) {
-                            open = true;
-                            break;
-                        }
-                    }
-                }
-            }
-            if (!open) {
-                const int r = hits ? (int)T.bbi[hit] : -1;
-                if (res_sorted) res_sorted[i] = r;
-                else out[oi] = r;
-            }
-        } else {
-            open = true;
-        }
-        if (open && res_sorted) res_sorted[i] = RES_OPEN;
+        open = cells_one<KT>(T, pts[oi], i, oi, out, res_sorted);
     }
-    // warp-aggregated append of the open queries
-    unsigned m = __ballot_sync(0xffffffffu, open);
-    if (m) {
-        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-        int b0 = 0;
-        if (lane == leader) b0 = atomicAdd(qcount, __popc(m));
-        b0 = __shfl_sync(0xffffffffu, b0, leader);
-        if (open) qlist[b0 + __popc(m & lane_lt())] = (int)i;
+    append_open(open, i, qlist, qcount);
+}
+
+// The same stage as a resident grid (MINB blocks per SM) striding over the
+// sorted queries with a two-deep software pipeline: while a thread tests one
+// query's cells, the point of its next query (read through the permutation)
+// and the permutation entry of the one after that are already in flight, so
+// the two dependent random reads that start every query overlap the work of
+// the previous one.
+template <int KT, bool MULTI, int MINB>
+__global__ void __launch_bounds__(LOC_THREADS, MINB)
+    k_cells_pipe(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
+                 const double2* __restrict__ pts, const int* __restrict__ order, int64_t n,
+                 int64_t* __restrict__ out, int* __restrict__ res_sorted, int* __restrict__ qlist,
+                 int* __restrict__ qcount) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int oi1 = 0, oi2 = 0;
+    double2 p1 = make_double2(0.0, 0.0);
+    if (i0 < n) {
+        oi1 = order ? order[i0] : (int)i0;
+        p1 = pts[oi1];
+    }
+    if (i0 + stride < n) oi2 = order ? order[i0 + stride] : (int)(i0 + stride);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int64_t i = base + threadIdx.x;
+        const int oi = oi1;
+        const double2 pp = p1;
+        if (i + stride < n) {  // next query's point: its permutation entry arrived during the last iteration
+            p1 = pts[oi2];
+            oi1 = oi2;
+        }
+        if (i + 2 * stride < n) oi2 = order ? order[i + 2 * stride] : (int)(i + 2 * stride);
+        bool open = false;
+        if (i < n) {
+            const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
+            open = cells_one<KT>(T, pp, i, oi, out, res_sorted);
+        }
+        append_open(open, i, qlist, qcount);
     }
 }
 
@@ -1080,18 +1132,44 @@ __device__ __forceinline__ bool tri_box(const float2 (&V)[3], const float2 (&D)[
 // (clipping them cost more build time than it saved queries in measurements
 // on mixed meshes) or non-finite coordinates keep the widened bbox in every
 // grid cell of its range.
-template <bool FILL, int KMAX>
+// Entries of one cell kept in its record slots by the counting pass (more
+// go through the geometry again in the filling pass).
+constexpr int CAND_SLOTS = 8;
+constexpr unsigned char CAND_OVERFLOW = 255;
+
+// Records of the counting pass: the kept (grid cell, clipped box) pairs of
+// every cell, so that the filling pass scatters them without repeating the
+// geometry.
+struct CandRecs {
+    int* g;           // n x CAND_SLOTS grid cells
+    float4* r;        // n x CAND_SLOTS clipped boxes
+    unsigned char* n; // kept pairs per cell, CAND_OVERFLOW when more than CAND_SLOTS
+    int* ovf;         // cells with more than CAND_SLOTS pairs
+    int* ovf_count;
+};
+
+// MODE 0: count the (cell, grid cell) pairs per grid cell; MODE 2: count and
+// record them (CandRecs); MODE 1: write the entries of the cells listed in
+// `cells` (all cells when null) at off[g] + cursor.
+template <int MODE, int KMAX>
 __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __restrict__ poly,
                              const uint8_t* __restrict__ plen, int K, int64_t n, double ox, double oy, int gnx,
                              int gny, double x0, double y0, double sx, double sy, double cw, double ch, double m,
                              float Mf, float e2f, float ea, unsigned long long* __restrict__ count,
                              const int64_t* __restrict__ off,
-                             int* __restrict__ idx, float4* __restrict__ lbox, unsigned int* __restrict__ err) {
+                             int* __restrict__ idx, float4* __restrict__ lbox, unsigned int* __restrict__ err,
+                             CandRecs rec, const int* __restrict__ cells, const int* __restrict__ cells_count) {
     const float u = 5.9604644775390625e-08f;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t nj = cells ? (int64_t)*cells_count : n;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nj; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = cells ? (int64_t)cells[t] : t;
         int a0, a1, b0, b1;
         const float4 b = box[j];
-        if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) continue;
+        int kept = 0;
+        if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) {
+            if (MODE == 2) rec.n[j] = 0;
+            continue;
+        }
         const int len = plen ? (int)plen[j] : K;
         const double2* pv = poly + (size_t)j * K;
         bool clip = KMAX <= 4 && len >= 3 && len <= KMAX;
@@ -1166,7 +1244,7 @@ __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __re
                 if (!keep) continue;
                 int64_t g = (int64_t)gy * gnx + gx;
                 unsigned long long k = atomicAdd(&count[g], 1ull);
-                if (FILL) {
+                if (MODE == 1) {
                     const int64_t e = off[g] + (int64_t)k;
                     if (e >= off[g + 1]) {  // the counting pass decided otherwise: never write past g
                         set_error(err, CT_DEVERR_CAPACITY);
@@ -1174,8 +1252,44 @@ __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __re
                     }
                     idx[e] = (int)j;
                     lbox[e] = r;
+                } else if (MODE == 2) {
+                    if (kept < CAND_SLOTS) {
+                        rec.g[j * CAND_SLOTS + kept] = (int)g;
+                        rec.r[j * CAND_SLOTS + kept] = r;
+                    }
+                    kept++;
                 }
             }
+        }
+        if (MODE == 2) {
+            if (kept > CAND_SLOTS) {
+                rec.n[j] = CAND_OVERFLOW;
+                rec.ovf[atomicAdd(rec.ovf_count, 1)] = (int)j;
+            } else {
+                rec.n[j] = (unsigned char)kept;
+            }
+        }
+    }
+}
+
+// Filling pass from the records: every recorded pair of a cell to its grid
+// cell's list (off[g] + cursor); cells that overflowed their slots are left
+// to the geometry pass (MODE 1 over rec.ovf).
+__global__ void k_cand_scatter(int64_t n, CandRecs rec, unsigned long long* __restrict__ cursor,
+                               const int64_t* __restrict__ off, int* __restrict__ idx, float4* __restrict__ lbox,
+                               unsigned int* __restrict__ err) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int c = rec.n[j];
+        if (c == CAND_OVERFLOW) continue;
+        for (int k = 0; k < c; k++) {
+            const int64_t g = rec.g[j * CAND_SLOTS + k];
+            const int64_t e = off[g] + (int64_t)atomicAdd(&cursor[g], 1ull);
+            if (e >= off[g + 1]) {
+                set_error(err, CT_DEVERR_CAPACITY);
+                continue;
+            }
+            idx[e] = (int)j;
+            lbox[e] = rec.r[j * CAND_SLOTS + k];
         }
     }
 }
@@ -1683,10 +1797,41 @@ static double grid_margin(const ct_tree* t) {
     return std::ldexp(std::max(ex, ey) + F, -19);
 }
 
+// Scratch of the candidate lists: grid-cell counts (then cursors), the scan's
+// workspace, and the counting pass's records.
+struct CandScratch {
+    unsigned long long* count;
+    void* scan_ws;
+    size_t scan_bytes;
+    CandRecs rec;
+};
+
+static size_t carve_cand(const ct_tree* t, void* scratch, CandScratch* C) {
+    const int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
+    const size_t n = (size_t)std::max<int64_t>(t->n_elements, 1);
+    char* base = (char*)scratch;
+    size_t off = 0;
+    auto take = [&](size_t b) {
+        char* p = base ? base + off : nullptr;
+        off += a256(b);
+        return p;
+    };
+    CandScratch c;
+    c.count = (unsigned long long*)take(8 * (size_t)(cells + 1));
+    c.scan_bytes = ct_scan_workspace_size(cells + 1);
+    c.scan_ws = take(c.scan_bytes);
+    c.rec.g = (int*)take(sizeof(int) * CAND_SLOTS * n);
+    c.rec.r = (float4*)take(sizeof(float4) * CAND_SLOTS * n);
+    c.rec.n = (unsigned char*)take(n);
+    c.rec.ovf = (int*)take(sizeof(int) * n);
+    c.rec.ovf_count = (int*)take(sizeof(int));
+    if (C) *C = c;
+    return off + 256;
+}
+
 size_t ct_cand_scratch_size(const ct_tree* t) {
     if (!t || t->grid_nx <= 0 || t->grid_ny <= 0) return 256;
-    int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
-    return a256(8 * (size_t)(cells + 1)) + a256(ct_scan_workspace_size(cells + 1)) + 256;
+    return carve_cand(t, nullptr, nullptr);
 }
 
 // widening of the region where a cell's predicate can be true: the on-edge
@@ -1705,25 +1850,27 @@ static float float_up(double v) {
     return f;
 }
 
-// counting (fill = false) or filling pass of the candidate lists
-static void launch_cand_lists(const ct_tree* t, bool fill, double M, unsigned long long* count, cudaStream_t st) {
+// Counting-and-recording pass (fill = false) or the geometry filling pass
+// over the cells that overflowed their record slots (fill = true).
+static void launch_cand_lists(const ct_tree* t, bool fill, double M, const CandScratch& C, cudaStream_t st) {
     int64_t n = t->n_elements;
     unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
     const uint8_t* plen = (t->n_max_vert == 3) ? nullptr : t->poly_len;
-#define CT_CAND_LISTS(FILL, KMAX)                                                                                  \
-    k_cand_lists<FILL, KMAX><<<blocks, 256, 0, st>>>(                                                              \
+#define CT_CAND_LISTS(MODE, KMAX)                                                                                  \
+    k_cand_lists<MODE, KMAX><<<blocks, 256, 0, st>>>(                                                              \
         (const float4*)t->cand_box, (const double2*)t->poly_f64, plen, t->n_max_vert, n, t->origin[0],             \
         t->origin[1], t->grid_nx, t->grid_ny, t->grid_x0, t->grid_y0, t->grid_sx, t->grid_sy,                     \
         1.0 / (double)t->grid_sx, 1.0 / (double)t->grid_sy, grid_margin(t),                                       \
         float_up(M), float_up(grid_margin(t) + M), (float)(4.0 * (double)t->abs_eps),                             \
-        count, FILL ? t->cand_off : nullptr, FILL ? t->cand_idx : nullptr, FILL ? (float4*)t->cand_lbox : nullptr, \
-        t->error_word)
+        C.count, MODE == 1 ? t->cand_off : nullptr, MODE == 1 ? t->cand_idx : nullptr,                             \
+        MODE == 1 ? (float4*)t->cand_lbox : nullptr, t->error_word, C.rec, MODE == 1 ? C.rec.ovf : nullptr,         \
+        C.rec.ovf_count)
     if (t->n_max_vert <= 4) {
-        if (fill) CT_CAND_LISTS(true, 4);
-        else CT_CAND_LISTS(false, 4);
+        if (fill) CT_CAND_LISTS(1, 4);
+        else CT_CAND_LISTS(2, 4);
     } else {
-        if (fill) CT_CAND_LISTS(true, 32);
-        else CT_CAND_LISTS(false, 32);
+        if (fill) CT_CAND_LISTS(1, 32);
+        else CT_CAND_LISTS(2, 32);
     }
 #undef CT_CAND_LISTS
 }
@@ -1741,19 +1888,20 @@ int ct_cand_count(ct_tree* t, double cover_tol, void* scratch, size_t scratch_by
     if (!(cover_tol >= 0.0) || !std::isfinite(cover_tol)) return ct_fail(CT_ERR_ARG, "cover_tol must be finite and >= 0");
     if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
     const int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
-    unsigned long long* count = (unsigned long long*)scratch;  // cells + 1 entries, the last stays 0
-    void* scan_ws = (char*)scratch + a256(8 * (size_t)(cells + 1));
-    size_t scan_bytes = scratch_bytes - a256(8 * (size_t)(cells + 1));
+    CandScratch C;
+    carve_cand(t, scratch, &C);  // counts: cells + 1 entries, the last stays 0
     const double M = cand_reach(t, cover_tol);
     int64_t n = t->n_elements;
     unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
     k_cand_box<<<blocks, 256, 0, st>>>(t->bb_coords, t->bb_indices, n, t->origin[0], t->origin[1], M,
                                        (float4*)t->cand_box);
-    CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)(cells + 1), st));
-    launch_cand_lists(t, false, M, count, st);
+    CT_CUDA(cudaMemsetAsync(C.count, 0, 8 * (size_t)(cells + 1), st));
+    CT_CUDA(cudaMemsetAsync(C.rec.ovf_count, 0, sizeof(int), st));
+    launch_cand_lists(t, false, M, C, st);
     CT_CHECK_LAUNCH("candidate counts");
     int64_t total = 0;
-    int s = ct_exclusive_scan((const int64_t*)count, cells + 1, t->cand_off, scan_ws, scan_bytes, &total, stream);
+    int s = ct_exclusive_scan((const int64_t*)C.count, cells + 1, t->cand_off, C.scan_ws, C.scan_bytes, &total,
+                              stream);
     if (s) return s;
     if (total > INT32_MAX) return CT_OK;  // too many entries for int offsets of the pairs: lists off
     t->cand_n = total;
@@ -1769,10 +1917,15 @@ int ct_cand_fill(ct_tree* t, void* scratch, size_t scratch_bytes, void* stream) 
     if ((!t->cand_idx || !t->cand_lbox) && t->cand_n > 0) return ct_fail(CT_ERR_ARG, "cand_idx / cand_lbox not set");
     if (!scratch || scratch_bytes < ct_cand_scratch_size(t)) return ct_fail(CT_ERR_WORKSPACE, "scratch too small");
     const int64_t cells = (int64_t)t->grid_nx * t->grid_ny;
-    unsigned long long* count = (unsigned long long*)scratch;
-    CT_CUDA(cudaMemsetAsync(count, 0, 8 * (size_t)cells, st));
+    CandScratch C;
+    carve_cand(t, scratch, &C);
+    CT_CUDA(cudaMemsetAsync(C.count, 0, 8 * (size_t)cells, st));  // now the lists' cursors
+    const int64_t n = t->n_elements;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 16));
+    k_cand_scatter<<<blocks, 256, 0, st>>>(n, C.rec, C.count, t->cand_off, t->cand_idx, (float4*)t->cand_lbox,
+                                           t->error_word);
     const double cover = (t->cand_tol == 1e-300) ? 0.0 : t->cand_tol;  // the count's cover_tol
-    launch_cand_lists(t, true, cand_reach(t, cover), count, st);
+    launch_cand_lists(t, true, cand_reach(t, cover), C, st);  // cells with more pairs than record slots
     CT_CHECK_LAUNCH("candidate lists");
     return CT_OK;
 }
@@ -1866,7 +2019,17 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     int* res_sorted = (lists && ord && n > RES_SCATTER_MIN) ? sorted_results(L) : nullptr;
 #define CT_FAST_STAGES(KT)                                                                                        \
     if (lists) {                                                                                                   \
-        if (cells_bpsm == 4)                                                                                       \
+        if (cells_bpsm < 0) {                                                                                      \
+            /* software-pipelined variant: a resident grid of -cells_bpsm blocks per SM */                         \
+            const int mb = cells_bpsm == -5 ? 5 : 6;                                                               \
+            const unsigned gp = (unsigned)std::min<int64_t>((int64_t)grid, (int64_t)sms * mb);                     \
+            if (mb == 5)                                                                                           \
+                k_cells_pipe<KT, false, 5><<<gp, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out,       \
+                                                                       res_sorted, L.open, &L.counters[3]);       \
+            else                                                                                                   \
+                k_cells_pipe<KT, false, 6><<<gp, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out,       \
+                                                                       res_sorted, L.open, &L.counters[3]);       \
+        } else if (cells_bpsm == 4)                                                                                \
             k_cells<KT, false, 4><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,   \
                                                                 L.open, &L.counters[3]);                           \
         else if (cells_bpsm == 8)                                                                                  \

@@ -181,6 +181,56 @@ def test_locate_host_pipeline_registers_pageable_input(oracle, monkeypatch, layo
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("cells_bpsm", [4, 6, 8, -6, -5])
+def test_candidate_list_launch_variants(oracle, cells_bpsm):
+    """Every launch shape of the candidate-list stage (plain grids at 4, 6 or
+    8 blocks per SM; the software-pipelined resident grid at 6 or 5) gives
+    the oracle's indices, on sorted batches with and without the bucketed
+    result scatter."""
+    import torch
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(150, 100, seed=24, extent=(150.0, 100.0), offset=(4.0e5, 3.0e6))
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    t = g._tree
+    tol = g.default_tolerance()
+    for n in (300_001, (1 << 23) + 77):
+        pts = syn.uniform_points(n, xy.min(0) - 0.5, xy.max(0) + 0.5, seed=25)
+        pts[::50] = syn.near_edge_points(xy, f, len(pts[::50]), dist=1e-9, seed=26)
+        p_d = torch.as_tensor(pts, device="cuda")
+        out = torch.empty(n, dtype=torch.int64, device="cuda")
+        t.locate(p_d, out, tol, "fp32", config={"sort_bits": 16, "cells_bpsm": cells_bpsm, "fast_bpsm": 16})
+        got = out.cpu().numpy()
+        sample = np.random.default_rng(27).integers(0, n, 100_000)
+        assert np.array_equal(got[sample], o.locate_points(pts[sample]))
+        g.precision = "fp64"
+        assert np.array_equal(got, g.locate_points(p_d).cpu().numpy())
+        g.precision = "fp32"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("density", [0.05, 16.0])
+def test_candidate_lists_at_grid_densities(oracle, density):
+    """Candidate lists on a coarse grid (many cells per grid cell) and a fine
+    one (most cells overlap more grid cells than the counting pass records
+    per cell, so the filling pass repeats their geometry): the batched float32
+    form gives the oracle's indices, near edges included."""
+    from numba_celltree_gb300 import CellTree2d
+
+    xy, f = syn.triangle_mesh(80, 60, seed=21, extent=(80.0, 60.0), offset=(1.0e5, 2.0e5))
+    g = CellTree2d(xy, f, -1)
+    g._tree.rebuild_index(density)
+    assert g._tree.cand_idx is not None
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    pts = np.concatenate([syn.uniform_points(200_000, xy.min(0) - 0.5, xy.max(0) + 0.5, seed=22),
+                          syn.near_edge_points(xy, f, 20_000, dist=1e-9, seed=23)])
+    g.precision = "fp32"
+    assert np.array_equal(g.locate_points(pts), o.locate_points(pts))
+    assert np.array_equal(g.locate_points(pts, 1e-4), o.locate_points(pts, 1e-4))
+
+
+@pytest.mark.gpu
 def test_locate_start_grid_edges(oracle):
     """Queries on the lines of the start-node grid, on the bbox boundary and
     just outside it, and on vertices: same result as the oracle in every
