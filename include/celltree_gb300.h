@@ -114,8 +114,7 @@ typedef struct ct_tree {
     int32_t* leaf_start;      /* device: n_elements: first leaf position of the leaf holding each position */
     /* launch shapes (host; 0 = the library default).  They change speed,
      * never results; an autotuner picks them per GPU and problem size. */
-    int32_t tune_cells_bpsm;  /* candidate-list pass compiled for 4, 6 or 8 resident blocks per SM (default 6);
-                                 -6 / -5: the software-pipelined variant on a resident grid of 6 / 5 blocks per SM */
+    int32_t tune_cells_bpsm;  /* candidate-list pass compiled for 4, 6 or 8 resident blocks per SM (default 6) */
     int32_t tune_fast_bpsm;   /* grid of the open-query traversal in blocks per SM, 1 .. 32 (default 16) */
     int32_t tune_query_threads; /* block size of the box and segment traversals: 64, 128 or 256
                                    (default 256 boxes, 128 segments; segments take at most 128) */

@@ -51,7 +51,7 @@ DEFAULTS: Dict[str, dict] = {
 
 # candidate values per knob
 SPACE: Dict[str, Dict[str, list]] = {
-    "locate": {"sort_bits": [0, 8, 16, 24], "cells_bpsm": [4, 6, 8, -6, -5], "fast_bpsm": [8, 16, 32]},
+    "locate": {"sort_bits": [0, 8, 16, 24], "cells_bpsm": [4, 6, 8], "fast_bpsm": [8, 16, 32]},
     "fp64": {"stack": [0, 512]},
     "boxes": {"threads": [64, 128, 256], "work_order": [False, True]},
     "segments": {"threads": [64, 128], "work_order": [False, True]},

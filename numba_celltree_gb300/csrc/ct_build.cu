@@ -837,7 +837,8 @@ struct SubSmem {
     unsigned short tmp[SMALL];
     unsigned short stk_p[SMALL + 2];  // local ptr
     unsigned short stk_n[SMALL + 2];  // size
-    unsigned char bkt[SMALL];
+    unsigned char bkt[SMALL];         // bucket of each position before the partition
+    unsigned char nbkt[SMALL];        // bucket of each position after it
     signed char stk_flag[SMALL + 2];  // dim, or dim - 2 after an all-in-one-bucket flip
 };
 static_assert(SMALL <= 65535, "subtree positions are 16-bit");
@@ -957,7 +958,11 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
             int b = i < n ? (int)S.bkt[i] : 255;
             unsigned grp = __match_any_sync(FULL, b);
             int rank = __popc(grp & lanemask_lt());
-            if (i < n) S.tmp[S.bstart[b] + S.brun[b] + rank] = S.perm[p + i];
+            if (i < n) {
+                const int dst = S.bstart[b] + S.brun[b] + rank;
+                S.tmp[dst] = S.perm[p + i];
+                S.nbkt[dst] = (unsigned char)b;
+            }
             __syncwarp();
             if (i < n && (int)(__ffs(grp) - 1) == lane) S.brun[b] += __popc(grp);
             __syncwarp();
@@ -986,20 +991,58 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
             __syncwarp();
             continue;
         }
-        // per-bucket bounds (creation.py:300-306)
-        for (int b = 0; b < NB; b++) {
-            int c = S.cnt[b];
-            double rmin = DBL_MAX, lmax = -DBL_MAX;
-            if (c > 0) {
-                rmin = warp_range_extreme(S, 2 * d, false, p + S.bstart[b], c);
-                lmax = warp_range_extreme(S, 2 * d + 1, true, p + S.bstart[b], c);
+        // per-bucket bounds (creation.py:300-306): the first-occurrence
+        // minimum of Rmin and maximum of Lmax of every bucket in one pass over
+        // the node's positions (after the partition bucket b is a contiguous
+        // run).  The lanes of one bucket reduce (key, position) together and
+        // their first lane folds the result into the bucket's running minimum
+        // (a later chunk never wins a tie: first occurrence).  Keys and
+        // positions use scratch the partition is done with: S.K (Rmin keys),
+        // S.bLmax viewed as keys (Lmax), S.brun / S.bstart (positions).
+        {
+            unsigned long long* kR = S.K;
+            unsigned long long* kL = reinterpret_cast<unsigned long long*>(S.bLmax);
+            if (lane < NB) {
+                kR[lane] = ~0ull;
+                kL[lane] = ~0ull;
             }
-            if (lane == 0) {
-                S.bRmin[b] = rmin;
-                S.bLmax[b] = lmax;
+            __syncwarp();
+            for (int c0 = 0; c0 < n; c0 += 32) {
+                const int i = c0 + lane;
+                int b = -1;
+                unsigned long long kr = ~0ull, kl = ~0ull;
+                if (i < n) {
+                    b = S.nbkt[i];
+                    const int e = S.perm[p + i];
+                    kr = fkey(S.F[2 * d][e]);
+                    kl = ~fkey(S.F[2 * d + 1][e]);
+                }
+                const unsigned grp = __match_any_sync(FULL, b);
+                unsigned long long mr, ml;
+                unsigned pr, pl;
+                group_min_kp(grp, kr, (unsigned)i, &mr, &pr);
+                group_min_kp(grp, kl, (unsigned)i, &ml, &pl);
+                if (b >= 0 && lane == (int)(__ffs(grp) - 1)) {
+                    if (mr < kR[b]) {
+                        kR[b] = mr;
+                        S.brun[b] = (int)pr;
+                    }
+                    if (ml < kL[b]) {
+                        kL[b] = ml;
+                        S.bstart[b] = (int)pl;
+                    }
+                }
+                __syncwarp();
             }
+            if (lane < NB) {
+                const bool any = S.cnt[lane] > 0;
+                const double rmin = any ? S.F[2 * d][S.perm[p + S.brun[lane]]] : DBL_MAX;
+                const double lmax = any ? S.F[2 * d + 1][S.perm[p + S.bstart[lane]]] : -DBL_MAX;
+                S.bRmin[lane] = rmin;
+                S.bLmax[lane] = lmax;  // replaces this bucket's key
+            }
+            __syncwarp();
         }
-        __syncwarp();
         Decision D = warp_decide(S.cnt, S.bRmin, S.bLmax, NB, n, R, Lr, bl);
         if (D.kind == 0) {
             // all cells in one bucket (creation.py:345-358)

@@ -473,45 +473,6 @@ __global__ void __launch_bounds__(LOC_THREADS, MINB)
     append_open(open, i, qlist, qcount);
 }
 
-// The same stage as a resident grid (MINB blocks per SM) striding over the
-// sorted queries with a two-deep software pipeline: while a thread tests one
-// query's cells, the point of its next query (read through the permutation)
-// and the permutation entry of the one after that are already in flight, so
-// the two dependent random reads that start every query overlap the work of
-// the previous one.
-template <int KT, bool MULTI, int MINB>
-__global__ void __launch_bounds__(LOC_THREADS, MINB)
-    k_cells_pipe(const __grid_constant__ TreeL T0, const TreeL* __restrict__ forest, const int* __restrict__ qtree,
-                 const double2* __restrict__ pts, const int* __restrict__ order, int64_t n,
-                 int64_t* __restrict__ out, int* __restrict__ res_sorted, int* __restrict__ qlist,
-                 int* __restrict__ qcount) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int oi1 = 0, oi2 = 0;
-    double2 p1 = make_double2(0.0, 0.0);
-    if (i0 < n) {
-        oi1 = order ? order[i0] : (int)i0;
-        p1 = pts[oi1];
-    }
-    if (i0 + stride < n) oi2 = order ? order[i0 + stride] : (int)(i0 + stride);
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const int64_t i = base + threadIdx.x;
-        const int oi = oi1;
-        const double2 pp = p1;
-        if (i + stride < n) {  // next query's point: its permutation entry arrived during the last iteration
-            p1 = pts[oi2];
-            oi1 = oi2;
-        }
-        if (i + 2 * stride < n) oi2 = order ? order[i + 2 * stride] : (int)(i + 2 * stride);
-        bool open = false;
-        if (i < n) {
-            const TreeL& T = tree_of<MULTI>(T0, forest, qtree, oi);
-            open = cells_one<KT>(T, pp, i, oi, out, res_sorted);
-        }
-        append_open(open, i, qlist, qcount);
-    }
-}
-
 // Results by sorted position -> out[order[i]], in two passes so that the
 // random 8-byte writes land in an L2-sized window at a time and leave the
 // cache as whole sectors: (1) regroup the (query, result) pairs by the
@@ -2019,17 +1980,7 @@ int ct_locate_fast(const ct_tree* t, const double* points, int64_t n, double tol
     int* res_sorted = (lists && ord && n > RES_SCATTER_MIN) ? sorted_results(L) : nullptr;
 #define CT_FAST_STAGES(KT)                                                                                        \
     if (lists) {                                                                                                   \
-        if (cells_bpsm < 0) {                                                                                      \
-            /* software-pipelined variant: a resident grid of -cells_bpsm blocks per SM */                         \
-            const int mb = cells_bpsm == -5 ? 5 : 6;                                                               \
-            const unsigned gp = (unsigned)std::min<int64_t>((int64_t)grid, (int64_t)sms * mb);                     \
-            if (mb == 5)                                                                                           \
-                k_cells_pipe<KT, false, 5><<<gp, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out,       \
-                                                                       res_sorted, L.open, &L.counters[3]);       \
-            else                                                                                                   \
-                k_cells_pipe<KT, false, 6><<<gp, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out,       \
-                                                                       res_sorted, L.open, &L.counters[3]);       \
-        } else if (cells_bpsm == 4)                                                                                \
+        if (cells_bpsm == 4)                                                                                       \
             k_cells<KT, false, 4><<<grid, LOC_THREADS, 0, st>>>(T, nullptr, nullptr, P, ord, n, out, res_sorted,   \
                                                                 L.open, &L.counters[3]);                           \
         else if (cells_bpsm == 8)                                                                                  \

@@ -22,7 +22,7 @@ def test_buckets_and_keys():
 
 def test_candidates_cover_the_space():
     c = at.candidates("locate")
-    assert len(c) == 4 * 5 * 3 and len({json.dumps(x, sort_keys=True) for x in c}) == len(c)
+    assert len(c) == 4 * 3 * 3 and len({json.dumps(x, sort_keys=True) for x in c}) == len(c)
     c = at.candidates("boxes", fixed={"work_order": True})
     assert len(c) == 3 and all(x["work_order"] is True for x in c)
 
