@@ -345,6 +345,25 @@ __device__ __forceinline__ double centroid_of(double lo, double hi) {
     return __dadd_rn(lo, __dmul_rn(0.5, __dsub_rn(hi, lo)));
 }
 
+// Bucket of the centroid of [lo, hi] (centroid_test creation.py:44-51)
+// without float64 arithmetic when possible: the rounded centroid lies between
+// lo and hi (hi - lo rounds to at most twice the exact half-width, and every
+// rounding is monotone), so when lo and hi fall in the same bucket it does
+// too.  Otherwise -- or for NaN, infinite or huge values, where hi - lo could
+// overflow -- the centroid is computed.  (GB300 runs float64 at 1/64 of the
+// float32 rate; the integer key comparisons replace three float64 operations
+// per cell and level.)
+__device__ __forceinline__ int bucket_of_box(const unsigned long long* K, int NB, double lo, double hi) {
+    const unsigned long long bl = (unsigned long long)__double_as_longlong(lo);
+    const unsigned long long bh = (unsigned long long)__double_as_longlong(hi);
+    const bool tame = ((bl >> 52) & 0x7ff) < 0x7fd && ((bh >> 52) & 0x7ff) < 0x7fd;  // |x| < 2^1022, not NaN
+    if (tame) {
+        const int b = find_bucket(K, NB, fkey(lo));
+        if (b >= 0 && b == find_bucket(K, NB, fkey(hi))) return b;
+    }
+    return find_bucket(K, NB, fkey(centroid_of(lo, hi)));
+}
+
 __global__ void k_init_elems(const double* __restrict__ bb, int n, WS ws) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double x0 = bb[4 * (size_t)i], x1 = bb[4 * (size_t)i + 1], y0 = bb[4 * (size_t)i + 2], y1 = bb[4 * (size_t)i + 3];
@@ -516,21 +535,19 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     for (int base = s; base < e; base += blockDim.x) {
         int i = base + tid;
         bool valid = i < e;
-        double v0 = 0, v1 = 0, v2 = 0, v3 = 0, c0 = 0, c1 = 0;
+        double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
         if (valid) {
             v0 = F0[i];
             v1 = F1[i];
             v2 = F2[i];
             v3 = F3[i];
-            c0 = centroid_of(v0, v1);
-            c1 = centroid_of(v2, v3);
         }
         unsigned long long k0 = fkey(v0), k1 = ~fkey(v1), k2 = fkey(v2), k3 = ~fkey(v3);
 #pragma unroll
         for (int d = 0; d < 2; d++) {
             int b = -2;
             if (valid) {
-                b = find_bucket(K[d], NB, fkey(d ? c1 : c0));
+                b = d ? bucket_of_box(K[1], NB, v2, v3) : bucket_of_box(K[0], NB, v0, v1);
                 if (b < 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
             }
             unsigned grp = __match_any_sync(FULL, b);
@@ -786,7 +803,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
     for (int b0 = s; b0 < e; b0 += blockDim.x) {
         int i = b0 + tid;
         bool valid = i < e;
-        int b = valid ? find_bucket(K, NB, fkey(centroid_of(Lo[i], Hi[i]))) : -2;
+        int b = valid ? bucket_of_box(K, NB, Lo[i], Hi[i]) : -2;
         if (valid && b < 0) b = -1;  // counted nowhere: flagged by k_stats
         unsigned grp = __match_any_sync(FULL, b);
         int rank = __popc(grp & lanemask_lt());
@@ -851,10 +868,6 @@ __device__ __forceinline__ void sub_push(SubSmem& S, int sp, int v, int p, int n
     S.stk_depth[sp] = depth;
 }
 
-// centroid of cell k along dimension d (creation.py:50), as k_init_elems computes it
-__device__ __forceinline__ double sub_centroid(const SubSmem& S, int d, int k) {
-    return centroid_of(S.F[2 * d][k], S.F[2 * d + 1][k]);
-}
 
 // First-occurrence min over perm[p .. p+n) of field f (min-form key: maxima
 // complemented when `is_max`); returns the exact value.  All lanes call.
@@ -929,7 +942,8 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         __syncwarp();
         bool lbad = false;
         for (int i = lane; i < n; i += 32) {
-            int b = find_bucket(S.K, NB, fkey(sub_centroid(S, d, S.perm[p + i])));
+            const int e = S.perm[p + i];
+            int b = bucket_of_box(S.K, NB, S.F[2 * d][e], S.F[2 * d + 1][e]);
             if (b < 0) {
                 lbad = true;
                 b = 0;

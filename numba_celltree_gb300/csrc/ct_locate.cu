@@ -876,12 +876,14 @@ __global__ void __launch_bounds__(RS_T) k_rs_scatter(const KI* __restrict__ kin,
 // The float32 node bounds are within `band` of the float64 bounds, so a
 // decision is certain when the cell range clears bound -/+ band (directed
 // rounding).
+// cw = 1 / sx and ch = 1 / sy (cell sizes, divided once by the caller): the
+// products differ from the quotients by an ulp or two, far inside the margin m.
 __device__ __forceinline__ int grid_cell_start(const float4* __restrict__ nf, int gx, int gy, float x0, float y0,
-                                               float sx, float sy, double m, float band, int max_steps) {
-    float xlo = __double2float_rd((double)x0 + (double)gx / (double)sx - m);
-    float xhi = __double2float_ru((double)x0 + (double)(gx + 1) / (double)sx + m);
-    float ylo = __double2float_rd((double)y0 + (double)gy / (double)sy - m);
-    float yhi = __double2float_ru((double)y0 + (double)(gy + 1) / (double)sy + m);
+                                               double cw, double ch, double m, float band, int max_steps) {
+    float xlo = __double2float_rd((double)x0 + (double)gx * cw - m);
+    float xhi = __double2float_ru((double)x0 + (double)(gx + 1) * cw + m);
+    float ylo = __double2float_rd((double)y0 + (double)gy * ch - m);
+    float yhi = __double2float_ru((double)y0 + (double)(gy + 1) * ch + m);
     int v = 0;
     for (int k = 0; k < max_steps; k++) {
         float4 q = nf[v];
@@ -904,11 +906,11 @@ __device__ __forceinline__ int grid_cell_start(const float4* __restrict__ nf, in
 }
 
 // One thread per grid cell of one tree.
-__global__ void k_grid_start(const float4* __restrict__ nf, int gnx, int gny, float x0, float y0, float sx, float sy,
+__global__ void k_grid_start(const float4* __restrict__ nf, int gnx, int gny, float x0, float y0, double cw, double ch,
                              double m, float band, int max_steps, int* __restrict__ start) {
     int64_t total = (int64_t)gnx * gny;
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x)
-        start[c] = grid_cell_start(nf, (int)(c % gnx), (int)(c / gnx), x0, y0, sx, sy, m, band, max_steps);
+        start[c] = grid_cell_start(nf, (int)(c % gnx), (int)(c / gnx), x0, y0, cw, ch, m, band, max_steps);
 }
 
 // ---------------------------------------------------------------------------
@@ -1442,7 +1444,7 @@ static int scatter_results(const LocWS& L, int64_t n, unsigned int* err, int64_t
 // here so that no value has to come back to the host between the build and
 // the locate.
 // ---------------------------------------------------------------------------
-constexpr int FX_WORDS = 8;  // summary words per tree: 5 reduction keys, grid margin
+constexpr int FX_WORDS = 8;  // summary words per tree: 5 reduction keys, grid margin, grid cell sizes
 
 // Stand-in tree of a build that overflowed its node capacity (its node
 // ranges are not usable): one empty leaf, so that every query of the batch
@@ -1567,6 +1569,8 @@ __global__ void k_fx_records(const __grid_constant__ ct_forest_index X, TreeL* _
     T.gnx = grid_ok ? gnx : 0;
     T.gny = grid_ok ? gny : 0;
     S[5] = (unsigned long long)__double_as_longlong(grid_ok ? ldexp(hmax(ex, ey) + F, -19) : 0.0);
+    S[6] = (unsigned long long)__double_as_longlong(grid_ok ? 1.0 / (double)T.gsx : 0.0);  // grid cell sizes
+    S[7] = (unsigned long long)__double_as_longlong(grid_ok ? 1.0 / (double)T.gsy : 0.0);
     T.coff = nullptr;  // no candidate lists
     T.K = K;
     T.S4 = poly32_stride(K);
@@ -1666,8 +1670,10 @@ __global__ void k_fx_grid_start(const __grid_constant__ ct_forest_index X, const
         }
         const int64_t local = c - X.grid_off[t];
         const double m = __longlong_as_double((long long)X.summary[(int64_t)t * FX_WORDS + 5]);
-        X.grid_start[c] = grid_cell_start(T.nf, (int)(local % T.gnx), (int)(local / T.gnx), T.gx0, T.gy0, T.gsx,
-                                          T.gsy, m, T.bandG, X.max_depth[t] + 2);
+        const double cw = __longlong_as_double((long long)X.summary[(int64_t)t * FX_WORDS + 6]);
+        const double ch = __longlong_as_double((long long)X.summary[(int64_t)t * FX_WORDS + 7]);
+        X.grid_start[c] = grid_cell_start(T.nf, (int)(local % T.gnx), (int)(local / T.gnx), T.gx0, T.gy0, cw, ch, m,
+                                          T.bandG, X.max_depth[t] + 2);
     }
 }
 
@@ -1744,8 +1750,9 @@ int ct_pack_grid(ct_tree* t, void* stream) {
     int64_t total = (int64_t)gnx * gny;
     unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, 152 * 16);
     k_grid_start<<<blocks, 256, 0, (cudaStream_t)stream>>>((const float4*)t->nodes_f32, gnx, gny, t->grid_x0,
-                                                          t->grid_y0, t->grid_sx, t->grid_sy, m, band,
-                                                          t->max_depth + 2, t->grid_start);
+                                                          t->grid_y0, 1.0 / (double)t->grid_sx,
+                                                          1.0 / (double)t->grid_sy, m, band, t->max_depth + 2,
+                                                          t->grid_start);
     CT_CHECK_LAUNCH("pack grid");
     return CT_OK;
 }
