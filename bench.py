@@ -643,7 +643,7 @@ def main():
 
     import ctypes
 
-    from numba_celltree_gb300 import _device, _lib
+    from numba_celltree_gb300 import _device, _lib, _pipeline
 
     t = tree._tree
     lib = _lib.load()
@@ -762,8 +762,9 @@ def main():
                "d2h_bytes_per_step": int(n * 8), "ms_per_step": round(e2e_s * 1e3, 3),
                "ms_steps": [round(x * 1e3, 2) for x in step_s], "statistic": "median of the timed steps",
                "link_ms": round(link_ms, 3), "frac_of_link_bound": round(link_ms / (e2e_s * 1e3), 3),
-               "path": "CellTree2d.locate_points(numpy in pinned memory) -> numpy; "
-                       "chunks of 2^25 points, upload / query / download overlapped on three streams"}
+               "path": "CellTree2d.locate_points(numpy in pinned memory) -> numpy; chunks of 2^25 points, "
+                       "upload / query / download overlapped (chunks queried on two streams in turn)",
+               "chunk_launch_shape": t.cached("locate", min(n, _pipeline.CHUNK_POINTS))}
         e2e_pageable = {"value": round(ws * n / e2e_page_s / 1e6, 3), "unit": UNIT,
                         "h2d_bytes_per_step": int(pts_h.nbytes), "d2h_bytes_per_step": int(n * 8),
                         "ms_per_step": round(e2e_page_s * 1e3, 3), "ms_steps": [round(x * 1e3, 2) for x in page_s],

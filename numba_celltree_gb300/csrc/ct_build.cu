@@ -345,25 +345,6 @@ __device__ __forceinline__ double centroid_of(double lo, double hi) {
     return __dadd_rn(lo, __dmul_rn(0.5, __dsub_rn(hi, lo)));
 }
 
-// Bucket of the centroid of [lo, hi] (centroid_test creation.py:44-51)
-// without float64 arithmetic when possible: the rounded centroid lies between
-// lo and hi (hi - lo rounds to at most twice the exact half-width, and every
-// rounding is monotone), so when lo and hi fall in the same bucket it does
-// too.  Otherwise -- or for NaN, infinite or huge values, where hi - lo could
-// overflow -- the centroid is computed.  (GB300 runs float64 at 1/64 of the
-// float32 rate; the integer key comparisons replace three float64 operations
-// per cell and level.)
-__device__ __forceinline__ int bucket_of_box(const unsigned long long* K, int NB, double lo, double hi) {
-    const unsigned long long bl = (unsigned long long)__double_as_longlong(lo);
-    const unsigned long long bh = (unsigned long long)__double_as_longlong(hi);
-    const bool tame = ((bl >> 52) & 0x7ff) < 0x7fd && ((bh >> 52) & 0x7ff) < 0x7fd;  // |x| < 2^1022, not NaN
-    if (tame) {
-        const int b = find_bucket(K, NB, fkey(lo));
-        if (b >= 0 && b == find_bucket(K, NB, fkey(hi))) return b;
-    }
-    return find_bucket(K, NB, fkey(centroid_of(lo, hi)));
-}
-
 __global__ void k_init_elems(const double* __restrict__ bb, int n, WS ws) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double x0 = bb[4 * (size_t)i], x1 = bb[4 * (size_t)i + 1], y0 = bb[4 * (size_t)i + 2], y1 = bb[4 * (size_t)i + 3];
@@ -547,7 +528,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
         for (int d = 0; d < 2; d++) {
             int b = -2;
             if (valid) {
-                b = d ? bucket_of_box(K[1], NB, v2, v3) : bucket_of_box(K[0], NB, v0, v1);
+                b = find_bucket(K[d], NB, fkey(d ? centroid_of(v2, v3) : centroid_of(v0, v1)));
                 if (b < 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
             }
             unsigned grp = __match_any_sync(FULL, b);
@@ -803,7 +784,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_scatter(WS ws, int parity, in
     for (int b0 = s; b0 < e; b0 += blockDim.x) {
         int i = b0 + tid;
         bool valid = i < e;
-        int b = valid ? bucket_of_box(K, NB, Lo[i], Hi[i]) : -2;
+        int b = valid ? find_bucket(K, NB, fkey(centroid_of(Lo[i], Hi[i]))) : -2;
         if (valid && b < 0) b = -1;  // counted nowhere: flagged by k_stats
         unsigned grp = __match_any_sync(FULL, b);
         int rank = __popc(grp & lanemask_lt());
@@ -943,7 +924,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
         bool lbad = false;
         for (int i = lane; i < n; i += 32) {
             const int e = S.perm[p + i];
-            int b = bucket_of_box(S.K, NB, S.F[2 * d][e], S.F[2 * d + 1][e]);
+            int b = find_bucket(S.K, NB, fkey(centroid_of(S.F[2 * d][e], S.F[2 * d + 1][e])));
             if (b < 0) {
                 lbad = true;
                 b = 0;
