@@ -1000,6 +1000,7 @@ __global__ void __launch_bounds__(SUB_WARPS * 32) k_subtree(WS ws, int NB, long 
             if (lane < NB) {
                 kR[lane] = ~0ull;
                 kL[lane] = ~0ull;
+                S.brun[lane] = S.bstart[lane];  // positions when every key of the bucket ties at ~0
             }
             __syncwarp();
             for (int c0 = 0; c0 < n; c0 += 32) {
