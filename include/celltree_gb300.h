@@ -392,8 +392,20 @@ typedef struct ct_forest_index {
     void* poly_f32;             /* 16 B units, tree i from poly32_off[i] (ct_poly32_stride(K_i) per cell) */
     uint8_t* poly_len;          /* n_total */
     uint8_t* poly_len32;        /* n_total */
-    unsigned long long* summary; /* scratch: n_trees x 8 words */
+    unsigned long long* summary; /* scratch: n_trees x 16 words */
     unsigned int* error_word;   /* device: CT_DEVERR_* bits */
+    /* candidate lists of the batch locate (as ct_cand_count / ct_cand_fill for
+     * one tree, covering each tree's query tolerance), built when
+     * cand_capacity > 0; a build whose entries exceed cand_capacity runs the
+     * locate without them (same results, slower) */
+    unsigned long long* cand_count; /* scratch: grid_cells + 1 */
+    int64_t* cand_off;          /* grid_cells + 1 offsets (of all trees' grid cells) */
+    void* cand_box;             /* n_total x 16 B */
+    int32_t* cand_idx;          /* cand_capacity entries: leaf positions within the tree */
+    void* cand_lbox;            /* cand_capacity x 16 B */
+    void* cand_scan_ws;         /* ct_scan_workspace_size(grid_cells + 1) bytes */
+    size_t cand_scan_bytes;
+    int64_t cand_capacity;
 } ct_forest_index;
 /* Fills `plan` (points per tree from point_off_host, n_trees + 1 host
  * offsets; kt and stack from the index's k_max and stack) and uploads the

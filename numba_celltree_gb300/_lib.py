@@ -124,7 +124,11 @@ class CtForestIndex(ctypes.Structure):
         ("pad_", _I32),
         ("tolerance", _D),
     ] + [(n, _P) for n in ("nodes_f32", "nodes_f64", "poly_f64", "poly_f32", "poly_len", "poly_len32", "summary",
-                           "error_word")]
+                           "error_word", "cand_count", "cand_off", "cand_box", "cand_idx", "cand_lbox",
+                           "cand_scan_ws")] + [
+        ("cand_scan_bytes", _SZ),
+        ("cand_capacity", _I64),
+    ]
 
 
 # name -> (restype, argtypes)

@@ -168,12 +168,14 @@ class ForestPipeline:
     The traversal stack is sized from the first build's deepest tree plus
     ``stack_headroom`` levels (at most 126 levels); a replay whose trees grow
     deeper than that, or whose build overflows the node capacity, raises in
-    ``check``.
+    ``check``.  Each build also gets candidate lists (for each mesh's query
+    tolerance) of up to ``candidate_entries_per_cell`` entries per cell in
+    total; a build with more entries locates without them (same results).
     """
 
     def __init__(self, meshes: Sequence, point_counts: Sequence[int], fill_value: int = -1, n_buckets: int = 4,
                  cells_per_leaf: int = 2, tolerance: Optional[float] = None, stack_headroom: int = 8,
-                 grid_density: float = 1.0):
+                 grid_density: float = 1.0, candidate_entries_per_cell: float = 8.0):
         _validate_params(n_buckets, cells_per_leaf)
         if len(meshes) == 0:
             raise ValueError("need at least one mesh")
@@ -256,7 +258,16 @@ class ForestPipeline:
         self.poly_f32 = E(4 * poly32_off[-1], torch.float32)
         self.poly_len = E(n_total, torch.uint8)
         self.poly_len32 = E(n_total, torch.uint8)
-        self.summary = E(8 * n_trees, torch.int64)
+        self.summary = E(16 * n_trees, torch.int64)
+        grid_cells = int(grid_off[-1])
+        self.cand_capacity = int(candidate_entries_per_cell * n_total) if grid_cells > 0 else 0
+        self.cand_count = E(grid_cells + 1, torch.int64)
+        self.cand_off = E(grid_cells + 1, torch.int64)
+        self.cand_box = E(4 * n_total, torch.float32)
+        self.cand_idx = E(self.cand_capacity, torch.int32)
+        self.cand_lbox = E(4 * self.cand_capacity, torch.float32)
+        scan_bytes = int(lib.ct_scan_workspace_size(grid_cells + 1))
+        self.cand_scan = E(scan_bytes, torch.uint8)
         self.error_word = torch.zeros((1,), dtype=torch.int32, device=device)
         P = _device.ptr
         fb = self.build
@@ -275,6 +286,9 @@ class ForestPipeline:
                                                             P(self.poly_f32))
         X.poly_len, X.poly_len32, X.summary, X.error_word = (P(self.poly_len), P(self.poly_len32), P(self.summary),
                                                              P(self.error_word))
+        X.cand_count, X.cand_off, X.cand_box = P(self.cand_count), P(self.cand_off), P(self.cand_box)
+        X.cand_idx, X.cand_lbox, X.cand_scan_ws = P(self.cand_idx), P(self.cand_lbox), P(self.cand_scan)
+        X.cand_scan_bytes, X.cand_capacity = scan_bytes, self.cand_capacity
         if tolerance is not None and not float(tolerance) > 0.0:
             raise ValueError("tolerance must be > 0")
         self.index = X
@@ -360,6 +374,11 @@ class ForestPipeline:
             self.launch()
         self.check()
         return self.out[:self.n_points]
+
+    def candidate_entries(self) -> int:
+        """Entries of the last build's candidate lists (above cand_capacity
+        the lists were off for that build)."""
+        return int(self.cand_off[-1].item()) if self.cand_capacity else 0
 
     def result(self, i: int):
         """Cell indices of mesh i's points after the last run."""

@@ -516,19 +516,21 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     for (int base = s; base < e; base += blockDim.x) {
         int i = base + tid;
         bool valid = i < e;
-        double v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+        double v0 = 0, v1 = 0, v2 = 0, v3 = 0, c0 = 0, c1 = 0;
         if (valid) {
             v0 = F0[i];
             v1 = F1[i];
             v2 = F2[i];
             v3 = F3[i];
+            c0 = centroid_of(v0, v1);
+            c1 = centroid_of(v2, v3);
         }
         unsigned long long k0 = fkey(v0), k1 = ~fkey(v1), k2 = fkey(v2), k3 = ~fkey(v3);
 #pragma unroll
         for (int d = 0; d < 2; d++) {
             int b = -2;
             if (valid) {
-                b = find_bucket(K[d], NB, fkey(d ? centroid_of(v2, v3) : centroid_of(v0, v1)));
+                b = find_bucket(K[d], NB, fkey(d ? c1 : c0));
                 if (b < 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
             }
             unsigned grp = __match_any_sync(FULL, b);

@@ -1114,6 +1114,124 @@ struct CandRecs {
 // MODE 0: count the (cell, grid cell) pairs per grid cell; MODE 2: count and
 // record them (CandRecs); MODE 1: write the entries of the cells listed in
 // `cells` (all cells when null) at off[g] + cursor.
+// One cell j (leaf order) with widened box b: the grid cells its predicate
+// region meets, each counted in count[g] and, by MODE, recorded or written.
+template <int MODE, int KMAX>
+__device__ __forceinline__ void cand_cell(int64_t j, float4 b, const double2* __restrict__ poly,
+                                          const uint8_t* __restrict__ plen, int K, double ox, double oy, int gnx,
+                                          int gny, double x0, double y0, double sx, double sy, double cw, double ch,
+                                          double m, float Mf, float e2f, float ea,
+                                          unsigned long long* __restrict__ count, const int64_t* __restrict__ off,
+                                          int* __restrict__ idx, float4* __restrict__ lbox,
+                                          unsigned int* __restrict__ err, const CandRecs& rec) {
+    const float u = 5.9604644775390625e-08f;
+    int a0, a1, b0, b1;
+    int kept = 0;
+    if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) {
+        if (MODE == 2) rec.n[j] = 0;
+        return;
+    }
+    const int len = plen ? (int)plen[j] : K;
+    const double2* pv = poly + (size_t)j * K;
+    bool clip = KMAX <= 4 && len >= 3 && len <= KMAX;
+    for (int k = 0; k < len && clip; k++) clip = isfinite(pv[k].x) && isfinite(pv[k].y);
+    double ax = 0.0, ay = 0.0;
+    float2 L[KMAX];
+    float Lm = 0.0f;
+    if (clip) {
+        ax = pv[0].x - ox;
+        ay = pv[0].y - oy;
+        for (int k = 0; k < len; k++) {
+            L[k] = make_float2((float)((pv[k].x - ox) - ax), (float)((pv[k].y - oy) - ay));
+            Lm = fmaxf(Lm, fmaxf(fabsf(L[k].x), fabsf(L[k].y)));
+        }
+    }
+    const float d = u * Lm + ea;
+    // triangle fast path: edges, reciprocals, constants, orientation
+    float2 V[3], D[3];
+    float rx[3], ry[3], cc[3];
+    bool tri = clip && len == 3;
+    float Dm = 0.0f;
+    if (tri) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) V[k] = L[k];
+        float area2 = 0.0f, csum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float2 P = V[k], Q = V[(k + 1) % 3];
+            D[k] = make_float2(Q.x - P.x, Q.y - P.y);
+            rx[k] = (D[k].x != 0.0f) ? __frcp_rn(D[k].x) : 0.0f;
+            ry[k] = (D[k].y != 0.0f) ? __frcp_rn(D[k].y) : 0.0f;
+            cc[k] = P.x * Q.y - P.y * Q.x;
+            area2 += cc[k];
+            csum += fabsf(cc[k]);
+            Dm = fmaxf(Dm, fmaxf(fabsf(D[k].x), fabsf(D[k].y)));
+        }
+        // twice the signed area, beyond its rounding and the vertices' own
+        tri = area2 > 4.0f * u * csum + 32.0f * u * Lm * Lm + 16.0f * d * Lm;
+    }
+    // cw = 1 / sx, ch = 1 / sy: grid cell sizes, divided once on the host
+    const float fcw = (float)cw, fch = (float)ch;
+    // lower-left corner of the range's first grid cell relative to the anchor
+    const float fbx0 = (float)((x0 + (double)a0 * cw) - ax), fby0 = (float)((y0 + (double)b0 * ch) - ay);
+    const float axf = (float)ax, ayf = (float)ay;
+    for (int gy = b0; gy <= b1; gy++) {
+        const float ry0 = fby0 + (float)(gy - b0) * fch;
+        for (int gx = a0; gx <= a1; gx++) {
+            float4 r = b;
+            bool keep = true;
+            if (clip) {
+                const float rx0 = fbx0 + (float)(gx - a0) * fcw;
+                const float S = Lm + fabsf(rx0) + fabsf(ry0) + fcw + fch + 2.0f * e2f;
+                // slack: far above every rounding of the rectangle's
+                // placement, of the clip and of the vertices
+                const float w = ldexpf(S, -14) + 4.0f * ea;
+                const float X0 = rx0 - e2f - w, X1 = rx0 + fcw + e2f + w;
+                const float Y0 = ry0 - e2f - w, Y1 = ry0 + fch + e2f + w;
+                float4 c;
+                keep = tri ? tri_box(V, D, rx, ry, cc, Lm, Dm, d, X0, X1, Y0, Y1, &c)
+                           : clip_box<KMAX>(L, len, X0, X1, Y0, Y1, S, ea, &c);
+                if (keep) {
+                    // back to the frame: the anchor's float32 rounding,
+                    // then M and the slack; rounded outward
+                    const float px = Mf + 2.0f * w + 2.0f * u * (fabsf(axf) + fabsf(c.x) + fabsf(c.y)) + 1e-30f;
+                    const float py = Mf + 2.0f * w + 2.0f * u * (fabsf(ayf) + fabsf(c.z) + fabsf(c.w)) + 1e-30f;
+                    r.x = fmaxf(b.x, __fsub_rd(__fadd_rd(axf, c.x), px));
+                    r.y = fminf(b.y, __fadd_ru(__fadd_ru(axf, c.y), px));
+                    r.z = fmaxf(b.z, __fsub_rd(__fadd_rd(ayf, c.z), py));
+                    r.w = fminf(b.w, __fadd_ru(__fadd_ru(ayf, c.w), py));
+                }
+            }
+            if (!keep) continue;
+            int64_t g = (int64_t)gy * gnx + gx;
+            unsigned long long k = atomicAdd(&count[g], 1ull);
+            if (MODE == 1) {
+                const int64_t e = off[g] + (int64_t)k;
+                if (e >= off[g + 1]) {  // the counting pass decided otherwise: never write past g
+                    set_error(err, CT_DEVERR_CAPACITY);
+                    continue;
+                }
+                idx[e] = (int)j;
+                lbox[e] = r;
+            } else if (MODE == 2) {
+                if (kept < CAND_SLOTS) {
+                    rec.g[j * CAND_SLOTS + kept] = (int)g;
+                    rec.r[j * CAND_SLOTS + kept] = r;
+                }
+                kept++;
+            }
+        }
+    }
+    if (MODE == 2) {
+        if (kept > CAND_SLOTS) {
+            rec.n[j] = CAND_OVERFLOW;
+            rec.ovf[atomicAdd(rec.ovf_count, 1)] = (int)j;
+        } else {
+            rec.n[j] = (unsigned char)kept;
+        }
+    }
+}
+
 template <int MODE, int KMAX>
 __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __restrict__ poly,
                              const uint8_t* __restrict__ plen, int K, int64_t n, double ox, double oy, int gnx,
@@ -1122,116 +1240,11 @@ __global__ void k_cand_lists(const float4* __restrict__ box, const double2* __re
                              const int64_t* __restrict__ off,
                              int* __restrict__ idx, float4* __restrict__ lbox, unsigned int* __restrict__ err,
                              CandRecs rec, const int* __restrict__ cells, const int* __restrict__ cells_count) {
-    const float u = 5.9604644775390625e-08f;
     const int64_t nj = cells ? (int64_t)*cells_count : n;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nj; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = cells ? (int64_t)cells[t] : t;
-        int a0, a1, b0, b1;
-        const float4 b = box[j];
-        int kept = 0;
-        if (!cand_range(b, gnx, gny, x0, y0, sx, sy, m, &a0, &a1, &b0, &b1)) {
-            if (MODE == 2) rec.n[j] = 0;
-            continue;
-        }
-        const int len = plen ? (int)plen[j] : K;
-        const double2* pv = poly + (size_t)j * K;
-        bool clip = KMAX <= 4 && len >= 3 && len <= KMAX;
-        for (int k = 0; k < len && clip; k++) clip = isfinite(pv[k].x) && isfinite(pv[k].y);
-        double ax = 0.0, ay = 0.0;
-        float2 L[KMAX];
-        float Lm = 0.0f;
-        if (clip) {
-            ax = pv[0].x - ox;
-            ay = pv[0].y - oy;
-            for (int k = 0; k < len; k++) {
-                L[k] = make_float2((float)((pv[k].x - ox) - ax), (float)((pv[k].y - oy) - ay));
-                Lm = fmaxf(Lm, fmaxf(fabsf(L[k].x), fabsf(L[k].y)));
-            }
-        }
-        const float d = u * Lm + ea;
-        // triangle fast path: edges, reciprocals, constants, orientation
-        float2 V[3], D[3];
-        float rx[3], ry[3], cc[3];
-        bool tri = clip && len == 3;
-        float Dm = 0.0f;
-        if (tri) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) V[k] = L[k];
-            float area2 = 0.0f, csum = 0.0f;
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                const float2 P = V[k], Q = V[(k + 1) % 3];
-                D[k] = make_float2(Q.x - P.x, Q.y - P.y);
-                rx[k] = (D[k].x != 0.0f) ? __frcp_rn(D[k].x) : 0.0f;
-                ry[k] = (D[k].y != 0.0f) ? __frcp_rn(D[k].y) : 0.0f;
-                cc[k] = P.x * Q.y - P.y * Q.x;
-                area2 += cc[k];
-                csum += fabsf(cc[k]);
-                Dm = fmaxf(Dm, fmaxf(fabsf(D[k].x), fabsf(D[k].y)));
-            }
-            // twice the signed area, beyond its rounding and the vertices' own
-            tri = area2 > 4.0f * u * csum + 32.0f * u * Lm * Lm + 16.0f * d * Lm;
-        }
-        // cw = 1 / sx, ch = 1 / sy: grid cell sizes, divided once on the host
-        const float fcw = (float)cw, fch = (float)ch;
-        // lower-left corner of the range's first grid cell relative to the anchor
-        const float fbx0 = (float)((x0 + (double)a0 * cw) - ax), fby0 = (float)((y0 + (double)b0 * ch) - ay);
-        const float axf = (float)ax, ayf = (float)ay;
-        for (int gy = b0; gy <= b1; gy++) {
-            const float ry0 = fby0 + (float)(gy - b0) * fch;
-            for (int gx = a0; gx <= a1; gx++) {
-                float4 r = b;
-                bool keep = true;
-                if (clip) {
-                    const float rx0 = fbx0 + (float)(gx - a0) * fcw;
-                    const float S = Lm + fabsf(rx0) + fabsf(ry0) + fcw + fch + 2.0f * e2f;
-                    // slack: far above every rounding of the rectangle's
-                    // placement, of the clip and of the vertices
-                    const float w = ldexpf(S, -14) + 4.0f * ea;
-                    const float X0 = rx0 - e2f - w, X1 = rx0 + fcw + e2f + w;
-                    const float Y0 = ry0 - e2f - w, Y1 = ry0 + fch + e2f + w;
-                    float4 c;
-                    keep = tri ? tri_box(V, D, rx, ry, cc, Lm, Dm, d, X0, X1, Y0, Y1, &c)
-                               : clip_box<KMAX>(L, len, X0, X1, Y0, Y1, S, ea, &c);
-                    if (keep) {
-                        // back to the frame: the anchor's float32 rounding,
-                        // then M and the slack; rounded outward
-                        const float px = Mf + 2.0f * w + 2.0f * u * (fabsf(axf) + fabsf(c.x) + fabsf(c.y)) + 1e-30f;
-                        const float py = Mf + 2.0f * w + 2.0f * u * (fabsf(ayf) + fabsf(c.z) + fabsf(c.w)) + 1e-30f;
-                        r.x = fmaxf(b.x, __fsub_rd(__fadd_rd(axf, c.x), px));
-                        r.y = fminf(b.y, __fadd_ru(__fadd_ru(axf, c.y), px));
-                        r.z = fmaxf(b.z, __fsub_rd(__fadd_rd(ayf, c.z), py));
-                        r.w = fminf(b.w, __fadd_ru(__fadd_ru(ayf, c.w), py));
-                    }
-                }
-                if (!keep) continue;
-                int64_t g = (int64_t)gy * gnx + gx;
-                unsigned long long k = atomicAdd(&count[g], 1ull);
-                if (MODE == 1) {
-                    const int64_t e = off[g] + (int64_t)k;
-                    if (e >= off[g + 1]) {  // the counting pass decided otherwise: never write past g
-                        set_error(err, CT_DEVERR_CAPACITY);
-                        continue;
-                    }
-                    idx[e] = (int)j;
-                    lbox[e] = r;
-                } else if (MODE == 2) {
-                    if (kept < CAND_SLOTS) {
-                        rec.g[j * CAND_SLOTS + kept] = (int)g;
-                        rec.r[j * CAND_SLOTS + kept] = r;
-                    }
-                    kept++;
-                }
-            }
-        }
-        if (MODE == 2) {
-            if (kept > CAND_SLOTS) {
-                rec.n[j] = CAND_OVERFLOW;
-                rec.ovf[atomicAdd(rec.ovf_count, 1)] = (int)j;
-            } else {
-                rec.n[j] = (unsigned char)kept;
-            }
-        }
+        cand_cell<MODE, KMAX>(j, box[j], poly, plen, K, ox, oy, gnx, gny, x0, y0, sx, sy, cw, ch, m, Mf, e2f, ea, count,
+                              off, idx, lbox, err, rec);
     }
 }
 
@@ -1444,7 +1457,8 @@ static int scatter_results(const LocWS& L, int64_t n, unsigned int* err, int64_t
 // here so that no value has to come back to the host between the build and
 // the locate.
 // ---------------------------------------------------------------------------
-constexpr int FX_WORDS = 8;  // summary words per tree: 5 reduction keys, grid margin, grid cell sizes
+constexpr int FX_WORDS = 16;  // summary words per tree: 5 reduction keys, grid margin, grid cell sizes,
+                              // candidate-list reach
 
 // Stand-in tree of a build that overflowed its node capacity (its node
 // ranges are not usable): one empty leaf, so that every query of the batch
@@ -1585,6 +1599,10 @@ __global__ void k_fx_records(const __grid_constant__ ct_forest_index X, TreeL* _
     }
     T.tol = tol;
     T.tolf = __double2float_ru(tol);
+    // reach of the candidate lists built for this tolerance (cand_reach)
+    S[8] = (unsigned long long)__double_as_longlong(grid_ok ? 2.0 * tol * (1.0 + 1e-6) + 16.0 * (double)T.dabs +
+                                                                  ldexp(F, -48)
+                                                            : 0.0);
     T.ohx = __double2float_rn(ox);
     T.olx = __double2float_rn(ox - (double)T.ohx);
     T.ohy = __double2float_rn(oy);
@@ -1675,6 +1693,69 @@ __global__ void k_fx_grid_start(const __grid_constant__ ct_forest_index X, const
         X.grid_start[c] = grid_cell_start(T.nf, (int)(local % T.gnx), (int)(local / T.gnx), T.gx0, T.gy0, cw, ch, m,
                                           T.bandG, X.max_depth[t] + 2);
     }
+}
+
+// Candidate lists of every tree (k_cand_box / k_cand_lists over the batch):
+// the widened box of each cell, then the counting (MODE 0) or filling
+// (MODE 1) pass with the cell's tree parameters; grid cell g of tree t is
+// entry grid_off[t] + g of the batch-wide counts and offsets, and an entry
+// stores the cell's leaf position within its tree.
+__global__ void k_fx_cand_box(const __grid_constant__ ct_forest_index X, const TreeL* __restrict__ trees) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < X.n_total;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tree_of_row(X.tree_off, X.n_trees, p);
+        const TreeL& T = trees[t];
+        const double M = __longlong_as_double((long long)X.summary[(int64_t)t * FX_WORDS + 8]);
+        const int64_t bi = X.bb_indices[p];
+        const int64_t rows = X.tree_off[t + 1] - X.tree_off[t];
+        if (!T.gstart || bi < 0 || bi >= rows) continue;
+        const double* b = X.bb_coords + 4 * (X.tree_off[t] + bi);
+        reinterpret_cast<float4*>(X.cand_box)[p] =
+            make_float4(__double2float_rd((b[0] - T.ox) - M), __double2float_ru((b[1] - T.ox) + M),
+                        __double2float_rd((b[2] - T.oy) - M), __double2float_ru((b[3] - T.oy) + M));
+    }
+}
+
+template <int MODE>
+__global__ void k_fx_cand_lists(const __grid_constant__ ct_forest_index X, const TreeL* __restrict__ trees) {
+    if (MODE == 1 && X.cand_off[X.grid_cells] > X.cand_capacity) return;  // lists off for this build
+    CandRecs none;
+    memset(&none, 0, sizeof(none));
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < X.n_total;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int t = tree_of_row(X.tree_off, X.n_trees, p);
+        const TreeL& T = trees[t];
+        if (!T.gstart) continue;  // no grid for this build: no lists
+        const unsigned long long* S = X.summary + (int64_t)t * FX_WORDS;
+        const double m = __longlong_as_double((long long)S[5]);
+        const double cw = __longlong_as_double((long long)S[6]), ch = __longlong_as_double((long long)S[7]);
+        const double M = __longlong_as_double((long long)S[8]);
+        const float Mf = __double2float_ru(M), e2f = __double2float_ru(m + M);
+        const float ea = __double2float_rn(4.0 * (double)T.dabs);
+        const int64_t j = p - X.tree_off[t];
+        const int64_t go = X.grid_off[t];
+        const float4 b = reinterpret_cast<const float4*>(X.cand_box)[p];
+        unsigned long long* count = X.cand_count + go;
+        const int64_t* off = MODE == 1 ? X.cand_off + go : nullptr;
+        if (T.K <= 4)
+            cand_cell<MODE, 4>(j, b, T.poly, T.plen, T.K, T.ox, T.oy, T.gnx, T.gny, (double)T.gx0, (double)T.gy0,
+                               (double)T.gsx, (double)T.gsy, cw, ch, m, Mf, e2f, ea, count, off, X.cand_idx,
+                               (float4*)X.cand_lbox, X.error_word, none);
+        else
+            cand_cell<MODE, 32>(j, b, T.poly, T.plen, T.K, T.ox, T.oy, T.gnx, T.gny, (double)T.gx0, (double)T.gy0,
+                                (double)T.gsx, (double)T.gsy, cw, ch, m, Mf, e2f, ea, count, off, X.cand_idx,
+                                (float4*)X.cand_lbox, X.error_word, none);
+    }
+}
+
+// Lists on for every tree with a grid when the batch's entries fit.
+__global__ void k_fx_cand_enable(const __grid_constant__ ct_forest_index X, TreeL* __restrict__ trees) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= X.n_trees || !trees[t].gstart) return;
+    if (X.cand_off[X.grid_cells] > X.cand_capacity) return;
+    trees[t].coff = X.cand_off + X.grid_off[t];
+    trees[t].cidx = X.cand_idx;
+    trees[t].cbox = (const float4*)X.cand_lbox;
 }
 
 }  // namespace ctl
@@ -2205,6 +2286,11 @@ static int check_index(const ct_forest_index* X) {
         !X->grid_ny || (X->grid_cells > 0 && !X->grid_start) || !X->nodes_f32 || !X->nodes_f64 || !X->poly_f64 ||
         !X->poly_f32 || !X->poly_len || !X->poly_len32 || !X->summary || !X->error_word)
         return ct_fail(CT_ERR_ARG, "index has a null array");
+    if (X->cand_capacity < 0) return ct_fail(CT_ERR_ARG, "cand_capacity must be >= 0");
+    if (X->cand_capacity > 0 &&
+        (!X->cand_count || !X->cand_off || !X->cand_box || !X->cand_idx || !X->cand_lbox || !X->cand_scan_ws ||
+         X->cand_scan_bytes < ct_scan_workspace_size(X->grid_cells + 1)))
+        return ct_fail(CT_ERR_ARG, "candidate-list arrays of the index are missing or too small");
     return CT_OK;
 }
 
@@ -2273,6 +2359,18 @@ int ct_forest_index_build(const ct_forest_index* X, const ct_forest_plan* plan, 
     k_fx_pack_nodes<<<blocks(X->node_capacity, 16), 256, 0, st>>>(*X, F.trees);
     k_fx_pack_cells<<<blocks(X->n_total, 16), 256, 0, st>>>(*X);
     if (X->grid_cells > 0) k_fx_grid_start<<<blocks(X->grid_cells, 16), 256, 0, st>>>(*X, F.trees);
+    if (X->cand_capacity > 0 && X->grid_cells > 0) {
+        const size_t cbytes = 8 * (size_t)(X->grid_cells + 1);
+        k_fx_cand_box<<<blocks(X->n_total, 16), 256, 0, st>>>(*X, F.trees);
+        CT_CUDA(cudaMemsetAsync(X->cand_count, 0, cbytes, st));
+        k_fx_cand_lists<0><<<blocks(X->n_total, 16), 256, 0, st>>>(*X, F.trees);
+        int sc = ct_exclusive_scan((const int64_t*)X->cand_count, X->grid_cells + 1, X->cand_off, X->cand_scan_ws,
+                                   X->cand_scan_bytes, nullptr, stream);
+        if (sc) return sc;
+        k_fx_cand_enable<<<(unsigned)((X->n_trees + 127) / 128), 128, 0, st>>>(*X, F.trees);
+        CT_CUDA(cudaMemsetAsync(X->cand_count, 0, cbytes, st));  // now the lists' cursors
+        k_fx_cand_lists<1><<<blocks(X->n_total, 16), 256, 0, st>>>(*X, F.trees);
+    }
     CT_CHECK_LAUNCH("forest index");
     return CT_OK;
 }

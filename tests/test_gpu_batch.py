@@ -253,6 +253,7 @@ def test_forest_pipeline_build_and_locate_replay_from_one_graph(oracle):
     counts = [len(p) for p in pts]
     pipe = ForestPipeline(meshes, counts)
     res = pipe.run(np.concatenate([xy for xy, _ in meshes]), np.concatenate(pts)).cpu().numpy()
+    assert 0 < pipe.candidate_entries() <= pipe.cand_capacity  # the locate used candidate lists
     for k, (xy, f) in enumerate(meshes):
         a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
         ref = oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])
@@ -269,6 +270,22 @@ def test_forest_pipeline_build_and_locate_replay_from_one_graph(oracle):
         for k, (xy, f) in enumerate(moved):
             a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
             assert np.array_equal(res[a:b], CellTree2d(xy, f, -1).locate_points(new[k])), (seed, k)
+
+
+@pytest.mark.gpu
+def test_forest_pipeline_without_room_for_candidate_lists(oracle):
+    """A candidate-list capacity below the build's entries: the build runs
+    the locate without lists, with the same results."""
+    from numba_celltree_gb300.batch import ForestPipeline
+
+    meshes = _meshes()[:6]
+    pts = _points(meshes, seed=5)
+    pipe = ForestPipeline(meshes, [len(p) for p in pts], candidate_entries_per_cell=0.01)
+    res = pipe.run(None, np.concatenate(pts)).cpu().numpy()
+    assert pipe.candidate_entries() > pipe.cand_capacity
+    for k, (xy, f) in enumerate(meshes):
+        a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
+        assert np.array_equal(res[a:b], oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k])), k
 
 
 @pytest.mark.gpu
