@@ -700,10 +700,25 @@ __global__ void __launch_bounds__(RS_T) k_keys(const double2* __restrict__ pts, 
     // chunks past the end are empty (e = s): a negative length would make the
     // vector loop bound below round down into the next chunk
     int64_t s = (int64_t)blockIdx.x * chunk, e = max(s, min(s + chunk, n));
-    for (int64_t i = s + t; i < e; i += RS_T) {
-        unsigned k = morton24(g, pts[i]);
-        key[i] = k;
-        atomicAdd(&h[w][(k >> shift) & 255u], 1);
+    // four points in flight per thread (one at a time left the loads too few
+    // to cover the memory latency)
+    constexpr int U = 4;
+    for (int64_t i0 = s + t; i0 < e; i0 += U * RS_T) {
+        double2 q[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t i = i0 + (int64_t)u * RS_T;
+            if (i < e) q[u] = pts[i];
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int64_t i = i0 + (int64_t)u * RS_T;
+            if (i < e) {
+                const unsigned k = morton24(g, q[u]);
+                key[i] = k;
+                atomicAdd(&h[w][(k >> shift) & 255u], 1);
+            }
+        }
     }
     __syncthreads();
     int c = 0;
