@@ -78,6 +78,20 @@ def test_build_degenerate_duplicates(oracle):
         _same_tree(g, o)
 
 
+def test_build_columns_flip_dimension_in_large_nodes(oracle):
+    """Columns and rows of cells one cell wide: every centroid of a large
+    node shares one bucket along the node's dimension, so the multi-CTA
+    levels flip it and split along the other (the second statistics pass)."""
+    from numba_celltree_gb300 import CellTree2d
+
+    for nx, ny in ((1, 3000), (3000, 1), (2, 1500)):
+        xy, f = syn.quad_mesh(nx, ny, seed=15, extent=(float(nx), float(ny)), jitter=0.0)
+        for nb, cpl in ((4, 2), (3, 1)):
+            g = CellTree2d(xy, f, -1, nb, cpl)
+            o = oracle.OracleCellTree2d(xy, f, -1, nb, cpl)
+            _same_tree(g, o)
+
+
 def test_build_signed_zero_bounds(oracle):
     """Boxes whose extremes are -0.0 and +0.0: first occurrence decides the sign."""
     from numba_celltree_gb300 import CellTree2d
