@@ -45,10 +45,7 @@ constexpr int TILE_MIN = 2048;     // minimum cells per tile
 constexpr int MAX_TILES = 512;     // maximum tiles per node
 constexpr int SUB_WARPS = 2;       // warps per CTA in the subtree kernel (8.1 KB of shared memory each)
 
-// K_RETRY: a pending node whose cells all fell in one bucket of its stored
-// dimension; its statistics along the other dimension are gathered and it is
-// decided again within the same level.
-enum : int { K_PENDING = 0, K_SPLIT = 1, K_LEAF = 2, K_SUBTREE = 3, K_RETRY = 4 };
+enum : int { K_PENDING = 0, K_SPLIT = 1, K_LEAF = 2, K_SUBTREE = 3 };
 
 // Phase-A node record.
 struct ARec {
@@ -481,16 +478,12 @@ __global__ void k_make_tiles(WS ws, int NB) {
     }
 }
 
-// Per tile: bucket membership along one dimension -- the node's stored one
-// (PASS 0, every pending node) or, for the nodes whose cells all fell in one
-// bucket of it, the other one (PASS 1, K_RETRY nodes; their dim was flipped
-// by k_decide) -- and per bucket: count, first-occurrence min of lo_x / lo_y
-// and max of hi_x / hi_y (as min-form keys) and the first position of a zero
-// value.  The other dimension is needed only by those rare nodes, so it is
-// not gathered for the rest.
+// Per tile: bucket membership in both dimensions; per (dim, bucket): count,
+// first-occurrence min of lo_x / lo_y and max of hi_x / hi_y (as min-form
+// keys) and the first position of a zero value.
 // LOOP: the device-driven level loop's form -- a fixed grid walks the tiles
 // whose count the make-tiles pass left on the device.
-template <bool LOOP, int PASS>
+template <bool LOOP>
 __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int NB) {
     __shared__ unsigned long long K[2][NBMAX + 1];
     __shared__ unsigned int cnt[2][NBMAX];
@@ -505,16 +498,15 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     int lb = ws.cnt->lb;
     const ARec* R = &ws.recs[r];
     int tid = threadIdx.x;
-    if (PASS == 1 && R->kind != K_RETRY) continue;  // block-uniform
-    const int dd = R->dim;  // the dimension of this pass
     for (int j = tid; j < 2 * NBMAX; j += blockDim.x) (&cnt[0][0])[j] = 0u;
     for (int j = tid; j < 2 * NBMAX * 4; j += blockDim.x) {
         (&key[0][0][0])[j] = ~0ull;
         (&zp[0][0][0])[j] = INT32_MAX;
     }
-    if (tid <= NB) {
-        double Rd = R->bnd[2 * dd], Ld = R->bnd[2 * dd + 1];
-        K[dd][tid] = fkey(bucket_edge(tid, bucket_len(Ld, Rd, NB), Rd));
+    if (tid < 2 * (NB + 1)) {
+        int d = tid / (NB + 1), j = tid % (NB + 1);
+        double Rd = R->bnd[2 * d], Ld = R->bnd[2 * d + 1];
+        K[d][j] = fkey(bucket_edge(j, bucket_len(Ld, Rd, NB), Rd));
     }
     __syncthreads();
     const double* F0 = ws.f[parity][0];
@@ -524,20 +516,21 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     for (int base = s; base < e; base += blockDim.x) {
         int i = base + tid;
         bool valid = i < e;
-        double v0 = 0, v1 = 0, v2 = 0, v3 = 0, c = 0;
+        double v0 = 0, v1 = 0, v2 = 0, v3 = 0, c0 = 0, c1 = 0;
         if (valid) {
             v0 = F0[i];
             v1 = F1[i];
             v2 = F2[i];
             v3 = F3[i];
-            c = dd ? centroid_of(v2, v3) : centroid_of(v0, v1);
+            c0 = centroid_of(v0, v1);
+            c1 = centroid_of(v2, v3);
         }
         unsigned long long k0 = fkey(v0), k1 = ~fkey(v1), k2 = fkey(v2), k3 = ~fkey(v3);
-        {
-            const int d = dd;
+#pragma unroll
+        for (int d = 0; d < 2; d++) {
             int b = -2;
             if (valid) {
-                b = find_bucket(K[d], NB, fkey(c));
+                b = find_bucket(K[d], NB, fkey(d ? c1 : c0));
                 if (b < 0) atomicOr(&ws.cnt->err, CT_DEVERR_BUCKET);
             }
             unsigned grp = __match_any_sync(FULL, b);
@@ -562,18 +555,17 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
     }
     __syncthreads();
     size_t sidx = (size_t)(r - lb);
-    for (int b = tid; b < NB; b += blockDim.x) {
-        const int j = dd * NB + b;
-        unsigned cb = cnt[dd][b];
-        ws.tile_cnt[(size_t)t * 2 * NB + j] = cb;
-        if (cb) atomicAdd(&ws.st_cnt[sidx * 2 * NB + j], cb);
+    for (int j = tid; j < 2 * NB; j += blockDim.x) {
+        int d = j / NB, b = j % NB;
+        unsigned c = cnt[d][b];
+        ws.tile_cnt[(size_t)t * 2 * NB + j] = c;
+        if (c) atomicAdd(&ws.st_cnt[sidx * 2 * NB + j], c);
     }
-    for (int q = tid; q < NB * 4; q += blockDim.x) {
-        const int b = q / 4, f = q % 4;
-        const int j = (dd * NB + b) * 4 + f;
-        if (cnt[dd][b]) {
-            atomicMin(&ws.st_key[sidx * 2 * NB * 4 + j], key[dd][b][f]);
-            if (zp[dd][b][f] != INT32_MAX) atomicMin(&ws.st_zp[sidx * 2 * NB * 4 + j], zp[dd][b][f]);
+    for (int j = tid; j < 2 * NB * 4; j += blockDim.x) {
+        int d = j / (NB * 4), b = (j / 4) % NB, f = j % 4;
+        if (cnt[d][b]) {
+            atomicMin(&ws.st_key[sidx * 2 * NB * 4 + j], key[d][b][f]);
+            if (zp[d][b][f] != INT32_MAX) atomicMin(&ws.st_zp[sidx * 2 * NB * 4 + j], zp[d][b][f]);
         }
     }
     }
@@ -581,11 +573,7 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(WS ws, int parity, int 
 
 // One warp per record of the current level: the upstream split decision for
 // pending nodes, children records, bucket bases and tile prefixes.
-// PASS 0 decides every pending node along its stored dimension; a node whose
-// cells all fall in one bucket has its stored dim flipped (creation.py:345-358)
-// and becomes K_RETRY.  PASS 1 decides the K_RETRY nodes along the flipped
-// dim once k_stats<PASS 1> has gathered it: a split, or else a leaf.
-template <bool LOOP, int PASS>
+template <bool LOOP>
 __global__ void k_decide(WS ws, int NB, long long cpl) {
     __shared__ int s_cnt[4][2][NBMAX];
     __shared__ double s_Rmin[4][2][NBMAX];
@@ -599,13 +587,12 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
     for (int r = lb + blockIdx.x * 4 + w; r < le; r += step) {
     __syncwarp();
     ARec* R = &ws.recs[r];
-    if (R->kind != (PASS == 0 ? K_PENDING : K_RETRY)) continue;
+    if (R->kind != K_PENDING) continue;
     int parity = R->parity;
     size_t sidx = (size_t)(r - lb);
     int size = R->size, ptr = R->ptr;
-    const int d0 = R->dim;  // the dimension gathered for this pass
-    // resolve per-bucket bounds of that dimension
-    for (int j = d0 * NB + lane; j < (d0 + 1) * NB; j += 32) {
+    // resolve per-bucket bounds of both dimensions
+    for (int j = lane; j < 2 * NB; j += 32) {
         int d = j / NB, b = j % NB;
         int c = (int)ws.st_cnt[sidx * 2 * NB + j];
         s_cnt[w][d][b] = c;
@@ -620,6 +607,7 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
         s_Lmax[w][d][b] = lmax;
     }
     __syncwarp();
+    int d0 = R->dim;
     int stored_dim = d0;
     int ds = -1;
     Decision D;
@@ -628,30 +616,28 @@ __global__ void k_decide(WS ws, int NB, long long cpl) {
     if ((long long)size <= cpl) {
         D.kind = 2;  // leaf (creation.py:267)
     } else {
-        const int d = d0;
-        int tot = 0;
-        for (int b = 0; b < NB; b++) tot += s_cnt[w][d][b];
-        if (tot != size) {
-            bad = true;
-        } else {
+        for (int attempt = 0; attempt < 2; attempt++) {
+            int d = attempt == 0 ? d0 : 1 - d0;
+            int tot = 0;
+            for (int b = 0; b < NB; b++) tot += s_cnt[w][d][b];
+            if (tot != size) {
+                bad = true;
+                break;
+            }
             double Rd = R->bnd[2 * d], Ld = R->bnd[2 * d + 1];
             double bl = bucket_len(Ld, Rd, NB);
             D = warp_decide(s_cnt[w][d], s_Rmin[w][d], s_Lmax[w][d], NB, size, Rd, Ld, bl);
             if (D.kind == 1) {
                 ds = d;
-            } else if (D.kind < 0) {
-                bad = true;
-            } else if (PASS == 0) {
-                // all cells in one bucket: flip the stored dim and decide
-                // again along it (PASS 1) once its statistics are gathered
-                if (lane == 0) {
-                    R->dim = 1 - d0;
-                    R->kind = K_RETRY;
-                }
-                continue;
-            } else {
-                D.kind = 2;  // all in one bucket along both: a leaf with the flipped dim
+                break;
             }
+            if (D.kind < 0) {
+                bad = true;
+                break;
+            }
+            // all cells in one bucket: flip the stored dim once, then give up
+            if (attempt == 0) stored_dim = 1 - d0;
+            else D.kind = 2;
         }
     }
     if (bad) {
@@ -1510,11 +1496,8 @@ static int build_levels(WS& ws, cudaStream_t st, int NB, int64_t cpl, bool run_p
             if (hc.err & 0x80000000u) return ct_fail(CT_ERR_WORKSPACE, "builder tile capacity exceeded");
             int ntiles = hc.tile_count;
             if (ntiles == 0) break;
-            k_stats<false, 0><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
-            k_decide<false, 0><<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
-            // nodes whose cells all fell in one bucket: the other dimension
-            k_stats<false, 1><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
-            k_decide<false, 1><<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
+            k_stats<false><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_decide<false><<<(width + 3) / 4, 128, 0, st>>>(ws, NB, (long long)cpl);
             k_scatter<false><<<ntiles, STATS_THREADS, 0, st>>>(ws, parity, NB);
             CT_CHECK_LAUNCH("phase A level");
             CT_CUDA(cudaMemcpyAsync(&hc, ws.cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st));
@@ -1741,10 +1724,8 @@ int ct_build_forest_async(const double* bb, int64_t n_total, const int64_t* tree
             const int parity = L & 1;
             k_level_start<<<1, 32, 0, st>>>(ws);
             k_make_tiles<<<G, 128, 0, st>>>(ws, NB);
-            k_stats<true, 0><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
-            k_decide<true, 0><<<G, 128, 0, st>>>(ws, NB, (long long)cpl);
-            k_stats<true, 1><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
-            k_decide<true, 1><<<G, 128, 0, st>>>(ws, NB, (long long)cpl);
+            k_stats<true><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
+            k_decide<true><<<G, 128, 0, st>>>(ws, NB, (long long)cpl);
             k_scatter<true><<<G, STATS_THREADS, 0, st>>>(ws, parity, NB);
             k_level_next<<<1, 32, 0, st>>>(ws, L);
         }
