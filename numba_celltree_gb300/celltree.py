@@ -10,7 +10,7 @@ import numpy as np
 
 from . import _device, _pipeline, _lib
 from .cast import cast_bboxes, cast_edges, cast_faces, cast_vertices, is_cuda_tensor
-from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, validate_elements
+from .celltree_base import CellTree2dBase, _GpuTree, _validate_params, prebuilt_from_nodes, validate_elements
 
 
 def _as_output(t, like_cuda: bool):
@@ -109,42 +109,18 @@ class CellTree2d(CellTree2dBase):
         torch = _device.torch()
         vertices = cast_vertices(vertices, copy=True)
         faces = np.ascontiguousarray(faces, dtype=np.int64)
-        nodes = np.asarray(nodes)
-        bb_indices = np.ascontiguousarray(bb_indices, dtype=np.int64)
         if faces.ndim != 2 or faces.shape[0] == 0 or faces.shape[1] < 3:
             raise ValueError("faces must have shape (n_face >= 1, n_max_vert >= 3)")
-        for name in ("child", "Lmax", "Rmin", "ptr", "size", "dim"):
-            if nodes.dtype.names is None or name not in nodes.dtype.names:
-                raise ValueError(f"nodes must be a NodeDType array (missing {name})")
         n = faces.shape[0]
-        if bb_indices.shape != (n,) or not np.array_equal(np.sort(bb_indices), np.arange(n)):
-            raise ValueError("bb_indices must be a permutation of the face indices")
-        nn = nodes.shape[0]
-        child = np.ascontiguousarray(nodes["child"], dtype=np.int64)
-        # depth of every node (children are numbered after their parent)
-        internal = child >= 0
-        if np.any(child[internal] <= np.nonzero(internal)[0]) or np.any(child[internal] + 1 >= nn):
-            raise ValueError("nodes: children must follow their parent and lie inside the array")
-        depth = np.zeros(nn, dtype=np.int64)
-        frontier, level = np.array([0], dtype=np.int64), 0
-        while frontier.size and level <= nn:
-            c = child[frontier]
-            c = c[c >= 0]
-            frontier = np.concatenate([c, c + 1])
-            level += 1
-            depth[frontier] = level
         v_d = _device.to_device(vertices, torch.float64, device)
         f_d = _device.to_device(faces, torch.int64, device)
         validate_elements(f_d, int(v_d.shape[0]), 3, "faces")
+        pre = prebuilt_from_nodes(nodes, bb_indices, n, device)
         lib = _lib.load()
         st = _device.stream()
         K = int(f_d.shape[1])
         bb = _device.empty((n, 4), torch.float64, device)
         _lib.check(lib.ct_face_bboxes(_device.ptr(v_d), _device.ptr(f_d), n, K, _device.ptr(bb), st), "face_bboxes")
-        dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), device=device).to(dt)
-        pre = (dev(child, torch.int64), dev(nodes["Lmax"], torch.float64), dev(nodes["Rmin"], torch.float64),
-               dev(nodes["ptr"], torch.int64), dev(nodes["size"], torch.int64),
-               dev(nodes["dim"].astype(np.uint8), torch.uint8), dev(bb_indices, torch.int64), int(depth.max()))
         tree = cls.__new__(cls)
         tree._tree = _GpuTree(device, f_d, v_d, bb, n_buckets, cells_per_leaf, prebuilt=pre)
         tree._host = {}

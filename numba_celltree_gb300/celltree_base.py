@@ -712,6 +712,40 @@ def validate_elements(elements, n_vertices: int, min_len: int, what: str) -> Non
         raise ValueError(f"{what} contain indices outside [0, n_vertices)")
 
 
+def prebuilt_from_nodes(nodes, bb_indices, n: int, device):
+    """Device copies of upstream ``nodes`` (NodeDType) and ``bb_indices`` of a
+    tree of n elements, checked for the structure the queries rely on
+    (children after their parent and inside the array, bb_indices a
+    permutation), plus the tree's depth: the ``prebuilt`` argument of
+    _GpuTree."""
+    torch = _device.torch()
+    nodes = np.asarray(nodes)
+    bb_indices = np.ascontiguousarray(bb_indices, dtype=np.int64)
+    for name in ("child", "Lmax", "Rmin", "ptr", "size", "dim"):
+        if nodes.dtype.names is None or name not in nodes.dtype.names:
+            raise ValueError(f"nodes must be a NodeDType array (missing {name})")
+    if bb_indices.shape != (n,) or not np.array_equal(np.sort(bb_indices), np.arange(n)):
+        raise ValueError("bb_indices must be a permutation of the element indices")
+    nn = nodes.shape[0]
+    child = np.ascontiguousarray(nodes["child"], dtype=np.int64)
+    # depth of every node (children are numbered after their parent)
+    internal = child >= 0
+    if np.any(child[internal] <= np.nonzero(internal)[0]) or np.any(child[internal] + 1 >= nn):
+        raise ValueError("nodes: children must follow their parent and lie inside the array")
+    depth = np.zeros(nn, dtype=np.int64)
+    frontier, level = np.array([0], dtype=np.int64), 0
+    while frontier.size and level <= nn:
+        c = child[frontier]
+        c = c[c >= 0]
+        frontier = np.concatenate([c, c + 1])
+        level += 1
+        depth[frontier] = level
+    dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a), device=device).to(dt)
+    return (dev(child, torch.int64), dev(nodes["Lmax"], torch.float64), dev(nodes["Rmin"], torch.float64),
+            dev(nodes["ptr"], torch.int64), dev(nodes["size"], torch.int64),
+            dev(nodes["dim"].astype(np.uint8), torch.uint8), dev(bb_indices, torch.int64), int(depth.max()))
+
+
 def _validate_params(n_buckets: int, cells_per_leaf: int) -> None:
     if n_buckets < 2:
         raise ValueError("n_buckets must be >= 2")

@@ -240,3 +240,35 @@ def test_pair_areas_on_degenerate_polygons_match_oracle(oracle):
         assert np.array_equal(got.cpu().numpy(), exp, equal_nan=True), grid
         assert int(err.item()) == 0
     del ctypes
+
+
+@pytest.mark.gpu
+def test_edge_tree_save_load_roundtrip(tmp_path, oracle):
+    """EdgeCellTree2d.save / load / from_celltree_data: same nodes, same
+    answers, no rebuild."""
+    from numba_celltree_gb300 import EdgeCellTree2d
+
+    rng = np.random.default_rng(31)
+    xy = rng.uniform(0.0, 50.0, (400, 2))
+    edges = rng.integers(0, 400, (900, 2))
+    edges = edges[edges[:, 0] != edges[:, 1]]
+    g = EdgeCellTree2d(xy, edges, n_buckets=5, cells_per_leaf=3)
+    path = tmp_path / "edges.npz"
+    g.save(path)
+    h = EdgeCellTree2d.load(path)
+    assert h.nodes.tobytes() == g.nodes.tobytes()
+    assert np.array_equal(h.bb_indices, g.bb_indices)
+    assert (h.n_buckets, h.cells_per_leaf) == (5, 3)
+    pts = np.concatenate([rng.uniform(0.0, 50.0, (5000, 2)), xy[edges[:300, 0]]])
+    segs = np.stack([rng.uniform(0.0, 50.0, (500, 2)), rng.uniform(0.0, 50.0, (500, 2))], 1)
+    assert np.array_equal(h.locate_points(pts), g.locate_points(pts))
+    for a, b in zip(h.intersect_edges(segs), g.intersect_edges(segs)):
+        assert np.array_equal(a, b, equal_nan=True)
+    o = oracle.OracleEdgeCellTree2d(xy, edges)
+    k = EdgeCellTree2d.from_celltree_data(o.celltree_data)
+    assert k.nodes.tobytes() == o.nodes.tobytes()
+    assert np.array_equal(k.locate_points(pts), o.locate_points(pts))
+    with pytest.raises(ValueError):
+        from numba_celltree_gb300 import CellTree2d
+
+        CellTree2d.load(path)  # not a face tree
