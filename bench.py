@@ -511,11 +511,13 @@ def query_suite(args, c5=None, verbose=False):
     # (segment, cell) pairs for 1M segments (chunked-output mode, not timed here)
     segment_row("C2", tree, ot, segments(np.random.default_rng(3), 0.0, 1000.0, 1_000_000, 20.0), 20_000)
     # the literal C2 shape, uniform endpoints over the whole domain: every
-    # cell of a segment's bounding box is a candidate (about 1e5 to 1e6 per
-    # segment, for upstream's traversal as for this one), so 1M of them
-    # cannot finish in a bench; a 200-segment sample against 20 on the oracle
-    ue = np.random.default_rng(8).uniform(0.0, 1000.0, (200, 2, 2))
-    segment_row("C2", tree, ot, ue, 20, reps=1, query="intersect_edges_uniform_endpoints_sample")
+    # cell of a segment's bounding box is a candidate (about 5e5 per segment
+    # on average, for upstream's traversal as for this one; each segment's
+    # traversal is split across threads here), so 1M of them (~5e11
+    # candidates, ~1.5e9 results) do not fit a bench; a 2000-segment sample
+    # against 20 on the oracle
+    ue = np.random.default_rng(8).uniform(0.0, 1000.0, (2000, 2, 2))
+    segment_row("C2", tree, ot, ue, 20, reps=3, query="intersect_edges_uniform_endpoints_sample")
     del tree, ot
     # ---- C4: tree of 500k quads (rotated 7 degrees, offset 0.37 cell); 1M query triangles; 1M points
     txy, tf = syn.quad_mesh(1000, 500, seed=4, extent=(100.0, 50.0), offset=(0.037, 0.037), rotate_deg=7.0)

@@ -488,6 +488,30 @@ int ct_count_edge_candidates(const ct_tree* tree, int32_t mode, const double* se
                               int64_t* counts, void* stream);
 int ct_write_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
                               const int64_t* offsets, int32_t* cand_seg, int32_t* cand_pos, void* stream);
+/* The same candidates with each segment's traversal split across threads
+ * (no upstream counterpart; a long segment's traversal otherwise runs on one
+ * thread).  ct_count/write_edge_items cut every segment's traversal `cut`
+ * levels below the root: the nodes at that depth (and the leaves above it)
+ * it reaches, in traversal order, as work items (segment, node), segment-
+ * major at the scanned per-segment offsets.  ct_count/write_item_candidates
+ * run the traversal from each item's node: concatenated in item order the
+ * candidates are ct_write_edge_candidates' (same pairs, same order).
+ * ct_segment_candidate_ranges turns the items' candidate offsets / counts
+ * into each segment's (for ct_compact_edge_hits).  Trees deeper than the
+ * stacked traversal allows (max_depth + 2 > 128) are refused (CT_ERR_ARG):
+ * they take the uncut entry points. */
+int ct_count_edge_items(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                        int32_t cut, int64_t* counts, void* stream);
+int ct_write_edge_items(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                        int32_t cut, const int64_t* offsets, int32_t* item_seg, int32_t* item_node, void* stream);
+int ct_count_item_candidates(const ct_tree* tree, int32_t mode, const double* segs, const int32_t* item_seg,
+                             const int32_t* item_node, int64_t n_items, int64_t* counts, void* stream);
+int ct_write_item_candidates(const ct_tree* tree, int32_t mode, const double* segs, const int32_t* item_seg,
+                             const int32_t* item_node, int64_t n_items, const int64_t* offsets, int32_t* cand_seg,
+                             int32_t* cand_pos, void* stream);
+int ct_segment_candidate_ranges(const int64_t* item_off, const int64_t* item_cnt, int64_t n,
+                                const int64_t* item_cand_off, const int64_t* item_cand_cnt, int64_t n_items,
+                                int64_t* cand_off, int64_t* cand_cnt, void* stream);
 int ct_test_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, const int32_t* cand_seg,
                             const int32_t* cand_pos, int64_t n_cand, int64_t* keep, double* xy, void* stream);
 int ct_compact_edge_hits(const ct_tree* tree, const int64_t* keep, const int64_t* pos, int64_t n_cand,

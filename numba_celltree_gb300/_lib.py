@@ -204,6 +204,11 @@ SIGNATURES = {
     "ct_work_order_workspace_size": (_SZ, [_I64]),
     "ct_count_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P]),
     "ct_write_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "ct_count_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P]),
+    "ct_write_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P, _P, _P]),
+    "ct_count_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P]),
+    "ct_write_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P, _P, _P]),
+    "ct_segment_candidate_ranges": (ctypes.c_int, [_P, _P, _I64, _P, _P, _I64, _P, _P, _P]),
     "ct_test_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P, _P]),
     "ct_compact_edge_hits": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _P, _I64, _P, _P, _P, _P, _P, _I64, _P, _P,
                                             _P, _P, _P, _P]),

@@ -475,14 +475,58 @@ class _GpuTree:
     def count_edge_candidates(self, segs_d, mode: int):
         """Candidate cells of every segment (device int64): an upper bound of
         its results."""
-        torch = _device.torch()
         n = int(segs_d.shape[0])
-        counts = _device.empty((n,), torch.int64, self.device)
         if mode == 1:
             self.ensure_box_index()
-        _lib.check(_lib.load().ct_count_edge_candidates(ctypes.byref(self.desc), mode, _device.ptr(segs_d), n, None,
-                                                        _device.ptr(counts), _device.stream()), "count_edges")
-        return counts
+        cfg = self.cached("segments", n)
+        self._apply("segments", cfg)
+        _, ccnt, _, _ = self.edge_candidate_ranges(segs_d, mode, None, self.edge_cut(cfg))
+        return ccnt
+
+    # cells under a work item of the split segment traversal (the default)
+    SPLIT_CELLS = 1024
+
+    def edge_cut(self, cfg: dict):
+        """Depth at which segment traversals are cut into work items (about
+        cfg["split"] cells under each), or None for the uncut traversal (no
+        split asked, a tree too small to split or too deep for the stacked
+        traversal)."""
+        split = int(cfg.get("split", self.SPLIT_CELLS) or 0)
+        if split <= 0 or self.n <= split or self.max_depth + 2 > self.BATCHED_MAX_STACK:
+            return None
+        return max(1, min(self.max_depth, int(np.ceil(np.log2(self.n / split)))))
+
+    def edge_candidate_ranges(self, segs_d, mode: int, order, cut):
+        """Every segment's candidate offset and count (device int64) and the
+        candidate total; with a cut, also the work items the writing pass
+        uses: (coff, ccnt, total, items)."""
+        torch = _device.torch()
+        lib = _lib.load()
+        st = _device.stream()
+        P = _device.ptr
+        n = int(segs_d.shape[0])
+        d = ctypes.byref(self.desc)
+        if cut is None:
+            ccnt = _device.empty((n,), torch.int64, self.device)
+            _lib.check(lib.ct_count_edge_candidates(d, mode, P(segs_d), n, P(order), P(ccnt), st), "intersect_edges")
+            coff, nc = self.scan(ccnt)
+            return coff, ccnt, nc, None
+        icnt = _device.empty((n,), torch.int64, self.device)
+        _lib.check(lib.ct_count_edge_items(d, mode, P(segs_d), n, P(order), cut, P(icnt), st), "intersect_edges")
+        ioff, ni = self.scan(icnt)
+        iseg = _device.empty((max(ni, 1),), torch.int32, self.device)
+        inode = _device.empty((max(ni, 1),), torch.int32, self.device)
+        _lib.check(lib.ct_write_edge_items(d, mode, P(segs_d), n, P(order), cut, P(ioff), P(iseg), P(inode), st),
+                   "intersect_edges")
+        iccnt = _device.empty((max(ni, 1),), torch.int64, self.device)
+        _lib.check(lib.ct_count_item_candidates(d, mode, P(segs_d), P(iseg), P(inode), ni, P(iccnt), st),
+                   "intersect_edges")
+        icoff, nc = self.scan(iccnt[:ni]) if ni > 0 else (iccnt[:0], 0)
+        coff = _device.empty((n,), torch.int64, self.device)
+        ccnt = _device.empty((n,), torch.int64, self.device)
+        _lib.check(lib.ct_segment_candidate_ranges(P(ioff), P(icnt), n, P(icoff), P(iccnt), ni, P(coff), P(ccnt),
+                                                   st), "intersect_edges")
+        return coff, ccnt, nc, (iseg, inode, ni, icoff)
 
     @staticmethod
     def chunk_ranges(counts: np.ndarray, max_results: int):
@@ -557,23 +601,26 @@ class _GpuTree:
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
-        ccnt = _device.empty((n,), torch.int64, self.device)
         self.reset_error()
         if mode == 1:
             self.ensure_box_index()
         self._apply("segments", config)
         order = self.work_order(segs_d, 1, config.get("work_order"))
         P = _device.ptr
-        _lib.check(lib.ct_count_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(ccnt), st),
-                   "intersect_edges")
-        coff, nc = self.scan(ccnt)
+        coff, ccnt, nc, items = self.edge_candidate_ranges(segs_d, mode, order, self.edge_cut(config))
         if budget is not None and nc > budget:
             self.last_counts = ccnt
             return None
         cseg = _device.empty((max(nc, 1),), torch.int32, self.device)
         cpos = _device.empty((max(nc, 1),), torch.int32, self.device)
-        _lib.check(lib.ct_write_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(coff),
-                                                P(cseg), P(cpos), st), "intersect_edges")
+        if items is None:
+            _lib.check(lib.ct_write_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(coff),
+                                                    P(cseg), P(cpos), st), "intersect_edges")
+        else:
+            iseg, inode, ni, icoff = items
+            _lib.check(lib.ct_write_item_candidates(ctypes.byref(self.desc), mode, P(segs_d), P(iseg), P(inode), ni,
+                                                    P(icoff), P(cseg), P(cpos), st), "intersect_edges")
+            del items, iseg, inode, icoff
         keep = _device.empty((max(nc, 1),), torch.int64, self.device)
         xy_c = _device.empty((max(nc, 1), 2, 2), torch.float64, self.device)
         _lib.check(lib.ct_test_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), P(cseg), P(cpos), nc,

@@ -255,6 +255,158 @@ __device__ __forceinline__ int cs_code_keys(unsigned long long kx, unsigned long
     return p;
 }
 
+// Segment a -> b against the cells of leaf `v` (nf q): the candidates that
+// Cohen-Sutherland's shared-outcode test does not reject (mode 1), or every
+// cell (mode 0), counted and, with WRITE, written at cseg / cj[base + count].
+template <bool WRITE, int MODE>
+__device__ __forceinline__ void edge_leaf(const TreeQ& T, float4 q, dpt a, dpt b, bool keys, unsigned long long kax,
+                                          unsigned long long kay, unsigned long long kbx, unsigned long long kby,
+                                          int64_t i, int64_t base, int64_t& count, int* __restrict__ cseg,
+                                          int* __restrict__ cj) {
+    int ptr = na(q), bq = nb(q);
+    for (int j = ptr; j < ptr + bq; j++) {
+        bool cand = true;
+        if (MODE == 1) {
+            dbox bx = leaf_box(T, j);
+            int k1, k2;
+            if (keys) {
+                unsigned long long x0 = fkey(bx.xmin), x1 = fkey(bx.xmax), y0 = fkey(bx.ymin), y1 = fkey(bx.ymax);
+                k1 = cs_code_keys(kax, kay, x0, x1, y0, y1);
+                k2 = cs_code_keys(kbx, kby, x0, x1, y0, y1);
+            } else {
+                k1 = cs_code(a, bx);
+                k2 = cs_code(b, bx);
+            }
+            cand = (k1 & k2) == 0;
+        }
+        if (cand) {
+            if (WRITE) {
+                cseg[base + count] = (int)i;
+                cj[base + count] = j;
+            }
+            count++;
+        }
+    }
+}
+
+// Children of internal node v the segment's traversal enters (locate_edge
+// query.py:410-441): `first` is visited first (the right child when both).
+__device__ __forceinline__ void edge_children(const TreeQ& T, int v, float4 q, dpt a, dpt b, dpt V, bool keys,
+                                              unsigned long long kax, unsigned long long kay,
+                                              unsigned long long kbx, unsigned long long kby, int* first,
+                                              int* second) {
+    int dim = -1 - nb(q);
+    double2 nd = T.nd[v];
+    double dx = dim ? V.y : V.x;
+    bool left, right;
+    if (keys) {
+        unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
+        bool pos = dx > 0.0;
+        left = fkey(nd.x) >= (pos ? ka : kb);
+        right = fkey(nd.y) <= (pos ? kb : ka);
+    } else {
+        double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
+        double dx_left, dx_right;
+        if (dx > 0.0) {
+            dx_left = nd.x - an;
+            dx_right = nd.y - bn;
+        } else {
+            dx_left = nd.x - bn;
+            dx_right = nd.y - an;
+        }
+        left = dx_left >= 0.0;
+        right = dx_right <= 0.0;
+        if (dx > 0.0) {
+            if (left) left = (dx_left / dx) >= 0.0;
+            if (right) right = (dx_right / dx) <= 1.0;
+        } else if (dx < 0.0) {
+            if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
+            if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
+        }
+    }
+    // pushed left, then right: the right child is visited first
+    int child = na(q);
+    *first = right ? child + 1 : (left ? child : -1);
+    *second = (left && right) ? child : -1;
+}
+
+struct EdgeKeys {
+    bool keys;
+    unsigned long long kax, kay, kbx, kby;
+};
+
+__device__ __forceinline__ EdgeKeys edge_keys(const TreeQ& T, dpt a, dpt b) {
+    dpt V = vsub(b, a);
+    EdgeKeys k;
+    k.keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) && is_fin(V.y);
+    k.kax = fkey(a.x);
+    k.kay = fkey(a.y);
+    k.kbx = fkey(b.x);
+    k.kby = fkey(b.y);
+    return k;
+}
+
+// Depth-first traversal of segment i from node `start` (stack form).  With
+// CUT the walk stops at the nodes `cut` levels below the start (and at
+// leaves above them) and, instead of their candidates, counts / writes those
+// nodes (item_seg / item_node): the cut splits one segment's traversal into
+// subtrees whose candidate lists, concatenated in this order, are the
+// traversal's.
+template <bool WRITE, int MODE, bool CUT>
+__device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_t i, int start, int cut,
+                                            int64_t base, int* __restrict__ cseg, int* __restrict__ cj) {
+    const dpt V = vsub(b, a);
+    const EdgeKeys K = edge_keys(T, a, b);
+    int st[STK];
+    unsigned char sd[CUT ? STK : 1];
+    int sp = 1;
+    st[0] = start;
+    sd[0] = 0;
+    int64_t count = 0;
+    int64_t budget = T.n_nodes;
+    while (sp > 0) {
+        if (--budget < 0) {
+            set_error(T.err, CT_DEVERR_LOOP);
+            break;
+        }
+        --sp;
+        const int v = st[sp];
+        const int depth = CUT ? sd[sp] : 0;
+        float4 q = T.nf[v];
+        const bool terminal = nb(q) >= 0;
+        if (CUT && (terminal || depth >= cut)) {
+            if (WRITE) {
+                cseg[base + count] = (int)i;
+                cj[base + count] = v;
+            }
+            count++;
+            continue;
+        }
+        if (terminal) {
+            edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj);
+            continue;
+        }
+        int first, second;
+        edge_children(T, v, q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
+        if (sp + 2 > STK) {
+            set_error(T.err, CT_DEVERR_STACK);
+            break;
+        }
+        const unsigned char nd1 = (unsigned char)min(depth + 1, 255);
+        if (second >= 0) {
+            st[sp] = second;
+            if (CUT) sd[sp] = nd1;
+            sp++;
+        }
+        if (first >= 0) {
+            st[sp] = first;
+            if (CUT) sd[sp] = nd1;
+            sp++;
+        }
+    }
+    return count;
+}
+
 template <bool WRITE, int MODE, bool DEEP>
 __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __restrict__ segs, int64_t n,
                                                     const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
@@ -270,90 +422,27 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
     int r = cohen_sutherland(a, b, T.bbox, &c, &d);
     if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
     if (r == 1) {
-        dpt V = vsub(b, a);
-        const bool keys = T.finite && is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y) && is_fin(V.x) &&
-                          is_fin(V.y);
-        const unsigned long long kax = fkey(a.x), kay = fkey(a.y), kbx = fkey(b.x), kby = fkey(b.y);
-        // depth-first walk: a stack, or (DEEP) the parent links (see k_boxes)
-        int st[DEEP ? 1 : STK];
-        int sp = 1;
-        st[0] = 0;
-        int dv = 0, from = -1;
-        bool down = true;
-        int64_t budget = DEEP ? 2 * T.n_nodes + 2 : T.n_nodes;
-        while (DEEP ? dv >= 0 : sp > 0) {
-            if (--budget < 0) {
-                set_error(T.err, CT_DEVERR_LOOP);
-                break;
-            }
-            const int v = DEEP ? dv : st[--sp];
-            float4 q = T.nf[v];
-            int bq = nb(q);
-            int first = -1, second = -1;
-            const bool terminal = bq >= 0;
-            if (terminal && (!DEEP || down)) {
-                int ptr = na(q);
-                for (int j = ptr; j < ptr + bq; j++) {
-                    bool cand = true;
-                    if (MODE == 1) {
-                        dbox bx = leaf_box(T, j);
-                        int k1, k2;
-                        if (keys) {
-                            unsigned long long x0 = fkey(bx.xmin), x1 = fkey(bx.xmax), y0 = fkey(bx.ymin),
-                                               y1 = fkey(bx.ymax);
-                            k1 = cs_code_keys(kax, kay, x0, x1, y0, y1);
-                            k2 = cs_code_keys(kbx, kby, x0, x1, y0, y1);
-                        } else {
-                            k1 = cs_code(a, bx);
-                            k2 = cs_code(b, bx);
-                        }
-                        cand = (k1 & k2) == 0;
-                    }
-                    if (cand) {
-                        if (WRITE) {
-                            cseg[base + count] = (int)i;
-                            cj[base + count] = j;
-                        }
-                        count++;
-                    }
+        if (!DEEP) {
+            count = edge_dfs<WRITE, MODE, false>(T, a, b, i, 0, -1, base, cseg, cj);
+        } else {
+            // depth-first walk through the parent links (see k_boxes)
+            const dpt V = vsub(b, a);
+            const EdgeKeys K = edge_keys(T, a, b);
+            int dv = 0, from = -1;
+            bool down = true;
+            int64_t budget = 2 * T.n_nodes + 2;
+            while (dv >= 0) {
+                if (--budget < 0) {
+                    set_error(T.err, CT_DEVERR_LOOP);
+                    break;
                 }
-            }
-            if (!terminal) {
-                int dim = -1 - bq;
-                double2 nd = T.nd[v];
-                double dx = dim ? V.y : V.x;
-                bool left, right;
-                if (keys) {
-                    unsigned long long ka = dim ? kay : kax, kb = dim ? kby : kbx;
-                    bool pos = dx > 0.0;
-                    left = fkey(nd.x) >= (pos ? ka : kb);
-                    right = fkey(nd.y) <= (pos ? kb : ka);
-                } else {
-                    double an = dim ? a.y : a.x, bn = dim ? b.y : b.x;
-                    double dx_left, dx_right;
-                    if (dx > 0.0) {
-                        dx_left = nd.x - an;
-                        dx_right = nd.y - bn;
-                    } else {
-                        dx_left = nd.x - bn;
-                        dx_right = nd.y - an;
-                    }
-                    left = dx_left >= 0.0;
-                    right = dx_right <= 0.0;
-                    if (dx > 0.0) {
-                        if (left) left = (dx_left / dx) >= 0.0;
-                        if (right) right = (dx_right / dx) <= 1.0;
-                    } else if (dx < 0.0) {
-                        if (left) left = (1.0 - (dx_left / dx)) >= 0.0;
-                        if (right) right = (1.0 - (dx_right / dx)) <= 1.0;
-                    }
-                }
-                // pushed left, then right: the right child is visited first
-                int child = na(q);
-                first = right ? child + 1 : (left ? child : -1);
-                second = (left && right) ? child : -1;
-            }
-            if (DEEP) {
+                const int v = dv;
+                float4 q = T.nf[v];
+                int first = -1, second = -1;
+                const bool terminal = nb(q) >= 0;
+                if (terminal && down)
+                    edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj);
+                if (!terminal) edge_children(T, v, q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
                 int next = terminal ? -1 : (down ? first : ((from == first) ? second : -1));
                 from = dv;
                 if (next >= 0) {
@@ -363,17 +452,65 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
                     dv = T.parent[dv];
                     down = false;
                 }
-            } else if (!terminal) {
-                if (sp + 2 > STK) {
-                    set_error(T.err, CT_DEVERR_STACK);
-                    break;
-                }
-                if (second >= 0) st[sp++] = second;
-                if (first >= 0) st[sp++] = first;
             }
         }
     }
     if (!WRITE) cnt_or_off[i] = count;
+}
+
+// The traversal of every segment cut `cut` levels below the root into work
+// items (segment, node) in traversal order: counts per segment (WRITE
+// false), then the items at their offsets.  Segments that miss the tree's
+// bbox (Cohen-Sutherland, as the uncut traversal) have none.
+template <bool WRITE, int MODE>
+__global__ void __launch_bounds__(128) k_edge_items(TreeQ T, const double4* __restrict__ segs, int64_t n,
+                                                    const int* __restrict__ order, int cut,
+                                                    int64_t* __restrict__ cnt_or_off, int* __restrict__ item_seg,
+                                                    int* __restrict__ item_node) {
+    int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tq >= n) return;
+    int64_t i = order ? (int64_t)order[tq] : tq;
+    double4 s4 = segs[i];
+    dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+    int64_t count = 0;
+    dpt c, d;
+    int r = cohen_sutherland(a, b, T.bbox, &c, &d);
+    if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
+    if (r == 1)
+        count = edge_dfs<WRITE, MODE, true>(T, a, b, i, 0, cut, WRITE ? cnt_or_off[i] : 0, item_seg, item_node);
+    if (!WRITE) cnt_or_off[i] = count;
+}
+
+// The candidates of every work item (the uncut traversal from the item's
+// node): counts per item, then the candidates at the items' offsets.
+template <bool WRITE, int MODE>
+__global__ void __launch_bounds__(128) k_item_cands(TreeQ T, const double4* __restrict__ segs,
+                                                    const int* __restrict__ item_seg,
+                                                    const int* __restrict__ item_node, int64_t n_items,
+                                                    int64_t* __restrict__ cnt_or_off, int* __restrict__ cseg,
+                                                    int* __restrict__ cj) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_items) return;
+    const int64_t i = item_seg[k];
+    double4 s4 = segs[i];
+    dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+    int64_t count = edge_dfs<WRITE, MODE, false>(T, a, b, i, item_node[k], -1, WRITE ? cnt_or_off[k] : 0, cseg, cj);
+    if (!WRITE) cnt_or_off[k] = count;
+}
+
+// Per segment: the offset and count of its candidates, from its items'
+// (items are segment-major; a segment's items are [ioff[s], ioff[s] + icnt[s])).
+__global__ void k_seg_from_items(const int64_t* __restrict__ ioff, const int64_t* __restrict__ icnt, int64_t n,
+                                 const int64_t* __restrict__ item_coff, const int64_t* __restrict__ item_ccnt,
+                                 int64_t n_items, int64_t* __restrict__ coff, int64_t* __restrict__ ccnt) {
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k0 = ioff[s], k1 = k0 + icnt[s];
+        const int64_t total = n_items > 0 ? item_coff[n_items - 1] + item_ccnt[n_items - 1] : 0;
+        const int64_t c0 = k0 < n_items ? item_coff[k0] : total;
+        const int64_t c1 = k1 < n_items ? item_coff[k1] : total;
+        coff[s] = c0;
+        ccnt[s] = c1 - c0;
+    }
 }
 
 // Sign of the cross product (v - a) x s used by Cyrus-Beck's crossing walk
@@ -1517,6 +1654,98 @@ int ct_write_edge_candidates(const ct_tree* t, int32_t mode, const double* segs,
         else k_edge_cands<true, 1, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos);
     }
     CT_CHECK_LAUNCH("write_edge_candidates");
+    return CT_OK;
+}
+
+static int check_split(const ct_tree* t, int32_t mode, int32_t cut) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (mode != 0 && mode != 1) return ct_fail(CT_ERR_ARG, "mode must be 0 or 1");
+    if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
+    if (cut < 0 || cut > 64) return ct_fail(CT_ERR_ARG, "cut depth must be in [0, 64]");
+    if (deep_tree(t)) return ct_fail(CT_ERR_ARG, "tree too deep for the split traversal");
+    return CT_OK;
+}
+
+int ct_count_edge_items(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                        int32_t cut, int64_t* counts, void* stream) {
+    int s = check_split(t, mode, cut);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    const int et = seg_threads(t);
+    const unsigned g = grid_of(n, et);
+    const double4* S = (const double4*)segs;
+    if (mode == 0) k_edge_items<false, 0><<<g, et, 0, st>>>(T, S, n, order, cut, counts, 0, 0);
+    else k_edge_items<false, 1><<<g, et, 0, st>>>(T, S, n, order, cut, counts, 0, 0);
+    CT_CHECK_LAUNCH("count_edge_items");
+    return CT_OK;
+}
+
+int ct_write_edge_items(const ct_tree* t, int32_t mode, const double* segs, int64_t n, const int32_t* order,
+                        int32_t cut, const int64_t* offsets, int32_t* item_seg, int32_t* item_node, void* stream) {
+    int s = check_split(t, mode, cut);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (n > INT32_MAX) return ct_fail(CT_ERR_ARG, "at most 2^31 - 1 segments");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    const int et = seg_threads(t);
+    const unsigned g = grid_of(n, et);
+    const double4* S = (const double4*)segs;
+    int64_t* off = (int64_t*)offsets;
+    if (mode == 0) k_edge_items<true, 0><<<g, et, 0, st>>>(T, S, n, order, cut, off, item_seg, item_node);
+    else k_edge_items<true, 1><<<g, et, 0, st>>>(T, S, n, order, cut, off, item_seg, item_node);
+    CT_CHECK_LAUNCH("write_edge_items");
+    return CT_OK;
+}
+
+int ct_count_item_candidates(const ct_tree* t, int32_t mode, const double* segs, const int32_t* item_seg,
+                             const int32_t* item_node, int64_t n_items, int64_t* counts, void* stream) {
+    int s = check_split(t, mode, 0);
+    if (s) return s;
+    if (n_items == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    const int et = seg_threads(t);
+    const unsigned g = grid_of(n_items, et);
+    const double4* S = (const double4*)segs;
+    if (mode == 0) k_item_cands<false, 0><<<g, et, 0, st>>>(T, S, item_seg, item_node, n_items, counts, 0, 0);
+    else k_item_cands<false, 1><<<g, et, 0, st>>>(T, S, item_seg, item_node, n_items, counts, 0, 0);
+    CT_CHECK_LAUNCH("count_item_candidates");
+    return CT_OK;
+}
+
+int ct_write_item_candidates(const ct_tree* t, int32_t mode, const double* segs, const int32_t* item_seg,
+                             const int32_t* item_node, int64_t n_items, const int64_t* offsets, int32_t* cand_seg,
+                             int32_t* cand_pos, void* stream) {
+    int s = check_split(t, mode, 0);
+    if (s) return s;
+    if (n_items == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    const int et = seg_threads(t);
+    const unsigned g = grid_of(n_items, et);
+    const double4* S = (const double4*)segs;
+    int64_t* off = (int64_t*)offsets;
+    if (mode == 0)
+        k_item_cands<true, 0><<<g, et, 0, st>>>(T, S, item_seg, item_node, n_items, off, cand_seg, cand_pos);
+    else
+        k_item_cands<true, 1><<<g, et, 0, st>>>(T, S, item_seg, item_node, n_items, off, cand_seg, cand_pos);
+    CT_CHECK_LAUNCH("write_item_candidates");
+    return CT_OK;
+}
+
+int ct_segment_candidate_ranges(const int64_t* item_off, const int64_t* item_cnt, int64_t n,
+                                const int64_t* item_cand_off, const int64_t* item_cand_cnt, int64_t n_items,
+                                int64_t* cand_off, int64_t* cand_cnt, void* stream) {
+    if (n < 0 || n_items < 0) return ct_fail(CT_ERR_ARG, "negative count");
+    if (n == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_seg_from_items<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 32), 256, 0, st>>>(
+        item_off, item_cnt, n, item_cand_off, item_cand_cnt, n_items, cand_off, cand_cnt);
+    CT_CHECK_LAUNCH("segment_candidate_ranges");
     return CT_OK;
 }
 

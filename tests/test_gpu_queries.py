@@ -127,6 +127,57 @@ def test_edge_tree_matches_oracle(oracle):
             same(a, b)
 
 
+def test_split_segment_traversal_matches_uncut(oracle):
+    """Segment traversals cut into subtree work items (several item sizes,
+    down to a few cells, i.e. cuts near the leaves) give the uncut
+    traversal's candidates and results, and the oracle's: long and short
+    segments, segments missing the mesh, points, NaN and inf endpoints,
+    face trees (mode 1) and edge trees (mode 0)."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, EdgeCellTree2d
+
+    xy, f = syn.mixed_mesh(70, 60, seed=31, extent=(70.0, 60.0))
+    rng = np.random.default_rng(32)
+    a0 = rng.uniform((0.0, 0.0), (70.0, 60.0), (600, 2))
+    segs = np.concatenate([
+        syn.random_segments(300, (-5.0, -5.0), (75.0, 65.0), seed=33),  # long, some leaving the mesh
+        np.stack([a0, a0 + rng.uniform(-2, 2, (600, 2))], 1),  # short
+        np.array([[[80.0, 80.0], [90.0, 95.0]], [[10.5, 10.5], [10.5, 10.5]], [[0.0, 30.0], [70.0, 30.0]],
+                  [[np.nan, 1.0], [3.0, 4.0]], [[1.0, 1.0], [np.inf, 4.0]], [[35.0, -10.0], [35.0, 70.0]]]),
+    ])
+    g = CellTree2d(xy, f, -1)
+    o = oracle.OracleCellTree2d(xy, f, -1)
+    t = g._tree
+    sd = torch.as_tensor(segs, device="cuda")
+    base = t.locate_edges(sd, 1, {"threads": 128, "work_order": False, "split": 0})
+    exp = o.intersect_edges(segs)
+    for a, b in zip(base, exp):
+        same(a.cpu().numpy(), b)
+    counts0 = t.count_edge_candidates(sd, 1)
+    for split in (2, 7, 64, 1024):
+        cfg = {"threads": 128, "work_order": split == 7, "split": split}
+        assert t.edge_cut(cfg) is not None
+        got = t.locate_edges(sd, 1, cfg)
+        for a, b in zip(got, base):
+            assert torch.equal(a, b), split
+        _, ccnt, _, items = t.edge_candidate_ranges(sd, 1, None, t.edge_cut(cfg))
+        assert items is not None and torch.equal(ccnt, counts0), split
+    # edge tree (edge-edge mode)
+    e = np.unique(np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]]]), axis=1), axis=0)
+    e = e[(e >= 0).all(1)]
+    ge = EdgeCellTree2d(xy, e)
+    oe = oracle.OracleEdgeCellTree2d(xy, e)
+    te = ge._tree
+    base = te.locate_edges(sd, 0, {"threads": 128, "work_order": False, "split": 0})
+    for split in (3, 50):
+        got = te.locate_edges(sd, 0, {"threads": 64, "work_order": False, "split": split})
+        for a, b in zip(got, base):
+            assert torch.equal(a, b), split
+    for a, b in zip(ge.intersect_edges(segs), oe.intersect_edges(segs)):
+        same(a, b)
+
+
 def test_long_segments_sorted(oracle):
     """Segments crossing thousands of cells: the per-segment sort runs in
     global memory (more than 1024 results per segment)."""
