@@ -510,14 +510,27 @@ def query_suite(args, c5=None, verbose=False):
     # cells each); uniform endpoints over the whole domain give ~1.4e9
     # (segment, cell) pairs for 1M segments (chunked-output mode, not timed here)
     segment_row("C2", tree, ot, segments(np.random.default_rng(3), 0.0, 1000.0, 1_000_000, 20.0), 20_000)
-    # the literal C2 shape, uniform endpoints over the whole domain: every
-    # cell of a segment's bounding box is a candidate (about 5e5 per segment
-    # on average, for upstream's traversal as for this one; each segment's
-    # traversal is split across threads here), so 1M of them (~5e11
-    # candidates, ~1.5e9 results) do not fit a bench; a 2000-segment sample
-    # against 20 on the oracle
-    ue = np.random.default_rng(8).uniform(0.0, 1000.0, (2000, 2, 2))
-    segment_row("C2", tree, ot, ue, 20, reps=3, query="intersect_edges_uniform_endpoints_sample")
+    # the literal C2 shape, 1M segments with uniform endpoints over the whole
+    # domain: upstream tests every cell of a segment's bounding box (~5e5 per
+    # segment); ~1.6e9 results (77 GB), streamed in ranges of segments whose
+    # candidates fit the device (iter_intersect_edges, device outputs
+    # dropped after each range); the oracle's rate from 20 segments
+    ue = np.random.default_rng(8).uniform(0.0, 1000.0, (1_000_000, 2, 2))
+    ued = torch.as_tensor(ue, device=dev)
+
+    def stream_all():
+        first, total = None, 0
+        for ch in tree.iter_intersect_edges(ued):
+            first = ch if first is None else first
+            total += int(ch[0].shape[0])
+        return first, total
+
+    (first, total), tg = wall(stream_all, reps=1)
+    m = 20
+    ro, tc = cpu(lambda: ot.intersect_edges(ue[:m]))
+    record("C2", "intersect_edges_uniform_endpoints", len(ue), "segments", tg, m, tc,
+           same_multi(first_queries(host(first), m), ro), results=total, bytes_q=32, bytes_r=48)
+    del ued, first
     del tree, ot
     # ---- C4: tree of 500k quads (rotated 7 degrees, offset 0.37 cell); 1M query triangles; 1M points
     txy, tf = syn.quad_mesh(1000, 500, seed=4, extent=(100.0, 50.0), offset=(0.037, 0.037), rotate_deg=7.0)
@@ -561,8 +574,9 @@ def query_suite(args, c5=None, verbose=False):
 def query_profile(args):
     """Small fixed run of the multi-result query kernels for ncu captures (no
     timing, no oracle): the C2 mixed mesh at a quarter of its cells (build,
-    100k boxes intersected, 100k segments of length U(0, 20) m) and the C4
-    regridding pair at a quarter of its cells (intersect_faces)."""
+    100k boxes intersected, 100k segments of length U(0, 20) m), the C4
+    regridding pair at a quarter of its cells (intersect_faces), then 200
+    segments with uniform endpoints on the C2 quarter mesh."""
     import torch
 
     from numba_celltree_gb300 import CellTree2d
@@ -582,9 +596,12 @@ def query_profile(args):
     qxy, qf = syn.triangle_mesh(500, 250, seed=5, extent=(50.0, 25.0))
     t4 = CellTree2d(torch.as_tensor(txy, device=dev), torch.as_tensor(tf, device=dev), -1)
     r3 = t4.intersect_faces(torch.as_tensor(qxy, device=dev), torch.as_tensor(qf, device=dev), -1)
+    ue = np.random.default_rng(8).uniform(0.0, 500.0, (200, 2, 2))
+    r4 = tree.intersect_edges(torch.as_tensor(ue, device=dev))
     torch.cuda.synchronize()
     print(json.dumps({"profile": "queries", "cells": [len(f), len(tf)],
-                      "pairs": [int(r1[0].shape[0]), int(r2[0].shape[0]), int(r3[0].shape[0])]}))
+                      "pairs": [int(r1[0].shape[0]), int(r2[0].shape[0]), int(r3[0].shape[0]),
+                                int(r4[0].shape[0])]}))
 
 
 def run_queries(args):

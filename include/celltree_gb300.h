@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define CT_ABI_VERSION 2
+#define CT_ABI_VERSION 3
 
 typedef enum ct_status {
     CT_OK = 0,
@@ -125,6 +125,11 @@ typedef struct ct_tree {
      * then traversed without a stack, in the same order; without it such
      * trees are refused. */
     int32_t* node_parent;
+    /* device, optional part of the box index: n_elements x float4, bb_leaf in
+     * the float32 frame rounded outward (filled by ct_pack_box_index when not
+     * NULL).  With it the segment traversals skip nodes and cells whose box
+     * the segment's line surely misses (they produce no results). */
+    void* bb_leaf32;
 } ct_tree;
 
 /* ---------------------------------------------------------------------- */
@@ -453,11 +458,13 @@ int ct_radix_pass(const unsigned* kin, const int* iin, int64_t n, int32_t shift,
 /* Box index of a packed face or edge tree (no upstream counterpart): the
  * cell boxes in leaf order, every node's bounding box and leaf range, and
  * every leaf position's leaf start, in caller-allocated arrays set in the
- * descriptor (bb_leaf, node_box, leaf_start).  With it the box queries
- * stop descending at nodes whose cells' bounding box lies strictly inside
- * the query box -- every cell below overlaps it -- and count or write that
- * subtree's cells in the upstream visiting order directly.  Results are
- * unchanged.  scratch: ct_box_index_scratch_size(tree) bytes; the call only
+ * descriptor (bb_leaf, node_box, leaf_start; bb_leaf32 optional).  With it
+ * the box queries stop descending at nodes whose cells' bounding box lies
+ * strictly inside the query box -- every cell below overlaps it -- and count
+ * or write that subtree's cells in the upstream visiting order directly; with
+ * bb_leaf32 too, the segment traversals skip nodes and cells whose box the
+ * segment's line misses by more than the float64 rounding of the clipping
+ * tests (certified in float32).  Results are unchanged.  scratch: ct_box_index_scratch_size(tree) bytes; the call only
  * enqueues work, so the scratch must stay allocated until that work has run
  * (stream order). */
 size_t ct_box_index_scratch_size(const ct_tree* tree);

@@ -12,7 +12,7 @@ import pathlib
 from . import build as _build
 
 LIB_PATH = _build.LIB_PATH
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 CT_OK = 0
 CT_ERR_CUDA = 1
@@ -89,6 +89,7 @@ class CtTree(ctypes.Structure):
         ("tune_query_threads", _I32),
         ("tune_fp64_stack", _I32),
         ("node_parent", _P),
+        ("bb_leaf32", _P),
     ]
 
 

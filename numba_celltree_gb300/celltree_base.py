@@ -442,23 +442,26 @@ class _GpuTree:
 
     def ensure_box_index(self):
         """Build the box index of the multi-result queries on first use (cell
-        boxes in leaf order, node bounding boxes and leaf ranges)."""
+        boxes in leaf order, also in the float32 frame, node bounding boxes
+        and leaf ranges)."""
         if self.desc.node_box or not self.desc.bounds_finite or self.n == 0:
             return
         torch = _device.torch()
         lib = _lib.load()
         self.bb_leaf = _device.empty((self.n, 4), torch.float64, self.device)
+        self.bb_leaf32 = _device.empty((self.n, 4), torch.float32, self.device)
         self.node_box = _device.empty((self.n_nodes, 8), torch.int32, self.device)
         self.leaf_start = _device.empty((self.n,), torch.int32, self.device)
         d = self.desc
         d.bb_leaf = _device.ptr(self.bb_leaf)
+        d.bb_leaf32 = _device.ptr(self.bb_leaf32)
         d.node_box = _device.ptr(self.node_box)
         d.leaf_start = _device.ptr(self.leaf_start)
         nbytes = int(lib.ct_box_index_scratch_size(ctypes.byref(d)))
         scratch = _device.empty((max(nbytes, 1),), torch.uint8, self.device)
         status = lib.ct_pack_box_index(ctypes.byref(d), _device.ptr(scratch), nbytes, _device.stream())
         if status != _lib.CT_OK:
-            d.bb_leaf = d.node_box = d.leaf_start = None
+            d.bb_leaf = d.bb_leaf32 = d.node_box = d.leaf_start = None
             _lib.check(status, "box index")
 
     # -- output-budgeted chunks of multi-result queries ------------------------
@@ -476,8 +479,7 @@ class _GpuTree:
         """Candidate cells of every segment (device int64): an upper bound of
         its results."""
         n = int(segs_d.shape[0])
-        if mode == 1:
-            self.ensure_box_index()
+        self.ensure_box_index()
         cfg = self.cached("segments", n)
         self._apply("segments", cfg)
         _, ccnt, _, _ = self.edge_candidate_ranges(segs_d, mode, None, self.edge_cut(cfg))
@@ -485,6 +487,8 @@ class _GpuTree:
 
     # cells under a work item of the split segment traversal (the default)
     SPLIT_CELLS = 1024
+    # work items from which their memory is checked against the free memory
+    ITEMS_CHECK_MIN = 1 << 20
 
     def edge_cut(self, cfg: dict):
         """Depth at which segment traversals are cut into work items (about
@@ -512,8 +516,18 @@ class _GpuTree:
             coff, nc = self.scan(ccnt)
             return coff, ccnt, nc, None
         icnt = _device.empty((n,), torch.int64, self.device)
-        _lib.check(lib.ct_count_edge_items(d, mode, P(segs_d), n, P(order), cut, P(icnt), st), "intersect_edges")
-        ioff, ni = self.scan(icnt)
+        while True:
+            _lib.check(lib.ct_count_edge_items(d, mode, P(segs_d), n, P(order), cut, P(icnt), st),
+                       "intersect_edges")
+            ioff, ni = self.scan(icnt)
+            # items take 24 bytes each in flight: a coarser cut when they
+            # would not fit (a level less about halves them)
+            if ni <= self.ITEMS_CHECK_MIN or cut <= 1:
+                break
+            room = self.device_budget(24)
+            if ni <= room:
+                break
+            cut = max(1, cut - int(np.ceil(np.log2(ni / room))))
         iseg = _device.empty((max(ni, 1),), torch.int32, self.device)
         inode = _device.empty((max(ni, 1),), torch.int32, self.device)
         _lib.check(lib.ct_write_edge_items(d, mode, P(segs_d), n, P(order), cut, P(ioff), P(iseg), P(inode), st),
@@ -602,8 +616,7 @@ class _GpuTree:
         lib = _lib.load()
         st = _device.stream()
         self.reset_error()
-        if mode == 1:
-            self.ensure_box_index()
+        self.ensure_box_index()
         self._apply("segments", config)
         order = self.work_order(segs_d, 1, config.get("work_order"))
         P = _device.ptr

@@ -44,6 +44,11 @@ struct TreeQ {
     const uint8_t* plen32;
     int S4;
     float dabs;                // float64 rounding of absolute coordinates
+    // line filter of the segment traversal (null bbl32: off)
+    const float4* bbl32;       // cell boxes in leaf order, float32 frame, rounded outward
+    float fX, fY;              // largest |x - ox|, |y - oy| over the tree's bbox
+    double babs;               // largest |coordinate| of the tree's bbox
+    double mext;               // 2^-37 x the tree's largest extent + 2^-47
 };
 
 // Bounding box of a node's cells in the float32 frame of the tree (x - ox,
@@ -255,6 +260,65 @@ __device__ __forceinline__ int cs_code_keys(unsigned long long kx, unsigned long
     return p;
 }
 
+// Line filter of the segment traversal (no upstream counterpart).  A cell
+// whose box the segment's line misses by more than a margin m cannot be a
+// result: Cohen-Sutherland (cohen_sutherland.py:32-101) then rejects it --
+// each clipping step puts an endpoint on a box edge line at most a few
+// float64 roundings (of the coordinates' magnitude C) off the line, so every
+// point it computes stays outside the box, on the side the exact algorithm's
+// does, and the exact algorithm rejects a segment that misses the box (a
+// segment whose line meets the box beyond an endpoint shares an outcode bit
+// and is rejected by the outcode test) -- and for edge trees
+// lines_intersect (geometry_utils.py:361-418) finds both tree edge
+// endpoints strictly on one side of the segment's line and not within its
+// tolerance (1e-12 of the edge length) of it.  m = 2^-40 C (C: the largest
+// |coordinate| of the segment and the tree's bbox) + 2^-37 x the tree's
+// extent + 2^-47 covers both by orders of magnitude.  The test runs in
+// float32 in the tree's frame on node boxes and cell boxes rounded outward:
+// f = n . (corner - a) at the corner nearest the line's side, against a
+// bound on the float32 and conversion errors (2^-19 of the products'
+// magnitudes plus the frame magnitudes) plus m |n|.  Pruning only removes
+// cells that produce no result, so results and their order are unchanged.
+struct LineF {
+    float ax, ay, nx, ny, K, em;
+    bool on;
+};
+
+__device__ __forceinline__ LineF line_filter(const TreeQ& T, dpt a, dpt b, dpt V, bool keys) {
+    LineF L;
+    L.on = keys && T.bbl32 != nullptr;
+    L.ax = L.ay = L.nx = L.ny = L.K = L.em = 0.0f;
+    if (!L.on) return L;
+    L.ax = __double2float_rn(a.x - T.ox);
+    L.ay = __double2float_rn(a.y - T.oy);
+    L.nx = __double2float_rn(-V.y);
+    L.ny = __double2float_rn(V.x);
+    const float anx = fabsf(L.nx), any = fabsf(L.ny);
+    L.K = __fadd_ru(__fmul_ru(anx, __fadd_ru(fabsf(L.ax), T.fX)), __fmul_ru(any, __fadd_ru(fabsf(L.ay), T.fY)));
+    const double C = fmax(fmax(fmax(fabs(a.x), fabs(a.y)), fmax(fabs(b.x), fabs(b.y))), T.babs);
+    const float m = __double2float_ru(__dadd_ru(__dmul_ru(C, 0x1p-40), T.mext));
+    L.em = __fmul_ru(__fmul_ru(m, __fadd_ru(anx, any)), 1.0f + 0x1p-18f);
+    // a non-finite term switches the filter off (its comparisons would be false anyway)
+    L.on = isfinite(L.K) && isfinite(L.em) && isfinite(L.ax) && isfinite(L.ay);
+    return L;
+}
+
+// Whether the segment's line surely misses the float32 box (frame of the tree).
+__device__ __forceinline__ bool line_misses(const LineF& L, float x0, float x1, float y0, float y1) {
+    const float px = L.nx > 0.0f ? x0 : x1, qx = L.nx > 0.0f ? x1 : x0;
+    const float py = L.ny > 0.0f ? y0 : y1, qy = L.ny > 0.0f ? y1 : y0;
+    const float dpx = __fsub_rn(px, L.ax), dpy = __fsub_rn(py, L.ay);
+    const float dqx = __fsub_rn(qx, L.ax), dqy = __fsub_rn(qy, L.ay);
+    const float t1 = __fmul_rn(L.nx, dpx), t2 = __fmul_rn(L.ny, dpy);
+    const float u1 = __fmul_rn(L.nx, dqx), u2 = __fmul_rn(L.ny, dqy);
+    const float fmin = __fadd_rn(t1, t2), fmax_ = __fadd_rn(u1, u2);
+    const float emin = __fadd_ru(__fmul_ru(__fadd_ru(__fadd_ru(fabsf(t1), fabsf(t2)), L.K), 0x1p-19f),
+                                 __fadd_ru(L.em, 0x1p-100f));
+    const float emax = __fadd_ru(__fmul_ru(__fadd_ru(__fadd_ru(fabsf(u1), fabsf(u2)), L.K), 0x1p-19f),
+                                 __fadd_ru(L.em, 0x1p-100f));
+    return fmin > emin || fmax_ < -emax;
+}
+
 // Segment a -> b against the cells of leaf `v` (nf q): the candidates that
 // Cohen-Sutherland's shared-outcode test does not reject (mode 1), or every
 // cell (mode 0), counted and, with WRITE, written at cseg / cj[base + count].
@@ -262,9 +326,13 @@ template <bool WRITE, int MODE>
 __device__ __forceinline__ void edge_leaf(const TreeQ& T, float4 q, dpt a, dpt b, bool keys, unsigned long long kax,
                                           unsigned long long kay, unsigned long long kbx, unsigned long long kby,
                                           int64_t i, int64_t base, int64_t& count, int* __restrict__ cseg,
-                                          int* __restrict__ cj) {
+                                          int* __restrict__ cj, const LineF* lf = nullptr) {
     int ptr = na(q), bq = nb(q);
     for (int j = ptr; j < ptr + bq; j++) {
+        if (lf && lf->on) {
+            const float4 c = T.bbl32[j];
+            if (line_misses(*lf, c.x, c.y, c.z, c.w)) continue;
+        }
         bool cand = true;
         if (MODE == 1) {
             dbox bx = leaf_box(T, j);
@@ -357,6 +425,7 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
                                             int64_t base, int* __restrict__ cseg, int* __restrict__ cj) {
     const dpt V = vsub(b, a);
     const EdgeKeys K = edge_keys(T, a, b);
+    const LineF LF = line_filter(T, a, b, V, K.keys);
     int st[STK];
     unsigned char sd[CUT ? STK : 1];
     int sp = 1;
@@ -372,6 +441,10 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
         --sp;
         const int v = st[sp];
         const int depth = CUT ? sd[sp] : 0;
+        if (LF.on) {
+            const float4 nbx = *reinterpret_cast<const float4*>(T.nbx + v);
+            if (line_misses(LF, nbx.x, nbx.y, nbx.z, nbx.w)) continue;
+        }
         float4 q = T.nf[v];
         const bool terminal = nb(q) >= 0;
         if (CUT && (terminal || depth >= cut)) {
@@ -383,7 +456,7 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
             continue;
         }
         if (terminal) {
-            edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj);
+            edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj, &LF);
             continue;
         }
         int first, second;
@@ -1238,6 +1311,13 @@ TreeQ make_q(const ct_tree* t) {
     T.lstart = box_index ? t->leaf_start : nullptr;
     T.ox = t->origin[0];
     T.oy = t->origin[1];
+    T.bbl32 = (box_index && t->bb_leaf32) ? (const float4*)t->bb_leaf32 : nullptr;
+    T.fX = (float)std::max(std::fabs(t->bbox[0] - T.ox), std::fabs(t->bbox[1] - T.ox)) * (1.0f + 0x1p-20f);
+    T.fY = (float)std::max(std::fabs(t->bbox[2] - T.oy), std::fabs(t->bbox[3] - T.oy)) * (1.0f + 0x1p-20f);
+    T.babs = std::max(std::max(std::fabs(t->bbox[0]), std::fabs(t->bbox[1])),
+                      std::max(std::fabs(t->bbox[2]), std::fabs(t->bbox[3])));
+    T.mext = 0x1p-37 * std::max(t->bbox[1] - t->bbox[0], t->bbox[3] - t->bbox[2]) + 0x1p-47;
+    if (!(T.fX <= 3.0e38f && T.fY <= 3.0e38f && T.babs <= 1.0e300 && T.mext <= 1.0e300)) T.bbl32 = nullptr;
     T.parent = t->node_parent;
     T.polyf = (const float4*)t->poly_f32;
     T.plen32 = t->poly_len32;
@@ -1260,6 +1340,17 @@ __global__ void k_bi_leaf_boxes(const int64_t* __restrict__ bbi, const double4* 
                                 double4* __restrict__ bbl) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
         bbl[p] = bb[bbi[p]];
+}
+
+// bb_leaf in the float32 frame, rounded outward (the subtraction of the
+// origin rounded outward too): contains the cell's box exactly.
+__global__ void k_bi_leaf32(const double4* __restrict__ bbl, int64_t n, double ox, double oy,
+                            float4* __restrict__ out) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const double4 b = bbl[p];
+        out[p] = make_float4(__double2float_rd(__dsub_rd(b.x, ox)), __double2float_ru(__dsub_ru(b.y, ox)),
+                             __double2float_rd(__dsub_rd(b.z, oy)), __double2float_ru(__dsub_ru(b.w, oy)));
+    }
 }
 
 __global__ void k_bi_parents(const int64_t* __restrict__ child, int64_t nn, int* __restrict__ parent,
@@ -1385,6 +1476,9 @@ int ct_pack_box_index(ct_tree* t, void* scratch, size_t scratch_bytes, void* str
     if (n > 0) {
         k_bi_leaf_boxes<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 8), 256, 0, st>>>(
             t->bb_indices, (const double4*)t->bb_coords, n, (double4*)t->bb_leaf);
+        if (t->bb_leaf32)
+            k_bi_leaf32<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 8), 256, 0, st>>>(
+                (const double4*)t->bb_leaf, n, t->origin[0], t->origin[1], (float4*)t->bb_leaf32);
     }
     k_bi_parents<<<grid_of(nn, 256), 256, 0, st>>>(t->node_child, nn, parent, keys);
     k_bi_leaves<<<grid_of(nn, 128), 128, 0, st>>>(t->node_child, t->node_ptr, t->node_size, nn,

@@ -24,6 +24,18 @@ def same(a, b):
         assert np.array_equal(a, b)
 
 
+def teq(a, b):
+    """Bitwise-equal device tensors, NaN equal to NaN."""
+    import torch
+
+    if a.shape != b.shape or a.dtype != b.dtype:
+        return False
+    if a.is_floating_point():
+        na, nb = torch.isnan(a), torch.isnan(b)
+        return torch.equal(na, nb) and torch.equal(torch.where(na, 0.0, a), torch.where(nb, 0.0, b))
+    return torch.equal(a, b)
+
+
 def case(i):
     p = f"c{i}_"
     return {k[len(p):]: G[k] for k in G.files if k.startswith(p)}
@@ -160,9 +172,25 @@ def test_split_segment_traversal_matches_uncut(oracle):
         assert t.edge_cut(cfg) is not None
         got = t.locate_edges(sd, 1, cfg)
         for a, b in zip(got, base):
-            assert torch.equal(a, b), split
+            assert teq(a, b), split
         _, ccnt, _, items = t.edge_candidate_ranges(sd, 1, None, t.edge_cut(cfg))
         assert items is not None and torch.equal(ccnt, counts0), split
+    # work items beyond the device budget: coarser cuts, same results
+    from numba_celltree_gb300 import celltree_base
+
+    cfg = {"threads": 128, "work_order": False, "split": 2}
+    n_items = t.edge_candidate_ranges(sd, 1, None, t.edge_cut(cfg))[3][2]
+    try:
+        t.ITEMS_CHECK_MIN = 0
+        t.device_budget = lambda b: n_items // 5
+        _, _, _, items = t.edge_candidate_ranges(sd, 1, None, t.edge_cut(cfg))
+        assert 0 < items[2] <= n_items // 5
+        got = t.locate_edges(sd, 1, cfg)
+        for a, b in zip(got, base):
+            assert teq(a, b)
+    finally:
+        del t.ITEMS_CHECK_MIN, t.device_budget
+    assert t.ITEMS_CHECK_MIN == celltree_base._GpuTree.ITEMS_CHECK_MIN
     # edge tree (edge-edge mode)
     e = np.unique(np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]]]), axis=1), axis=0)
     e = e[(e >= 0).all(1)]
@@ -173,8 +201,108 @@ def test_split_segment_traversal_matches_uncut(oracle):
     for split in (3, 50):
         got = te.locate_edges(sd, 0, {"threads": 64, "work_order": False, "split": split})
         for a, b in zip(got, base):
-            assert torch.equal(a, b), split
+            assert teq(a, b), split
     for a, b in zip(ge.intersect_edges(segs), oe.intersect_edges(segs)):
+        same(a, b)
+
+
+def _grazing_segments(xy, f, n, seed):
+    """Segments that run along cell edges, through vertices, one ulp off
+    edges and vertices, axis-aligned on grid lines and nearly parallel to
+    edges: where a filter that is not certified would drop a result."""
+    rng = np.random.default_rng(seed)
+    fi = rng.integers(0, len(f), n)
+    v0, v1 = xy[f[fi, 0]], xy[f[fi, 1]]
+    span = float((xy.max(0) - xy.min(0)).max())
+    d = v1 - v0
+    far = xy[f[rng.integers(0, len(f), n), 2]]
+    out = [
+        np.stack([v0, v1], 1),  # exactly an edge
+        np.stack([v0 - 3.0 * d, v1 + 5.0 * d], 1),  # an edge's line, extended over neighbours
+        np.stack([np.nextafter(v0, v0 + 1.0), np.nextafter(v1, v1 - 1.0)], 1),  # one ulp off
+        np.stack([v0 + np.array([0.0, 1e-12]) * span, v1 + np.array([0.0, -1e-12]) * span], 1),
+        np.stack([v0, far], 1),  # vertex to vertex across cells
+        np.stack([v0, v0 + (far - v0) * (1.0 + 2.0 ** -40)], 1),  # just past a vertex
+        np.stack([v0 - d * 1e6, v0 + np.array([d[:, 1], -d[:, 0]]).T * 1e-9 + d * 1e6], 1),  # nearly parallel
+    ]
+    ys = xy[rng.integers(0, len(xy), n // 4), 1]
+    lo, hi = xy.min(0), xy.max(0)
+    out.append(np.stack([np.stack([np.full_like(ys, lo[0] - 1.0), ys], 1),
+                         np.stack([np.full_like(ys, hi[0] + 1.0), ys], 1)], 1))  # horizontal on grid lines
+    xs = xy[rng.integers(0, len(xy), n // 4), 0]
+    out.append(np.stack([np.stack([xs, np.full_like(xs, hi[1] + 1.0)], 1),
+                         np.stack([xs, np.full_like(xs, lo[1] - 1.0)], 1)], 1))  # vertical, downwards
+    return np.concatenate(out)
+
+
+@pytest.mark.parametrize("name", ["grid_tri", "utm_tri", "mixed"])
+def test_line_filter_keeps_results(oracle, name):
+    """The traversal's line filter (nodes and cells whose box the segment's
+    line surely misses are skipped) prunes candidates but never a result:
+    results with and without it are identical, and equal to the oracle's, on
+    segments along and one ulp off cell edges, through vertices, on grid
+    lines (an unjittered grid), with UTM-size offsets; edge trees too."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, EdgeCellTree2d
+
+    if name == "grid_tri":
+        xy, f = syn.triangle_mesh(40, 30, seed=41, extent=(40.0, 30.0), jitter=0.0)
+    elif name == "utm_tri":
+        xy, f = syn.triangle_mesh(50, 40, seed=42, extent=(50.0, 40.0), offset=(5.0e5, 4.2e6))
+    else:
+        xy, f = syn.mixed_mesh(50, 40, seed=43, extent=(50.0, 40.0))
+    lo, hi = xy.min(0), xy.max(0)
+    segs = np.concatenate([_grazing_segments(xy, f, 300, 44),
+                           syn.random_segments(200, lo - 1.0, hi + 1.0, seed=45)])
+    sd = torch.as_tensor(segs, device="cuda")
+    g = CellTree2d(xy, f, -1)
+    t = g._tree
+    cfg = {"threads": 128, "work_order": False, "split": 0}
+    on = t.locate_edges(sd, 1, cfg)
+    cnt_on = int(t.count_edge_candidates(sd, 1).sum())
+    assert t.desc.bb_leaf32
+    keep, t.desc.bb_leaf32 = t.desc.bb_leaf32, None
+    try:
+        off = t.locate_edges(sd, 1, cfg)
+        cnt_off = int(t.count_edge_candidates(sd, 1).sum())
+    finally:
+        t.desc.bb_leaf32 = keep
+    assert cnt_on < cnt_off
+    for a, b in zip(on, off):
+        assert teq(a, b)
+    split = t.locate_edges(sd, 1, {"threads": 64, "work_order": True, "split": 16})
+    for a, b in zip(split, on):
+        assert teq(a, b)
+    exp = oracle.OracleCellTree2d(xy, f, -1).intersect_edges(segs)
+    for a, b in zip(on, exp):
+        same(a.cpu().numpy(), b)
+    # edge tree over the mesh's edges (edge-edge mode, lines_intersect)
+    e = np.unique(np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]]]), axis=1), axis=0)
+    e = e[(e >= 0).all(1)]
+    if name == "utm_tri":
+        # the padded box of an axis-aligned edge at this offset has its
+        # centroid past the last bucket: upstream's build fails on it (its
+        # partition runs out of buckets), and so do the oracle and this build
+        from numba_celltree_gb300._lib import CellTreeError
+
+        with pytest.raises(CellTreeError, match="outside every bucket"):
+            EdgeCellTree2d(xy, e)
+        with pytest.raises(RuntimeError, match="outside every bucket"):
+            oracle.OracleEdgeCellTree2d(xy, e)
+        return
+    ge = EdgeCellTree2d(xy, e)
+    te = ge._tree
+    on = te.locate_edges(sd, 0, cfg)
+    keep, te.desc.bb_leaf32 = te.desc.bb_leaf32, None
+    try:
+        off = te.locate_edges(sd, 0, cfg)
+    finally:
+        te.desc.bb_leaf32 = keep
+    assert keep
+    for a, b in zip(on, off):
+        assert teq(a, b)
+    for a, b in zip(ge.intersect_edges(segs), oracle.OracleEdgeCellTree2d(xy, e).intersect_edges(segs)):
         same(a, b)
 
 
