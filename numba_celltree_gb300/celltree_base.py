@@ -594,9 +594,12 @@ class _GpuTree:
         jj = _device.empty((total,), torch.int64, self.device)
         # the writing pass repeats the counting pass's traversal: a condition
         # it could report has been reported by the count
+        wsz = int(lib.ct_write_boxes_workspace_size(total))
+        ws = _device.empty((wsz,), torch.uint8, self.device)
         _lib.check(
-            lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
-                               _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), st),
+            lib.ct_write_boxes_ws(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                  _device.ptr(offsets), total, _device.ptr(ii), _device.ptr(jj), _device.ptr(ws),
+                                  wsz, st),
             "locate_boxes",
         )
         return ii, jj

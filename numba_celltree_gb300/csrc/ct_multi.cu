@@ -92,10 +92,20 @@ __device__ __forceinline__ dbox leaf_box(const TreeQ& T, int64_t j) {
 // ---------------------------------------------------------------------------
 // locate_box query.py:177-244
 // ---------------------------------------------------------------------------
+// A subtree wholly inside a query box whose cells the writing pass leaves to
+// k_box_jobs: its output offset, the query box and its leaf range.
+struct BoxJob {
+    int64_t out, box;
+    int ptr, size, pad0, pad1;
+};
+constexpr int BOX_JOB_MIN = 64;  // smaller subtrees are written in line
+
 template <bool WRITE, bool DEEP>
 __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restrict__ boxes, int64_t n,
                                                const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
-                                               int64_t* __restrict__ ii, int64_t* __restrict__ jj) {
+                                               int64_t* __restrict__ ii, int64_t* __restrict__ jj,
+                                               BoxJob* __restrict__ jobs = nullptr,
+                                               unsigned long long* __restrict__ njobs = nullptr, int64_t job_cap = 0) {
     int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tq >= n) return;
     // queries in work order (similar work in one warp); results by query index
@@ -150,7 +160,22 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                         // the whole subtree, in upstream's visiting order: right
                         // child first, i.e. leaves by decreasing position, each
                         // leaf's cells by increasing position
-                        if (WRITE) {
+                        int64_t jk = -1;
+                        if (WRITE && jobs && nbv.size >= BOX_JOB_MIN) {
+                            jk = (int64_t)atomicAdd(njobs, 1ull);
+                            if (jk < job_cap) {
+                                BoxJob J;
+                                J.out = base + count;
+                                J.box = i;
+                                J.ptr = nbv.ptr;
+                                J.size = nbv.size;
+                                J.pad0 = J.pad1 = 0;
+                                jobs[jk] = J;
+                            } else {
+                                jk = -1;  // no room (cannot happen with the sized buffer): write in line
+                            }
+                        }
+                        if (WRITE && jk < 0) {
                             int qq = nbv.ptr + nbv.size;
                             int64_t c = count;
                             while (qq > nbv.ptr) {
@@ -235,6 +260,40 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
         }
     }
     if (!WRITE) cnt_or_off[i] = count;
+}
+
+// The cells of each deferred subtree, one warp per subtree, in upstream's
+// visiting order (leaves by decreasing position, each leaf's cells by
+// increasing position): output o takes reversed position q = end - 1 - o,
+// whose leaf [s, e) contributes position s + (e - 1 - q).  Writes and the
+// bb_indices reads are coalesced across the warp.
+__global__ void __launch_bounds__(256) k_box_jobs(const BoxJob* __restrict__ jobs,
+                                                  const unsigned long long* __restrict__ njobs,
+                                                  int64_t job_cap, const int* __restrict__ lstart,
+                                                  const int64_t* __restrict__ bbi, int64_t* __restrict__ ii,
+                                                  int64_t* __restrict__ jj, unsigned int* __restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t nj = (int64_t)min(*njobs, (unsigned long long)job_cap);
+    for (int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < nj; k += warps) {
+        const BoxJob J = jobs[k];
+        const int end = J.ptr + J.size;
+        bool bad = false;
+        for (int o = lane; o < J.size; o += 32) {
+            const int q = end - 1 - o;
+            const int s0 = lstart[q];
+            int e = q + 1;
+            while (e < end && lstart[e] == s0) e++;
+            const int p = s0 + (e - 1 - q);
+            if (s0 < J.ptr || s0 > q) {  // corrupt index: leave the slot, report
+                bad = true;
+                continue;
+            }
+            ii[J.out + o] = J.box;
+            jj[J.out + o] = bbi[p];
+        }
+        if (bad) set_error(err, CT_DEVERR_LOOP);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1539,6 +1598,39 @@ int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     else
         k_boxes<true, false><<<grid_of(n, bt), bt, 0, (cudaStream_t)stream>>>(make_q(t), (const double4*)boxes, n,
                                                                               order, (int64_t*)offsets, ii, jj);
+    CT_CHECK_LAUNCH("write_boxes");
+    return CT_OK;
+}
+
+size_t ct_write_boxes_workspace_size(int64_t total_pairs) {
+    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / BOX_JOB_MIN + 1;
+    return 256 + (size_t)cap * sizeof(BoxJob);
+}
+
+int ct_write_boxes_ws(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order,
+                      const int64_t* offsets, int64_t total_pairs, int64_t* ii, int64_t* jj, void* ws,
+                      size_t ws_bytes, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (total_pairs < 0) return ct_fail(CT_ERR_ARG, "negative pair count");
+    if (!ws || ws_bytes < ct_write_boxes_workspace_size(total_pairs))
+        return ct_fail(CT_ERR_WORKSPACE, "write_boxes workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    if (!T.nbx) return ct_write_boxes(t, boxes, n, order, offsets, ii, jj, stream);  // no box index: no subtrees
+    unsigned long long* njobs = (unsigned long long*)ws;
+    BoxJob* jobs = (BoxJob*)((char*)ws + 256);
+    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / BOX_JOB_MIN + 1;
+    CT_CUDA(cudaMemsetAsync(njobs, 0, sizeof(unsigned long long), st));
+    const int bt = box_threads(t);
+    if (deep_tree(t))
+        k_boxes<true, true><<<grid_of(n, bt), bt, 0, st>>>(T, (const double4*)boxes, n, order, (int64_t*)offsets,
+                                                           ii, jj, jobs, njobs, cap);
+    else
+        k_boxes<true, false><<<grid_of(n, bt), bt, 0, st>>>(T, (const double4*)boxes, n, order, (int64_t*)offsets,
+                                                            ii, jj, jobs, njobs, cap);
+    k_box_jobs<<<152 * 8, 256, 0, st>>>(jobs, njobs, cap, T.lstart, T.bbi, ii, jj, T.err);
     CT_CHECK_LAUNCH("write_boxes");
     return CT_OK;
 }

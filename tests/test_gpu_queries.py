@@ -206,6 +206,43 @@ def test_split_segment_traversal_matches_uncut(oracle):
         same(a, b)
 
 
+def test_box_subtree_jobs_match_inline(oracle):
+    """Subtrees wholly inside a query box written by one warp per subtree
+    after the traversal (ct_write_boxes_ws) give the pairs the box's own
+    thread writes in line (ct_write_boxes) and the oracle's: big boxes over
+    whole subtrees, small ones, boxes beyond the mesh, cells_per_leaf 1-3."""
+    import ctypes
+
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, _device, _lib
+
+    xy, f = syn.mixed_mesh(90, 70, seed=51, extent=(90.0, 70.0))
+    boxes = np.concatenate([
+        syn.random_boxes(2500, (-5.0, -5.0), (95.0, 75.0), 0.2, 60.0, seed=52, log_uniform=True),
+        np.array([[-10.0, 100.0, -10.0, 80.0], [0.0, 90.0, 0.0, 70.0], [40.0, 40.5, 30.0, 30.5]]),
+    ])
+    bd = torch.as_tensor(boxes, device="cuda")
+    for cpl in (1, 2, 3):
+        g = CellTree2d(xy, f, -1, 4, cpl)
+        t = g._tree
+        ii, jj = t.locate_boxes(bd, {"threads": 256, "work_order": cpl == 2})
+        n = len(boxes)
+        counts = t.count_boxes(bd)
+        offsets, total = t.scan(counts)
+        assert total == int(ii.shape[0]) and total > 100_000
+        i2 = torch.empty_like(ii)
+        j2 = torch.empty_like(jj)
+        _lib.check(_lib.load().ct_write_boxes(ctypes.byref(t.desc), _device.ptr(bd), n, None, _device.ptr(offsets),
+                                              _device.ptr(i2), _device.ptr(j2), _device.stream()), "inline")
+        assert torch.equal(ii, i2) and torch.equal(jj, j2), cpl
+        o = oracle.OracleCellTree2d(xy, f, -1, 4, cpl)
+        for a, b in zip((ii, jj), o.locate_boxes(boxes)):
+            same(a.cpu().numpy(), b)
+        for a, b in zip(g.intersect_boxes(boxes[:300]), o.intersect_boxes(boxes[:300])):
+            same(a, b)
+
+
 def _grazing_segments(xy, f, n, seed):
     """Segments that run along cell edges, through vertices, one ulp off
     edges and vertices, axis-aligned on grid lines and nearly parallel to
