@@ -479,16 +479,16 @@ int ct_count_boxes(const ct_tree* tree, const double* boxes, int64_t n, const in
  * in traversal order -- upstream's locate_boxes output order. */
 int ct_write_boxes(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order, const int64_t* offsets,
                    int64_t* ii, int64_t* jj, void* stream);
-/* The same output; subtrees of at least 64 cells wholly inside a query box
- * (box index) are queued in the workspace and their cells written by one
- * warp per subtree, coalesced, after the traversal, instead of by the box's
- * own thread.  total_pairs: the scanned total (sizes the queue);
- * workspace: ct_write_boxes_workspace_size(total_pairs) bytes, in use until
- * the enqueued work has run. */
-size_t ct_write_boxes_workspace_size(int64_t total_pairs);
+/* The same output; subtrees of at least min_job_cells cells (0: 8) wholly
+ * inside a query box (box index) are queued in the workspace and their cells
+ * written by one warp per subtree, coalesced, after the traversal, instead
+ * of by the box's own thread.  total_pairs: the scanned total (sizes the
+ * queue); workspace: ct_write_boxes_workspace_size(total_pairs,
+ * min_job_cells) bytes, in use until the enqueued work has run. */
+size_t ct_write_boxes_workspace_size(int64_t total_pairs, int32_t min_job_cells);
 int ct_write_boxes_ws(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order,
-                      const int64_t* offsets, int64_t total_pairs, int64_t* ii, int64_t* jj, void* workspace,
-                      size_t workspace_bytes, void* stream);
+                      const int64_t* offsets, int64_t total_pairs, int32_t min_job_cells, int64_t* ii, int64_t* jj,
+                      void* workspace, size_t workspace_bytes, void* stream);
 
 /* locate_edge query.py:357-455 over segments (n x 2 x 2).  mode 1: edge vs
  * face (Cohen-Sutherland + Cyrus-Beck, compute_edge_face_intersect

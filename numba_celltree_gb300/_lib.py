@@ -205,9 +205,9 @@ SIGNATURES = {
     "ct_work_order_workspace_size": (_SZ, [_I64]),
     "ct_count_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P]),
     "ct_write_edge_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _P]),
-    "ct_write_boxes_workspace_size": (ctypes.c_size_t, [_I64]),
-    "ct_write_boxes_ws": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _I64, _P, _P, _P, ctypes.c_size_t,
-                                         _P]),
+    "ct_write_boxes_workspace_size": (ctypes.c_size_t, [_I64, _I32]),
+    "ct_write_boxes_ws": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _I64, _I32, _P, _P, _P,
+                                         ctypes.c_size_t, _P]),
     "ct_count_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P]),
     "ct_write_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P, _P, _P]),
     "ct_count_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P]),

@@ -44,8 +44,8 @@ FORMAT = 1
 DEFAULTS: Dict[str, dict] = {
     "locate": {"sort_bits": None, "cells_bpsm": 6, "fast_bpsm": 16},
     "fp64": {"stack": 0},
-    "boxes": {"threads": 256, "work_order": None},
-    "segments": {"threads": 128, "work_order": None, "split": 1024},
+    "boxes": {"threads": 256, "work_order": None, "job_cells": 0},
+    "segments": {"threads": 128, "work_order": None, "split": None},
     "index": {"grid_density": 1.0},
 }
 
@@ -54,7 +54,7 @@ SPACE: Dict[str, Dict[str, list]] = {
     "locate": {"sort_bits": [0, 8, 16, 24], "cells_bpsm": [4, 6, 8], "fast_bpsm": [8, 16, 32]},
     "fp64": {"stack": [0, 512]},
     "boxes": {"threads": [64, 128, 256], "work_order": [False, True]},
-    "segments": {"threads": [64, 128], "work_order": [False, True], "split": [0, 256, 1024, 4096]},
+    "segments": {"threads": [64, 128], "work_order": [False, True]},
     "index": {"grid_density": [0.5, 1.0, 2.0]},
 }
 

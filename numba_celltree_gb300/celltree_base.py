@@ -482,7 +482,7 @@ class _GpuTree:
         self.ensure_box_index()
         cfg = self.cached("segments", n)
         self._apply("segments", cfg)
-        _, ccnt, _, _ = self.edge_candidate_ranges(segs_d, mode, None, self.edge_cut(cfg))
+        _, ccnt, _, _ = self.edge_candidate_ranges(segs_d, mode, None, self.edge_cut(cfg, n))
         return ccnt
 
     # cells under a work item of the split segment traversal (the default)
@@ -490,12 +490,20 @@ class _GpuTree:
     # work items from which their memory is checked against the free memory
     ITEMS_CHECK_MIN = 1 << 20
 
-    def edge_cut(self, cfg: dict):
+    # batches from which segment traversals run uncut by default (enough
+    # segments to fill the GPU; the split then only adds its item pass)
+    SPLIT_MAX_SEGMENTS = 1 << 17
+
+    def edge_cut(self, cfg: dict, n_segments: int = 0):
         """Depth at which segment traversals are cut into work items (about
-        cfg["split"] cells under each), or None for the uncut traversal (no
-        split asked, a tree too small to split or too deep for the stacked
-        traversal)."""
-        split = int(cfg.get("split", self.SPLIT_CELLS) or 0)
+        cfg["split"] cells under each; by default SPLIT_CELLS for batches
+        below SPLIT_MAX_SEGMENTS, else uncut), or None for the uncut
+        traversal (no split asked, a tree too small to split or too deep for
+        the stacked traversal)."""
+        split = cfg.get("split")
+        if split is None:
+            split = self.SPLIT_CELLS if n_segments < self.SPLIT_MAX_SEGMENTS else 0
+        split = int(split or 0)
         if split <= 0 or self.n <= split or self.max_depth + 2 > self.BATCHED_MAX_STACK:
             return None
         return max(1, min(self.max_depth, int(np.ceil(np.log2(self.n / split)))))
@@ -565,6 +573,10 @@ class _GpuTree:
         free, _ = torch.cuda.mem_get_info(self.device)
         return max(1 << 20, int(free // 4 // max(bytes_per_result, 1)))
 
+    # pairs from which subtrees inside a box are written by a warp each after
+    # the traversal (below, the extra launch costs more than it saves)
+    BOX_JOBS_MIN_PAIRS = 1 << 20
+
     def locate_boxes(self, boxes_d, config=None, budget=None):
         """Pairs (box, cell) of every box query, box-major in upstream order;
         with `budget`, returns None instead when the pairs would exceed it
@@ -594,12 +606,20 @@ class _GpuTree:
         jj = _device.empty((total,), torch.int64, self.device)
         # the writing pass repeats the counting pass's traversal: a condition
         # it could report has been reported by the count
-        wsz = int(lib.ct_write_boxes_workspace_size(total))
+        if total < self.BOX_JOBS_MIN_PAIRS:
+            _lib.check(
+                lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                   _device.ptr(offsets), _device.ptr(ii), _device.ptr(jj), st),
+                "locate_boxes",
+            )
+            return ii, jj
+        jm = int(config.get("job_cells") or 0)
+        wsz = int(lib.ct_write_boxes_workspace_size(total, jm))
         ws = _device.empty((wsz,), torch.uint8, self.device)
         _lib.check(
             lib.ct_write_boxes_ws(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
-                                  _device.ptr(offsets), total, _device.ptr(ii), _device.ptr(jj), _device.ptr(ws),
-                                  wsz, st),
+                                  _device.ptr(offsets), total, jm, _device.ptr(ii), _device.ptr(jj),
+                                  _device.ptr(ws), wsz, st),
             "locate_boxes",
         )
         return ii, jj
@@ -623,7 +643,7 @@ class _GpuTree:
         self._apply("segments", config)
         order = self.work_order(segs_d, 1, config.get("work_order"))
         P = _device.ptr
-        coff, ccnt, nc, items = self.edge_candidate_ranges(segs_d, mode, order, self.edge_cut(config))
+        coff, ccnt, nc, items = self.edge_candidate_ranges(segs_d, mode, order, self.edge_cut(config, n))
         if budget is not None and nc > budget:
             self.last_counts = ccnt
             return None

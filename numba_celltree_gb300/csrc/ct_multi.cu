@@ -98,14 +98,15 @@ struct BoxJob {
     int64_t out, box;
     int ptr, size, pad0, pad1;
 };
-constexpr int BOX_JOB_MIN = 64;  // smaller subtrees are written in line
+constexpr int BOX_JOB_MIN = 8;  // default: smaller subtrees are written in line
 
 template <bool WRITE, bool DEEP>
 __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restrict__ boxes, int64_t n,
                                                const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
                                                int64_t* __restrict__ ii, int64_t* __restrict__ jj,
                                                BoxJob* __restrict__ jobs = nullptr,
-                                               unsigned long long* __restrict__ njobs = nullptr, int64_t job_cap = 0) {
+                                               unsigned long long* __restrict__ njobs = nullptr, int64_t job_cap = 0,
+                                               int job_min = BOX_JOB_MIN) {
     int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tq >= n) return;
     // queries in work order (similar work in one warp); results by query index
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                         // child first, i.e. leaves by decreasing position, each
                         // leaf's cells by increasing position
                         int64_t jk = -1;
-                        if (WRITE && jobs && nbv.size >= BOX_JOB_MIN) {
+                        if (WRITE && jobs && nbv.size >= job_min) {
                             jk = (int64_t)atomicAdd(njobs, 1ull);
                             if (jk < job_cap) {
                                 BoxJob J;
@@ -1602,34 +1603,37 @@ int ct_write_boxes(const ct_tree* t, const double* boxes, int64_t n, const int32
     return CT_OK;
 }
 
-size_t ct_write_boxes_workspace_size(int64_t total_pairs) {
-    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / BOX_JOB_MIN + 1;
+static int box_job_min(int32_t m) { return m > 0 ? (m < 2 ? 2 : m) : BOX_JOB_MIN; }
+
+size_t ct_write_boxes_workspace_size(int64_t total_pairs, int32_t min_job_cells) {
+    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / box_job_min(min_job_cells) + 1;
     return 256 + (size_t)cap * sizeof(BoxJob);
 }
 
 int ct_write_boxes_ws(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order,
-                      const int64_t* offsets, int64_t total_pairs, int64_t* ii, int64_t* jj, void* ws,
-                      size_t ws_bytes, void* stream) {
+                      const int64_t* offsets, int64_t total_pairs, int32_t min_job_cells, int64_t* ii, int64_t* jj,
+                      void* ws, size_t ws_bytes, void* stream) {
     int s = check_tree(t);
     if (s) return s;
     if (n == 0) return CT_OK;
     if (total_pairs < 0) return ct_fail(CT_ERR_ARG, "negative pair count");
-    if (!ws || ws_bytes < ct_write_boxes_workspace_size(total_pairs))
+    if (!ws || ws_bytes < ct_write_boxes_workspace_size(total_pairs, min_job_cells))
         return ct_fail(CT_ERR_WORKSPACE, "write_boxes workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
     TreeQ T = make_q(t);
     if (!T.nbx) return ct_write_boxes(t, boxes, n, order, offsets, ii, jj, stream);  // no box index: no subtrees
+    const int jm = box_job_min(min_job_cells);
     unsigned long long* njobs = (unsigned long long*)ws;
     BoxJob* jobs = (BoxJob*)((char*)ws + 256);
-    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / BOX_JOB_MIN + 1;
+    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / jm + 1;
     CT_CUDA(cudaMemsetAsync(njobs, 0, sizeof(unsigned long long), st));
     const int bt = box_threads(t);
     if (deep_tree(t))
         k_boxes<true, true><<<grid_of(n, bt), bt, 0, st>>>(T, (const double4*)boxes, n, order, (int64_t*)offsets,
-                                                           ii, jj, jobs, njobs, cap);
+                                                           ii, jj, jobs, njobs, cap, jm);
     else
         k_boxes<true, false><<<grid_of(n, bt), bt, 0, st>>>(T, (const double4*)boxes, n, order, (int64_t*)offsets,
-                                                            ii, jj, jobs, njobs, cap);
+                                                            ii, jj, jobs, njobs, cap, jm);
     k_box_jobs<<<152 * 8, 256, 0, st>>>(jobs, njobs, cap, T.lstart, T.bbi, ii, jj, T.err);
     CT_CHECK_LAUNCH("write_boxes");
     return CT_OK;

@@ -46,7 +46,7 @@ def test_pick_and_cache_round_trip(tmp_path, monkeypatch):
     # lookup merges over the defaults and ignores unknown knobs
     at._cache = None
     cfg = at.lookup("boxes", "x")
-    assert cfg == {"threads": 128, "work_order": False}
+    assert cfg == dict(at.DEFAULTS["boxes"], threads=128, work_order=False)
     assert at.lookup("boxes", "missing") == at.DEFAULTS["boxes"]
     # a damaged file reads as empty and is rewritten on the next put
     path.write_text("{not json")

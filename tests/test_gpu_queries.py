@@ -226,6 +226,7 @@ def test_box_subtree_jobs_match_inline(oracle):
     for cpl in (1, 2, 3):
         g = CellTree2d(xy, f, -1, 4, cpl)
         t = g._tree
+        t.BOX_JOBS_MIN_PAIRS = 0  # the queued path at any size
         ii, jj = t.locate_boxes(bd, {"threads": 256, "work_order": cpl == 2})
         n = len(boxes)
         counts = t.count_boxes(bd)
