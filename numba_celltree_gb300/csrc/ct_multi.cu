@@ -128,13 +128,25 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
     // cell.xmax >= node.xmin > box.xmin, ...); the traversal would visit all
     // of it.  The query box in the float32 frame is rounded inward, the node
     // boxes outward, so a float32 "strictly inside" implies the float64 one.
+    // A node whose cells' bounding box lies strictly beyond a side of the
+    // query box has no overlapping cell (boxes_intersect needs
+    // box.xmin < cell.xmax <= node.xmax, ...): its subtree is skipped.  The
+    // query box rounded outward, the node boxes outward: since x -> fl(x - o)
+    // is monotonic, node.xmax_f32 < float_rd(fl(box.xmin - o)) implies
+    // node.xmax < box.xmin.  Skipped subtrees hold no result, so the output
+    // and its order are unchanged.
     const bool idx = keys && T.nbx != nullptr;
     float qx0 = 0.0f, qx1 = 0.0f, qy0 = 0.0f, qy1 = 0.0f;
+    float ox0 = 0.0f, ox1 = 0.0f, oy0 = 0.0f, oy1 = 0.0f;
     if (idx) {
         qx0 = __double2float_ru(box.xmin - T.ox);
         qx1 = __double2float_rd(box.xmax - T.ox);
         qy0 = __double2float_ru(box.ymin - T.oy);
         qy1 = __double2float_rd(box.ymax - T.oy);
+        ox0 = __double2float_rd(box.xmin - T.ox);
+        ox1 = __double2float_ru(box.xmax - T.ox);
+        oy0 = __double2float_rd(box.ymin - T.oy);
+        oy1 = __double2float_ru(box.ymax - T.oy);
     }
     if (boxes_intersect(box, T.bbox)) {
         // depth-first walk: a stack, or (DEEP, trees deeper than the stack)
@@ -157,7 +169,9 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
             if (!DEEP || down) {
                 if (idx) {
                     const NodeBox nbv = T.nbx[v];
-                    if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
+                    if (nbv.xmax < ox0 || nbv.xmin > ox1 || nbv.ymax < oy0 || nbv.ymin > oy1) {
+                        terminal = true;  // no cell below overlaps the box
+                    } else if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
                         // the whole subtree, in upstream's visiting order: right
                         // child first, i.e. leaves by decreasing position, each
                         // leaf's cells by increasing position

@@ -244,6 +244,34 @@ def test_box_subtree_jobs_match_inline(oracle):
             same(a, b)
 
 
+def test_box_queries_on_grid_lines(oracle):
+    """Boxes whose sides lie exactly on cell edges of an unjittered grid (and
+    one ulp either side), at a UTM-size offset too: the node-box pruning and
+    the inside-subtree shortcut keep upstream's strict overlap test."""
+    from numba_celltree_gb300 import CellTree2d
+
+    rng = np.random.default_rng(61)
+    for off in ((0.0, 0.0), (5.0e5, 4.2e6)):
+        xy, f = syn.triangle_mesh(60, 50, seed=62, extent=(60.0, 50.0), offset=off, jitter=0.0)
+        g = CellTree2d(xy, f, -1)
+        o = oracle.OracleCellTree2d(xy, f, -1)
+        x0 = off[0] + rng.integers(-2, 60, 3000).astype(np.float64)
+        y0 = off[1] + rng.integers(-2, 50, 3000).astype(np.float64)
+        w = rng.integers(0, 30, 3000).astype(np.float64)
+        h = rng.integers(0, 30, 3000).astype(np.float64)
+        boxes = np.stack([x0, x0 + w, y0, y0 + h], 1)
+        nud = boxes.copy()
+        nud[0::2, 0] = np.nextafter(nud[0::2, 0], -np.inf)
+        nud[1::2, 1] = np.nextafter(nud[1::2, 1], np.inf)
+        nud[0::3, 2] = np.nextafter(nud[0::3, 2], np.inf)
+        nud[1::3, 3] = np.nextafter(nud[1::3, 3], -np.inf)
+        boxes = np.concatenate([boxes, nud])
+        for a, b in zip(g.locate_boxes(boxes), o.locate_boxes(boxes)):
+            same(a, b)
+        for a, b in zip(g.intersect_boxes(boxes[:1500]), o.intersect_boxes(boxes[:1500])):
+            same(a, b)
+
+
 def _grazing_segments(xy, f, n, seed):
     """Segments that run along cell edges, through vertices, one ulp off
     edges and vertices, axis-aligned on grid lines and nearly parallel to
