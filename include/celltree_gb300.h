@@ -490,6 +490,19 @@ int ct_write_boxes_ws(const ct_tree* tree, const double* boxes, int64_t n, const
                       const int64_t* offsets, int64_t total_pairs, int32_t min_job_cells, int64_t* ii, int64_t* jj,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* Small batches in one traversal (no upstream counterpart): the counting
+ * pass also writes each box's first spec_cap cells (in output order) into
+ * spec (n x spec_cap int32, 1 <= spec_cap <= 4096); the writing call then
+ * copies the boxes whose count fits from spec and traverses again only for
+ * the others (workspace as ct_write_boxes_ws).  Same output as
+ * ct_count_boxes + ct_write_boxes. */
+int ct_count_boxes_spec(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order, int64_t* counts,
+                        int32_t* spec, int32_t spec_cap, void* stream);
+int ct_write_boxes_spec(const ct_tree* tree, const double* boxes, int64_t n, const int32_t* order,
+                        const int64_t* counts, const int64_t* offsets, const int32_t* spec, int32_t spec_cap,
+                        int64_t total_pairs, int32_t min_job_cells, int64_t* ii, int64_t* jj, void* workspace,
+                        size_t workspace_bytes, void* stream);
+
 /* locate_edge query.py:357-455 over segments (n x 2 x 2).  mode 1: edge vs
  * face (Cohen-Sutherland + Cyrus-Beck, compute_edge_face_intersect
  * query.py:309-328); mode 0: edge vs edge (lines_intersect,

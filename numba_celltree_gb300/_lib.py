@@ -208,6 +208,9 @@ SIGNATURES = {
     "ct_write_boxes_workspace_size": (ctypes.c_size_t, [_I64, _I32]),
     "ct_write_boxes_ws": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _I64, _I32, _P, _P, _P,
                                          ctypes.c_size_t, _P]),
+    "ct_count_boxes_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _I32, _P]),
+    "ct_write_boxes_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P, _I32, _I64, _I32, _P, _P,
+                                           _P, ctypes.c_size_t, _P]),
     "ct_count_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P]),
     "ct_write_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P, _P, _P]),
     "ct_count_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P]),

@@ -576,6 +576,10 @@ class _GpuTree:
     # pairs from which subtrees inside a box are written by a warp each after
     # the traversal (below, the extra launch costs more than it saves)
     BOX_JOBS_MIN_PAIRS = 1 << 20
+    # batches up to this many boxes count and keep each box's first SPEC_CAP
+    # pairs in one traversal (latency of small batches: one traversal less)
+    SPEC_MAX_BOXES = 1 << 16
+    SPEC_CAP = 64
 
     def locate_boxes(self, boxes_d, config=None, budget=None):
         """Pairs (box, cell) of every box query, box-major in upstream order;
@@ -594,8 +598,16 @@ class _GpuTree:
         self.ensure_box_index()
         self._apply("boxes", config)
         order = self.work_order(boxes_d, 0, config.get("work_order"))
-        _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
-                                      _device.ptr(counts), st), "locate_boxes")
+        spec = None
+        if n <= self.SPEC_MAX_BOXES:
+            # one traversal: the counting pass also keeps each box's first pairs
+            spec = _device.empty((n, self.SPEC_CAP), torch.int32, self.device)
+            _lib.check(lib.ct_count_boxes_spec(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                               _device.ptr(counts), _device.ptr(spec), self.SPEC_CAP, st),
+                       "locate_boxes")
+        else:
+            _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                          _device.ptr(counts), st), "locate_boxes")
         self.stage_error()
         offsets, total = self.scan(counts)
         self.raise_on_staged_error()
@@ -606,6 +618,17 @@ class _GpuTree:
         jj = _device.empty((total,), torch.int64, self.device)
         # the writing pass repeats the counting pass's traversal: a condition
         # it could report has been reported by the count
+        if spec is not None:
+            jm = int(config.get("job_cells") or 0)
+            wsz = int(lib.ct_write_boxes_workspace_size(total, jm))
+            ws = _device.empty((wsz,), torch.uint8, self.device)
+            _lib.check(
+                lib.ct_write_boxes_spec(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
+                                        _device.ptr(counts), _device.ptr(offsets), _device.ptr(spec), self.SPEC_CAP,
+                                        total, jm, _device.ptr(ii), _device.ptr(jj), _device.ptr(ws), wsz, st),
+                "locate_boxes",
+            )
+            return ii, jj
         if total < self.BOX_JOBS_MIN_PAIRS:
             _lib.check(
                 lib.ct_write_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),

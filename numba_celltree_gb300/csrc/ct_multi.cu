@@ -106,11 +106,16 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                                                int64_t* __restrict__ ii, int64_t* __restrict__ jj,
                                                BoxJob* __restrict__ jobs = nullptr,
                                                unsigned long long* __restrict__ njobs = nullptr, int64_t job_cap = 0,
-                                               int job_min = BOX_JOB_MIN) {
+                                               int job_min = BOX_JOB_MIN, int* __restrict__ spec = nullptr,
+                                               int spec_cap = 0, const int64_t* __restrict__ spec_cnt = nullptr) {
     int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tq >= n) return;
     // queries in work order (similar work in one warp); results by query index
     int64_t i = order ? (int64_t)order[tq] : tq;
+    // writing pass after a speculative count: boxes whose pairs all fit the
+    // per-box scratch were written from it (k_boxes_spec_emit)
+    if (WRITE && spec_cnt && spec_cnt[i] <= spec_cap) return;
+    int* sp_out = (!WRITE && spec) ? spec + i * (int64_t)spec_cap : nullptr;
     double4 q4 = boxes[i];
     dbox box;
     box.xmin = q4.x;
@@ -165,10 +170,14 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
             }
             const int v = DEEP ? dv : st[--sp];
             bool terminal = false;
-            float4 q;
+            // the node's three records loaded together (one memory round trip
+            // per visited node instead of a chain of three)
+            const float4 q = T.nf[v];
+            const double2 nd_v = T.nd[v];
+            NodeBox nbv;
+            if (idx && (!DEEP || down)) nbv = T.nbx[v];
             if (!DEEP || down) {
                 if (idx) {
-                    const NodeBox nbv = T.nbx[v];
                     if (nbv.xmax < ox0 || nbv.xmin > ox1 || nbv.ymax < oy0 || nbv.ymin > oy1) {
                         terminal = true;  // no cell below overlaps the box
                     } else if (qx0 < nbv.xmin && nbv.xmax < qx1 && qy0 < nbv.ymin && nbv.ymax < qy1) {
@@ -190,18 +199,22 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                                 jk = -1;  // no room (cannot happen with the sized buffer): write in line
                             }
                         }
-                        if (WRITE && jk < 0) {
+                        if ((WRITE && jk < 0) || (sp_out && count < spec_cap)) {
                             int qq = nbv.ptr + nbv.size;
                             int64_t c = count;
-                            while (qq > nbv.ptr) {
+                            while (qq > nbv.ptr && (WRITE || c < spec_cap)) {
                                 int s = T.lstart[qq - 1];
                                 if (s < nbv.ptr || s >= qq) {  // corrupt index: stop rather than loop
                                     set_error(T.err, CT_DEVERR_LOOP);
                                     break;
                                 }
                                 for (int j = s; j < qq; j++) {
-                                    ii[base + c] = i;
-                                    jj[base + c] = T.bbi[j];
+                                    if (WRITE) {
+                                        ii[base + c] = i;
+                                        jj[base + c] = T.bbi[j];
+                                    } else if (c < spec_cap) {
+                                        sp_out[c] = (int)T.bbi[j];
+                                    }
                                     c++;
                                 }
                                 qq = s;
@@ -212,7 +225,6 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                     }
                 }
                 if (!terminal) {
-                    q = T.nf[v];
                     int b = nb(q);
                     if (b >= 0) {
                         int ptr = na(q);
@@ -226,6 +238,8 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                                 if (WRITE) {
                                     ii[base + count] = i;
                                     jj[base + count] = T.bbi[j];
+                                } else if (sp_out && count < spec_cap) {
+                                    sp_out[count] = (int)T.bbi[j];
                                 }
                                 count++;
                             }
@@ -233,13 +247,11 @@ __global__ void __launch_bounds__(256) k_boxes(TreeQ T, const double4* __restric
                         terminal = true;
                     }
                 }
-            } else {
-                q = T.nf[v];  // back from a child: an internal node, not contained
             }
             int first = -1, second = -1;
             if (!terminal) {
                 int dim = -1 - nb(q);
-                double2 d = T.nd[v];
+                const double2 d = nd_v;
                 bool left, right;
                 if (keys) {
                     left = (dim ? ky0 : kx0) <= fkey(d.x);
@@ -308,6 +320,23 @@ __global__ void __launch_bounds__(256) k_box_jobs(const BoxJob* __restrict__ job
             jj[J.out + o] = bbi[p];
         }
         if (bad) set_error(err, CT_DEVERR_LOOP);
+    }
+}
+
+// Pairs of the boxes whose count fits the speculative scratch: one thread per
+// scratch slot, box-major, so the writes of a box's pairs are contiguous.
+__global__ void k_boxes_spec_emit(const int64_t* __restrict__ cnt, const int64_t* __restrict__ off, int64_t n,
+                                  const int* __restrict__ spec, int cap, int64_t* __restrict__ ii,
+                                  int64_t* __restrict__ jj) {
+    const int64_t total = n * (int64_t)cap;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k / cap;
+        const int c = (int)(k - i * cap);
+        const int64_t m = cnt[i];
+        if (m > cap || c >= m) continue;
+        ii[off[i] + c] = i;
+        jj[off[i] + c] = spec[k];
     }
 }
 
@@ -433,12 +462,11 @@ __device__ __forceinline__ void edge_leaf(const TreeQ& T, float4 q, dpt a, dpt b
 
 // Children of internal node v the segment's traversal enters (locate_edge
 // query.py:410-441): `first` is visited first (the right child when both).
-__device__ __forceinline__ void edge_children(const TreeQ& T, int v, float4 q, dpt a, dpt b, dpt V, bool keys,
+__device__ __forceinline__ void edge_children(const TreeQ& T, double2 nd, float4 q, dpt a, dpt b, dpt V, bool keys,
                                               unsigned long long kax, unsigned long long kay,
                                               unsigned long long kbx, unsigned long long kby, int* first,
                                               int* second) {
     int dim = -1 - nb(q);
-    double2 nd = T.nd[v];
     double dx = dim ? V.y : V.x;
     bool left, right;
     if (keys) {
@@ -515,11 +543,13 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
         --sp;
         const int v = st[sp];
         const int depth = CUT ? sd[sp] : 0;
+        // the node's records loaded together (one round trip per node)
+        const float4 q = T.nf[v];
+        const double2 nd_v = T.nd[v];
         if (LF.on) {
             const float4 nbx = *reinterpret_cast<const float4*>(T.nbx + v);
             if (line_misses(LF, nbx.x, nbx.y, nbx.z, nbx.w)) continue;
         }
-        float4 q = T.nf[v];
         const bool terminal = nb(q) >= 0;
         if (CUT && (terminal || depth >= cut)) {
             if (WRITE) {
@@ -534,7 +564,7 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
             continue;
         }
         int first, second;
-        edge_children(T, v, q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
+        edge_children(T, nd_v, q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
         if (sp + 2 > STK) {
             set_error(T.err, CT_DEVERR_STACK);
             break;
@@ -589,7 +619,8 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
                 const bool terminal = nb(q) >= 0;
                 if (terminal && down)
                     edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj);
-                if (!terminal) edge_children(T, v, q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
+                if (!terminal)
+                    edge_children(T, T.nd[v], q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
                 int next = terminal ? -1 : (down ? first : ((from == first) ? second : -1));
                 from = dv;
                 if (next >= 0) {
@@ -1650,6 +1681,61 @@ int ct_write_boxes_ws(const ct_tree* t, const double* boxes, int64_t n, const in
                                                             ii, jj, jobs, njobs, cap, jm);
     k_box_jobs<<<152 * 8, 256, 0, st>>>(jobs, njobs, cap, T.lstart, T.bbi, ii, jj, T.err);
     CT_CHECK_LAUNCH("write_boxes");
+    return CT_OK;
+}
+
+int ct_count_boxes_spec(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order, int64_t* counts,
+                        int32_t* spec, int32_t spec_cap, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (!spec || spec_cap < 1 || spec_cap > 4096) return ct_fail(CT_ERR_ARG, "spec_cap must be in [1, 4096]");
+    if (t->n_elements >= INT32_MAX) return ct_fail(CT_ERR_ARG, "tree size out of range");
+    const int bt = box_threads(t);
+    cudaStream_t st = (cudaStream_t)stream;
+    const TreeQ T = make_q(t);
+    const double4* B = (const double4*)boxes;
+    if (deep_tree(t))
+        k_boxes<false, true><<<grid_of(n, bt), bt, 0, st>>>(T, B, n, order, counts, nullptr, nullptr, nullptr, nullptr,
+                                                            0, BOX_JOB_MIN, spec, spec_cap, nullptr);
+    else
+        k_boxes<false, false><<<grid_of(n, bt), bt, 0, st>>>(T, B, n, order, counts, nullptr, nullptr, nullptr,
+                                                             nullptr, 0, BOX_JOB_MIN, spec, spec_cap, nullptr);
+    CT_CHECK_LAUNCH("count_boxes_spec");
+    return CT_OK;
+}
+
+int ct_write_boxes_spec(const ct_tree* t, const double* boxes, int64_t n, const int32_t* order,
+                        const int64_t* counts, const int64_t* offsets, const int32_t* spec, int32_t spec_cap,
+                        int64_t total_pairs, int32_t min_job_cells, int64_t* ii, int64_t* jj, void* ws,
+                        size_t ws_bytes, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (!spec || spec_cap < 1 || spec_cap > 4096) return ct_fail(CT_ERR_ARG, "spec_cap must be in [1, 4096]");
+    if (total_pairs < 0) return ct_fail(CT_ERR_ARG, "negative pair count");
+    if (!ws || ws_bytes < ct_write_boxes_workspace_size(total_pairs, min_job_cells))
+        return ct_fail(CT_ERR_WORKSPACE, "write_boxes workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    const TreeQ T = make_q(t);
+    k_boxes_spec_emit<<<(unsigned)std::min<int64_t>(grid_of(n * (int64_t)spec_cap, 256), 152 * 16), 256, 0, st>>>(
+        counts, offsets, n, spec, spec_cap, ii, jj);
+    const int jm = box_job_min(min_job_cells);
+    unsigned long long* njobs = (unsigned long long*)ws;
+    BoxJob* jobs = T.nbx ? (BoxJob*)((char*)ws + 256) : nullptr;
+    const int64_t cap = (total_pairs > 0 ? total_pairs : 0) / jm + 1;
+    CT_CUDA(cudaMemsetAsync(njobs, 0, sizeof(unsigned long long), st));
+    const int bt = box_threads(t);
+    const double4* B = (const double4*)boxes;
+    int64_t* off = (int64_t*)offsets;
+    if (deep_tree(t))
+        k_boxes<true, true><<<grid_of(n, bt), bt, 0, st>>>(T, B, n, order, off, ii, jj, jobs, njobs, cap, jm,
+                                                           nullptr, spec_cap, counts);
+    else
+        k_boxes<true, false><<<grid_of(n, bt), bt, 0, st>>>(T, B, n, order, off, ii, jj, jobs, njobs, cap, jm,
+                                                            nullptr, spec_cap, counts);
+    if (jobs) k_box_jobs<<<152 * 8, 256, 0, st>>>(jobs, njobs, cap, T.lstart, T.bbi, ii, jj, T.err);
+    CT_CHECK_LAUNCH("write_boxes_spec");
     return CT_OK;
 }
 

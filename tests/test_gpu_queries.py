@@ -208,9 +208,12 @@ def test_split_segment_traversal_matches_uncut(oracle):
 
 def test_box_subtree_jobs_match_inline(oracle):
     """Subtrees wholly inside a query box written by one warp per subtree
-    after the traversal (ct_write_boxes_ws) give the pairs the box's own
-    thread writes in line (ct_write_boxes) and the oracle's: big boxes over
-    whole subtrees, small ones, boxes beyond the mesh, cells_per_leaf 1-3."""
+    after the traversal (ct_write_boxes_ws), and small batches counted and
+    written in one traversal with a per-box scratch (ct_count_boxes_spec /
+    ct_write_boxes_spec, a scratch of 3 pairs forcing most boxes through the
+    second traversal), give the pairs the box's own thread writes in line
+    (ct_write_boxes) and the oracle's: big boxes over whole subtrees, small
+    ones, boxes beyond the mesh, cells_per_leaf 1-3."""
     import ctypes
 
     import torch
@@ -223,11 +226,13 @@ def test_box_subtree_jobs_match_inline(oracle):
         np.array([[-10.0, 100.0, -10.0, 80.0], [0.0, 90.0, 0.0, 70.0], [40.0, 40.5, 30.0, 30.5]]),
     ])
     bd = torch.as_tensor(boxes, device="cuda")
-    for cpl in (1, 2, 3):
+    for cpl, spec_max, spec_cap in ((1, 0, 64), (2, 0, 64), (3, 0, 64), (2, 1 << 16, 64), (1, 1 << 16, 3)):
         g = CellTree2d(xy, f, -1, 4, cpl)
         t = g._tree
         t.BOX_JOBS_MIN_PAIRS = 0  # the queued path at any size
-        ii, jj = t.locate_boxes(bd, {"threads": 256, "work_order": cpl == 2})
+        t.SPEC_MAX_BOXES = spec_max  # 0: two traversals; else one, with SPEC_CAP pairs kept per box
+        t.SPEC_CAP = spec_cap
+        ii, jj = t.locate_boxes(bd, {"threads": 256, "work_order": cpl == 2, "job_cells": 8 * cpl})
         n = len(boxes)
         counts = t.count_boxes(bd)
         offsets, total = t.scan(counts)
@@ -236,7 +241,7 @@ def test_box_subtree_jobs_match_inline(oracle):
         j2 = torch.empty_like(jj)
         _lib.check(_lib.load().ct_write_boxes(ctypes.byref(t.desc), _device.ptr(bd), n, None, _device.ptr(offsets),
                                               _device.ptr(i2), _device.ptr(j2), _device.stream()), "inline")
-        assert torch.equal(ii, i2) and torch.equal(jj, j2), cpl
+        assert torch.equal(ii, i2) and torch.equal(jj, j2), (cpl, spec_max, spec_cap)
         o = oracle.OracleCellTree2d(xy, f, -1, 4, cpl)
         for a, b in zip((ii, jj), o.locate_boxes(boxes)):
             same(a.cpu().numpy(), b)
