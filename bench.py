@@ -546,6 +546,9 @@ def query_suite(args, c5=None, verbose=False):
     ro, tc = cpu(lambda: ot.intersect_faces(qxy, qf[:m], -1))
     record("C4", "intersect_faces", len(qf), "faces", tg, m, tc, same_multi(first_queries(host(r), m), ro),
            results=int(r[0].shape[0]), bytes_q=8 * 3 + 16 * len(qxy) / len(qf), bytes_r=24)
+    adjoint = adjoint_check(tree, qxy, qf, wall)
+    if verbose:
+        print(json.dumps({"adjoint": adjoint}), flush=True)
     bp = syn.uniform_points(1_000_000, txy.min(0), txy.max(0), seed=6)
     bpd = torch.as_tensor(bp, device=dev)
     r, tg = wall(lambda: tree.compute_barycentric_weights(bpd))
@@ -568,7 +571,93 @@ def query_suite(args, c5=None, verbose=False):
     return {"summary": "build and every query vs the oracle on the survey shapes", "host_cores": cores,
             "min_speedup": min(x["speedup"] for x in rows),
             "min_speedup_multi_result": min(x["speedup"] for x in multi),
-            "all_identical": all(x["identical_on_sample"] for x in rows), "rows": rows}
+            "all_identical": all(x["identical_on_sample"] for x in rows), "adjoint_C4": adjoint, "rows": rows}
+
+
+def adjoint_check(tree, qxy, qf, wall, n_samples=10_000, h=1e-6, seed=9):
+    """The adjoint of intersect_faces at the C4 scale (no upstream
+    counterpart): time of the forward + backward pass over every candidate
+    pair, and central differences at n_samples sampled vertex coordinates
+    (both meshes) against the gradient.  The samples are chosen so that no
+    pair touches two of them; all are then perturbed at once and each pair's
+    change is summed into its sample, so four forward passes (+-h, +-h/2)
+    check every sample.  A sample whose two quotients disagree by more than
+    1e-4 (a vertex crossing another mesh's edge line within h) is counted as
+    a kink and set aside."""
+    import torch
+
+    from numba_celltree_gb300 import autodiff
+
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(seed)
+    ClipArea = autodiff._functions()[0]
+    t = tree._tree
+    v = torch.tensor(qxy, device=dev)
+    tv = t.vertices.clone()
+    v_d, f_d = tree._faces_on_device(v, qf)
+    ii, jj = tree._locate_faces_dev(v_d, f_d)
+    err, te = t.error_word, t.elements
+    n = int(ii.shape[0])
+    gw = torch.tensor(rng.normal(size=n), device=dev)
+    vg, tvg = v.clone().requires_grad_(True), tv.clone().requires_grad_(True)
+
+    def fwd_bwd():
+        return torch.autograd.grad((ClipArea.apply(vg, tvg, f_d, te, ii, jj, err) * gw).sum(), [vg, tvg])
+
+    (gv, gtv), t_fb = wall(fwd_bwd)
+    _, t_f = wall(lambda: ClipArea.apply(v, tv, f_d, te, ii, jj, err))
+    # pairs of every vertex of either mesh (CSR), then a greedy choice of
+    # vertices whose pair sets are disjoint
+    iih, jjh = ii.cpu().numpy(), jj.cpu().numpy()
+    qfh, tfh = f_d.cpu().numpy(), te.cpu().numpy()
+    nq = len(qxy)
+    verts = np.concatenate([qfh[iih].reshape(-1), nq + tfh[jjh].reshape(-1)])
+    pair_of = np.concatenate([np.repeat(np.arange(n), qfh.shape[1]), np.repeat(np.arange(n), tfh.shape[1])])
+    ok = verts >= 0
+    ok[len(iih) * qfh.shape[1]:] &= tfh[jjh].reshape(-1) >= 0
+    verts, pair_of = verts[ok], pair_of[ok]
+    o = np.argsort(verts, kind="stable")
+    verts, pair_of = verts[o], pair_of[o]
+    uv, start = np.unique(verts, return_index=True)
+    end = np.append(start[1:], len(verts))
+    owner = np.full(n, -1, dtype=np.int64)
+    chosen = []
+    for c in rng.permutation(len(uv)):
+        ps = pair_of[start[c]:end[c]]
+        if (owner[ps] >= 0).any():
+            continue
+        owner[ps] = len(chosen)
+        chosen.append((int(uv[c]), int(rng.integers(0, 2))))
+        if len(chosen) == n_samples:
+            break
+    ks = np.array([k for k, _ in chosen])
+    cs = np.array([c for _, c in chosen])
+    isq = ks < nq
+    owned = owner >= 0
+    own_d = torch.as_tensor(owner[owned], device=dev)
+    sel_d = torch.as_tensor(np.nonzero(owned)[0], device=dev)
+    fd = []
+    with torch.no_grad():
+        for hh in (h, 0.5 * h):
+            vals = []
+            for sgn in (1.0, -1.0):
+                vp, tvp = v.clone(), tv.clone()
+                vp[torch.as_tensor(ks[isq], device=dev), torch.as_tensor(cs[isq], device=dev)] += sgn * hh
+                tvp[torch.as_tensor(ks[~isq] - nq, device=dev), torch.as_tensor(cs[~isq], device=dev)] += sgn * hh
+                vals.append(ClipArea.apply(vp, tvp, f_d, te, ii, jj, err) * gw)
+            d = ((vals[0] - vals[1]) / (2 * hh))[sel_d]
+            fd.append(torch.zeros(len(chosen), dtype=torch.float64, device=dev).index_add_(0, own_d, d).cpu().numpy())
+    an = np.where(isq, gv.detach().cpu().numpy()[np.minimum(ks, nq - 1), cs],
+                  gtv.detach().cpu().numpy()[np.maximum(ks - nq, 0), cs])
+    scale = np.maximum(1.0, np.abs(an))
+    kink = np.abs(fd[0] - fd[1]) > 1e-4 * scale
+    rel = np.abs(fd[0] - an) / scale
+    good = ~kink
+    return {"pairs": n, "forward_ms": round(t_f * 1e3, 3), "forward_backward_ms": round(t_fb * 1e3, 3),
+            "fd_samples": len(chosen), "fd_h": h, "query_vertex_samples": int(isq.sum()),
+            "kinks": int(kink.sum()), "max_rel_err": float(rel[good].max()) if good.any() else None,
+            "within_1e-6": bool((rel[good] <= 1e-6).all()),
+            "check": "central differences of sum(g * area) at h and h/2, g ~ N(0, 1), indices held fixed"}
 
 
 def query_profile(args):
