@@ -518,6 +518,18 @@ int ct_count_edge_candidates(const ct_tree* tree, int32_t mode, const double* se
                               int64_t* counts, void* stream);
 int ct_write_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, int64_t n, const int32_t* order,
                               const int64_t* offsets, int32_t* cand_seg, int32_t* cand_pos, void* stream);
+/* One traversal for most segments (no upstream counterpart): the counting
+ * pass also keeps each segment's first spec_cap candidates (leaf positions,
+ * traversal order) in spec (n x spec_cap int32, 1 <= spec_cap <= 4096); the
+ * writing call copies the segments whose count fits from spec and traverses
+ * again only for the others.  Same candidates as the uncut pair above. */
+int ct_count_edge_candidates_spec(const ct_tree* tree, int32_t mode, const double* segs, int64_t n,
+                                  const int32_t* order, int64_t* counts, int32_t* spec, int32_t spec_cap,
+                                  void* stream);
+int ct_write_edge_candidates_spec(const ct_tree* tree, int32_t mode, const double* segs, int64_t n,
+                                  const int32_t* order, const int64_t* counts, const int64_t* offsets,
+                                  const int32_t* spec, int32_t spec_cap, int32_t* cand_seg, int32_t* cand_pos,
+                                  void* stream);
 /* The same candidates with each segment's traversal split across threads
  * (no upstream counterpart; a long segment's traversal otherwise runs on one
  * thread).  ct_count/write_edge_items cut every segment's traversal `cut`

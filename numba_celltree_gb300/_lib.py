@@ -211,6 +211,9 @@ SIGNATURES = {
     "ct_count_boxes_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _I32, _P]),
     "ct_write_boxes_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _I64, _P, _P, _P, _P, _I32, _I64, _I32, _P, _P,
                                            _P, ctypes.c_size_t, _P]),
+    "ct_count_edge_candidates_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _I32, _P]),
+    "ct_write_edge_candidates_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _I32, _P,
+                                                     _P, _P]),
     "ct_count_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P]),
     "ct_write_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P, _P, _P]),
     "ct_count_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P]),

@@ -508,10 +508,17 @@ class _GpuTree:
             return None
         return max(1, min(self.max_depth, int(np.ceil(np.log2(self.n / split)))))
 
-    def edge_candidate_ranges(self, segs_d, mode: int, order, cut):
+    # uncut batches up to this many segments keep each segment's first
+    # SPEC_CAP candidates in the counting pass (one traversal for most)
+    SPEC_MAX_SEGMENTS = 1 << 22
+    SPEC_CAP = 64
+
+    def edge_candidate_ranges(self, segs_d, mode: int, order, cut, keep: bool = False):
         """Every segment's candidate offset and count (device int64) and the
-        candidate total; with a cut, also the work items the writing pass
-        uses: (coff, ccnt, total, items)."""
+        candidate total, and what the writing pass uses: (coff, ccnt, total,
+        items) -- items None (traverse again), ("spec", scratch) with `keep`
+        (the counting pass kept each segment's first candidates), or with a
+        cut the work items (item_seg, item_node, n_items, item offsets)."""
         torch = _device.torch()
         lib = _lib.load()
         st = _device.stream()
@@ -520,6 +527,12 @@ class _GpuTree:
         d = ctypes.byref(self.desc)
         if cut is None:
             ccnt = _device.empty((n,), torch.int64, self.device)
+            if keep and 0 < n <= self.SPEC_MAX_SEGMENTS:
+                spec = _device.empty((n, self.SPEC_CAP), torch.int32, self.device)
+                _lib.check(lib.ct_count_edge_candidates_spec(d, mode, P(segs_d), n, P(order), P(ccnt), P(spec),
+                                                             self.SPEC_CAP, st), "intersect_edges")
+                coff, nc = self.scan(ccnt)
+                return coff, ccnt, nc, ("spec", spec)
             _lib.check(lib.ct_count_edge_candidates(d, mode, P(segs_d), n, P(order), P(ccnt), st), "intersect_edges")
             coff, nc = self.scan(ccnt)
             return coff, ccnt, nc, None
@@ -666,7 +679,7 @@ class _GpuTree:
         self._apply("segments", config)
         order = self.work_order(segs_d, 1, config.get("work_order"))
         P = _device.ptr
-        coff, ccnt, nc, items = self.edge_candidate_ranges(segs_d, mode, order, self.edge_cut(config, n))
+        coff, ccnt, nc, items = self.edge_candidate_ranges(segs_d, mode, order, self.edge_cut(config, n), keep=True)
         if budget is not None and nc > budget:
             self.last_counts = ccnt
             return None
@@ -675,6 +688,11 @@ class _GpuTree:
         if items is None:
             _lib.check(lib.ct_write_edge_candidates(ctypes.byref(self.desc), mode, P(segs_d), n, P(order), P(coff),
                                                     P(cseg), P(cpos), st), "intersect_edges")
+        elif isinstance(items[0], str):
+            _lib.check(lib.ct_write_edge_candidates_spec(ctypes.byref(self.desc), mode, P(segs_d), n, P(order),
+                                                         P(ccnt), P(coff), P(items[1]), self.SPEC_CAP, P(cseg),
+                                                         P(cpos), st), "intersect_edges")
+            del items
         else:
             iseg, inode, ni, icoff = items
             _lib.check(lib.ct_write_item_candidates(ctypes.byref(self.desc), mode, P(segs_d), P(iseg), P(inode), ni,

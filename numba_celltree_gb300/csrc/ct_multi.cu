@@ -340,6 +340,22 @@ __global__ void k_boxes_spec_emit(const int64_t* __restrict__ cnt, const int64_t
     }
 }
 
+// Candidates of the segments whose count fits the counting pass's scratch.
+__global__ void k_edge_spec_emit(const int64_t* __restrict__ cnt, const int64_t* __restrict__ off, int64_t n,
+                                 const int* __restrict__ spec, int cap, int* __restrict__ cseg,
+                                 int* __restrict__ cpos) {
+    const int64_t total = n * (int64_t)cap;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k / cap;
+        const int c = (int)(k - i * cap);
+        const int64_t m = cnt[i];
+        if (m > cap || c >= m) continue;
+        cseg[off[i] + c] = (int)i;
+        cpos[off[i] + c] = spec[k];
+    }
+}
+
 // ---------------------------------------------------------------------------
 // locate_edge query.py:357-455 with compute_edge_edge_intersect (292-306,
 // mode 0) or compute_edge_face_intersect (309-328, mode 1)
@@ -429,7 +445,7 @@ template <bool WRITE, int MODE>
 __device__ __forceinline__ void edge_leaf(const TreeQ& T, float4 q, dpt a, dpt b, bool keys, unsigned long long kax,
                                           unsigned long long kay, unsigned long long kbx, unsigned long long kby,
                                           int64_t i, int64_t base, int64_t& count, int* __restrict__ cseg,
-                                          int* __restrict__ cj, const LineF* lf = nullptr) {
+                                          int* __restrict__ cj, const LineF* lf = nullptr, int spcap = 0) {
     int ptr = na(q), bq = nb(q);
     for (int j = ptr; j < ptr + bq; j++) {
         if (lf && lf->on) {
@@ -454,6 +470,8 @@ __device__ __forceinline__ void edge_leaf(const TreeQ& T, float4 q, dpt a, dpt b
             if (WRITE) {
                 cseg[base + count] = (int)i;
                 cj[base + count] = j;
+            } else if (count < spcap) {
+                cj[count] = j;  // counting pass: the segment's scratch row
             }
             count++;
         }
@@ -524,7 +542,8 @@ __device__ __forceinline__ EdgeKeys edge_keys(const TreeQ& T, dpt a, dpt b) {
 // traversal's.
 template <bool WRITE, int MODE, bool CUT>
 __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_t i, int start, int cut,
-                                            int64_t base, int* __restrict__ cseg, int* __restrict__ cj) {
+                                            int64_t base, int* __restrict__ cseg, int* __restrict__ cj,
+                                            int spcap = 0) {
     const dpt V = vsub(b, a);
     const EdgeKeys K = edge_keys(T, a, b);
     const LineF LF = line_filter(T, a, b, V, K.keys);
@@ -560,7 +579,8 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
             continue;
         }
         if (terminal) {
-            edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj, &LF);
+            edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj, &LF,
+                                   spcap);
             continue;
         }
         int first, second;
@@ -584,13 +604,20 @@ __device__ __forceinline__ int64_t edge_dfs(const TreeQ& T, dpt a, dpt b, int64_
     return count;
 }
 
+// spcap > 0: in the counting pass cj is a scratch of spcap entries per
+// segment that keeps its first candidates; in the writing pass spec_cnt
+// holds the counts and segments whose candidates fit were copied from the
+// scratch (k_edge_spec_emit), so they return at once.
 template <bool WRITE, int MODE, bool DEEP>
 __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __restrict__ segs, int64_t n,
                                                     const int* __restrict__ order, int64_t* __restrict__ cnt_or_off,
-                                                    int* __restrict__ cseg, int* __restrict__ cj) {
+                                                    int* __restrict__ cseg, int* __restrict__ cj, int spcap = 0,
+                                                    const int64_t* __restrict__ spec_cnt = nullptr) {
     int64_t tq = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (tq >= n) return;
     int64_t i = order ? (int64_t)order[tq] : tq;
+    if (WRITE && spec_cnt && spec_cnt[i] <= spcap) return;
+    if (!WRITE && spcap > 0) cj += i * (int64_t)spcap;
     double4 s4 = segs[i];
     dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
     int64_t count = 0;
@@ -600,7 +627,7 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
     if (r < 0) set_error(T.err, CT_DEVERR_LOOP);
     if (r == 1) {
         if (!DEEP) {
-            count = edge_dfs<WRITE, MODE, false>(T, a, b, i, 0, -1, base, cseg, cj);
+            count = edge_dfs<WRITE, MODE, false>(T, a, b, i, 0, -1, base, cseg, cj, WRITE ? 0 : spcap);
         } else {
             // depth-first walk through the parent links (see k_boxes)
             const dpt V = vsub(b, a);
@@ -618,7 +645,8 @@ __global__ void __launch_bounds__(128) k_edge_cands(TreeQ T, const double4* __re
                 int first = -1, second = -1;
                 const bool terminal = nb(q) >= 0;
                 if (terminal && down)
-                    edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj);
+                    edge_leaf<WRITE, MODE>(T, q, a, b, K.keys, K.kax, K.kay, K.kbx, K.kby, i, base, count, cseg, cj,
+                                           nullptr, WRITE ? 0 : spcap);
                 if (!terminal)
                     edge_children(T, T.nd[v], q, a, b, V, K.keys, K.kax, K.kay, K.kbx, K.kby, &first, &second);
                 int next = terminal ? -1 : (down ? first : ((from == first) ? second : -1));
@@ -2036,6 +2064,64 @@ int ct_segment_candidate_ranges(const int64_t* item_off, const int64_t* item_cnt
     k_seg_from_items<<<(unsigned)std::min<int64_t>(grid_of(n, 256), 152 * 32), 256, 0, st>>>(
         item_off, item_cnt, n, item_cand_off, item_cand_cnt, n_items, cand_off, cand_cnt);
     CT_CHECK_LAUNCH("segment_candidate_ranges");
+    return CT_OK;
+}
+
+int ct_count_edge_candidates_spec(const ct_tree* t, int32_t mode, const double* segs, int64_t n,
+                                  const int32_t* order, int64_t* counts, int32_t* spec, int32_t spec_cap,
+                                  void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (mode != 0 && mode != 1) return ct_fail(CT_ERR_ARG, "mode must be 0 or 1");
+    if (mode == 0 && t->n_max_vert != 2) return ct_fail(CT_ERR_ARG, "edge-edge mode needs an edge tree");
+    if (!spec || spec_cap < 1 || spec_cap > 4096) return ct_fail(CT_ERR_ARG, "spec_cap must be in [1, 4096]");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    const int et = seg_threads(t);
+    const double4* S = (const double4*)segs;
+    const unsigned g = grid_of(n, et);
+    if (deep_tree(t)) {
+        if (mode == 0) k_edge_cands<false, 0, true><<<g, et, 0, st>>>(T, S, n, order, counts, 0, spec, spec_cap);
+        else k_edge_cands<false, 1, true><<<g, et, 0, st>>>(T, S, n, order, counts, 0, spec, spec_cap);
+    } else {
+        if (mode == 0) k_edge_cands<false, 0, false><<<g, et, 0, st>>>(T, S, n, order, counts, 0, spec, spec_cap);
+        else k_edge_cands<false, 1, false><<<g, et, 0, st>>>(T, S, n, order, counts, 0, spec, spec_cap);
+    }
+    CT_CHECK_LAUNCH("count_edge_candidates_spec");
+    return CT_OK;
+}
+
+int ct_write_edge_candidates_spec(const ct_tree* t, int32_t mode, const double* segs, int64_t n,
+                                  const int32_t* order, const int64_t* counts, const int64_t* offsets,
+                                  const int32_t* spec, int32_t spec_cap, int32_t* cand_seg, int32_t* cand_pos,
+                                  void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n == 0) return CT_OK;
+    if (n > INT32_MAX) return ct_fail(CT_ERR_ARG, "at most 2^31 - 1 segments");
+    if (mode != 0 && mode != 1) return ct_fail(CT_ERR_ARG, "mode must be 0 or 1");
+    if (!spec || spec_cap < 1 || spec_cap > 4096) return ct_fail(CT_ERR_ARG, "spec_cap must be in [1, 4096]");
+    cudaStream_t st = (cudaStream_t)stream;
+    TreeQ T = make_q(t);
+    k_edge_spec_emit<<<(unsigned)std::min<int64_t>(grid_of(n * (int64_t)spec_cap, 256), 152 * 16), 256, 0, st>>>(
+        counts, offsets, n, spec, spec_cap, cand_seg, cand_pos);
+    const int et = seg_threads(t);
+    const double4* S = (const double4*)segs;
+    const unsigned g = grid_of(n, et);
+    int64_t* off = (int64_t*)offsets;
+    if (deep_tree(t)) {
+        if (mode == 0)
+            k_edge_cands<true, 0, true><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos, spec_cap, counts);
+        else
+            k_edge_cands<true, 1, true><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos, spec_cap, counts);
+    } else {
+        if (mode == 0)
+            k_edge_cands<true, 0, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos, spec_cap, counts);
+        else
+            k_edge_cands<true, 1, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos, spec_cap, counts);
+    }
+    CT_CHECK_LAUNCH("write_edge_candidates_spec");
     return CT_OK;
 }
 

@@ -166,6 +166,14 @@ def test_split_segment_traversal_matches_uncut(oracle):
     exp = o.intersect_edges(segs)
     for a, b in zip(base, exp):
         same(a.cpu().numpy(), b)
+    # uncut, without the counting pass's scratch, and with a scratch of 2
+    # candidates (most segments through the second traversal)
+    for spec_max, spec_cap in ((0, 64), (1 << 22, 2)):
+        t.SPEC_MAX_SEGMENTS, t.SPEC_CAP = spec_max, spec_cap
+        got = t.locate_edges(sd, 1, {"threads": 64, "work_order": True, "split": 0})
+        for a, b in zip(got, base):
+            assert teq(a, b), (spec_max, spec_cap)
+    del t.SPEC_MAX_SEGMENTS, t.SPEC_CAP
     counts0 = t.count_edge_candidates(sd, 1)
     for split in (2, 7, 64, 1024):
         cfg = {"threads": 128, "work_order": split == 7, "split": split}
