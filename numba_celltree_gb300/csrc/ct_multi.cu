@@ -851,6 +851,153 @@ __device__ __forceinline__ bool cyrus_beck_f32(dpt a, dpt b, const dpt* poly, in
     return false;
 }
 
+// ---------------------------------------------------------------------------
+// Cohen-Sutherland's verdict in float32 intervals (no upstream counterpart)
+// ---------------------------------------------------------------------------
+// cohen_sutherland() above is replayed in the cell's local frame (the float32
+// cell: its first vertex split hi + lo, the other vertices as offsets) on
+// intervals with directed rounding.  Every interval encloses the float64 value
+// upstream's code computes at that step: inputs enclose the exact local
+// coordinates, each operation's result is widened by the float64 rounding of
+// that operation (2^-51 of its magnitude, plus 2^-50 of the largest absolute
+// coordinate where the result is an absolute coordinate).  When every outcode
+// test and every dx == dy == 0 test is decided for the whole interval, the
+// float64 run takes the same path, so its verdict is known: 1 accept, 0
+// reject; -1 when any test is undecided (the caller runs the float64 clip).
+// Only the verdict is used: upstream overwrites the clipped points with
+// Cyrus-Beck's.
+struct FI {
+    float lo, hi;
+};
+__device__ __forceinline__ FI fi_sub(FI a, FI b) { return FI{__fsub_rd(a.lo, b.hi), __fsub_ru(a.hi, b.lo)}; }
+__device__ __forceinline__ FI fi_add(FI a, FI b) { return FI{__fadd_rd(a.lo, b.lo), __fadd_ru(a.hi, b.hi)}; }
+__device__ __forceinline__ FI fi_mul(FI a, FI b) {
+    const float l = fminf(fminf(__fmul_rd(a.lo, b.lo), __fmul_rd(a.lo, b.hi)),
+                          fminf(__fmul_rd(a.hi, b.lo), __fmul_rd(a.hi, b.hi)));
+    const float h = fmaxf(fmaxf(__fmul_ru(a.lo, b.lo), __fmul_ru(a.lo, b.hi)),
+                          fmaxf(__fmul_ru(a.hi, b.lo), __fmul_ru(a.hi, b.hi)));
+    return FI{l, h};
+}
+// b must exclude 0
+__device__ __forceinline__ FI fi_div(FI a, FI b) {
+    const float l = fminf(fminf(__fdiv_rd(a.lo, b.lo), __fdiv_rd(a.lo, b.hi)),
+                          fminf(__fdiv_rd(a.hi, b.lo), __fdiv_rd(a.hi, b.hi)));
+    const float h = fmaxf(fmaxf(__fdiv_ru(a.lo, b.lo), __fdiv_ru(a.lo, b.hi)),
+                          fmaxf(__fdiv_ru(a.hi, b.lo), __fdiv_ru(a.hi, b.hi)));
+    return FI{l, h};
+}
+__device__ __forceinline__ bool fi_ok(FI a) { return isfinite(a.lo) && isfinite(a.hi) && a.lo <= a.hi; }
+__device__ __forceinline__ bool fi_has0(FI a) { return !(a.lo > 0.0f || a.hi < 0.0f); }
+// float64 rounding of one operation: 2^-51 of the result's magnitude, plus
+// `w` (2^-50 of the largest absolute coordinate) for absolute coordinates
+__device__ __forceinline__ FI fi_round(FI a, float w) {
+    const float e = __fadd_ru(__fmul_ru(fmaxf(fabsf(a.lo), fabsf(a.hi)), 0x1p-51f), w + 0x1p-126f);
+    return FI{__fsub_rd(a.lo, e), __fadd_ru(a.hi, e)};
+}
+
+// Outcode of an interval point (-1: undecided); a coordinate set to a box
+// side (tag >= 0) is exactly that side.
+__device__ __forceinline__ int fi_code(FI x, FI y, int tx, int ty, const FI* B) {
+    int p = 0;
+    if (tx < 0) {
+        if (x.hi < B[0].lo) p |= CS_LEFT;
+        else if (x.lo >= B[0].hi && x.lo > B[1].hi) p |= CS_RIGHT;
+        else if (!(x.lo >= B[0].hi && x.hi <= B[1].lo)) return -1;
+    }
+    if (ty < 0) {
+        if (y.hi < B[2].lo) p |= CS_LOWER;
+        else if (y.lo >= B[2].hi && y.lo > B[3].hi) p |= CS_UPPER;
+        else if (!(y.lo >= B[2].hi && y.hi <= B[3].lo)) return -1;
+    }
+    return p;
+}
+
+__device__ __forceinline__ int cs_f32(dpt a, dpt b, const dbox& box, const float4* __restrict__ cellf, int len32,
+                                      float dabs) {
+    // non-finite endpoints and cells of fewer than two distinct vertices
+    // (no float32 frame) take the float64 clip
+    if (!(is_fin(a.x) && is_fin(a.y) && is_fin(b.x) && is_fin(b.y)) || len32 < 2) return -1;
+    // the exact tests on the inputs, as upstream
+    if (g_eq_finite(a.x, b.x) && g_eq_finite(a.y, b.y)) return 0;
+    int k1 = cs_code(a, box), k2 = cs_code(b, box);
+    if ((k1 | k2) == 0) return 1;
+    if ((k1 & k2) != 0) return 0;
+    // local frame: intervals of the endpoints and the box sides
+    const PtSplit Pa = split_point(a.x, a.y), Pb = split_point(b.x, b.y);
+    float ax, ay, ea, bx, by, eb;
+    local_delta(Pa, cellf[0], &ax, &ay, &ea);
+    local_delta(Pb, cellf[0], &bx, &by, &eb);
+    const float2* rel = reinterpret_cast<const float2*>(cellf + 1);
+    float x0 = 0.0f, x1 = 0.0f, y0 = 0.0f, y1 = 0.0f, vmax = 0.0f;
+    for (int i = 1; i < len32 && i < 8; i++) {
+        const float2 r = rel[i - 1];
+        x0 = fminf(x0, r.x);
+        x1 = fmaxf(x1, r.x);
+        y0 = fminf(y0, r.y);
+        y1 = fmaxf(y1, r.y);
+        vmax = fmaxf(vmax, fmaxf(fabsf(r.x), fabsf(r.y)));
+    }
+    // stored offsets: float32 roundings of the float64 differences
+    const float ev = __fadd_ru(__fmul_ru(vmax, 0x1p-22f), dabs + 0x1p-126f);
+    const float ep = fmaxf(ea, eb) + dabs + 0x1p-126f;
+    FI B[4] = {FI{__fsub_rd(x0, ev), __fadd_ru(x0, ev)}, FI{__fsub_rd(x1, ev), __fadd_ru(x1, ev)},
+               FI{__fsub_rd(y0, ev), __fadd_ru(y0, ev)}, FI{__fsub_rd(y1, ev), __fadd_ru(y1, ev)}};
+    FI Ax{__fsub_rd(ax, ep), __fadd_ru(ax, ep)}, Ay{__fsub_rd(ay, ep), __fadd_ru(ay, ep)};
+    FI Bx{__fsub_rd(bx, ep), __fadd_ru(bx, ep)}, By{__fsub_rd(by, ep), __fadd_ru(by, ep)};
+    int tax = -1, tay = -1, tbx = -1, tby = -1;
+    // 2^-50 of the largest absolute coordinate of the segment and the cell
+    const float C = fmaxf(fmaxf(fmaxf(fabsf(Pa.xh), fabsf(Pa.yh)), fmaxf(fabsf(Pb.xh), fabsf(Pb.yh))),
+                          fmaxf(fabsf(cellf[0].x), fabsf(cellf[0].z)) + vmax);
+    const float w = __fmul_ru(__fmul_ru(C, 1.0f + 0x1p-20f), 0x1p-50f);
+    if (!(fi_ok(Ax) && fi_ok(Ay) && fi_ok(Bx) && fi_ok(By) && isfinite(w))) return -1;
+    for (int iter = 0; iter < 8; iter++) {
+        if ((k1 | k2) == 0) return 1;
+        if ((k1 & k2) != 0) return 0;
+        const int opt = k1 ? k1 : k2;
+        const FI DX = fi_round(fi_sub(Bx, Ax), 0.0f), DY = fi_round(fi_sub(By, Ay), 0.0f);
+        FI x, y;
+        int tx = -1, ty = -1;
+        if (opt & (CS_UPPER | CS_LOWER)) {
+            if (fi_has0(DY)) return -1;
+            const int side = (opt & CS_UPPER) ? 3 : 2;
+            const FI t = fi_round(fi_div(fi_round(fi_mul(DX, fi_round(fi_sub(B[side], Ay), 0.0f)), 0.0f), DY), 0.0f);
+            x = fi_round(fi_add(Ax, t), w);
+            y = B[side];
+            ty = side;
+        } else {
+            if (fi_has0(DX)) return -1;
+            const int side = (opt & CS_RIGHT) ? 1 : 0;
+            const FI t = fi_round(fi_div(fi_round(fi_mul(DY, fi_round(fi_sub(B[side], Ax), 0.0f)), 0.0f), DX), 0.0f);
+            y = fi_round(fi_add(Ay, t), w);
+            x = B[side];
+            tx = side;
+        }
+        if (!(fi_ok(x) && fi_ok(y))) return -1;
+        if (opt == k1) {
+            Ax = x;
+            Ay = y;
+            tax = tx;
+            tay = ty;
+            k1 = fi_code(Ax, Ay, tax, tay, B);
+            if (k1 < 0) return -1;
+        } else {
+            Bx = x;
+            By = y;
+            tbx = tx;
+            tby = ty;
+            k2 = fi_code(Bx, By, tbx, tby, B);
+            if (k2 < 0) return -1;
+        }
+        // dx == 0 and dy == 0: equal coordinates are certain when both were
+        // set to the same box side, unequal when the intervals are disjoint
+        const bool xeq = tax >= 0 && tax == tbx, yeq = tay >= 0 && tay == tby;
+        const bool xne = Ax.hi < Bx.lo || Bx.hi < Ax.lo, yne = Ay.hi < By.lo || By.hi < Ay.lo;
+        if (xeq && yeq) return 0;
+        if (!(xne || yne)) return -1;
+    }
+    return -1;
+}
+
 // The float64 cell test of every candidate (compute_edge_face_intersect
 // query.py:309-328 / compute_edge_edge_intersect 292-306).
 template <int MODE>
@@ -871,8 +1018,12 @@ __global__ void __launch_bounds__(128) k_edge_test(TreeQ T, const double4* __res
             d = c;
         } else {
             dbox bx = leaf_box(T, j);
-            int rr = cohen_sutherland(a, b, bx, &c, &d);
-            if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
+            int rr = -1;
+            if (T.polyf && T.K <= 8) rr = cs_f32(a, b, bx, T.polyf + (size_t)j * T.S4, (int)T.plen32[j], T.dabs);
+            if (rr < 0) {
+                rr = cohen_sutherland(a, b, bx, &c, &d);
+                if (rr < 0) set_error(T.err, CT_DEVERR_LOOP);
+            }
             hit = rr == 1;
             if (hit) {
                 const dpt* poly = reinterpret_cast<const dpt*>(T.poly + (size_t)j * T.K);
