@@ -554,6 +554,15 @@ int ct_write_item_candidates(const ct_tree* tree, int32_t mode, const double* se
 int ct_segment_candidate_ranges(const int64_t* item_off, const int64_t* item_cnt, int64_t n,
                                 const int64_t* item_cand_off, const int64_t* item_cand_cnt, int64_t n_items,
                                 int64_t* cand_off, int64_t* cand_cnt, void* stream);
+/* Diagnostics for tests of the segment test's float32 certificates (face
+ * trees): per (segment, leaf position) pair, out[3t] = upstream's float64
+ * Cohen-Sutherland verdict (1 accept, 0 reject), out[3t+1] = the float32
+ * interval verdict used by ct_test_edge_candidates (1, 0, or -1 undecided),
+ * out[3t+2] = 1 when the traversal's line filter surely misses the cell's
+ * box (needs bb_leaf32).  A certificate is sound when out[3t+1] is -1 or
+ * equals out[3t], and out[3t+2] = 1 only where out[3t] = 0. */
+int ct_cs_certificates(const ct_tree* tree, const double* segs, const int32_t* cand_seg, const int32_t* cand_pos,
+                       int64_t n_cand, int8_t* out, void* stream);
 int ct_test_edge_candidates(const ct_tree* tree, int32_t mode, const double* segs, const int32_t* cand_seg,
                             const int32_t* cand_pos, int64_t n_cand, int64_t* keep, double* xy, void* stream);
 int ct_compact_edge_hits(const ct_tree* tree, const int64_t* keep, const int64_t* pos, int64_t n_cand,

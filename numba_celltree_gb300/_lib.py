@@ -214,6 +214,7 @@ SIGNATURES = {
     "ct_count_edge_candidates_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _I32, _P]),
     "ct_write_edge_candidates_spec": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _P, _P, _P, _I32, _P,
                                                      _P, _P]),
+    "ct_cs_certificates": (ctypes.c_int, [ctypes.POINTER(CtTree), _P, _P, _P, _I64, _P, _P]),
     "ct_count_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P]),
     "ct_write_edge_items": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _I64, _P, _I32, _P, _P, _P, _P]),
     "ct_count_item_candidates": (ctypes.c_int, [ctypes.POINTER(CtTree), _I32, _P, _P, _P, _I64, _P, _P]),

@@ -1041,6 +1041,34 @@ __global__ void __launch_bounds__(128) k_edge_test(TreeQ T, const double4* __res
     }
 }
 
+// Diagnostics of the segment test's float32 certificates (tests only): per
+// pair, upstream's float64 Cohen-Sutherland verdict (1 accept, 0 reject, -1
+// loop cap), the float32 interval verdict (cs_f32: 1, 0, -1 undecided) and
+// whether the traversal's line filter surely misses the cell's box (1/0; 0
+// when the filter is off).
+__global__ void k_cs_certificates(TreeQ T, const double4* __restrict__ segs, const int* __restrict__ cseg,
+                                  const int* __restrict__ cj, int64_t nc, int8_t* __restrict__ out) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nc; t += (int64_t)gridDim.x * blockDim.x) {
+        double4 s4 = segs[cseg[t]];
+        dpt a = mkp(s4.x, s4.y), b = mkp(s4.z, s4.w);
+        const int j = cj[t];
+        dbox bx = leaf_box(T, j);
+        dpt c, d;
+        out[3 * t] = (int8_t)cohen_sutherland(a, b, bx, &c, &d);
+        out[3 * t + 1] = (int8_t)((T.polyf && T.K <= 8)
+                                      ? cs_f32(a, b, bx, T.polyf + (size_t)j * T.S4, (int)T.plen32[j], T.dabs)
+                                      : -1);
+        const EdgeKeys K = edge_keys(T, a, b);
+        const LineF LF = line_filter(T, a, b, vsub(b, a), K.keys);
+        int miss = 0;
+        if (LF.on) {
+            const float4 q = T.bbl32[j];
+            miss = line_misses(LF, q.x, q.y, q.z, q.w) ? 1 : 0;
+        }
+        out[3 * t + 2] = (int8_t)miss;
+    }
+}
+
 // Hits in candidate order (segment-major, traversal order within a segment),
 // and every segment's hit offset and count.
 __global__ void k_edge_compact(const int64_t* __restrict__ keep, const int64_t* __restrict__ pos, int64_t nc,
@@ -2273,6 +2301,18 @@ int ct_write_edge_candidates_spec(const ct_tree* t, int32_t mode, const double* 
             k_edge_cands<true, 1, false><<<g, et, 0, st>>>(T, S, n, order, off, cand_seg, cand_pos, spec_cap, counts);
     }
     CT_CHECK_LAUNCH("write_edge_candidates_spec");
+    return CT_OK;
+}
+
+int ct_cs_certificates(const ct_tree* t, const double* segs, const int32_t* cand_seg, const int32_t* cand_pos,
+                       int64_t n_cand, int8_t* out, void* stream) {
+    int s = check_tree(t);
+    if (s) return s;
+    if (n_cand == 0) return CT_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_cs_certificates<<<(unsigned)std::min<int64_t>(grid_of(n_cand, 128), 152 * 64), 128, 0, st>>>(
+        make_q(t), (const double4*)segs, cand_seg, cand_pos, n_cand, out);
+    CT_CHECK_LAUNCH("cs_certificates");
     return CT_OK;
 }
 

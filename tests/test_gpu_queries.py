@@ -385,6 +385,61 @@ def test_line_filter_keeps_results(oracle, name):
         same(a, b)
 
 
+@pytest.mark.parametrize("name", ["grid_tri", "utm_tri", "mixed"])
+def test_float32_certificates_are_sound(name):
+    """The segment test's float32 certificates against upstream's float64
+    Cohen-Sutherland verdict on every (segment, cell) pair the unfiltered
+    traversal produces: the interval verdict is undecided or equal, and the
+    line filter claims a miss only where the float64 clip rejects.  Random
+    and grazing segments (along and one ulp off edges, through vertices, on
+    grid lines), UTM-size offsets."""
+    import ctypes
+
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, _device, _lib
+
+    if name == "grid_tri":
+        xy, f = syn.triangle_mesh(60, 50, seed=81, extent=(60.0, 50.0), jitter=0.0)
+    elif name == "utm_tri":
+        xy, f = syn.triangle_mesh(60, 50, seed=82, extent=(60.0, 50.0), offset=(5.0e5, 4.2e6))
+    else:
+        xy, f = syn.mixed_mesh(60, 50, seed=83, extent=(60.0, 50.0))
+    lo, hi = xy.min(0), xy.max(0)
+    rng = np.random.default_rng(84)
+    a0 = rng.uniform(lo, hi, (20_000, 2))
+    segs = np.concatenate([_grazing_segments(xy, f, 2000, 85), syn.random_segments(2000, lo - 1.0, hi + 1.0, seed=86),
+                           np.stack([a0, a0 + rng.uniform(-3, 3, (20_000, 2))], 1)])
+    sd = torch.as_tensor(segs, device="cuda")
+    t = CellTree2d(xy, f, -1)._tree
+    t.ensure_box_index()
+    lib = _lib.load()
+    P, st = _device.ptr, _device.stream()
+    keep, t.desc.bb_leaf32 = t.desc.bb_leaf32, None  # candidates of the unfiltered traversal
+    try:
+        n = len(segs)
+        cnt = torch.empty(n, dtype=torch.int64, device="cuda")
+        _lib.check(lib.ct_count_edge_candidates(ctypes.byref(t.desc), 1, P(sd), n, None, P(cnt), st), "count")
+        off, nc = t.scan(cnt)
+        cseg = torch.empty(nc, dtype=torch.int32, device="cuda")
+        cpos = torch.empty(nc, dtype=torch.int32, device="cuda")
+        _lib.check(lib.ct_write_edge_candidates(ctypes.byref(t.desc), 1, P(sd), n, None, P(off), P(cseg), P(cpos),
+                                                st), "write")
+    finally:
+        t.desc.bb_leaf32 = keep
+    assert nc > 500_000
+    out = torch.empty((nc, 3), dtype=torch.int8, device="cuda")
+    _lib.check(lib.ct_cs_certificates(ctypes.byref(t.desc), P(sd), P(cseg), P(cpos), nc, P(out), st), "cert")
+    o = out.cpu().numpy().astype(np.int64)
+    f64, f32, miss = o[:, 0], o[:, 1], o[:, 2]
+    assert (f64 >= 0).all()
+    decided = f32 >= 0
+    assert (f32[decided] == f64[decided]).all(), np.nonzero(decided & (f32 != f64))[0][:10]
+    assert decided.mean() > 0.8, decided.mean()  # the float32 verdict settles most pairs (grazing ones aside)
+    assert (f64[miss == 1] == 0).all()
+    assert miss.sum() > 0 and (f64 == 1).sum() > 0
+
+
 def test_long_segments_sorted(oracle):
     """Segments crossing thousands of cells: the per-segment sort runs in
     global memory (more than 1024 results per segment)."""
