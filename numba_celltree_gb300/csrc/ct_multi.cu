@@ -1225,20 +1225,20 @@ constexpr int SORT_SMEM = 1024;  // 2 x 1024 x (8 + 8) B = 32 KB static shared m
 // rank is its rank in its own run plus the number of smaller elements in the
 // partner run (binary search).  Small segments are sorted in shared memory,
 // large ones in global memory (A/B ping-pong); the result lands in `idx_out`.
+// Segments of more than WARP_SORT_MAX results (listed by k_segsort_warp).
 __global__ void __launch_bounds__(SORT_T) k_segsort(const int64_t* __restrict__ off, const int64_t* __restrict__ cnt,
-                                                    int64_t nseg, unsigned long long* __restrict__ kA,
-                                                    int64_t* __restrict__ iA, unsigned long long* __restrict__ kB,
-                                                    int64_t* __restrict__ iB, int64_t* __restrict__ idx_out) {
+                                                    const int* __restrict__ list,
+                                                    const unsigned long long* __restrict__ nlist,
+                                                    unsigned long long* __restrict__ kA, int64_t* __restrict__ iA,
+                                                    unsigned long long* __restrict__ kB, int64_t* __restrict__ iB,
+                                                    int64_t* __restrict__ idx_out) {
     __shared__ unsigned long long sk[2][SORT_SMEM];
     __shared__ int64_t si[2][SORT_SMEM];
-    int64_t sgi = blockIdx.x;
-    if (sgi >= nseg) return;
+    const int64_t nl = (int64_t)*nlist;
+    for (int64_t li = blockIdx.x; li < nl; li += gridDim.x) {
+    __syncthreads();
+    const int64_t sgi = list[li];
     int64_t c = cnt[sgi], o = off[sgi];
-    if (c <= 0) return;
-    if (c == 1) {
-        if (threadIdx.x == 0) idx_out[o] = iA[o];
-        return;
-    }
     bool smem = c <= SORT_SMEM;
     unsigned long long* k0 = smem ? sk[0] : kA + o;
     int64_t* i0 = smem ? si[0] : iA + o;
@@ -1281,6 +1281,101 @@ __global__ void __launch_bounds__(SORT_T) k_segsort(const int64_t* __restrict__ 
         i1 = ti;
     }
     for (int64_t t = threadIdx.x; t < c; t += blockDim.x) idx_out[o + t] = i0[t];
+    }
+}
+
+// One warp per segment: bitonic sort of up to 32 x E (key, idx) pairs in
+// registers (element r * 32 + lane in register r of the lane; pads sort
+// last).  (key, idx) pairs are unique, so the order is the stable sort's.
+constexpr int WARP_SORT_MAX = 128;
+
+template <int E>
+__device__ __forceinline__ void warp_bitonic(unsigned long long (&k)[E], int64_t (&x)[E], int lane) {
+    const unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int size = 2; size <= 32 * E; size <<= 1) {
+#pragma unroll
+        for (int j = size >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int rj = j >> 5;
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int rp = r ^ rj;
+                    if (rp > r) {
+                        const bool asc = ((r * 32 + lane) & size) == 0;
+                        const bool less_rp = kless(k[rp], x[rp], k[r], x[r]);
+                        if (asc ? less_rp : !less_rp) {
+                            const unsigned long long tk = k[r];
+                            k[r] = k[rp];
+                            k[rp] = tk;
+                            const int64_t tx = x[r];
+                            x[r] = x[rp];
+                            x[rp] = tx;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const unsigned long long pk = __shfl_xor_sync(FULL, k[r], j);
+                    const int64_t px = __shfl_xor_sync(FULL, x[r], j);
+                    const bool asc = ((r * 32 + lane) & size) == 0;
+                    const bool lower = (lane & j) == 0;
+                    const bool pless = kless(pk, px, k[r], x[r]);
+                    if ((lower == asc) ? pless : !pless) {
+                        k[r] = pk;
+                        x[r] = px;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int E>
+__device__ __forceinline__ void warp_sort_segment(const unsigned long long* __restrict__ kA,
+                                                  const int64_t* __restrict__ iA, int64_t o, int64_t c, int lane,
+                                                  int64_t* __restrict__ idx_out) {
+    unsigned long long k[E];
+    int64_t x[E];
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const int64_t e = r * 32 + lane;
+        k[r] = e < c ? kA[o + e] : ~0ull;
+        x[r] = e < c ? iA[o + e] : INT64_MAX;
+    }
+    warp_bitonic<E>(k, x, lane);
+#pragma unroll
+    for (int r = 0; r < E; r++) {
+        const int64_t e = r * 32 + lane;
+        if (e < c) idx_out[o + e] = x[r];
+    }
+}
+
+// Segments of up to WARP_SORT_MAX results sorted by a warp each; longer ones
+// are listed for k_segsort.
+__global__ void __launch_bounds__(256) k_segsort_warp(const int64_t* __restrict__ off,
+                                                      const int64_t* __restrict__ cnt, int64_t nseg,
+                                                      const unsigned long long* __restrict__ kA,
+                                                      const int64_t* __restrict__ iA, int64_t* __restrict__ idx_out,
+                                                      int* __restrict__ list, unsigned long long* __restrict__ nlist) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t sgi = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); sgi < nseg; sgi += warps) {
+        const int64_t c = cnt[sgi], o = off[sgi];
+        if (c <= 0) continue;
+        if (c == 1) {
+            if (lane == 0) idx_out[o] = iA[o];
+        } else if (c <= 32) {
+            warp_sort_segment<1>(kA, iA, o, c, lane, idx_out);
+        } else if (c <= 64) {
+            warp_sort_segment<2>(kA, iA, o, c, lane, idx_out);
+        } else if (c <= WARP_SORT_MAX) {
+            warp_sort_segment<4>(kA, iA, o, c, lane, idx_out);
+        } else if (lane == 0) {
+            list[atomicAdd(nlist, 1ull)] = (int)sgi;
+        }
+    }
 }
 
 __global__ void k_gather_results(const int64_t* __restrict__ perm, int64_t total, const int64_t* __restrict__ jj_in,
@@ -1946,7 +2041,10 @@ int ct_write_boxes_spec(const ct_tree* t, const double* boxes, int64_t n, const 
     return CT_OK;
 }
 
-size_t ct_sort_workspace_size(int64_t total) { return (size_t)(total > 0 ? total : 1) * 4 * 8 + 1024; }
+size_t ct_sort_workspace_size(int64_t total) {
+    const size_t t = (size_t)(total > 0 ? total : 1);
+    return t * 4 * 8 + (t / (WARP_SORT_MAX + 1) + 2) * sizeof(int) + 1024 + 256;
+}
 
 int ct_sort_intersections(const double* segs, int64_t n_segs, const int64_t* offsets, const int64_t* counts,
                           const int64_t* ii, const int64_t* jj_in, const double* xy_in, int64_t total,
@@ -1958,8 +2056,14 @@ int ct_sort_intersections(const double* segs, int64_t n_segs, const int64_t* off
     int64_t* iA = (int64_t*)(kA + total);
     unsigned long long* kB = (unsigned long long*)(iA + total);
     int64_t* iB = (int64_t*)(kB + total);
+    unsigned long long* nlist = (unsigned long long*)(iB + total);  // 8 B, then the list of long segments
+    int* list = (int*)(nlist + 1);
+    if (n_segs > INT32_MAX) return ct_fail(CT_ERR_ARG, "at most 2^31 - 1 segments");
+    CT_CUDA(cudaMemsetAsync(nlist, 0, sizeof(unsigned long long), st));
     k_tkeys<<<grid_of(total, 256), 256, 0, st>>>((const double4*)segs, ii, (const double4*)xy_in, total, kA, iA);
-    k_segsort<<<(unsigned)n_segs, SORT_T, 0, st>>>(offsets, counts, n_segs, kA, iA, kB, iB, iB);
+    k_segsort_warp<<<(unsigned)std::min<int64_t>(grid_of(n_segs * 32, 256), 152 * 32), 256, 0, st>>>(
+        offsets, counts, n_segs, kA, iA, iB, list, nlist);
+    k_segsort<<<152 * 4, SORT_T, 0, st>>>(offsets, counts, list, nlist, kA, iA, kB, iB, iB);
     // iB now holds, per segment, the sorted source positions (segments of one
     // result write them directly)
     k_gather_results<<<grid_of(total, 256), 256, 0, st>>>(iB, total, jj_in, (const double4*)xy_in, jj_out,

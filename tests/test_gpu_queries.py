@@ -624,3 +624,50 @@ def test_output_budgeted_chunks_reassemble_the_full_results(monkeypatch):
     # empty batches
     for got in (g.locate_boxes(boxes[:0]), g.intersect_edges(segs[:0])):
         assert all(len(x) == 0 for x in got)
+
+
+def test_segment_sort_sizes_and_ties():
+    """sort_intersections_by_edge (geometry_utils.py:564-574) on segments of
+    every size class of the sort -- one result, warp sorts of up to 32, 64
+    and 128, the block sort in shared and in global memory -- with equal
+    distances (stable: candidate order kept) and NaN points (last)."""
+    import ctypes
+
+    import torch
+
+    from numba_celltree_gb300 import _device, _lib
+
+    rng = np.random.default_rng(91)
+    sizes = [1, 2, 31, 32, 33, 63, 64, 65, 127, 128, 129, 500, 1023, 1024, 1025, 3000, 0, 7]
+    n = len(sizes)
+    segs = rng.uniform(-10, 10, (n, 2, 2))
+    counts = np.array(sizes, dtype=np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)[:-1]]).astype(np.int64)
+    total = int(counts.sum())
+    ii = np.repeat(np.arange(n), counts).astype(np.int64)
+    xy = rng.uniform(-10, 10, (total, 2, 2))
+    # ties: repeat some points within segments; NaNs
+    rep = rng.choice(total, total // 5, replace=False)
+    xy[rep] = xy[np.maximum(rep - 1, 0)]
+    xy[rng.choice(total, total // 50, replace=False)] = np.nan
+    jj = rng.integers(0, 1 << 40, total).astype(np.int64)
+    dev = "cuda"
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=dev)  # noqa: E731
+    s_d, o_d, c_d, ii_d, jj_d, xy_d = T(segs), T(offsets), T(counts), T(ii), T(jj), T(xy)
+    jj2 = torch.empty_like(jj_d)
+    xy2 = torch.empty_like(xy_d)
+    lib = _lib.load()
+    wsz = int(lib.ct_sort_workspace_size(total))
+    ws = torch.empty(wsz, dtype=torch.uint8, device=dev)
+    P = _device.ptr
+    _lib.check(lib.ct_sort_intersections(P(s_d), n, P(o_d), P(c_d), P(ii_d), P(jj_d), P(xy_d), total, P(jj2), P(xy2),
+                                         P(ws), wsz, _device.stream()), "sort")
+    # expected: per segment, stable order by t = (c - a) . (b - a), NaN last
+    a = segs[ii, 0]
+    b = segs[ii, 1]
+    t = (xy[:, 0, 0] - a[:, 0]) * (b[:, 0] - a[:, 0]) + (xy[:, 0, 1] - a[:, 1]) * (b[:, 1] - a[:, 1])
+    tk = np.where(np.isnan(t), np.inf, t)
+    nan_last = np.isnan(t).astype(np.int64)
+    order = np.lexsort((np.arange(total), tk, nan_last, ii))
+    same(jj2.cpu().numpy(), jj[order])
+    same(xy2.cpu().numpy(), xy[order])
