@@ -509,9 +509,9 @@ class _GpuTree:
         return max(1, min(self.max_depth, int(np.ceil(np.log2(self.n / split)))))
 
     # uncut batches up to this many segments keep each segment's first
-    # SPEC_CAP candidates in the counting pass (one traversal for most)
+    # SEG_SPEC_CAP candidates in the counting pass (one traversal for most)
     SPEC_MAX_SEGMENTS = 1 << 22
-    SPEC_CAP = 64
+    SEG_SPEC_CAP = 64
 
     def edge_candidate_ranges(self, segs_d, mode: int, order, cut, keep: bool = False):
         """Every segment's candidate offset and count (device int64) and the
@@ -528,9 +528,9 @@ class _GpuTree:
         if cut is None:
             ccnt = _device.empty((n,), torch.int64, self.device)
             if keep and 0 < n <= self.SPEC_MAX_SEGMENTS:
-                spec = _device.empty((n, self.SPEC_CAP), torch.int32, self.device)
+                spec = _device.empty((n, self.SEG_SPEC_CAP), torch.int32, self.device)
                 _lib.check(lib.ct_count_edge_candidates_spec(d, mode, P(segs_d), n, P(order), P(ccnt), P(spec),
-                                                             self.SPEC_CAP, st), "intersect_edges")
+                                                             self.SEG_SPEC_CAP, st), "intersect_edges")
                 coff, nc = self.scan(ccnt)
                 return coff, ccnt, nc, ("spec", spec)
             _lib.check(lib.ct_count_edge_candidates(d, mode, P(segs_d), n, P(order), P(ccnt), st), "intersect_edges")
@@ -589,10 +589,14 @@ class _GpuTree:
     # pairs from which subtrees inside a box are written by a warp each after
     # the traversal (below, the extra launch costs more than it saves)
     BOX_JOBS_MIN_PAIRS = 1 << 20
-    # batches up to this many boxes count and keep each box's first SPEC_CAP
-    # pairs in one traversal (latency of small batches: one traversal less)
+    # the counting pass keeps each box's first SPEC_CAP pairs (batches up to
+    # SPEC_MAX_BOXES boxes; SPEC_CAP_LARGE beyond, scratch up to
+    # SPEC_MAX_BYTES), so boxes whose pairs fit are traversed once;
+    # SPEC_MAX_BOXES = 0 switches it off
     SPEC_MAX_BOXES = 1 << 16
     SPEC_CAP = 64
+    SPEC_CAP_LARGE = 16
+    SPEC_MAX_BYTES = 1 << 30
 
     def locate_boxes(self, boxes_d, config=None, budget=None):
         """Pairs (box, cell) of every box query, box-major in upstream order;
@@ -612,11 +616,12 @@ class _GpuTree:
         self._apply("boxes", config)
         order = self.work_order(boxes_d, 0, config.get("work_order"))
         spec = None
-        if n <= self.SPEC_MAX_BOXES:
+        cap = self.SPEC_CAP if n <= self.SPEC_MAX_BOXES else self.SPEC_CAP_LARGE
+        if self.SPEC_MAX_BOXES > 0 and 0 < n and n * cap * 4 <= self.SPEC_MAX_BYTES:
             # one traversal: the counting pass also keeps each box's first pairs
-            spec = _device.empty((n, self.SPEC_CAP), torch.int32, self.device)
+            spec = _device.empty((n, cap), torch.int32, self.device)
             _lib.check(lib.ct_count_boxes_spec(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
-                                               _device.ptr(counts), _device.ptr(spec), self.SPEC_CAP, st),
+                                               _device.ptr(counts), _device.ptr(spec), cap, st),
                        "locate_boxes")
         else:
             _lib.check(lib.ct_count_boxes(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
@@ -637,7 +642,7 @@ class _GpuTree:
             ws = _device.empty((wsz,), torch.uint8, self.device)
             _lib.check(
                 lib.ct_write_boxes_spec(ctypes.byref(self.desc), _device.ptr(boxes_d), n, _device.ptr(order),
-                                        _device.ptr(counts), _device.ptr(offsets), _device.ptr(spec), self.SPEC_CAP,
+                                        _device.ptr(counts), _device.ptr(offsets), _device.ptr(spec), cap,
                                         total, jm, _device.ptr(ii), _device.ptr(jj), _device.ptr(ws), wsz, st),
                 "locate_boxes",
             )
@@ -690,7 +695,7 @@ class _GpuTree:
                                                     P(cseg), P(cpos), st), "intersect_edges")
         elif isinstance(items[0], str):
             _lib.check(lib.ct_write_edge_candidates_spec(ctypes.byref(self.desc), mode, P(segs_d), n, P(order),
-                                                         P(ccnt), P(coff), P(items[1]), self.SPEC_CAP, P(cseg),
+                                                         P(ccnt), P(coff), P(items[1]), self.SEG_SPEC_CAP, P(cseg),
                                                          P(cpos), st), "intersect_edges")
             del items
         else:

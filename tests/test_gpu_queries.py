@@ -169,11 +169,11 @@ def test_split_segment_traversal_matches_uncut(oracle):
     # uncut, without the counting pass's scratch, and with a scratch of 2
     # candidates (most segments through the second traversal)
     for spec_max, spec_cap in ((0, 64), (1 << 22, 2)):
-        t.SPEC_MAX_SEGMENTS, t.SPEC_CAP = spec_max, spec_cap
+        t.SPEC_MAX_SEGMENTS, t.SEG_SPEC_CAP = spec_max, spec_cap
         got = t.locate_edges(sd, 1, {"threads": 64, "work_order": True, "split": 0})
         for a, b in zip(got, base):
             assert teq(a, b), (spec_max, spec_cap)
-    del t.SPEC_MAX_SEGMENTS, t.SPEC_CAP
+    del t.SPEC_MAX_SEGMENTS, t.SEG_SPEC_CAP
     counts0 = t.count_edge_candidates(sd, 1)
     for split in (2, 7, 64, 1024):
         cfg = {"threads": 128, "work_order": split == 7, "split": split}
@@ -234,7 +234,7 @@ def test_box_subtree_jobs_match_inline(oracle):
         np.array([[-10.0, 100.0, -10.0, 80.0], [0.0, 90.0, 0.0, 70.0], [40.0, 40.5, 30.0, 30.5]]),
     ])
     bd = torch.as_tensor(boxes, device="cuda")
-    for cpl, spec_max, spec_cap in ((1, 0, 64), (2, 0, 64), (3, 0, 64), (2, 1 << 16, 64), (1, 1 << 16, 3)):
+    for cpl, spec_max, spec_cap in ((1, 0, 64), (2, 0, 64), (3, 0, 64), (2, 1 << 16, 64), (1, 1 << 16, 3), (3, 1, 64)):
         g = CellTree2d(xy, f, -1, 4, cpl)
         t = g._tree
         t.BOX_JOBS_MIN_PAIRS = 0  # the queued path at any size
