@@ -121,7 +121,9 @@ struct WS {
 static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Carves the workspace; returns total bytes.  base == nullptr -> size only.
-static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_trees = 1) {
+// `forest`: the layout of the forest builds, whose per-element tree index is
+// written and read for every element even when the batch holds one tree.
+static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_trees = 1, bool forest = false) {
     size_t off = 0;
     auto take = [&](size_t bytes) -> char* {
         char* p = base ? base + off : nullptr;
@@ -158,7 +160,7 @@ static size_t carve(char* base, int64_t n, int NB, int factor, WS* ws, int n_tre
     w.lvl_e = (int*)take(sizeof(int) * (DEV_MAX_LEVELS + 1));
     w.n_roots = n_trees;
     w.tree_off = (int64_t*)take(sizeof(int64_t) * ((size_t)n_trees + 1));
-    w.elem_tree = (int*)take(n_trees > 1 ? sizeof(int) * nn : 16);
+    w.elem_tree = (int*)take((forest || n_trees > 1) ? sizeof(int) * nn : 16);
     w.root_key = (unsigned long long*)take(sizeof(unsigned long long) * 4 * (size_t)n_trees);
     w.root_zp = (int*)take(sizeof(int) * 4 * (size_t)n_trees);
     w.tree_depth = (int*)take(sizeof(int) * (size_t)n_trees);
@@ -1617,7 +1619,7 @@ int ct_build_emit(const void* workspace, int64_t n, int32_t NB, int32_t factor, 
 
 size_t ct_build_forest_workspace_size(int64_t n_total, int32_t n_trees, int32_t NB, int32_t factor) {
     if (NB < 2 || NB > NBMAX || n_total < 0 || factor < 1 || n_trees < 1) return 0;
-    return carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+    return carve(nullptr, n_total, NB, factor, nullptr, n_trees, true);
 }
 
 int ct_build_forest(const double* bb, int64_t n_total, const int64_t* tree_off_host, int32_t n_trees, int32_t NB,
@@ -1637,11 +1639,11 @@ int ct_build_forest(const double* bb, int64_t n_total, const int64_t* tree_off_h
         if (m < 1) return ct_fail(CT_ERR_ARG, "every tree needs at least one element");
         any_large |= m > SMALL;
     }
-    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees, true);
     if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
     if (!bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
     WS ws;
-    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees, true);
     int ni = (int)n_total;
     CT_CUDA(cudaMemcpyAsync(ws.tree_off, tree_off_host, sizeof(int64_t) * ((size_t)n_trees + 1),
                             cudaMemcpyHostToDevice, st));
@@ -1697,11 +1699,11 @@ int ct_build_forest_async(const double* bb, int64_t n_total, const int64_t* tree
         if (m < 1) return ct_fail(CT_ERR_ARG, "every tree needs at least one element");
         any_large |= m > SMALL;
     }
-    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees);
+    size_t need = carve(nullptr, n_total, NB, factor, nullptr, n_trees, true);
     if (!workspace || ws_bytes < need) return ct_fail(CT_ERR_WORKSPACE, "build workspace too small");
     if (!bb) return ct_fail(CT_ERR_ARG, "bb_coords is null");
     WS ws;
-    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees, true);
     CT_CUDA(cudaMemcpyAsync(ws.tree_off, tree_off_dev, sizeof(int64_t) * ((size_t)n_trees + 1),
                             cudaMemcpyDeviceToDevice, st));
     const int ni = (int)n_total;
@@ -1751,7 +1753,7 @@ int ct_build_forest_emit(const void* workspace, int64_t n_total, int32_t n_trees
     if (NB < 2 || NB > NBMAX || factor < 1 || n_trees < 1) return ct_fail(CT_ERR_ARG, "bad arguments");
     if (!node_off) return ct_fail(CT_ERR_ARG, "node_off is null");
     WS ws;
-    carve((char*)workspace, n_total, NB, factor, &ws, n_trees);
+    carve((char*)workspace, n_total, NB, factor, &ws, n_trees, true);
     return emit_nodes(ws, n_total, 0, node_off, child, Lmax, Rmin, ptr, size, dim, bb_indices, st);
 }
 

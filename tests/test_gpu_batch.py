@@ -302,3 +302,32 @@ def test_forest_pipeline_given_tolerance_and_empty_mesh_points(oracle):
     for k, (xy, f) in enumerate(meshes):
         a, b = int(pipe.offsets[k]), int(pipe.offsets[k + 1])
         assert np.array_equal(res[a:b], oracle.OracleCellTree2d(xy, f, -1).locate_points(pts[k], 1e-3)), k
+
+
+@pytest.mark.gpu
+def test_batches_of_one_mesh(oracle):
+    """A batch holding a single mesh (host-driven and device-driven forest
+    builds, the pipeline) equals the mesh built and queried alone: the forest
+    layout keeps a per-element tree index even for one tree."""
+    import torch
+
+    from numba_celltree_gb300 import CellTree2d, CellTreeBatch
+    from numba_celltree_gb300.batch import ForestBuild, ForestPipeline
+
+    xy, f = syn.triangle_mesh(120, 90, seed=21, extent=(120.0, 90.0))
+    alone = CellTree2d(xy, f, -1)
+    for device_levels in (False, True):
+        batch = CellTreeBatch([(xy, f)], -1, device_levels=device_levels)
+        assert batch[0].nodes.tobytes() == alone.nodes.tobytes(), device_levels
+        assert np.array_equal(batch[0].bb_indices, alone.bb_indices), device_levels
+    fb = ForestBuild([len(f)], torch.device("cuda", 0))
+    fb.launch(alone._tree.bb_coords)
+    node_off, depth = fb.result()
+    nn = int(node_off[1])
+    assert nn == len(alone.nodes) and depth[0] == alone._tree.max_depth
+    assert np.array_equal(fb.child[:nn].cpu().numpy(), alone.nodes["child"])
+    assert np.array_equal(fb.bb_indices.cpu().numpy(), alone.bb_indices)
+    pts = syn.uniform_points(20_000, xy.min(0), xy.max(0), seed=22, margin=0.02)
+    pipe = ForestPipeline([(xy, f)], [len(pts)])
+    res = pipe.run(xy, pts).cpu().numpy()
+    assert np.array_equal(res, oracle.OracleCellTree2d(xy, f, -1).locate_points(pts))
