@@ -331,3 +331,21 @@ def test_batches_of_one_mesh(oracle):
     pipe = ForestPipeline([(xy, f)], [len(pts)])
     res = pipe.run(xy, pts).cpu().numpy()
     assert np.array_equal(res, oracle.OracleCellTree2d(xy, f, -1).locate_points(pts))
+
+
+@pytest.mark.gpu
+def test_batch_of_small_meshes_only():
+    """Every mesh at most one subtree (128 cells): the level loops have no
+    work and the warp subtrees build every tree; both forest builds equal
+    the meshes built alone."""
+    from numba_celltree_gb300 import CellTree2d, CellTreeBatch
+
+    meshes = [syn.triangle_mesh(nx, ny, seed=30 + nx, extent=(float(nx), float(ny)))
+              for nx, ny in [(1, 1), (2, 3), (8, 8), (5, 6), (7, 9)]]
+    assert max(len(f) for _, f in meshes) <= 128
+    for device_levels in (False, True):
+        batch = CellTreeBatch(meshes, -1, device_levels=device_levels)
+        for k, (xy, f) in enumerate(meshes):
+            alone = CellTree2d(xy, f, -1)
+            assert batch[k].nodes.tobytes() == alone.nodes.tobytes(), (device_levels, k)
+            assert np.array_equal(batch[k].bb_indices, alone.bb_indices), (device_levels, k)
