@@ -110,3 +110,49 @@ def test_library_exports_every_declared_entry_point():
     missing = sorted(n for n in names if not hasattr(lib, n))
     assert not missing, missing
     assert set(_lib.SIGNATURES) <= names, sorted(set(_lib.SIGNATURES) - names)
+
+
+def test_new_entry_points_reject_bad_arguments_before_any_launch():
+    """The box and segment entry points validate their arguments on the host
+    and fail with CT_ERR_ARG / CT_ERR_WORKSPACE before touching the device
+    (runs without a GPU): bad modes, cut depths and scratch caps, too-small
+    workspaces, trees without nodes."""
+    import ctypes
+
+    from numba_celltree_gb300 import _lib
+
+    lib = _lib.load()
+    empty = _lib.CtTree()
+    t = _lib.CtTree()
+    t.n_nodes, t.max_depth, t.n_max_vert, t.n_elements = 1, 0, 3, 1
+    T, E = ctypes.byref(t), ctypes.byref(empty)
+    dummy = 64  # never dereferenced: every call below fails its checks first
+    ARG, WS = _lib.CT_ERR_ARG, _lib.CT_ERR_WORKSPACE
+    assert lib.ct_count_edge_items(E, 1, dummy, 5, None, 4, dummy, None) == ARG  # no nodes
+    assert lib.ct_count_edge_items(T, 2, dummy, 5, None, 4, dummy, None) == ARG  # mode
+    assert lib.ct_count_edge_items(T, 0, dummy, 5, None, 4, dummy, None) == ARG  # edge mode on a face tree
+    assert lib.ct_count_edge_items(T, 1, dummy, 5, None, 65, dummy, None) == ARG  # cut depth
+    assert lib.ct_count_edge_items(T, 1, dummy, 5, None, -1, dummy, None) == ARG
+    assert lib.ct_write_edge_items(T, 1, dummy, 5, None, 99, dummy, dummy, dummy, None) == ARG
+    assert lib.ct_count_item_candidates(T, 3, dummy, dummy, dummy, 5, dummy, None) == ARG
+    assert lib.ct_segment_candidate_ranges(dummy, dummy, -1, dummy, dummy, 0, dummy, dummy, None) == ARG
+    assert lib.ct_count_edge_candidates_spec(T, 1, dummy, 5, None, dummy, dummy, 0, None) == ARG  # cap
+    assert lib.ct_count_edge_candidates_spec(T, 1, dummy, 5, None, dummy, dummy, 4097, None) == ARG
+    assert lib.ct_count_edge_candidates_spec(T, 1, dummy, 5, None, dummy, None, 64, None) == ARG  # no scratch
+    assert lib.ct_write_edge_candidates_spec(T, 1, dummy, 5, None, dummy, dummy, dummy, 0, dummy, dummy,
+                                             None) == ARG
+    assert lib.ct_count_boxes_spec(T, dummy, 5, None, dummy, dummy, 0, None) == ARG
+    assert lib.ct_count_boxes_spec(E, dummy, 5, None, dummy, dummy, 16, None) == ARG
+    wsz = int(lib.ct_write_boxes_workspace_size(1000, 8))
+    assert wsz >= 256 + (1000 // 8 + 1) * 32
+    assert int(lib.ct_write_boxes_workspace_size(1000, 0)) == wsz  # 0 means the default, 8 cells
+    assert int(lib.ct_write_boxes_workspace_size(1000, 1)) == int(lib.ct_write_boxes_workspace_size(1000, 2))
+    assert lib.ct_write_boxes_ws(T, dummy, 5, None, dummy, 1000, 8, dummy, dummy, dummy, wsz - 1, None) == WS
+    assert lib.ct_write_boxes_ws(T, dummy, 5, None, dummy, -1, 8, dummy, dummy, dummy, wsz, None) == ARG
+    assert lib.ct_write_boxes_spec(T, dummy, 5, None, dummy, dummy, dummy, 16, 1000, 8, dummy, dummy, dummy,
+                                   wsz - 1, None) == WS
+    swz = int(lib.ct_sort_workspace_size(1000))
+    assert swz >= 1000 * 32 + (1000 // 129 + 2) * 4
+    assert lib.ct_sort_intersections(dummy, 5, dummy, dummy, dummy, dummy, dummy, 1000, dummy, dummy, dummy,
+                                     swz - 1, None) == WS
+    assert lib.ct_cs_certificates(E, dummy, dummy, dummy, 5, dummy, None) == ARG
