@@ -509,15 +509,18 @@ class _GpuTree:
         return max(1, min(self.max_depth, int(np.ceil(np.log2(self.n / split)))))
 
     # uncut batches up to this many segments keep each segment's first
-    # SEG_SPEC_CAP candidates in the counting pass (one traversal for most)
+    # SEG_SPEC_CAP candidates in the counting pass (one traversal for most;
+    # halved until the scratch fits SEG_SPEC_MAX_BYTES, none below 8)
     SPEC_MAX_SEGMENTS = 1 << 22
-    SEG_SPEC_CAP = 64
+    SEG_SPEC_CAP = 128
+    SEG_SPEC_MAX_BYTES = 1 << 31
 
     def edge_candidate_ranges(self, segs_d, mode: int, order, cut, keep: bool = False):
         """Every segment's candidate offset and count (device int64) and the
         candidate total, and what the writing pass uses: (coff, ccnt, total,
-        items) -- items None (traverse again), ("spec", scratch) with `keep`
-        (the counting pass kept each segment's first candidates), or with a
+        items) -- items None (traverse again), ("spec", scratch, cap) with
+        `keep` (the counting pass kept each segment's first `cap`
+        candidates), or with a
         cut the work items (item_seg, item_node, n_items, item offsets)."""
         torch = _device.torch()
         lib = _lib.load()
@@ -527,12 +530,15 @@ class _GpuTree:
         d = ctypes.byref(self.desc)
         if cut is None:
             ccnt = _device.empty((n,), torch.int64, self.device)
-            if keep and 0 < n <= self.SPEC_MAX_SEGMENTS:
-                spec = _device.empty((n, self.SEG_SPEC_CAP), torch.int32, self.device)
+            cap = int(self.SEG_SPEC_CAP)
+            while cap >= 8 and n * cap * 4 > self.SEG_SPEC_MAX_BYTES:
+                cap //= 2
+            if keep and 0 < n <= self.SPEC_MAX_SEGMENTS and cap >= 1 and (cap >= 8 or cap == self.SEG_SPEC_CAP):
+                spec = _device.empty((n, cap), torch.int32, self.device)
                 _lib.check(lib.ct_count_edge_candidates_spec(d, mode, P(segs_d), n, P(order), P(ccnt), P(spec),
-                                                             self.SEG_SPEC_CAP, st), "intersect_edges")
+                                                             cap, st), "intersect_edges")
                 coff, nc = self.scan(ccnt)
-                return coff, ccnt, nc, ("spec", spec)
+                return coff, ccnt, nc, ("spec", spec, cap)
             _lib.check(lib.ct_count_edge_candidates(d, mode, P(segs_d), n, P(order), P(ccnt), st), "intersect_edges")
             coff, nc = self.scan(ccnt)
             return coff, ccnt, nc, None
@@ -695,7 +701,7 @@ class _GpuTree:
                                                     P(cseg), P(cpos), st), "intersect_edges")
         elif isinstance(items[0], str):
             _lib.check(lib.ct_write_edge_candidates_spec(ctypes.byref(self.desc), mode, P(segs_d), n, P(order),
-                                                         P(ccnt), P(coff), P(items[1]), self.SEG_SPEC_CAP, P(cseg),
+                                                         P(ccnt), P(coff), P(items[1]), items[2], P(cseg),
                                                          P(cpos), st), "intersect_edges")
             del items
         else:
