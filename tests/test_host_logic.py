@@ -156,3 +156,28 @@ def test_new_entry_points_reject_bad_arguments_before_any_launch():
     assert lib.ct_sort_intersections(dummy, 5, dummy, dummy, dummy, dummy, dummy, 1000, dummy, dummy, dummy,
                                      swz - 1, None) == WS
     assert lib.ct_cs_certificates(E, dummy, dummy, dummy, 5, dummy, None) == ARG
+
+
+def test_segment_split_rule():
+    """edge_cut: segment traversals are cut into work items about `split`
+    cells large below SPLIT_MAX_SEGMENTS segments (by default), never for
+    trees of at most `split` cells or too deep for the stacked traversal."""
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    from numba_celltree_gb300.celltree_base import _GpuTree
+
+    G = _GpuTree
+    t = SimpleNamespace(n=5_000_000, max_depth=24, BATCHED_MAX_STACK=G.BATCHED_MAX_STACK,
+                        SPLIT_CELLS=G.SPLIT_CELLS, SPLIT_MAX_SEGMENTS=G.SPLIT_MAX_SEGMENTS)
+    cut = G.edge_cut(t, {}, 200)
+    assert cut == int(np.ceil(np.log2(5_000_000 / G.SPLIT_CELLS)))  # 13: about 1024 cells per item
+    assert G.edge_cut(t, {}, G.SPLIT_MAX_SEGMENTS) is None  # large batches run uncut
+    assert G.edge_cut(t, {"split": 0}, 200) is None
+    assert G.edge_cut(t, {"split": 256}, 10**7) == int(np.ceil(np.log2(5_000_000 / 256)))
+    assert G.edge_cut(t, {"split": 2}, 200) == 24  # at most the tree depth
+    t.n = 900
+    assert G.edge_cut(t, {}, 200) is None  # a tree of at most `split` cells
+    t.n, t.max_depth = 5_000_000, G.BATCHED_MAX_STACK - 1
+    assert G.edge_cut(t, {}, 200) is None  # too deep for the stacked traversal
