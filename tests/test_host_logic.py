@@ -176,7 +176,9 @@ def test_segment_split_rule():
     assert G.edge_cut(t, {}, G.SPLIT_MAX_SEGMENTS) is None  # large batches run uncut
     assert G.edge_cut(t, {"split": 0}, 200) is None
     assert G.edge_cut(t, {"split": 256}, 10**7) == int(np.ceil(np.log2(5_000_000 / 256)))
-    assert G.edge_cut(t, {"split": 2}, 200) == 24  # at most the tree depth
+    t.max_depth = 20
+    assert G.edge_cut(t, {"split": 2}, 200) == 20  # at most the tree depth (log2(2.5e6) > 21)
+    t.max_depth = 24
     t.n = 900
     assert G.edge_cut(t, {}, 200) is None  # a tree of at most `split` cells
     t.n, t.max_depth = 5_000_000, G.BATCHED_MAX_STACK - 1
